@@ -1,0 +1,66 @@
+"""The CPU oracle against the golden vectors produced by the reference's own routines
+(tests/golden/gen_golden.py).  Fixed refinement levels 0 and 1 and the adaptive mode, per pair
+class; tolerance 1e-12 relative per pair (the FP64 parity bar)."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+MESHES = ["ico2", "ico2_jitter", "ico1_r20"]
+TOL = 1e-12
+
+
+def _close(a, b, tol=TOL):
+    scale = np.maximum(np.linalg.norm(b, axis=1), 1e-12 * np.abs(b).max())
+    return (np.linalg.norm(a - b, axis=1) / scale).max()
+
+
+@pytest.mark.parametrize("mesh", MESHES)
+@pytest.mark.parametrize("cls", [O.VERTEX, O.EDGE, O.FAR])
+def test_fixed_levels_match_reference(mesh, cls):
+    g = np.load(os.path.join(GOLD, f"{mesh}.npz"))
+    pairs = g[f"pairs_{cls}"]
+    for tag, lev in (("L0", 0), ("L1", 1)):
+        raw, J, _, _ = O.integrate(cls, pairs, g["V"], g["C"], mode=O.FIXED, level=lev)
+        assert _close(J, g[f"J_{cls}_{tag}"]) < TOL, (mesh, cls, tag)
+        if tag == "L0":
+            assert _close(raw, g[f"raw_{cls}_L0"]) < TOL
+
+
+@pytest.mark.parametrize("mesh", ["ico2_jitter", "ico1_r20"])
+@pytest.mark.parametrize("cls", [O.VERTEX, O.EDGE, O.FAR])
+def test_adaptive_compat_matches_reference(mesh, cls):
+    g = np.load(os.path.join(GOLD, f"{mesh}.npz"))
+    pairs = g[f"pairs_{cls}"]
+    raw, J, _, lev = O.integrate(cls, pairs, g["V"], g["C"], mode=O.ADAPTIVE_COMPAT)
+    assert _close(J, g[f"J_{cls}_adaptive"]) < 1e-12
+    it = g[f"iters_{cls}_adaptive"].astype(int)
+    # the kept level is the stop iteration or the one before it (buffer parity)
+    assert np.all((lev == it) | (lev == it - 1))
+
+
+def test_two_triangle_fixtures():
+    d = np.load(os.path.join(GOLD, "cases.npz"))
+    names = sorted({k.split("|")[0] for k in d.files})
+    assert len(names) >= 30
+    for nm in names:
+        g = {k.split("|")[1]: d[k] for k in d.files if k.startswith(nm + "|")}
+        cls = int(g["cls"])
+        for tag, mode, lev in (("J_L0", O.FIXED, 0), ("J_L1", O.FIXED, 1), ("J_adaptive", O.ADAPTIVE_COMPAT, 0)):
+            raw, J, _, _ = O.integrate(cls, g["pairs"], g["V"], g["C"], mode=mode, level=lev)
+            ok = ~g["uninit"]
+            assert _close(J[ok], g[tag][ok]) < TOL, (nm, tag)
+
+
+def test_theta_psi_points():
+    rows = np.load(os.path.join(GOLD, "theta_psi_points.npz"))["rows"]
+    L = O.lib()
+    for r in rows:
+        x, A, B, C, ref = r[0:3].copy(), r[3:6].copy(), r[6:9].copy(), r[9:12].copy(), r[12:16]
+        out = np.zeros(4)
+        L.o_theta_psi(O._p(x), O._p(A), O._p(B), O._p(C), O._p(out))
+        assert np.abs(out - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
