@@ -1,0 +1,354 @@
+"""Benchmark of the pair-integral path on one GB300.
+
+Workload (one "step"): every ordered pair of the four pair classes of a 20,480-triangle
+icosphere (5 subdivisions) whose vertices carry a seeded tangential Gaussian jitter of 0.15 x
+mean edge length, reprojected to the unit sphere: common-vertex, common-edge, self, and
+disjoint pairs with centroid distance < 3 x mean edge length (1,415,878 ordered pairs), each
+producing J (3-vector) and P.  Refinement: relative error control (|J_L - J_{L-1}| <= tol |J_L|,
+levels 0..5) with the 13-point degree-7 rule; the potential of adjacent pairs uses the graded
+Duffy rule.  Data are synthetic (no data set exists for this path).
+
+value  = pair-integrals/s with pair lists and outputs resident in HBM (CUDA events on the
+         launching stream, L2 flushed between steps by a 512 MiB write).
+e2e    = the same through the C-ABI from pinned host lists: H2D of the lists and D2H of J and P
+         inside the timed region.
+roofline: the pair kernels are bounded by the FP64 pipe; peaks are measured live by
+         i2_calibrate_pipes (MEASURED_PEAKS.json carries only HBM and bf16 figures).
+cpu_baseline: the oracle (a C restatement of the reference's formulas, OpenMP) on the host.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CLASSES = (0, 1, 2, 3)  # vertex, edge, near-field, self
+SEED = 2026
+NEAR = 3.0
+
+
+# ------------------------------------------------------------------ workload
+def workload():
+    from integrator2_gb300 import meshes, pairs
+    V, C = meshes.jittered_icosphere(5, 0.15, SEED)
+    pl = pairs.build_pairs(V, C, NEAR)
+    return V, C, {c: np.ascontiguousarray(pl.by_class(c)) for c in CLASSES}
+
+
+# ------------------------------------------------------------------ algorithmic work model
+# Frozen per-integrand-evaluation operation counts of the restated formulas (FP64):
+# (arithmetic flops, sqrt, divide, log, atan2).  Far: theta/psi + potential (a1 + a18);
+# edge / vertex: fused regular part (a1 - a2 / a1 - a3); duffy: inner potential per Duffy
+# point; closed forms (a4 / a5) per adjacent pair: (flops, sqrt, div, log, atan2, sincos, acos).
+POINT_OPS = {"far": (160, 3, 3, 3, 1), "edge": (175, 3, 0, 2, 3), "vertex": (185, 3, 1, 3, 3),
+             "duffy": (175, 3, 3, 3, 1)}
+CLOSED_OPS = {"edge": (260, 0, 14, 11, 4, 5, 4), "vertex": (420, 0, 22, 14, 10, 12, 3)}
+
+
+def flop_weights(cal):
+    """flop equivalents (2 per FMA time unit) of sqrt, div, log, atan2, sincos, acos"""
+    return {k: 2.0 * cal[2 + i] for i, k in enumerate(("sqrt", "div", "log", "atan2", "sincos", "acos"))}
+
+
+def point_flops(kind, w):
+    a, s, d, l, t = POINT_OPS[kind]
+    return a + s * w["sqrt"] + d * w["div"] + l * w["log"] + t * w["atan2"]
+
+
+def closed_flops(kind, w):
+    a, s, d, l, t, sc, ac = CLOSED_OPS[kind]
+    return a + s * w["sqrt"] + d * w["div"] + l * w["log"] + t * w["atan2"] + sc * w["sincos"] + ac * w["acos"]
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", "0", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU leg
+def cpu_run(V, C, lists, frac, tol, nthreads=0):
+    """the oracle on a seeded sample (fraction frac of every class) with the product's rules;
+    returns (pairs, seconds, threads)"""
+    from oracle import oracle as O
+    L = O.lib()
+    L.o_set_potential_rule.argtypes = [ctypes.c_int] * 3
+    L.o_set_potential_rule(10, 8, 3)
+    rng = np.random.default_rng(1)
+    n = 0
+    t0 = time.perf_counter()
+    for cls in CLASSES:
+        pr = lists[cls]
+        k = max(1, int(len(pr) * frac))
+        sub = pr[np.sort(rng.choice(len(pr), k, replace=False))]
+        O.integrate(cls, sub, V, C, mode=O.ADAPTIVE_RELATIVE, tol=tol, nthreads=nthreads)
+        n += k
+    dt = time.perf_counter() - t0
+    L.o_set_potential_rule(40, 32, 3)
+    return n, dt, (nthreads or L.o_max_threads())
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    V, C, lists = workload()
+    total = sum(len(v) for v in lists.values())
+    frac = args.cpu_fraction
+    for _ in range(args.warmup):
+        cpu_run(V, C, lists, frac * 0.1, args.tol)
+    rates, n, threads = [], 0, 1
+    for _ in range(args.steps):
+        n, dt, threads = cpu_run(V, C, lists, frac, args.tol)
+        rates.append(n / dt)
+    v = float(np.median(rates))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "pair-integrals/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "jittered icosphere s5 (20480 triangles), 4 pair classes, near < 3h", "pairs": total,
+                       "tol": args.tol, "rule": "qf3D13 + graded Duffy 10x8", "parallelism": "host cores"},
+            "cpu_baseline": {"value": v, "unit": "pair-integrals/s", "cores": threads, "kind": "port",
+                             "sample": f"{frac:.3f} of every class per step ({n} pairs), oracle C restatement, OpenMP"},
+            "e2e": {"value": v, "unit": "pair-integrals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+METRIC = "pair-integrals/s at <=1e-6 rel err"
+
+
+# ------------------------------------------------------------------ GPU arm
+def accuracy(V, C, lists, J, P, levels, nsample=150):
+    """max relative error per class and channel on a seeded sample against the oracle's
+    high-order answer (fixed level 4 of the 13-point rule for J, 40x32 Duffy for adjacent P)"""
+    from oracle import oracle as O
+    rng = np.random.default_rng(5)
+    out = {}
+    names = {0: "vertex", 1: "edge", 2: "near", 3: "self"}
+    for cls in CLASSES:
+        pr = lists[cls]
+        idx = np.sort(rng.choice(len(pr), min(nsample, len(pr)), replace=False))
+        _, oJ, oP, _ = O.integrate(cls, pr[idx], V, C, mode=O.FIXED, level=4 if cls != 3 else 0)
+        j = J[cls][idx]
+        scale = np.maximum(np.linalg.norm(oJ, axis=1), 1e-300)
+        eJ = float((np.linalg.norm(j - oJ, axis=1) / scale).max()) if cls != 3 else float(np.abs(j - oJ).max())
+        eP = float((np.abs(P[cls][idx] - oP) / np.abs(oP)).max())
+        out[names[cls]] = {"J": eJ, "P": eP, "sample": int(len(idx))}
+    return out
+
+
+def gpu_arm(args):
+    import torch
+    from integrator2_gb300 import api
+    from integrator2_gb300._lib import lib
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    V, C, lists = workload()
+    total = sum(len(v) for v in lists.values())
+
+    cal = np.zeros(8)
+    lib().i2_calibrate_pipes(cal.ctypes.data_as(ctypes.c_void_p))
+    w = flop_weights(cal)
+
+    m = api.Mesh3D()
+    m.setGeometry(V, C)
+    m.prepareMesh(NEAR)
+    it = api.NumericalIntegrator3D(m, api.qf3D13)
+    it.setErrorControl(api.RELATIVE_ERROR_CONTROL, args.tol, 5)
+    ev = api.EvaluatorJ3DK(m, it)
+    stream = torch.cuda.Stream()
+    ev.setStream(stream.cuda_stream)
+
+    d_pairs = {c: torch.from_numpy(lists[c]).to("cuda") for c in CLASSES}
+    d_J = {c: torch.empty(len(lists[c]), 3, dtype=torch.float64, device="cuda") for c in CLASSES}
+    d_P = {c: torch.empty(len(lists[c]), dtype=torch.float64, device="cuda") for c in CLASSES}
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step():
+        for c in CLASSES:
+            ev.runClassDevice(c, d_pairs[c].data_ptr(), len(lists[c]), 0, d_J[c].data_ptr(), d_P[c].data_ptr())
+
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            step()
+        stream.synchronize()
+        # per-class and whole-step device time
+        ev_start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ev_cls = [[torch.cuda.Event(enable_timing=True) for _ in CLASSES] for _ in range(args.steps)]
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler() as clk:
+            for s in range(args.steps):
+                flush.fill_(float(s))
+                ev_start[s].record(stream)
+                for k, c in enumerate(CLASSES):
+                    ev.runClassDevice(c, d_pairs[c].data_ptr(), len(lists[c]), 0, d_J[c].data_ptr(), d_P[c].data_ptr())
+                    ev_cls[s][k].record(stream)
+            torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        step_ms = [ev_start[s].elapsed_time(ev_cls[s][-1]) for s in range(args.steps)]
+        cls_ms = np.zeros(len(CLASSES))
+        for s in range(args.steps):
+            prev = ev_start[s]
+            for k in range(len(CLASSES)):
+                cls_ms[k] += prev.elapsed_time(ev_cls[s][k])
+                prev = ev_cls[s][k]
+        cls_ms /= args.steps
+    ms = float(np.sum(step_ms))
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = total * world * args.steps / (ms * 1e-3)
+
+    # levels reached per class (work model) and results for the accuracy check
+    J = {c: d_J[c].cpu().numpy() for c in CLASSES}
+    P = {c: d_P[c].cpu().numpy() for c in CLASSES}
+    levels = {}
+    for c in CLASSES:
+        ev.runClass(c, lists[c])  # host path, same results, also records the level per pair
+        levels[c] = ev.getLevels(c)
+        assert np.array_equal(ev.getResults(c), J[c]), "host and device paths disagree"
+
+    # e2e: host lists (pinned) -> H2D, compute, D2H of J and P inside the timed region
+    h_pairs = {c: torch.from_numpy(lists[c]).pin_memory() for c in CLASSES}
+    h_J = {c: torch.empty(len(lists[c]), 3, dtype=torch.float64).pin_memory() for c in CLASSES}
+    h_P = {c: torch.empty(len(lists[c]), dtype=torch.float64).pin_memory() for c in CLASSES}
+    h2d = sum(h_pairs[c].numel() * 4 for c in CLASSES)
+    d2h = sum(h_J[c].numel() * 8 + h_P[c].numel() * 8 for c in CLASSES)
+    e2e_ms = []
+    with torch.cuda.stream(stream):
+        for s in range(args.steps):
+            flush.fill_(float(s))
+            stream.synchronize()
+            t0 = time.perf_counter()
+            for c in CLASSES:
+                d_pairs[c].copy_(h_pairs[c], non_blocking=True)
+                ev.runClassDevice(c, d_pairs[c].data_ptr(), len(lists[c]), 0, d_J[c].data_ptr(), d_P[c].data_ptr())
+                h_J[c].copy_(d_J[c], non_blocking=True)
+                h_P[c].copy_(d_P[c], non_blocking=True)
+            stream.synchronize()
+            e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    e2e_value = total * world / (np.median(e2e_ms) * 1e-3)
+
+    if rank != 0:
+        return
+    # roofline of the dominant chain: the near-field class (levels 0..5 of k_level<far>)
+    far = lists[2]
+    lev = levels[2]
+    # a pair that stopped at level L visited levels 0..L: count sub-cell evaluations of every visited level
+    evals = int(sum(np.sum(lev >= L) * 4 ** L for L in range(6)))
+    far_flops = evals * 13 * point_flops("far", w)
+    far_ms = cls_ms[2]
+    achieved = far_flops / (far_ms * 1e-3) / 1e12
+    peak = float(cal[0])
+    acc = accuracy(V, C, lists, J, P, levels)
+    n_cpu, dt_cpu, thr = cpu_run(V, C, lists, args.cpu_fraction, args.tol)
+    launches_per_step = 8 + 8 + 7 + 1
+    line = {
+        "metric": METRIC, "value": value, "unit": "pair-integrals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "jittered icosphere s5 (20480 triangles, sigma 0.15h, seed 2026): common-vertex, "
+                               "common-edge, self and near-field (< 3h) ordered pairs",
+                   "pairs": total, "form": "plain FP64", "error_control": f"relative tol {args.tol}, levels 0..5",
+                   "rule": "qf3D13; adjacent potential graded Duffy 10x8 (t^3)", "l2": "flushed (512 MiB write) between steps",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": "pair-integrals/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "fp64", "kernel": "k_level<far> chain (levels 0..5)", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": "measured live by i2_calibrate_pipes (FP64 FMA chains); MEASURED_PEAKS.json has no FP64 figure",
+                     "flops_per_far_point": point_flops("far", w)},
+        "class_ms": {n: float(t) for n, t in zip(("vertex", "edge", "near", "self"), cls_ms)},
+        "levels": {n: np.bincount(levels[c][levels[c] >= 0], minlength=6).tolist() for n, c in
+                   zip(("vertex", "edge", "near"), (0, 1, 2))},
+        "accuracy": acc,
+        "calibration": {"fp64_tflops": float(cal[0]), "fp32_tflops": float(cal[1]),
+                        "fma_units": dict(zip(("sqrt", "div", "log", "atan2", "sincos", "acos"), map(float, cal[2:8])))},
+        "cpu_baseline": {"value": n_cpu / dt_cpu, "unit": "pair-integrals/s", "cores": thr, "kind": "port",
+                         "sample": f"{args.cpu_fraction:.3f} of every class ({n_cpu} pairs), oracle C restatement, OpenMP, same rules"},
+        "clocks": clk.summary(),
+        "gpu_launches": launches_per_step * args.steps,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--tol", type=float, default=1e-6)
+    ap.add_argument("--cpu-fraction", type=float, default=0.02)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

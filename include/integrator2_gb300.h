@@ -1,0 +1,178 @@
+/*
+ * integrator2_gb300.h -- C-ABI of the GB300 (sm_103a) pair-integral library.
+ *
+ * Computes, for ordered pairs (i, j) of triangles K_i, K_j of a surface mesh, the gradient
+ * integral of the Newtonian kernel
+ *     J(K_i, K_j) = int_{K_i} int_{K_j} grad_y 1/(4 pi |x - y|) dS_y dS_x
+ *                 = (1/4pi) (Theta n_j + Psi x n_j)      (Theta, Psi integrated over K_i)
+ * and the potential integral P(K_i, K_j) = int_{K_i} int_{K_j} 1/(4 pi |x - y|) dS_y dS_x,
+ * for the four pair classes: common vertex ("simple neighbours" in the reference's naming),
+ * common edge ("attached neighbours"), disjoint ("not neighbours"; a near-field subset when
+ * the pair lists are built with a distance cutoff) and self.
+ *
+ * It is a drop-in for the pair-integral path of andreyypopov/integrator2 (Mesh3D,
+ * NumericalIntegrator3D, Evaluator3D, EvaluatorJ3DK).  Each entry point names the reference
+ * interface it replaces (paths relative to the reference's repository).  Differences:
+ *   - every call returns an i2_status instead of calling exit() on CUDA errors;
+ *   - quadrature state is per integrator handle (the reference keeps it in process-global
+ *     __constant__ memory, src/NumericalIntegrator3d.cu:9-11);
+ *   - results can be read at full precision (the reference exposes them only through a
+ *     6-significant-digit text export, src/evaluators/evaluator3d.cu:354-457);
+ *   - pair lists are plain (i, j[, k]) rows; the result index is the row index (the reference
+ *     requires k == row index, src/evaluators/evaluatorJ3DK.cu:94);
+ *   - the potential channel and the self class are additions.
+ *
+ * Threading: handles are not thread-safe; distinct handles may be used from distinct threads.
+ * All device work of an evaluator runs on its stream (i2_evaluator_set_stream).
+ */
+#ifndef INTEGRATOR2_GB300_H
+#define INTEGRATOR2_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+typedef struct i2_mesh i2_mesh_t;
+typedef struct i2_integrator i2_integrator_t;
+typedef struct i2_evaluator i2_evaluator_t;
+
+typedef enum i2_status {
+    I2_OK = 0,
+    I2_ERR_INVALID_ARGUMENT = 1,
+    I2_ERR_CUDA = 2,
+    I2_ERR_OUT_OF_MEMORY = 3,
+    I2_ERR_IO = 4,
+    I2_ERR_STATE = 5,       /* call out of order, e.g. run before prepare */
+    I2_ERR_UNSUPPORTED = 6
+} i2_status;
+
+/* values 0..2 are the reference's neighbour_type_enum (src/Mesh3d.cuh:18-23) */
+typedef enum i2_pair_class {
+    I2_SIMPLE_NEIGHBORS = 0,    /* one shared vertex */
+    I2_ATTACHED_NEIGHBORS = 1,  /* one shared edge */
+    I2_NOT_NEIGHBORS = 2,       /* no shared vertex */
+    I2_SELF = 3                 /* i == j (not in the reference) */
+} i2_pair_class;
+
+/* values 0..1 are the reference's error_control_type_enum (src/NumericalIntegrator3d.cuh:16-19) */
+typedef enum i2_error_control {
+    I2_FIXED_REFINEMENT_LEVEL = 0,
+    I2_AUTOMATIC_ERROR_CONTROL = 1,  /* the reference's Runge loop, including its buffer parity */
+    I2_RELATIVE_ERROR_CONTROL = 2    /* scale-invariant: |J_L - J_{L-1}| <= tol |J_L| */
+} i2_error_control;
+
+typedef enum i2_precision { I2_PRECISION_FP64 = 0, I2_PRECISION_MIXED = 1 } i2_precision;
+
+typedef enum i2_channel {
+    I2_CHANNEL_J = 0,      /* 3 doubles per pair */
+    I2_CHANNEL_P = 1,      /* 1 double per pair */
+    I2_CHANNEL_RAW = 2,    /* (Psi, Theta) before finalisation, 4 doubles per pair */
+    I2_CHANNEL_ERROR = 3,  /* antisymmetry delta after run_all_pairs(check=1), 1 double per pair */
+    I2_CHANNEL_LEVEL = 4   /* refinement level kept per pair (as double), -1 in fixed mode */
+} i2_channel;
+
+/* values of the reference's output_format_enum (src/evaluators/evaluator3d.cuh:19-22) + full precision */
+typedef enum i2_output_format { I2_PLAIN_TEXT = 0, I2_CSV = 1, I2_CSV_FULL_PRECISION = 2 } i2_output_format;
+
+const char *i2_status_string(i2_status s);
+/* message of the last failed call on this thread ("" if none) */
+const char *i2_last_error(void);
+int32_t i2_version(void);
+
+/* ------------------------------------------------------------------ Mesh3D */
+i2_status i2_mesh_create(i2_mesh_t **out);
+void i2_mesh_destroy(i2_mesh_t *mesh);
+/* Mesh3D::loadMeshFromFile (src/Mesh3d.cuh:55, src/Mesh3d.cu:159-217): reference .dat format */
+i2_status i2_mesh_load_file(i2_mesh_t *mesh, const char *path, double scale);
+/* host arrays: vertices 3*nv doubles, cells 3*nc 0-based ints (no reference counterpart) */
+i2_status i2_mesh_set_geometry(i2_mesh_t *mesh, const double *vertices, int32_t nv, const int32_t *cells, int32_t nc);
+/* Mesh3D::prepareMesh (src/Mesh3d.cuh:63, src/Mesh3d.cu:219-262): cell normals, measures,
+ * centres and the pair lists.  near_factor > 0 keeps disjoint pairs whose centroid distance is
+ * below near_factor x mean edge length; near_factor <= 0 keeps every disjoint pair, as the
+ * reference's all-pairs classifier does.  Lists are built in O(N) (vertex incidence + a
+ * uniform grid over centroids) instead of the reference's O(N^2) kernel. */
+i2_status i2_mesh_prepare(i2_mesh_t *mesh, double near_factor);
+i2_status i2_mesh_sizes(const i2_mesh_t *mesh, int32_t *nv, int32_t *nc);
+/* Mesh3D::getSimpleNeighbors / getAttachedNeighbors / getNotNeighbors ().size: unordered
+ * (i < j) pairs of a class; the self class has nc entries */
+i2_status i2_mesh_pair_count(const i2_mesh_t *mesh, i2_pair_class cls, int64_t *n);
+/* copies the unordered list as int3 rows (i, j, k = row index), the reference's layout */
+i2_status i2_mesh_copy_pairs(const i2_mesh_t *mesh, i2_pair_class cls, int32_t *rows, int64_t n);
+/* Mesh3D::getCellNormals / getCellMeasures (src/Mesh3d.cuh:110-126); any pointer may be NULL */
+i2_status i2_mesh_copy_cell_data(const i2_mesh_t *mesh, double *normals, double *measures, double *centres);
+
+/* ------------------------------------------------------------------ QuadratureFormula3D */
+/* the reference's built-in rules qf3D1, qf3D3, qf3D4, qf3D6, qf3D7, qf3D9, qf3D12, qf3D13
+ * (src/QuadratureFormula3d.cuh:34-213): npoints selects the rule; coords receives 2*npoints
+ * barycentric (L1, L2) pairs, weights npoints values, order the Runge order */
+i2_status i2_quadrature_builtin(int32_t npoints, double *coords, double *weights, int32_t *order);
+
+/* ------------------------------------------------------------------ NumericalIntegrator3D */
+/* NumericalIntegrator3D(mesh, qf) (src/NumericalIntegrator3d.cuh:73, .cu:197-222);
+ * default: automatic error control as in the reference */
+i2_status i2_integrator_create(const i2_mesh_t *mesh, const double *coords, const double *weights, int32_t npoints,
+                               int32_t order, i2_integrator_t **out);
+void i2_integrator_destroy(i2_integrator_t *it);
+/* NumericalIntegrator3D::setFixedRefinementLevel (src/NumericalIntegrator3d.cu:225-229) */
+i2_status i2_integrator_set_fixed_refinement_level(i2_integrator_t *it, int32_t level);
+/* error control: mode, relative tolerance (relative mode), maximum level (1..5) */
+i2_status i2_integrator_set_error_control(i2_integrator_t *it, i2_error_control mode, double rel_tol, int32_t max_level);
+i2_status i2_integrator_get_error_control(const i2_integrator_t *it, i2_error_control *mode, int32_t *level);
+i2_status i2_integrator_set_precision(i2_integrator_t *it, i2_precision precision);
+/* potential rule of common-edge / common-vertex pairs (graded Duffy, n_radial x n_angular per
+ * piece, radial grading exponent) and of self pairs (n_self points per edge) */
+i2_status i2_integrator_set_potential_rule(i2_integrator_t *it, int32_t n_radial, int32_t n_angular, int32_t grading,
+                                           int32_t n_self);
+/* self-class normal convention: 0 principal value (J = 0), +1 / -1 one-sided limit */
+i2_status i2_integrator_set_self_convention(i2_integrator_t *it, int32_t sign);
+
+/* ------------------------------------------------------------------ EvaluatorJ3DK */
+/* EvaluatorJ3DK(mesh, integrator) (src/evaluators/evaluatorJ3DK.cuh:140-211) */
+i2_status i2_evaluator_create(const i2_mesh_t *mesh, i2_integrator_t *it, i2_evaluator_t **out);
+void i2_evaluator_destroy(i2_evaluator_t *ev);
+/* cudaStream_t passed as void* (default: the legacy default stream) */
+i2_status i2_evaluator_set_stream(i2_evaluator_t *ev, void *stream);
+/* Evaluator3D::runAllPairs (src/evaluators/evaluator3d.cu:120-204): every pair of the mesh's
+ * lists in both orders (rows 0..n-1 = (i,j), rows n..2n-1 = (j,i)), self class included;
+ * check_correctness != 0 also computes the antisymmetry delta of each (i,j)/(j,i) pair */
+i2_status i2_evaluator_run_all_pairs(i2_evaluator_t *ev, int32_t check_correctness);
+/* Evaluator3D::runPairs (src/evaluators/evaluator3d.cu:213-288): host int3 rows per class */
+i2_status i2_evaluator_run_pairs(i2_evaluator_t *ev, const int32_t *simple, int64_t n_simple, const int32_t *attached,
+                                 int64_t n_attached, const int32_t *not_neighbors, int64_t n_not);
+/* one class from host rows (row_stride 2 or 3 int32 per row), self class included */
+i2_status i2_evaluator_run_class(i2_evaluator_t *ev, i2_pair_class cls, const int32_t *rows, int64_t n, int32_t row_stride);
+/* device-resident hot path: d_pairs = n int2 (i, j) rows in device memory; outputs are device
+ * buffers (d_raw4: 4n, d_J: 3n, d_P: n doubles; any may be NULL to keep them in the
+ * evaluator).  Enqueues the class's kernel chain on the evaluator's stream and returns without
+ * synchronising.  Scratch memory is owned by the evaluator and reused across calls. */
+i2_status i2_evaluator_run_class_device(i2_evaluator_t *ev, i2_pair_class cls, const int32_t *d_pairs, int64_t n,
+                                        double *d_raw4, double *d_J, double *d_P);
+i2_status i2_evaluator_synchronize(i2_evaluator_t *ev);
+/* number of results held for a class after the last run */
+i2_status i2_evaluator_result_count(const i2_evaluator_t *ev, i2_pair_class cls, int64_t *n);
+/* full-precision copy of a result channel (replaces subclassing for d_*Results) */
+i2_status i2_evaluator_copy_results(const i2_evaluator_t *ev, i2_pair_class cls, i2_channel channel, double *out,
+                                    int64_t n);
+/* Evaluator3D::outputResultsToFile (src/evaluators/evaluator3d.cu:354-457) to a given path */
+i2_status i2_evaluator_output_results(const i2_evaluator_t *ev, i2_pair_class cls, i2_output_format format,
+                                      const char *path);
+
+/* ------------------------------------------------------------------ measurement */
+/* measured pipe peaks of the current GPU for the kernels' roofline (no reference counterpart):
+ * out[0] FP64 FMA TFLOP/s, out[1] FP32 FMA TFLOP/s, out[2..7] time of one FP64 sqrt, divide,
+ * log, atan2, sincos, acos in units of one FP64 FMA */
+i2_status i2_calibrate_pipes(double *out);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#ifdef __cplusplus
+}
+#endif
+#endif

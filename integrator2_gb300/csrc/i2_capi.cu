@@ -1,0 +1,964 @@
+// i2_capi.cu -- host side of the library behind the C-ABI declared in include/integrator2_gb300.h.
+//
+// Handles own their device buffers (RAII, no shallow copies).  Every CUDA call is checked and
+// turned into an i2_status with a thread-local message; nothing calls exit().
+#include "integrator2_gb300.h"
+#include "i2_engine.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iomanip>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_error;
+
+struct Failure {
+    i2_status code;
+    std::string msg;
+};
+
+#define I2_CHECK_CUDA(call)                                                                                            \
+    do {                                                                                                               \
+        cudaError_t e_ = (call);                                                                                       \
+        if (e_ != cudaSuccess) {                                                                                       \
+            throw Failure{e_ == cudaErrorMemoryAllocation ? I2_ERR_OUT_OF_MEMORY : I2_ERR_CUDA,                        \
+                          std::string(#call) + ": " + cudaGetErrorString(e_)};                                         \
+        }                                                                                                              \
+    } while (0)
+
+#define I2_REQUIRE(cond, code, text)                                                                                   \
+    do {                                                                                                               \
+        if (!(cond)) throw Failure{code, text};                                                                        \
+    } while (0)
+
+template <class F>
+i2_status guarded(F &&f)
+{
+    try {
+        f();
+        g_error.clear();
+        return I2_OK;
+    } catch (const Failure &x) {
+        g_error = x.msg;
+        return x.code;
+    } catch (const std::bad_alloc &) {
+        g_error = "host allocation failed";
+        return I2_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception &x) {
+        g_error = x.what();
+        return I2_ERR_INVALID_ARGUMENT;
+    }
+}
+
+// device buffer owned by one handle
+template <class T>
+struct DevBuf {
+    T *ptr = nullptr;
+    size_t count = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        count = 0;
+    }
+    void reserve(size_t n)
+    {
+        if (n <= count && ptr) return;
+        release();
+        if (n == 0) return;
+        I2_CHECK_CUDA(cudaMalloc(&ptr, n * sizeof(T)));
+        count = n;
+    }
+};
+
+// ------------------------------------------------------------------ quadrature
+struct Rule {
+    std::vector<double> c, w;
+    int order;
+};
+
+// The reference's built-in rules (src/QuadratureFormula3d.cuh:34-213): Cowper's published
+// tables, stored as (L1, L2, w) rows in the published point order.
+const Rule *builtin_rule(int npoints)
+{
+    static const std::unordered_map<int, Rule> rules = [] {
+        std::unordered_map<int, Rule> r;
+        auto add = [&](int n, int order, std::initializer_list<double> rows) {
+            Rule q;
+            q.order = order;
+            std::vector<double> v(rows);
+            for (size_t k = 0; k + 2 < v.size(); k += 3) {
+                q.c.push_back(v[k]);
+                q.c.push_back(v[k + 1]);
+                q.w.push_back(v[k + 2]);
+            }
+            r[n] = q;
+        };
+        const double t = 0.3333333333333333;
+        add(1, 2, {t, t, 1.0});
+        add(3, 2, {0.1666666666666667, 0.1666666666666667, 0.3333333333333333, 0.6666666666666667, 0.1666666666666667,
+                   0.3333333333333333, 0.1666666666666667, 0.6666666666666667, 0.3333333333333333});
+        add(4, 3, {t, t, -0.5625, 0.6, 0.2, 0.5208333333333333, 0.2, 0.6, 0.5208333333333333, 0.2, 0.2, 0.5208333333333333});
+        {
+            const double a = 0.816847572980459, b = 0.091576213509771, wa = 0.109951743655322;
+            const double c = 0.445948490915965, d = 0.108103018168070, wc = 0.223381589678011;
+            add(6, 4, {a, b, wa, b, a, wa, b, b, wa, c, d, wc, d, c, wc, c, c, wc});
+        }
+        {
+            const double a = 0.101286507323456, b = 0.797426985353087, wa = 0.125939180544827;
+            const double c = 0.470142064105115, d = 0.059715871789770, wc = 0.132394152788506;
+            add(7, 5, {t, t, 0.225, a, b, wa, b, a, wa, a, a, wa, c, d, wc, d, c, wc, c, c, wc});
+        }
+        {
+            const double a = 0.437525248383384, b = 0.124949503233232, wa = 0.205950504760887;
+            const double c = 0.797112651860071, d = 0.165409927389841, e = 0.037477420750088, wc = 0.063691414286223;
+            add(9, 5, {a, b, wa, b, a, wa, a, a, wa, c, d, wc, d, c, wc, c, e, wc, e, c, wc, d, e, wc, e, d, wc});
+        }
+        {
+            const double a = 0.873821971016996, b = 0.063089014491502, wa = 0.050844906370207;
+            const double c = 0.501426509658179, d = 0.249286745170910, wc = 0.116786275726379;
+            const double e = 0.636502499121399, f = 0.310352451033785, g = 0.053145049844816, we = 0.082851075618374;
+            add(12, 6, {a, b, wa, b, a, wa, b, b, wa, c, d, wc, d, c, wc, d, d, wc,
+                        e, f, we, f, e, we, e, g, we, g, e, we, f, g, we, g, f, we});
+        }
+        {
+            const double a = 0.479308067841923, b = 0.260345966079038, wa = 0.175615257433204;
+            const double c = 0.869739794195598, d = 0.065130102902216, wc = 0.053347235608839;
+            const double e = 0.638444188569809, f = 0.312865496004875, g = 0.048690315425316, we = 0.077113760890257;
+            const double m = 0.333333333333333;
+            add(13, 7, {m, m, -0.149570044467670, a, b, wa, b, a, wa, b, b, wa, c, d, wc, d, c, wc, d, d, wc,
+                        e, f, we, f, e, we, e, g, we, g, e, we, f, g, we, g, f, we});
+        }
+        return r;
+    }();
+    auto it = rules.find(npoints);
+    return it == rules.end() ? nullptr : &it->second;
+}
+
+// Gauss-Legendre nodes/weights on [0, 1] (Newton iteration on the Legendre recurrence)
+void gauss_legendre01(int n, std::vector<double> &x, std::vector<double> &w)
+{
+    x.resize(n);
+    w.resize(n);
+    for (int k = 0; k < n; ++k) {
+        double z = std::cos(M_PI * (k + 0.75) / (n + 0.5)), dp = 1.0;
+        for (int it = 0; it < 100; ++it) {
+            double p0 = 1.0, p1 = 0.0;
+            for (int m = 1; m <= n; ++m) {
+                const double p2 = p1;
+                p1 = p0;
+                p0 = ((2.0 * m - 1.0) * z * p1 - (m - 1.0) * p2) / m;
+            }
+            dp = n * (z * p0 - p1) / (z * z - 1.0);
+            const double dz = p0 / dp;
+            z -= dz;
+            if (std::fabs(dz) < 1e-16) break;
+        }
+        x[n - 1 - k] = 0.5 * (z + 1.0);
+        w[n - 1 - k] = 1.0 / ((1.0 - z * z) * dp * dp);
+    }
+}
+
+// ------------------------------------------------------------------ .dat reader
+// Reference semantics (src/Mesh3d.cu:159-217): header 'nv nc', nv lines 'idx x y z', then
+// elements 'idx type ...'; type 203 = triangle 'a b c' (1-based); other types consume two more
+// tokens and lower the cell count; the kept cells are the first (count - skipped) triangles.
+// With trailing whitespace the reference's read loop turns once more on a failed read that
+// keeps the last type value: a triangle type changes nothing, any other type skips one more.
+bool read_dat(const std::string &path, double scale, std::vector<double> &V, std::vector<int> &C, std::string &err)
+{
+    std::ifstream f(path);
+    if (!f.is_open()) {
+        err = "cannot open " + path;
+        return false;
+    }
+    std::stringstream ss;
+    ss << f.rdbuf();
+    const std::string text = ss.str();
+    std::istringstream in(text);
+    std::vector<std::string> tok;
+    std::string s;
+    while (in >> s) tok.push_back(s);
+    if (tok.size() < 2) {
+        err = "truncated mesh header";
+        return false;
+    }
+    size_t p = 0;
+    const long nv = std::stol(tok[p++]);
+    long nc = std::stol(tok[p++]);
+    if (nv < 0 || nc < 0 || p + 4 * (size_t)nv > tok.size()) {
+        err = "bad vertex section";
+        return false;
+    }
+    V.resize(3 * nv);
+    for (long k = 0; k < nv; ++k) {
+        ++p;
+        for (int d = 0; d < 3; ++d) V[3 * k + d] = scale * std::stod(tok[p++]);
+    }
+    std::vector<int> cells;
+    long last_type = 0;
+    while (p < tok.size()) {
+        last_type = p + 1 < tok.size() ? std::stol(tok[p + 1]) : 0;
+        if (last_type == 203) {
+            if (p + 4 >= tok.size()) {
+                err = "truncated triangle";
+                return false;
+            }
+            for (int d = 0; d < 3; ++d) cells.push_back(std::stoi(tok[p + 2 + d]) - 1);
+            p += 5;
+        } else {
+            --nc;
+            p += 4;
+        }
+    }
+    if (!text.empty() && std::isspace((unsigned char)text.back()) && last_type != 203) --nc;
+    if (nc < 0) nc = 0;
+    if ((long)cells.size() / 3 < nc) nc = cells.size() / 3;
+    cells.resize(3 * nc);
+    for (int c : cells)
+        if (c < 0 || c >= nv) {
+            err = "cell references a missing vertex";
+            return false;
+        }
+    C.swap(cells);
+    return true;
+}
+
+} // namespace
+
+// ------------------------------------------------------------------ handles
+struct i2_mesh {
+    std::vector<double> V;
+    std::vector<int> C;
+    std::vector<double> normals, measures, centres;
+    std::vector<int> lists[4];  // unordered (i < j) pairs per class, flattened (i, j)
+    bool prepared = false;   // host geometry and pair lists ready
+    bool on_device = false;  // vertices, cells and panels uploaded (first run)
+    double near_factor = 3.0;
+    DevBuf<double> dV;
+    DevBuf<int> dC;
+    DevBuf<i2::Panel> dPanels;
+    int nv() const { return (int)(V.size() / 3); }
+    int nc() const { return (int)(C.size() / 3); }
+};
+
+struct i2_integrator {
+    const i2_mesh *mesh = nullptr;
+    std::vector<double> coords, weights;
+    int order = 7;
+    i2::RunConfig cfg;
+    int precision = I2_PRECISION_FP64;
+    int pot_nu = 10, pot_nv = 8, pot_grade = 3, pot_nself = 16;
+    i2::QuadTables tables() const
+    {
+        i2::QuadTables Q;
+        std::memset(&Q, 0, sizeof Q);
+        Q.npts = (int)weights.size();
+        for (int g = 0; g < Q.npts; ++g) {
+            Q.L1[g] = coords[2 * g];
+            Q.L2[g] = coords[2 * g + 1];
+            Q.L3[g] = 1.0 - coords[2 * g] - coords[2 * g + 1];
+            Q.w[g] = weights[g];
+        }
+        Q.order = order;
+        Q.pow2p = (double)(1 << order);
+        std::vector<double> x, w;
+        gauss_legendre01(pot_nu, x, w);
+        Q.nu = pot_nu;
+        for (int a = 0; a < pot_nu; ++a) {
+            Q.du_u[a] = std::pow(x[a], pot_grade);
+            Q.du_w[a] = w[a] * pot_grade * std::pow(x[a], pot_grade - 1);
+        }
+        gauss_legendre01(pot_nv, x, w);
+        Q.nv = pot_nv;
+        for (int b = 0; b < pot_nv; ++b) {
+            Q.dv_v[b] = x[b];
+            Q.dv_w[b] = w[b];
+        }
+        gauss_legendre01(pot_nself, x, w);
+        Q.nself = pot_nself;
+        for (int k = 0; k < pot_nself; ++k) {
+            const double t = x[k];
+            Q.sx[k] = t * t * (3.0 - 2.0 * t);
+            Q.sw[k] = w[k] * 6.0 * t * (1.0 - t);
+        }
+        return Q;
+    }
+};
+
+namespace {
+
+struct ClassResult {
+    int64_t n = 0;
+    std::vector<int2> host_pairs;  // rows of the last host-side run (for output_results)
+    DevBuf<double> raw4, J, P;
+    DevBuf<int> level;
+    std::vector<double> errors;  // antisymmetry deltas (host)
+};
+
+struct Workspace {
+    DevBuf<double> cur, fin_a, fin_b, sing, padj;
+    DevBuf<int> stop, act_a, act_b, cnt, maxlev;
+    DevBuf<int2> pairs;
+};
+
+} // namespace
+
+struct i2_evaluator {
+    const i2_mesh *mesh = nullptr;
+    i2_integrator *integrator = nullptr;
+    cudaStream_t stream = 0;
+    ClassResult results[4];
+    Workspace ws;
+    int persistent_blocks = 0;
+};
+
+// ------------------------------------------------------------------ pair lists (O(N))
+namespace {
+
+void build_pair_lists(i2_mesh &m, double near_factor)
+{
+    const int nc = m.nc(), nv = m.nv();
+    for (auto &l : m.lists) l.clear();
+    // vertex -> incident cells (CSR)
+    std::vector<int> deg(nv + 1, 0);
+    for (int v : m.C) deg[v + 1]++;
+    for (int k = 0; k < nv; ++k) deg[k + 1] += deg[k];
+    std::vector<int> inc(m.C.size()), fill(deg.begin(), deg.end() - 1);
+    for (int c = 0; c < nc; ++c)
+        for (int d = 0; d < 3; ++d) inc[fill[m.C[3 * c + d]]++] = c;
+    // shared-vertex counts of the touching pairs of each cell
+    std::vector<int> mark(nc, -1), shared(nc, 0), touched;
+    for (int i = 0; i < nc; ++i) {
+        touched.clear();
+        for (int d = 0; d < 3; ++d) {
+            const int v = m.C[3 * i + d];
+            for (int q = deg[v]; q < deg[v + 1]; ++q) {
+                const int j = inc[q];
+                if (j <= i) continue;
+                if (mark[j] != i) {
+                    mark[j] = i;
+                    shared[j] = 0;
+                    touched.push_back(j);
+                }
+                shared[j]++;
+            }
+        }
+        std::sort(touched.begin(), touched.end());
+        for (int j : touched) {
+            if (shared[j] == 1) { m.lists[I2_SIMPLE_NEIGHBORS].push_back(i); m.lists[I2_SIMPLE_NEIGHBORS].push_back(j); }
+            else if (shared[j] == 2) { m.lists[I2_ATTACHED_NEIGHBORS].push_back(i); m.lists[I2_ATTACHED_NEIGHBORS].push_back(j); }
+        }
+        m.lists[I2_SELF].push_back(i);
+        m.lists[I2_SELF].push_back(i);
+    }
+    // disjoint pairs: every pair (reference semantics) or centroid distance < near_factor x mean edge
+    auto touching = [&](int i, int j) {
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b)
+                if (m.C[3 * i + a] == m.C[3 * j + b]) return true;
+        return false;
+    };
+    auto &far = m.lists[I2_NOT_NEIGHBORS];
+    if (near_factor <= 0) {
+        I2_REQUIRE((long long)nc * nc <= 4000000000LL, I2_ERR_UNSUPPORTED, "all-pairs lists above 63k cells are not supported");
+        for (int i = 0; i < nc; ++i)
+            for (int j = i + 1; j < nc; ++j)
+                if (!touching(i, j)) { far.push_back(i); far.push_back(j); }
+        return;
+    }
+    double hsum = 0.0;
+    long long hcnt = 0;
+    {
+        // mean length over unique edges
+        std::vector<std::pair<int, int>> edges;
+        edges.reserve(m.C.size());
+        for (int c = 0; c < nc; ++c)
+            for (int d = 0; d < 3; ++d) {
+                int a = m.C[3 * c + d], b = m.C[3 * c + (d + 1) % 3];
+                if (a > b) std::swap(a, b);
+                edges.emplace_back(a, b);
+            }
+        std::sort(edges.begin(), edges.end());
+        edges.erase(std::unique(edges.begin(), edges.end()), edges.end());
+        for (auto &e : edges) {
+            const double *p = &m.V[3 * e.first], *q = &m.V[3 * e.second];
+            hsum += std::sqrt((p[0] - q[0]) * (p[0] - q[0]) + (p[1] - q[1]) * (p[1] - q[1]) + (p[2] - q[2]) * (p[2] - q[2]));
+            ++hcnt;
+        }
+    }
+    const double r = near_factor * (hcnt ? hsum / hcnt : 0.0), r2 = r * r;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int c = 0; c < nc; ++c)
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = std::min(lo[d], m.centres[3 * c + d]);
+            hi[d] = std::max(hi[d], m.centres[3 * c + d]);
+        }
+    long long dims[3];
+    for (int d = 0; d < 3; ++d) dims[d] = std::max(1LL, std::min(1LL << 20, (long long)std::floor((hi[d] - lo[d]) / r) + 1));
+    auto key = [&](long long x, long long y, long long z) { return (x * dims[1] + y) * dims[2] + z; };
+    std::unordered_map<long long, std::vector<int>> grid;
+    grid.reserve(nc);
+    std::vector<long long> cx(nc), cy(nc), cz(nc);
+    for (int c = 0; c < nc; ++c) {
+        cx[c] = std::min(dims[0] - 1, (long long)((m.centres[3 * c] - lo[0]) / r));
+        cy[c] = std::min(dims[1] - 1, (long long)((m.centres[3 * c + 1] - lo[1]) / r));
+        cz[c] = std::min(dims[2] - 1, (long long)((m.centres[3 * c + 2] - lo[2]) / r));
+        grid[key(cx[c], cy[c], cz[c])].push_back(c);
+    }
+    std::vector<int> cand;
+    for (int i = 0; i < nc; ++i) {
+        cand.clear();
+        for (long long dx = -1; dx <= 1; ++dx)
+            for (long long dy = -1; dy <= 1; ++dy)
+                for (long long dz = -1; dz <= 1; ++dz) {
+                    const long long x = cx[i] + dx, y = cy[i] + dy, z = cz[i] + dz;
+                    if (x < 0 || y < 0 || z < 0 || x >= dims[0] || y >= dims[1] || z >= dims[2]) continue;
+                    auto it = grid.find(key(x, y, z));
+                    if (it == grid.end()) continue;
+                    for (int j : it->second)
+                        if (j > i) cand.push_back(j);
+                }
+        std::sort(cand.begin(), cand.end());
+        for (int j : cand) {
+            const double *p = &m.centres[3 * i], *q = &m.centres[3 * j];
+            const double d2 = (p[0] - q[0]) * (p[0] - q[0]) + (p[1] - q[1]) * (p[1] - q[1]) + (p[2] - q[2]) * (p[2] - q[2]);
+            if (d2 < r2 && !touching(i, j)) { far.push_back(i); far.push_back(j); }
+        }
+    }
+}
+
+void host_cell_geometry(i2_mesh &m)
+{
+    const int nc = m.nc();
+    m.normals.assign(3 * nc, 0.0);
+    m.measures.assign(nc, 0.0);
+    m.centres.assign(3 * nc, 0.0);
+    for (int c = 0; c < nc; ++c) {
+        const double *A = &m.V[3 * m.C[3 * c]], *B = &m.V[3 * m.C[3 * c + 1]], *Cc = &m.V[3 * m.C[3 * c + 2]];
+        const double u[3] = {B[0] - A[0], B[1] - A[1], B[2] - A[2]}, v[3] = {Cc[0] - A[0], Cc[1] - A[1], Cc[2] - A[2]};
+        const double cr[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+        const double len = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+        const double inv = 1.0 / len;
+        for (int d = 0; d < 3; ++d) {
+            m.normals[3 * c + d] = cr[d] * inv;
+            m.centres[3 * c + d] = 0.3333333333333333 * (A[d] + B[d] + Cc[d]);
+        }
+        m.measures[c] = len * 0.5;
+    }
+}
+
+void upload_mesh(i2_mesh &m)
+{
+    m.dV.reserve(m.V.size());
+    m.dC.reserve(m.C.size());
+    m.dPanels.reserve(m.nc());
+    I2_CHECK_CUDA(cudaMemcpy(m.dV.ptr, m.V.data(), m.V.size() * sizeof(double), cudaMemcpyHostToDevice));
+    I2_CHECK_CUDA(cudaMemcpy(m.dC.ptr, m.C.data(), m.C.size() * sizeof(int), cudaMemcpyHostToDevice));
+    i2::launch_prepare_panels(m.nc(), m.dV.ptr, m.dC.ptr, m.dPanels.ptr, 0);
+    I2_CHECK_CUDA(cudaGetLastError());
+    I2_CHECK_CUDA(cudaDeviceSynchronize());
+    m.on_device = true;
+}
+
+i2_pair_class checked_class(int cls)
+{
+    I2_REQUIRE(cls >= 0 && cls <= 3, I2_ERR_INVALID_ARGUMENT, "pair class must be 0..3");
+    return (i2_pair_class)cls;
+}
+
+// enqueue one class on the evaluator's stream; results land in the evaluator's buffers (or
+// the caller's device buffers when given)
+void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n, double *out_raw, double *out_J,
+                      double *out_P)
+{
+    I2_REQUIRE(ev->mesh->prepared, I2_ERR_STATE, "mesh not prepared");
+    if (!ev->mesh->on_device) upload_mesh(const_cast<i2_mesh &>(*ev->mesh));
+    const i2_mesh &m = *ev->mesh;
+    I2_REQUIRE(n >= 0 && n < (1LL << 31), I2_ERR_INVALID_ARGUMENT, "pair count out of range");
+    I2_REQUIRE(ev->integrator->precision == I2_PRECISION_FP64, I2_ERR_UNSUPPORTED, "mixed precision is not available in this build");
+    ClassResult &R = ev->results[cls];
+    R.n = n;
+    R.errors.clear();
+    R.host_pairs.clear();
+    if (n == 0) return;
+    if (!out_raw) { R.raw4.reserve(4 * n); out_raw = R.raw4.ptr; }
+    if (!out_J) { R.J.reserve(3 * n); out_J = R.J.ptr; }
+    if (!out_P) { R.P.reserve(n); out_P = R.P.ptr; }
+    R.level.reserve(n);
+    const i2::RunConfig cfg = ev->integrator->cfg;
+    Workspace &W = ev->ws;
+    const bool adaptive = cfg.mode != i2::kFixed && cls != I2_SELF;
+    W.cur.reserve(5 * n);
+    if (adaptive) {
+        W.fin_a.reserve(5 * n);
+        W.fin_b.reserve(5 * n);
+        W.stop.reserve(n);
+        W.act_a.reserve(n);
+        W.act_b.reserve(n);
+    }
+    W.cnt.reserve(8);
+    W.maxlev.reserve(1);
+    if (cls == I2_SIMPLE_NEIGHBORS || cls == I2_ATTACHED_NEIGHBORS) {
+        W.sing.reserve(4 * n);
+        W.padj.reserve(n);
+    }
+    I2_CHECK_CUDA(cudaMemsetAsync(W.cnt.ptr, 0, 8 * sizeof(int), ev->stream));
+    I2_CHECK_CUDA(cudaMemsetAsync(W.maxlev.ptr, 0, sizeof(int), ev->stream));
+    i2::ClassArgs A;
+    A.n = (int)n;
+    A.pairs = d_pairs;
+    A.cells = reinterpret_cast<const int3 *>(m.dC.ptr);
+    A.panels = m.dPanels.ptr;
+    A.cur = W.cur.ptr;
+    A.fin_a = W.fin_a.ptr;
+    A.fin_b = W.fin_b.ptr;
+    A.stop = W.stop.ptr;
+    A.act_a = W.act_a.ptr;
+    A.act_b = W.act_b.ptr;
+    A.cnt = W.cnt.ptr;
+    A.maxlev = W.maxlev.ptr;
+    A.sing = W.sing.ptr;
+    A.padj = W.padj.ptr;
+    A.raw4 = out_raw;
+    A.J3 = out_J;
+    A.P = out_P;
+    A.level_out = R.level.ptr;
+    if (ev->persistent_blocks == 0) {
+        int dev = 0, sms = 0;
+        I2_CHECK_CUDA(cudaGetDevice(&dev));
+        I2_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        ev->persistent_blocks = std::max(1, sms) * 8;
+    }
+    const i2::QuadTables Q = ev->integrator->tables();
+    i2::launch_class_fp64(cls, A, Q, cfg, ev->persistent_blocks, ev->stream);
+    I2_CHECK_CUDA(cudaGetLastError());
+    if (cls == I2_SELF) I2_CHECK_CUDA(cudaMemsetAsync(R.level.ptr, 0xff, n * sizeof(int), ev->stream));
+    // keep the evaluator's copies coherent when the caller supplied output buffers
+    if (out_raw != R.raw4.ptr) { R.raw4.reserve(4 * n); I2_CHECK_CUDA(cudaMemcpyAsync(R.raw4.ptr, out_raw, 4 * n * sizeof(double), cudaMemcpyDeviceToDevice, ev->stream)); }
+    if (out_J != R.J.ptr) { R.J.reserve(3 * n); I2_CHECK_CUDA(cudaMemcpyAsync(R.J.ptr, out_J, 3 * n * sizeof(double), cudaMemcpyDeviceToDevice, ev->stream)); }
+    if (out_P != R.P.ptr) { R.P.reserve(n); I2_CHECK_CUDA(cudaMemcpyAsync(R.P.ptr, out_P, n * sizeof(double), cudaMemcpyDeviceToDevice, ev->stream)); }
+}
+
+void run_class_host(i2_evaluator *ev, int cls, const int32_t *rows, int64_t n, int stride)
+{
+    const int nc = ev->mesh->nc();
+    std::vector<int2> pairs(n);
+    for (int64_t k = 0; k < n; ++k) {
+        const int i = rows[stride * k], j = rows[stride * k + 1];
+        I2_REQUIRE(i >= 0 && i < nc && j >= 0 && j < nc, I2_ERR_INVALID_ARGUMENT, "pair index outside the mesh");
+        pairs[k] = make_int2(i, j);
+    }
+    Workspace &W = ev->ws;
+    W.pairs.reserve(std::max<int64_t>(n, 1));
+    if (n) I2_CHECK_CUDA(cudaMemcpyAsync(W.pairs.ptr, pairs.data(), n * sizeof(int2), cudaMemcpyHostToDevice, ev->stream));
+    run_class_device(ev, cls, W.pairs.ptr, n, nullptr, nullptr, nullptr);
+    I2_CHECK_CUDA(cudaStreamSynchronize(ev->stream));
+    ev->results[cls].host_pairs.swap(pairs);
+}
+
+} // namespace
+
+// ------------------------------------------------------------------ C-ABI
+extern "C" {
+
+const char *i2_status_string(i2_status s)
+{
+    switch (s) {
+    case I2_OK: return "ok";
+    case I2_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case I2_ERR_CUDA: return "CUDA error";
+    case I2_ERR_OUT_OF_MEMORY: return "out of memory";
+    case I2_ERR_IO: return "I/O error";
+    case I2_ERR_STATE: return "call out of order";
+    case I2_ERR_UNSUPPORTED: return "unsupported";
+    }
+    return "unknown status";
+}
+
+const char *i2_last_error(void) { return g_error.c_str(); }
+int32_t i2_version(void) { return 100; }
+
+i2_status i2_mesh_create(i2_mesh_t **out)
+{
+    return guarded([&] {
+        I2_REQUIRE(out, I2_ERR_INVALID_ARGUMENT, "null output pointer");
+        *out = new i2_mesh();
+    });
+}
+
+void i2_mesh_destroy(i2_mesh_t *mesh) { delete mesh; }
+
+i2_status i2_mesh_load_file(i2_mesh_t *mesh, const char *path, double scale)
+{
+    return guarded([&] {
+        I2_REQUIRE(mesh && path, I2_ERR_INVALID_ARGUMENT, "null argument");
+        std::vector<double> V;
+        std::vector<int> C;
+        std::string err;
+        if (!read_dat(path, scale, V, C, err)) throw Failure{I2_ERR_IO, err};
+        mesh->V.swap(V);
+        mesh->C.swap(C);
+        mesh->prepared = false;
+    });
+}
+
+i2_status i2_mesh_set_geometry(i2_mesh_t *mesh, const double *vertices, int32_t nv, const int32_t *cells, int32_t nc)
+{
+    return guarded([&] {
+        I2_REQUIRE(mesh && (nv == 0 || vertices) && (nc == 0 || cells), I2_ERR_INVALID_ARGUMENT, "null argument");
+        I2_REQUIRE(nv >= 0 && nc >= 0, I2_ERR_INVALID_ARGUMENT, "negative size");
+        for (int64_t k = 0; k < 3LL * nc; ++k)
+            I2_REQUIRE(cells[k] >= 0 && cells[k] < nv, I2_ERR_INVALID_ARGUMENT, "cell references a missing vertex");
+        mesh->V.assign(vertices, vertices + 3LL * nv);
+        mesh->C.assign(cells, cells + 3LL * nc);
+        mesh->prepared = false;
+    });
+}
+
+i2_status i2_mesh_prepare(i2_mesh_t *mesh, double near_factor)
+{
+    return guarded([&] {
+        I2_REQUIRE(mesh, I2_ERR_INVALID_ARGUMENT, "null mesh");
+        I2_REQUIRE(mesh->nc() > 0, I2_ERR_STATE, "mesh has no cells");
+        host_cell_geometry(*mesh);
+        for (int c = 0; c < mesh->nc(); ++c)
+            I2_REQUIRE(mesh->measures[c] > 0.0 && std::isfinite(mesh->measures[c]), I2_ERR_INVALID_ARGUMENT,
+                       "degenerate cell " + std::to_string(c));
+        build_pair_lists(*mesh, near_factor);
+        mesh->near_factor = near_factor;
+        mesh->on_device = false;
+        mesh->prepared = true;
+    });
+}
+
+i2_status i2_mesh_sizes(const i2_mesh_t *mesh, int32_t *nv, int32_t *nc)
+{
+    return guarded([&] {
+        I2_REQUIRE(mesh, I2_ERR_INVALID_ARGUMENT, "null mesh");
+        if (nv) *nv = mesh->nv();
+        if (nc) *nc = mesh->nc();
+    });
+}
+
+i2_status i2_mesh_pair_count(const i2_mesh_t *mesh, i2_pair_class cls, int64_t *n)
+{
+    return guarded([&] {
+        I2_REQUIRE(mesh && n, I2_ERR_INVALID_ARGUMENT, "null argument");
+        I2_REQUIRE(mesh->prepared, I2_ERR_STATE, "mesh not prepared");
+        *n = (int64_t)mesh->lists[checked_class(cls)].size() / 2;
+    });
+}
+
+i2_status i2_mesh_copy_pairs(const i2_mesh_t *mesh, i2_pair_class cls, int32_t *rows, int64_t n)
+{
+    return guarded([&] {
+        I2_REQUIRE(mesh && rows, I2_ERR_INVALID_ARGUMENT, "null argument");
+        I2_REQUIRE(mesh->prepared, I2_ERR_STATE, "mesh not prepared");
+        const auto &l = mesh->lists[checked_class(cls)];
+        I2_REQUIRE(n == (int64_t)l.size() / 2, I2_ERR_INVALID_ARGUMENT, "row count does not match the list");
+        for (int64_t k = 0; k < n; ++k) {
+            rows[3 * k] = l[2 * k];
+            rows[3 * k + 1] = l[2 * k + 1];
+            rows[3 * k + 2] = (int32_t)k;
+        }
+    });
+}
+
+i2_status i2_mesh_copy_cell_data(const i2_mesh_t *mesh, double *normals, double *measures, double *centres)
+{
+    return guarded([&] {
+        I2_REQUIRE(mesh, I2_ERR_INVALID_ARGUMENT, "null mesh");
+        I2_REQUIRE(mesh->prepared, I2_ERR_STATE, "mesh not prepared");
+        if (normals) std::memcpy(normals, mesh->normals.data(), mesh->normals.size() * sizeof(double));
+        if (measures) std::memcpy(measures, mesh->measures.data(), mesh->measures.size() * sizeof(double));
+        if (centres) std::memcpy(centres, mesh->centres.data(), mesh->centres.size() * sizeof(double));
+    });
+}
+
+i2_status i2_quadrature_builtin(int32_t npoints, double *coords, double *weights, int32_t *order)
+{
+    return guarded([&] {
+        const Rule *r = builtin_rule(npoints);
+        I2_REQUIRE(r, I2_ERR_INVALID_ARGUMENT, "no built-in rule with that many points (1,3,4,6,7,9,12,13)");
+        if (coords) std::memcpy(coords, r->c.data(), r->c.size() * sizeof(double));
+        if (weights) std::memcpy(weights, r->w.data(), r->w.size() * sizeof(double));
+        if (order) *order = r->order;
+    });
+}
+
+i2_status i2_integrator_create(const i2_mesh_t *mesh, const double *coords, const double *weights, int32_t npoints,
+                               int32_t order, i2_integrator_t **out)
+{
+    return guarded([&] {
+        I2_REQUIRE(mesh && coords && weights && out, I2_ERR_INVALID_ARGUMENT, "null argument");
+        I2_REQUIRE(npoints >= 1 && npoints <= i2::kMaxGauss, I2_ERR_INVALID_ARGUMENT, "1..16 quadrature points");
+        I2_REQUIRE(order >= 1 && order <= 30, I2_ERR_INVALID_ARGUMENT, "order must be 1..30");
+        auto it = std::make_unique<i2_integrator>();
+        it->mesh = mesh;
+        it->coords.assign(coords, coords + 2 * npoints);
+        it->weights.assign(weights, weights + npoints);
+        it->order = order;
+        it->cfg.mode = i2::kAdaptiveCompat;  // the reference's default (NumericalIntegrator3d.cu:213)
+        *out = it.release();
+    });
+}
+
+void i2_integrator_destroy(i2_integrator_t *it) { delete it; }
+
+i2_status i2_integrator_set_fixed_refinement_level(i2_integrator_t *it, int32_t level)
+{
+    return guarded([&] {
+        I2_REQUIRE(it, I2_ERR_INVALID_ARGUMENT, "null integrator");
+        I2_REQUIRE(level >= 0 && level <= 8, I2_ERR_INVALID_ARGUMENT, "fixed level must be 0..8");
+        it->cfg.mode = i2::kFixed;
+        it->cfg.level = level;
+    });
+}
+
+i2_status i2_integrator_set_error_control(i2_integrator_t *it, i2_error_control mode, double rel_tol, int32_t max_level)
+{
+    return guarded([&] {
+        I2_REQUIRE(it, I2_ERR_INVALID_ARGUMENT, "null integrator");
+        I2_REQUIRE(mode >= 0 && mode <= 2, I2_ERR_INVALID_ARGUMENT, "unknown error-control mode");
+        if (mode == I2_FIXED_REFINEMENT_LEVEL) {
+            it->cfg.mode = i2::kFixed;
+            return;
+        }
+        I2_REQUIRE(max_level >= 1 && max_level <= i2::kMaxLevel, I2_ERR_INVALID_ARGUMENT, "max level must be 1..5");
+        I2_REQUIRE(mode != I2_RELATIVE_ERROR_CONTROL || (rel_tol > 0 && rel_tol < 1), I2_ERR_INVALID_ARGUMENT,
+                   "relative tolerance must be in (0, 1)");
+        it->cfg.mode = mode == I2_AUTOMATIC_ERROR_CONTROL ? i2::kAdaptiveCompat : i2::kAdaptiveRelative;
+        it->cfg.tol = rel_tol;
+        it->cfg.max_level = max_level;
+    });
+}
+
+i2_status i2_integrator_get_error_control(const i2_integrator_t *it, i2_error_control *mode, int32_t *level)
+{
+    return guarded([&] {
+        I2_REQUIRE(it, I2_ERR_INVALID_ARGUMENT, "null integrator");
+        if (mode) *mode = (i2_error_control)it->cfg.mode;
+        if (level) *level = it->cfg.mode == i2::kFixed ? it->cfg.level : it->cfg.max_level;
+    });
+}
+
+i2_status i2_integrator_set_precision(i2_integrator_t *it, i2_precision precision)
+{
+    return guarded([&] {
+        I2_REQUIRE(it, I2_ERR_INVALID_ARGUMENT, "null integrator");
+        I2_REQUIRE(precision == I2_PRECISION_FP64 || precision == I2_PRECISION_MIXED, I2_ERR_INVALID_ARGUMENT,
+                   "unknown precision");
+        it->precision = precision;
+    });
+}
+
+i2_status i2_integrator_set_potential_rule(i2_integrator_t *it, int32_t n_radial, int32_t n_angular, int32_t grading,
+                                           int32_t n_self)
+{
+    return guarded([&] {
+        I2_REQUIRE(it, I2_ERR_INVALID_ARGUMENT, "null integrator");
+        I2_REQUIRE(n_radial >= 2 && n_radial <= i2::kMaxDuffy && n_angular >= 2 && n_angular <= i2::kMaxDuffy,
+                   I2_ERR_INVALID_ARGUMENT, "Duffy rule sizes must be 2..16");
+        I2_REQUIRE(grading >= 1 && grading <= 6, I2_ERR_INVALID_ARGUMENT, "grading must be 1..6");
+        I2_REQUIRE(n_self >= 2 && n_self <= i2::kMaxSelf, I2_ERR_INVALID_ARGUMENT, "self rule size must be 2..32");
+        it->pot_nu = n_radial;
+        it->pot_nv = n_angular;
+        it->pot_grade = grading;
+        it->pot_nself = n_self;
+    });
+}
+
+i2_status i2_integrator_set_self_convention(i2_integrator_t *it, int32_t sign)
+{
+    return guarded([&] {
+        I2_REQUIRE(it, I2_ERR_INVALID_ARGUMENT, "null integrator");
+        I2_REQUIRE(sign >= -1 && sign <= 1, I2_ERR_INVALID_ARGUMENT, "sign must be -1, 0 or 1");
+        it->cfg.self_sign = sign;
+    });
+}
+
+i2_status i2_evaluator_create(const i2_mesh_t *mesh, i2_integrator_t *it, i2_evaluator_t **out)
+{
+    return guarded([&] {
+        I2_REQUIRE(mesh && it && out, I2_ERR_INVALID_ARGUMENT, "null argument");
+        auto ev = std::make_unique<i2_evaluator>();
+        ev->mesh = mesh;
+        ev->integrator = it;
+        *out = ev.release();
+    });
+}
+
+void i2_evaluator_destroy(i2_evaluator_t *ev) { delete ev; }
+
+i2_status i2_evaluator_set_stream(i2_evaluator_t *ev, void *stream)
+{
+    return guarded([&] {
+        I2_REQUIRE(ev, I2_ERR_INVALID_ARGUMENT, "null evaluator");
+        ev->stream = (cudaStream_t)stream;
+    });
+}
+
+i2_status i2_evaluator_run_class(i2_evaluator_t *ev, i2_pair_class cls, const int32_t *rows, int64_t n, int32_t row_stride)
+{
+    return guarded([&] {
+        I2_REQUIRE(ev && (n == 0 || rows), I2_ERR_INVALID_ARGUMENT, "null argument");
+        I2_REQUIRE(row_stride == 2 || row_stride == 3, I2_ERR_INVALID_ARGUMENT, "row stride must be 2 or 3");
+        run_class_host(ev, checked_class(cls), rows, n, row_stride);
+    });
+}
+
+i2_status i2_evaluator_run_pairs(i2_evaluator_t *ev, const int32_t *simple, int64_t n_simple, const int32_t *attached,
+                                 int64_t n_attached, const int32_t *not_neighbors, int64_t n_not)
+{
+    return guarded([&] {
+        I2_REQUIRE(ev, I2_ERR_INVALID_ARGUMENT, "null evaluator");
+        I2_REQUIRE((n_simple == 0 || simple) && (n_attached == 0 || attached) && (n_not == 0 || not_neighbors),
+                   I2_ERR_INVALID_ARGUMENT, "null list");
+        // the reference returns without work when all lists are empty (evaluator3d.cu:215-216)
+        if (n_simple) run_class_host(ev, I2_SIMPLE_NEIGHBORS, simple, n_simple, 3);
+        if (n_attached) run_class_host(ev, I2_ATTACHED_NEIGHBORS, attached, n_attached, 3);
+        if (n_not) run_class_host(ev, I2_NOT_NEIGHBORS, not_neighbors, n_not, 3);
+    });
+}
+
+i2_status i2_evaluator_run_all_pairs(i2_evaluator_t *ev, int32_t check_correctness)
+{
+    return guarded([&] {
+        I2_REQUIRE(ev, I2_ERR_INVALID_ARGUMENT, "null evaluator");
+        const i2_mesh &m = *ev->mesh;
+        I2_REQUIRE(m.prepared, I2_ERR_STATE, "mesh not prepared");
+        for (int cls = 0; cls < 4; ++cls) {
+            const auto &l = m.lists[cls];
+            const int64_t u = (int64_t)l.size() / 2;
+            std::vector<int32_t> rows;
+            if (cls == I2_SELF) {
+                rows.assign(l.begin(), l.end());
+            } else {
+                // rows 0..u-1 = (i, j), rows u..2u-1 = (j, i)  (kAddReversedPairs, evaluator3d.cu:22-31)
+                rows.resize(4 * u);
+                for (int64_t k = 0; k < u; ++k) {
+                    rows[2 * k] = l[2 * k];
+                    rows[2 * k + 1] = l[2 * k + 1];
+                    rows[2 * (u + k)] = l[2 * k + 1];
+                    rows[2 * (u + k) + 1] = l[2 * k];
+                }
+            }
+            run_class_host(ev, cls, rows.data(), (int64_t)rows.size() / 2, 2);
+            if (check_correctness && cls != I2_SELF && u > 0) {
+                // kCalculateIntegrationError (evaluator3d.cu:45-57)
+                std::vector<double> J(6 * u);
+                I2_CHECK_CUDA(cudaMemcpy(J.data(), ev->results[cls].J.ptr, J.size() * sizeof(double), cudaMemcpyDeviceToHost));
+                auto &err = ev->results[cls].errors;
+                err.assign(2 * u, 0.0);
+                for (int64_t k = 0; k < u; ++k) {
+                    const double *a = &J[3 * k], *b = &J[3 * (u + k)];
+                    const double s = std::fabs(a[0] + b[0]) + std::fabs(a[1] + b[1]) + std::fabs(a[2] + b[2]);
+                    const double na = std::fabs(a[0]) + std::fabs(a[1]) + std::fabs(a[2]);
+                    const double nb = std::fabs(b[0]) + std::fabs(b[1]) + std::fabs(b[2]);
+                    err[k] = err[u + k] = s / std::max(na, nb);
+                }
+            }
+        }
+    });
+}
+
+i2_status i2_evaluator_run_class_device(i2_evaluator_t *ev, i2_pair_class cls, const int32_t *d_pairs, int64_t n,
+                                        double *d_raw4, double *d_J, double *d_P)
+{
+    return guarded([&] {
+        I2_REQUIRE(ev && (n == 0 || d_pairs), I2_ERR_INVALID_ARGUMENT, "null argument");
+        run_class_device(ev, checked_class(cls), reinterpret_cast<const int2 *>(d_pairs), n, d_raw4, d_J, d_P);
+    });
+}
+
+i2_status i2_evaluator_synchronize(i2_evaluator_t *ev)
+{
+    return guarded([&] {
+        I2_REQUIRE(ev, I2_ERR_INVALID_ARGUMENT, "null evaluator");
+        I2_CHECK_CUDA(cudaStreamSynchronize(ev->stream));
+    });
+}
+
+i2_status i2_evaluator_result_count(const i2_evaluator_t *ev, i2_pair_class cls, int64_t *n)
+{
+    return guarded([&] {
+        I2_REQUIRE(ev && n, I2_ERR_INVALID_ARGUMENT, "null argument");
+        *n = ev->results[checked_class(cls)].n;
+    });
+}
+
+i2_status i2_evaluator_copy_results(const i2_evaluator_t *ev, i2_pair_class cls, i2_channel channel, double *out, int64_t n)
+{
+    return guarded([&] {
+        I2_REQUIRE(ev && (n == 0 || out), I2_ERR_INVALID_ARGUMENT, "null argument");
+        const ClassResult &R = ev->results[checked_class(cls)];
+        I2_REQUIRE(n == R.n, I2_ERR_INVALID_ARGUMENT, "count does not match the last run of this class");
+        if (n == 0) return;
+        I2_CHECK_CUDA(cudaStreamSynchronize(ev->stream));
+        switch (channel) {
+        case I2_CHANNEL_J: I2_CHECK_CUDA(cudaMemcpy(out, R.J.ptr, 3 * n * sizeof(double), cudaMemcpyDeviceToHost)); break;
+        case I2_CHANNEL_P: I2_CHECK_CUDA(cudaMemcpy(out, R.P.ptr, n * sizeof(double), cudaMemcpyDeviceToHost)); break;
+        case I2_CHANNEL_RAW: I2_CHECK_CUDA(cudaMemcpy(out, R.raw4.ptr, 4 * n * sizeof(double), cudaMemcpyDeviceToHost)); break;
+        case I2_CHANNEL_ERROR:
+            I2_REQUIRE(!R.errors.empty(), I2_ERR_STATE, "no antisymmetry check was run for this class");
+            std::memcpy(out, R.errors.data(), n * sizeof(double));
+            break;
+        case I2_CHANNEL_LEVEL: {
+            std::vector<int> lv(n);
+            I2_CHECK_CUDA(cudaMemcpy(lv.data(), R.level.ptr, n * sizeof(int), cudaMemcpyDeviceToHost));
+            for (int64_t k = 0; k < n; ++k) out[k] = lv[k];
+            break;
+        }
+        default: throw Failure{I2_ERR_INVALID_ARGUMENT, "unknown channel"};
+        }
+    });
+}
+
+i2_status i2_evaluator_output_results(const i2_evaluator_t *ev, i2_pair_class cls, i2_output_format format, const char *path)
+{
+    return guarded([&] {
+        I2_REQUIRE(ev && path, I2_ERR_INVALID_ARGUMENT, "null argument");
+        const int c = checked_class(cls);
+        const ClassResult &R = ev->results[c];
+        I2_REQUIRE(R.n > 0, I2_ERR_STATE, "no results for this class");
+        std::vector<double> J(3 * R.n);
+        I2_CHECK_CUDA(cudaStreamSynchronize(ev->stream));
+        I2_CHECK_CUDA(cudaMemcpy(J.data(), R.J.ptr, J.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        I2_REQUIRE((int64_t)R.host_pairs.size() == R.n, I2_ERR_STATE, "the last run of this class came from device rows");
+        const std::vector<int2> &pairs = R.host_pairs;
+        std::ofstream f(path);
+        if (!f.is_open()) throw Failure{I2_ERR_IO, std::string("cannot open ") + path};
+        if (format == I2_CSV_FULL_PRECISION) f << std::setprecision(17);
+        const bool errors = !R.errors.empty();
+        if (format != I2_PLAIN_TEXT) {
+            f << "\"TaskI\";\"TaskJ\";\"IntegralX\";\"IntegralY\";\"IntegralZ\"";
+            if (errors) f << ";\"Error\"";
+            f << "\n";
+        }
+        for (int64_t k = 0; k < R.n; ++k) {
+            if (format == I2_PLAIN_TEXT) {
+                f << "(" << pairs[k].x << ", " << pairs[k].y << "): [" << J[3 * k] << ", " << J[3 * k + 1] << ", " << J[3 * k + 2] << "]";
+                if (errors) f << ", error = " << R.errors[k];
+            } else {
+                f << pairs[k].x << ";" << pairs[k].y << ";" << J[3 * k] << ";" << J[3 * k + 1] << ";" << J[3 * k + 2];
+                if (errors) f << ";" << R.errors[k];
+            }
+            f << "\n";
+        }
+    });
+}
+
+} // extern "C"

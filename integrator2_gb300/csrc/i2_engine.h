@@ -1,0 +1,50 @@
+// i2_engine.h -- internal interfaces between the C-ABI layer (i2_capi.cu) and the kernels.
+#pragma once
+
+#include <algorithm>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "i2_device.cuh"
+
+namespace i2 {
+
+// pair classes (values of the reference's neighbour_type_enum, src/Mesh3d.cuh:18-23, plus self)
+enum { kVertex = 0, kEdge = 1, kFar = 2, kSelf = 3 };
+// refinement / error-control modes
+enum { kFixed = 0, kAdaptiveCompat = 1, kAdaptiveRelative = 2 };
+
+struct RunConfig {
+    int mode = kFixed;
+    int level = 0;        // fixed refinement level
+    int max_level = kMaxLevel;
+    double tol = 1e-6;    // relative tolerance of the adaptive relative mode
+    int self_sign = 0;    // self-class normal convention
+};
+
+// everything a class's kernel chain reads and writes (device pointers)
+struct ClassArgs {
+    int n = 0;
+    const int2 *pairs = nullptr;  // (i, j) per pair
+    const int3 *cells = nullptr;
+    const Panel *panels = nullptr;
+    // per-pair state: regular-part sums (Psi, Theta, potential)
+    double *cur = nullptr, *fin_a = nullptr, *fin_b = nullptr;
+    int *stop = nullptr;
+    int *act_a = nullptr, *act_b = nullptr;  // active-list ping-pong buffers
+    int *act_in = nullptr, *act_out = nullptr;
+    int *cnt = nullptr;                       // cnt[level] = pairs still active after level
+    int *cnt_in = nullptr, *cnt_out = nullptr;
+    int *maxlev = nullptr;
+    double *sing = nullptr;                   // closed-form singular part (Psi, Theta)
+    double *padj = nullptr;                   // potential of adjacent pairs
+    // outputs
+    double *raw4 = nullptr, *J3 = nullptr, *P = nullptr;
+    int *level_out = nullptr;
+};
+
+void launch_prepare_panels(int nc, const double *V, const int *C, Panel *out, cudaStream_t s);
+void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks,
+                       cudaStream_t s);
+
+} // namespace i2

@@ -1,0 +1,414 @@
+// i2_kernels_fp64.cu -- plain FP64 form of the pair-integral path (sm_103a).
+//
+// Kernel chain per pair class (all launches on one stream, no host synchronisation, so the
+// whole chain can be captured into a CUDA graph):
+//   k_prepare_panels           once per mesh: 256-byte panel record per cell
+//   k_singular<EDGE|VERTEX>    closed-form singular parts + graded-Duffy potential, 1 thread/pair
+//   k_self                     self pairs (J convention + closed-form-in-angle potential)
+//   k_level<CLS>(L)            regular part at refinement level L; 4^L sub-cells per pair spread
+//                              over min(4^L, 32) lanes, warp-shuffle reduction; in adaptive mode
+//                              it also runs the convergence test and appends unconverged pairs
+//                              to the next level's active list (device-side counter)
+//   k_finalize<CLS>            kept level, singular part, J = (Theta n_j + Psi x n_j)/4pi
+#include "i2_engine.h"
+
+namespace i2 {
+
+// ------------------------------------------------------------------ mesh preparation
+__global__ void k_prepare_panels(int nc, const double *__restrict__ V, const int *__restrict__ C, Panel *__restrict__ out)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    const int ia = C[3 * c], ib = C[3 * c + 1], ic = C[3 * c + 2];
+    const d3 A = mk(V[3 * ia], V[3 * ia + 1], V[3 * ia + 2]);
+    const d3 B = mk(V[3 * ib], V[3 * ib + 1], V[3 * ib + 2]);
+    const d3 Cc = mk(V[3 * ic], V[3 * ic + 1], V[3 * ic + 2]);
+    // src/Mesh3d.cu:23-71: n = unit((B-A)x(C-A)), S = |(B-A)x(C-A)|/2
+    const d3 cr = cross(B - A, Cc - A);
+    const d3 n = unit(cr);
+    const double S = norm(cr) * 0.5;
+    const d3 ea = Cc - B, eb = A - Cc, ec = B - A;
+    const double la = norm(ea), lb = norm(eb), lc = norm(ec);
+    const d3 ta = unit(ea), tb = unit(eb), tc = unit(ec);
+    const d3 ctr = 0.3333333333333333 * (A + B + Cc);
+    Panel p;
+    p.v[0] = make_double4_32a(A.x, A.y, A.z, S);
+    p.v[1] = make_double4_32a(B.x, B.y, B.z, 2.0 * S);
+    p.v[2] = make_double4_32a(Cc.x, Cc.y, Cc.z, 0.0);
+    p.v[3] = make_double4_32a(n.x, n.y, n.z, 0.0);
+    p.v[4] = make_double4_32a(ta.x, ta.y, ta.z, la);
+    p.v[5] = make_double4_32a(tb.x, tb.y, tb.z, lb);
+    p.v[6] = make_double4_32a(tc.x, tc.y, tc.z, lc);
+    p.v[7] = make_double4_32a(ctr.x, ctr.y, ctr.z, fmax(la, fmax(lb, lc)));
+    out[c] = p;
+}
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ Tri rotate(Tri t, int s)
+{
+    if (s == 0) return t;
+    if (s == 1) return Tri{t.b, t.c, t.a};
+    return Tri{t.c, t.a, t.b};
+}
+
+__device__ __forceinline__ acc5 shfl_xor5(acc5 a, int off)
+{
+    acc5 r;
+    r.px = __shfl_xor_sync(0xffffffffu, a.px, off);
+    r.py = __shfl_xor_sync(0xffffffffu, a.py, off);
+    r.pz = __shfl_xor_sync(0xffffffffu, a.pz, off);
+    r.th = __shfl_xor_sync(0xffffffffu, a.th, off);
+    r.pot = __shfl_xor_sync(0xffffffffu, a.pot, off);
+    return r;
+}
+
+__device__ __forceinline__ void store5(double *p, const acc5 &a)
+{
+    p[0] = a.px; p[1] = a.py; p[2] = a.pz; p[3] = a.th; p[4] = a.pot;
+}
+__device__ __forceinline__ acc5 load5(const double *p) { return acc5{p[0], p[1], p[2], p[3], p[4]}; }
+
+// J = (Theta n_j + Psi x n_j)/4pi, with the p-fix of the common-vertex class
+// (evaluatorJ3DK.cu:224-264)
+__device__ __forceinline__ d3 finalize_j(int cls, d3 psi, double th, d3 nj, double Si)
+{
+    if (cls == kVertex) {
+        int p = 0;
+        const double ref = kTwoPi * Si;
+        if (th > ref) p = -((int)trunc((th - ref) / (2.0 * ref)) + 1);
+        else if (th < -ref) p = ((int)trunc((-ref - th) / (2.0 * ref)) + 1);
+        th = th + 2.0 * p * ref;
+    }
+    return kInv4Pi * (th * nj + cross(psi, nj));
+}
+
+// Runge criterion of the reference on the regular-part sums (evaluator3d.cu:76-99 with
+// divide()/norm1() of cuda_math.cuh:270-300)
+__device__ __forceinline__ bool runge_unconverged(const acc5 &cur, const acc5 &prev, double pow2p)
+{
+    const double c[4] = {cur.px, cur.py, cur.pz, cur.th}, p[4] = {prev.px, prev.py, prev.pz, prev.th};
+    double crit = 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const double num = c[k] - p[k], den = pow2p * p[k] - c[k];
+        const double lim = k < 3 ? kDoubleMin : kEps2;
+        crit += fabs((fabs(num) < lim && fabs(den) < lim) ? 0.0 : num / den);
+    }
+    return crit > kEpsRunge;
+}
+
+// ------------------------------------------------------------------ regular part, one level
+template <int CLS>
+__global__ void __launch_bounds__(128) k_level(ClassArgs A, QuadTables Q, int level, int mode, double tol, int kmax)
+{
+    const int nsub = 1 << (2 * level);
+    const int G = nsub < 32 ? nsub : 32;          // lanes per pair
+    const int per_lane = nsub / G;                // sub-cells per lane
+    const bool listed = A.act_in != nullptr;
+    const int count = listed ? *A.cnt_in : A.n;
+    const long long total = (long long)count * G;
+    const long long total_r = (total + 31) & ~31LL;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const double sub_scale = ldexp(1.0, -2 * level);  // measure of a sub-cell / measure of K_i
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total_r; idx += stride) {
+        const bool valid = idx < total;
+        const int slot = (int)(idx / G);
+        const int lane_g = (int)(idx % G);
+        const int t = valid ? (listed ? A.act_in[slot] : slot) : 0;
+        acc5 acc = zero5();
+        int2 pr = make_int2(0, 0);
+        if (valid) {
+            pr = A.pairs[t];
+            const PanelJ K = load_panel(A.panels, pr.y);
+            const Tri Ti = load_tri(A.panels, pr.x);
+            const double Ssub = A.panels[pr.x].v[0].w * sub_scale;
+            FarCtx F;
+            EdgeCtx E;
+            VertexCtx Vx;
+            if (CLS == kFar) F = make_far_ctx(K);
+            if (CLS == kEdge || CLS == kVertex) {
+                const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
+                int si, sj;
+                if (CLS == kEdge) {
+                    shifts_edge(ci, cj, si, sj);
+                    E = make_edge_ctx(K, sj);
+                } else {
+                    shifts_vertex(ci, cj, si, sj);
+                    const double4_32a ni = A.panels[pr.x].v[3];
+                    Vx = make_vertex_ctx(K, sj, mk(ni.x, ni.y, ni.z), A.panels[pr.x].v[0].w);
+                }
+            }
+            for (int s = lane_g * per_lane; s < (lane_g + 1) * per_lane; ++s) {
+                const Tri T = subcell(Ti, level, s);
+                acc5 cell = zero5();
+#pragma unroll 1
+                for (int g = 0; g < Q.npts; ++g) {
+                    const d3 x = Q.L1[g] * T.a + Q.L2[g] * T.b + Q.L3[g] * T.c;
+                    d3 psi;
+                    double th, pot = 0.0;
+                    if (CLS == kFar) far_integrand(x, K, F, psi, th, pot);
+                    else if (CLS == kEdge) edge_integrand(x, K, E, psi, th);
+                    else vertex_integrand(x, K, Vx, psi, th);
+                    axpy5(cell, Q.w[g], psi, th, pot);
+                }
+                acc.px += Ssub * cell.px;
+                acc.py += Ssub * cell.py;
+                acc.pz += Ssub * cell.pz;
+                acc.th += Ssub * cell.th;
+                acc.pot += Ssub * cell.pot;
+            }
+        }
+        // segmented butterfly over the G lanes of this pair (groups never straddle a warp)
+        for (int off = 1; off < G; off <<= 1) {
+            const acc5 o = shfl_xor5(acc, off);
+            acc.px += o.px; acc.py += o.py; acc.pz += o.pz; acc.th += o.th; acc.pot += o.pot;
+        }
+        if (!valid || lane_g != 0) continue;
+        double *cur = A.cur + 5 * (long long)t;
+        if (mode == kFixed || level == 0) {
+            store5(cur, acc);
+            continue;
+        }
+        const acc5 prev = load5(cur);
+        store5(cur, acc);
+        bool unconv;
+        if (mode == kAdaptiveCompat) {
+            unconv = runge_unconverged(acc, prev, Q.pow2p);
+        } else {
+            const double4_32a nj4 = A.panels[pr.y].v[3];
+            const d3 nj = mk(nj4.x, nj4.y, nj4.z);
+            const double Si = A.panels[pr.x].v[0].w;
+            d3 spsi = mk(0, 0, 0);
+            double sth = 0.0;
+            if (CLS != kFar) {
+                const double *sg = A.sing + 4 * (long long)t;
+                spsi = mk(sg[0], sg[1], sg[2]);
+                sth = sg[3];
+            }
+            const d3 Jc = finalize_j(CLS, mk(acc.px, acc.py, acc.pz) + spsi, acc.th + sth, nj, Si);
+            const d3 dJ = kInv4Pi * ((acc.th - prev.th) * nj + cross(mk(acc.px - prev.px, acc.py - prev.py, acc.pz - prev.pz), nj));
+            unconv = norm(dJ) > tol * norm(Jc);
+            if (CLS == kFar) unconv = unconv || fabs(acc.pot - prev.pot) > tol * fabs(acc.pot);
+        }
+        atomicMax(A.maxlev, level);
+        if (!unconv || level >= kmax) {
+            A.stop[t] = level;
+            store5(A.fin_a + 5 * (long long)t, acc);
+            store5(A.fin_b + 5 * (long long)t, prev);
+        } else {
+            const int pos = atomicAdd(A.cnt_out, 1);
+            A.act_out[pos] = t;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ singular parts (edge/vertex)
+template <int CLS>
+__global__ void __launch_bounds__(128) k_singular(ClassArgs A, QuadTables Q)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.n) return;
+    const int2 pr = A.pairs[t];
+    const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
+    const PanelJ K = load_panel(A.panels, pr.y);
+    const Tri Ti0 = load_tri(A.panels, pr.x);
+    const Tri Tj0 = Tri{K.A, K.B, K.C};
+    const double4_32a ni4 = A.panels[pr.x].v[3];
+    const d3 ni = mk(ni4.x, ni4.y, ni4.z);
+    const double Si = A.panels[pr.x].v[0].w;
+    int si, sj;
+    if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
+    else shifts_vertex(ci, cj, si, sj);
+    const Tri Ti = rotate(Ti0, si), Tj = rotate(Tj0, sj);
+    d3 psi;
+    double th;
+    if (CLS == kEdge) closed_edge(Ti, Tj, ni, K.n, Si, psi, th);
+    else closed_vertex(Ti, Tj, ni, K.n, Si, psi, th);
+    double *sg = A.sing + 4 * (long long)t;
+    sg[0] = psi.x; sg[1] = psi.y; sg[2] = psi.z; sg[3] = th;
+
+    // potential: graded Duffy rule around the shared vertex (vertex class) or around each end
+    // of the shared edge after subtracting the s ln s term along it (edge class)
+    const FarCtx F = make_far_ctx(K);
+    double total = 0.0;
+    const int npieces = CLS == kEdge ? 2 : 1;
+    PotEdge pe;
+    if (CLS == kEdge) {
+        const d3 JB = Tj.b, JC = Tj.c;
+        const d3 tau = unit(JC - JB);
+        const d3 m = cross(tau, K.n);
+        const d3 w = Ti.a - JB;
+        const d3 perp = w - dot(w, tau) * tau;
+        pe.P1 = JB;
+        pe.h = norm(perp);
+        pe.m_in = (1.0 / pe.h) * perp;
+        pe.c = -dot(m, pe.m_in);
+        total = (5.0 / 9.0) * pe.c * Si * pe.h;
+    }
+    for (int piece = 0; piece < npieces; ++piece) {
+        d3 Vx, B, Cc;
+        if (CLS == kVertex) { Vx = Ti.a; B = Ti.b; Cc = Ti.c; }
+        else {
+            const d3 M = 0.5 * (Ti.b + Ti.c);
+            if (piece == 0) { Vx = Ti.b; B = M; Cc = Ti.a; }
+            else { Vx = Ti.c; B = Ti.a; Cc = M; }
+        }
+        const d3 eB = B - Vx, eC = Cc - Vx;
+        const double area2 = norm(cross(eB, eC));
+        double acc = 0.0;
+#pragma unroll 1
+        for (int a = 0; a < Q.nu; ++a) {
+            const double u = Q.du_u[a];
+            double row = 0.0;
+#pragma unroll 1
+            for (int b = 0; b < Q.nv; ++b) {
+                const double v = Q.dv_v[b];
+                const d3 x = Vx + u * ((1.0 - v) * eB + v * eC);
+                double g = potential_inner(x, K, F);
+                if (CLS == kEdge) g -= pot_edge_sigma(x, pe);
+                row += Q.dv_w[b] * g;
+            }
+            acc += Q.du_w[a] * u * row;
+        }
+        total += area2 * acc;
+    }
+    A.padj[t] = kInv4Pi * total;
+}
+
+// ------------------------------------------------------------------ self pairs
+// J(K_i, K_i): tangential part 0 by antisymmetry; normal part 0 (principal value) or the
+// one-sided limit +-(1/4pi) 2 pi S_i n_i.  Potential: with d = 0 the inner potential is
+// sum_e t_e L_e; per edge, int_K t_e L_e dS = int_e dl_y int_0^pi sin(phi) R(phi,y)^2/2 dphi
+// with the phi integral in closed form on the two sides the ray can hit.
+__device__ __forceinline__ double ray_side(double a, double alpha, double u1)
+{
+    double sa, ca;
+    sincos(alpha, &sa, &ca);
+    const double F1 = ca * log(tan(0.5 * u1)) + sa / sin(u1);
+    const double F0 = ca * log(tan(0.5 * alpha)) + 1.0;  // lower limit u = alpha
+    return 0.5 * a * a * sa * sa * (F1 - F0);
+}
+
+__global__ void __launch_bounds__(128) k_self(ClassArgs A, QuadTables Q, int self_sign)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.n) return;
+    const int i = A.pairs[t].x;
+    const PanelJ K = load_panel(A.panels, i);
+    const double th = self_sign == 0 ? 0.0 : (self_sign > 0 ? kTwoPi : -kTwoPi) * K.S;
+    const d3 J = kInv4Pi * (th * K.n);
+    double *raw = A.raw4 + 4 * (long long)t;
+    raw[0] = 0.0; raw[1] = 0.0; raw[2] = 0.0; raw[3] = th;
+    double *Jo = A.J3 + 3 * (long long)t;
+    Jo[0] = J.x; Jo[1] = J.y; Jo[2] = J.z;
+    const d3 P[3] = {K.A, K.B, K.C};
+    double total = 0.0;
+#pragma unroll 1
+    for (int e = 0; e < 3; ++e) {
+        const d3 P1 = P[e], P2 = P[(e + 1) % 3], P3 = P[(e + 2) % 3];
+        const double L = norm(P2 - P1);
+        const d3 tau = (1.0 / L) * (P2 - P1);
+        const double al1 = angle_ref(P2 - P1, P3 - P1);
+        const double al2 = angle_ref(P1 - P2, P3 - P2);
+        double acc = 0.0;
+#pragma unroll 1
+        for (int k = 0; k < Q.nself; ++k) {
+            const double b = L * Q.sx[k], a = L - b;
+            const d3 y = P1 + b * tau;
+            const double phis = angle_ref(tau, P3 - y);
+            acc += Q.sw[k] * (ray_side(a, al2, phis + al2) + ray_side(b, al1, (kPi - phis) + al1));
+        }
+        total += L * acc;
+    }
+    A.P[t] = kInv4Pi * total;
+}
+
+// ------------------------------------------------------------------ finalisation
+template <int CLS>
+__global__ void __launch_bounds__(128) k_finalize(ClassArgs A, int mode)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.n) return;
+    const int2 pr = A.pairs[t];
+    acc5 v;
+    if (mode == kFixed) {
+        v = load5(A.cur + 5 * (long long)t);
+    } else {
+        // compat: the reference swaps two buffers per iteration and rewrites only unconverged
+        // entries (evaluatorJ3DK.cu:966-1011), so a pair that stopped at level L keeps I_L when
+        // the class-wide loop ran an even number of further iterations, else I_{L-1}
+        const int K = *A.maxlev, L = A.stop[t];
+        const bool older = (mode == kAdaptiveCompat) && ((K - L) & 1);
+        v = load5((older ? A.fin_b : A.fin_a) + 5 * (long long)t);
+    }
+    d3 psi = mk(v.px, v.py, v.pz);
+    double th = v.th;
+    if (CLS != kFar) {
+        const double *sg = A.sing + 4 * (long long)t;
+        psi = psi + mk(sg[0], sg[1], sg[2]);
+        th += sg[3];
+    }
+    const double4_32a nj4 = A.panels[pr.y].v[3];
+    const d3 J = finalize_j(CLS, psi, th, mk(nj4.x, nj4.y, nj4.z), A.panels[pr.x].v[0].w);
+    double *raw = A.raw4 + 4 * (long long)t;
+    raw[0] = psi.x; raw[1] = psi.y; raw[2] = psi.z; raw[3] = th;
+    double *Jo = A.J3 + 3 * (long long)t;
+    Jo[0] = J.x; Jo[1] = J.y; Jo[2] = J.z;
+    A.P[t] = CLS == kFar ? kInv4Pi * v.pot : A.padj[t];
+    if (A.level_out) A.level_out[t] = mode == kFixed ? -1 : A.stop[t];
+}
+
+// ------------------------------------------------------------------ host-side launchers
+static int blocks_for(long long n, int tpb) { return (int)((n + tpb - 1) / tpb); }
+
+void launch_prepare_panels(int nc, const double *V, const int *C, Panel *out, cudaStream_t s)
+{
+    if (nc > 0) k_prepare_panels<<<blocks_for(nc, 128), 128, 0, s>>>(nc, V, C, out);
+}
+
+template <int CLS>
+static void level_chain(const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s)
+{
+    const int tpb = 128;
+    if (cfg.mode == kFixed) {
+        const long long work = (long long)A.n * (cfg.level <= 2 ? (1 << (2 * cfg.level)) : 32);
+        k_level<CLS><<<std::max(1, std::min(blocks_for(work, tpb), persistent_blocks * 8)), tpb, 0, s>>>(A, Q, cfg.level, cfg.mode, cfg.tol, cfg.max_level);
+        k_finalize<CLS><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, cfg.mode);
+        return;
+    }
+    // adaptive: level 0 over all pairs, then levels 1..max over device-side active lists
+    k_level<CLS><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q, 0, cfg.mode, cfg.tol, cfg.max_level);
+    ClassArgs B = A;
+    for (int lev = 1; lev <= cfg.max_level; ++lev) {
+        B.act_in = lev == 1 ? nullptr : (lev % 2 ? A.act_b : A.act_a);
+        B.cnt_in = lev == 1 ? nullptr : A.cnt + (lev - 1);
+        B.act_out = lev % 2 ? A.act_a : A.act_b;
+        B.cnt_out = A.cnt + lev;
+        k_level<CLS><<<persistent_blocks, tpb, 0, s>>>(B, Q, lev, cfg.mode, cfg.tol, cfg.max_level);
+    }
+    k_finalize<CLS><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, cfg.mode);
+}
+
+void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s)
+{
+    if (A.n <= 0) return;
+    const int tpb = 128;
+    switch (cls) {
+    case kSelf:
+        k_self<<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q, cfg.self_sign);
+        break;
+    case kEdge:
+        k_singular<kEdge><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q);
+        level_chain<kEdge>(A, Q, cfg, persistent_blocks, s);
+        break;
+    case kVertex:
+        k_singular<kVertex><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q);
+        level_chain<kVertex>(A, Q, cfg, persistent_blocks, s);
+        break;
+    default:
+        level_chain<kFar>(A, Q, cfg, persistent_blocks, s);
+        break;
+    }
+}
+
+} // namespace i2

@@ -171,7 +171,7 @@ def write_dat(path: str, v: np.ndarray, f: np.ndarray) -> None:
     with open(path, "w") as fh:
         fh.write(f"{len(v)}\t{len(f)}\n")
         for k, p in enumerate(v):
-            fh.write(f"{k + 1}\t{p[0]!r}\t{p[1]!r}\t{p[2]!r}\n")
+            fh.write(f"{k + 1}\t{float(p[0])!r}\t{float(p[1])!r}\t{float(p[2])!r}\n")
         for k, c in enumerate(f):
             fh.write(f"{k + 1}\t203\t{c[0] + 1}\t{c[1] + 1}\t{c[2] + 1}\n")
 

@@ -610,6 +610,63 @@ double o_self_potential(const double *Ap, const double *Bp, const double *Cp, in
     return O_INV_4PI * total;
 }
 
+/* Potential of common-edge and common-vertex pairs: graded Duffy rule around each shared
+ * vertex.  A piece (V, B, C) of K_i with the singular corner V is mapped from the unit square,
+ * x = V + u[(1-v)(B-V) + v(C-V)], dS = 2|piece| u du dv, with u = t^g graded towards V and
+ * Gauss-Legendre in t and v.  A common-vertex pair uses K_i as one piece; a common-edge pair
+ * splits K_i at the shared edge's midpoint M into (P1, M, A) and (P2, A, M) and also subtracts
+ * the s ln s term along the shared edge (pot_edge_sigma), added back in closed form. */
+static int g_pot_nu = 40, g_pot_nv = 32, g_pot_grade = 3;
+
+void o_set_potential_rule(int nu, int nv, int grade)
+{
+    g_pot_nu = nu < 2 ? 2 : (nu > 256 ? 256 : nu);
+    g_pot_nv = nv < 2 ? 2 : (nv > 256 ? 256 : nv);
+    g_pot_grade = grade < 1 ? 1 : grade;
+}
+
+static double duffy_piece(v3 Vx, v3 B, v3 Cc, v3 JA, v3 JB, v3 JC, const pot_edge_ctx *pe)
+{
+    double tu[256], wu[256], tv[256], wv[256];
+    gauss_legendre(g_pot_nu, tu, wu);
+    gauss_legendre(g_pot_nv, tv, wv);
+    double area2 = len(crs(sub(B, Vx), sub(Cc, Vx)));
+    double acc = 0.0;
+    for (int a = 0; a < g_pot_nu; ++a) {
+        double t = 0.5 * (tu[a] + 1.0), wt = 0.5 * wu[a];
+        double u = pow(t, g_pot_grade), du = g_pot_grade * pow(t, g_pot_grade - 1) * wt;
+        for (int b = 0; b < g_pot_nv; ++b) {
+            double v = 0.5 * (tv[b] + 1.0), wvv = 0.5 * wv[b];
+            v3 x = add(Vx, scl(u, add(scl(1.0 - v, sub(B, Vx)), scl(v, sub(Cc, Vx)))));
+            tp_full f = theta_psi_full(x, JA, JB, JC);
+            double g = potential_from(x, JA, JB, JC, &f);
+            if (pe) g -= pot_edge_sigma(x, pe);
+            acc += du * wvv * area2 * u * g;
+        }
+    }
+    return acc;
+}
+
+static double potential_adjacent(int cls, int i, int j, const double *V, const int *C, const double *N, const double *S)
+{
+    v3 JA, JB, JC;
+    tri_of(V, C, j, &JA, &JB, &JC);
+    if (cls == O_VERTEX) {
+        int si, sj, ri[3];
+        shifts_vertex(C + 3 * i, C + 3 * j, &si, &sj);
+        rotated(C + 3 * i, si, ri);
+        return O_INV_4PI * duffy_piece(ld(V + 3 * ri[0]), ld(V + 3 * ri[1]), ld(V + 3 * ri[2]), JA, JB, JC, NULL);
+    }
+    int si, sj, ri[3];
+    shifts_edge(C + 3 * i, C + 3 * j, &si, &sj);
+    rotated(C + 3 * i, si, ri);
+    v3 A = ld(V + 3 * ri[0]), P1 = ld(V + 3 * ri[1]), P2 = ld(V + 3 * ri[2]);
+    v3 M = scl(0.5, add(P1, P2));
+    pot_edge_ctx pe = make_pot_edge_ctx(i, j, V, C, N, S);
+    double acc = duffy_piece(P1, M, A, JA, JB, JC, &pe) + duffy_piece(P2, A, M, JA, JB, JC, &pe);
+    return O_INV_4PI * (acc + pot_edge_sigma_integral(&pe));
+}
+
 /* ---------------------------------------------------------------- quadrature + refinement */
 typedef struct { v3 a, b, c; } tri3;
 
@@ -826,9 +883,8 @@ int o_integrate_class(int cls, int ntasks, const int *ti, const int *tj,
         } else {
             qp5 *h = hist + (size_t)t * (O_MAX_LEVEL + 1);
             q4 sing = q4zero();
-            double psing = 0.0;
             if (mode == O_ADAPTIVE_RELATIVE) {
-                if (cls == O_EDGE) { sing = closed_edge(i, j, V, C, N, S); psing = pot_edge_sigma_integral(&ctx.pctx); }
+                if (cls == O_EDGE) sing = closed_edge(i, j, V, C, N, S);
                 else if (cls == O_VERTEX) sing = closed_vertex(i, j, V, C, N, S);
             }
             h[0] = level_integral(&ctx, root, S[i], 0);
@@ -837,8 +893,8 @@ int o_integrate_class(int cls, int ntasks, const int *ti, const int *tj,
                 h[k] = level_integral(&ctx, root, S[i], k);
                 int unconv;
                 if (mode == O_ADAPTIVE_COMPAT) unconv = runge_unconverged(h[k].r, h[k - 1].r, pow2p);
-                else unconv = rel_change(cls, h[k].r, h[k - 1].r, sing, h[k].p + psing, h[k - 1].p + psing,
-                                         nj, S[i]) / (pow2p - 1.0) > tol;
+                else if (cls == O_FAR) unconv = rel_change(cls, h[k].r, h[k - 1].r, sing, h[k].p, h[k - 1].p, nj, S[i]) > tol;
+                else unconv = rel_change(cls, h[k].r, h[k - 1].r, sing, 1.0, 1.0, nj, S[i]) > tol;
                 if (!unconv) break;
             }
             if (k > O_MAX_LEVEL) k = O_MAX_LEVEL;
@@ -846,8 +902,8 @@ int o_integrate_class(int cls, int ntasks, const int *ti, const int *tj,
             continue;  /* finalised below, once the class-wide loop end is known */
         }
         q4 r = val.r;
-        if (cls == O_EDGE) { r = q4add(r, closed_edge(i, j, V, C, N, S)); val.p += pot_edge_sigma_integral(&ctx.pctx); }
-        else if (cls == O_VERTEX) r = q4add(r, closed_vertex(i, j, V, C, N, S));
+        if (cls == O_EDGE) { r = q4add(r, closed_edge(i, j, V, C, N, S)); val.p = 4.0 * O_PI * potential_adjacent(cls, i, j, V, C, N, S); }
+        else if (cls == O_VERTEX) { r = q4add(r, closed_vertex(i, j, V, C, N, S)); val.p = 4.0 * O_PI * potential_adjacent(cls, i, j, V, C, N, S); }
         v3 J = finalize_j(cls, r, nj, S[i]);
         if (raw4) memcpy(raw4 + 4 * t, r.v, sizeof r.v);
         if (J3) { J3[3 * t] = J.x; J3[3 * t + 1] = J.y; J3[3 * t + 2] = J.z; }
@@ -873,10 +929,12 @@ int o_integrate_class(int cls, int ntasks, const int *ti, const int *tj,
             qp5 val = hist[(size_t)t * (O_MAX_LEVEL + 1) + keep];
             q4 r = val.r;
             if (cls == O_EDGE) {
-                pot_edge_ctx pc = make_pot_edge_ctx(i, j, V, C, N, S);
                 r = q4add(r, closed_edge(i, j, V, C, N, S));
-                val.p += pot_edge_sigma_integral(&pc);
-            } else if (cls == O_VERTEX) r = q4add(r, closed_vertex(i, j, V, C, N, S));
+                val.p = 4.0 * O_PI * potential_adjacent(cls, i, j, V, C, N, S);
+            } else if (cls == O_VERTEX) {
+                r = q4add(r, closed_vertex(i, j, V, C, N, S));
+                val.p = 4.0 * O_PI * potential_adjacent(cls, i, j, V, C, N, S);
+            }
             v3 J = finalize_j(cls, r, ld(N + 3 * j), S[i]);
             if (raw4) memcpy(raw4 + 4 * t, r.v, sizeof r.v);
             if (J3) { J3[3 * t] = J.x; J3[3 * t + 1] = J.y; J3[3 * t + 2] = J.z; }

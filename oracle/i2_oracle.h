@@ -49,6 +49,11 @@ void o_sing_vertex(const double *x, int i, int j, const double *V, const int *C,
 void o_closed_edge(int i, int j, const double *V, const int *C, const double *N, const double *S, double *out4);
 void o_closed_vertex(int i, int j, const double *V, const int *C, const double *N, const double *S, double *out4);
 
+/* graded Duffy rule used for the potential of common-edge / common-vertex pairs
+ * (nu radial x nv angular Gauss-Legendre points per piece, radial grading u = t^grade);
+ * default 40 x 32, grade 3 */
+void o_set_potential_rule(int nu, int nv, int grade);
+
 /* potential of a self pair (1/4pi included) */
 double o_self_potential(const double *A, const double *B, const double *C, int nquad);
 

@@ -1,0 +1,202 @@
+"""FP64 parity of the CUDA path, called through the C-ABI, against the golden vectors made by
+the reference's own routines (tests/golden/) and against the oracle.  Tolerance: 1e-12
+relative per pair for J (the FP64 parity bar); the potential and self class (no reference
+counterpart) are compared with the oracle at 1e-12 for the same rule and at 1e-6 against the
+oracle's high-order rule."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from tests._util import GOLD, ensure_built, rel_rows
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def api():
+    ensure_built()
+    from integrator2_gb300 import api as A
+    return A
+
+
+def run(api, V, C, cls, pairs, mode="fixed", level=0, tol=1e-6, max_level=5, rule=(10, 8, 3, 16), self_sign=0):
+    m = api.Mesh3D()
+    m.setGeometry(V, C)
+    m.prepareMesh(3.0)
+    it = api.NumericalIntegrator3D(m, api.qf3D13)
+    if mode == "fixed":
+        it.setFixedRefinementLevel(level)
+    elif mode == "compat":
+        it.setErrorControl(api.AUTOMATIC_ERROR_CONTROL, 1e-6, max_level)
+    else:
+        it.setErrorControl(api.RELATIVE_ERROR_CONTROL, tol, max_level)
+    it.setPotentialRule(*rule)
+    it.setSelfConvention(self_sign)
+    ev = api.EvaluatorJ3DK(m, it)
+    ev.runClass(cls, np.asarray(pairs, np.int32)[:, :2])
+    return ev.getIntegrals(cls), ev.getResults(cls), ev.getPotentials(cls), ev.getLevels(cls)
+
+
+def oracle_set_rule(nu, nv, g):
+    from oracle import oracle as O
+    L = O.lib()
+    L.o_set_potential_rule.argtypes = [ctypes.c_int] * 3
+    L.o_set_potential_rule(nu, nv, g)
+
+
+@pytest.mark.parametrize("mesh", ["ico2", "ico2_jitter", "ico1_r20"])
+@pytest.mark.parametrize("cls", [0, 1, 2])
+def test_fixed_levels_match_reference(api, mesh, cls):
+    g = np.load(os.path.join(GOLD, f"{mesh}.npz"))
+    pairs = g[f"pairs_{cls}"]
+    for tag, lev in (("L0", 0), ("L1", 1)):
+        raw, J, _, _ = run(api, g["V"], g["C"], cls, pairs, "fixed", lev)
+        assert rel_rows(J, g[f"J_{cls}_{tag}"]).max() < TOL, (mesh, cls, tag)
+        if tag == "L0":
+            assert rel_rows(raw, g[f"raw_{cls}_L0"]).max() < TOL
+
+
+@pytest.mark.parametrize("mesh", ["ico2_jitter", "ico1_r20"])
+@pytest.mark.parametrize("cls", [0, 1, 2])
+def test_adaptive_compat_matches_reference(api, mesh, cls):
+    g = np.load(os.path.join(GOLD, f"{mesh}.npz"))
+    pairs = g[f"pairs_{cls}"]
+    _, J, _, lev = run(api, g["V"], g["C"], cls, pairs, "compat")
+    assert rel_rows(J, g[f"J_{cls}_adaptive"]).max() < TOL
+    it = g[f"iters_{cls}_adaptive"].astype(int)
+    assert np.all(lev == it)
+
+
+def test_two_triangle_fixtures(api):
+    d = np.load(os.path.join(GOLD, "cases.npz"))
+    names = sorted({k.split("|")[0] for k in d.files})
+    for nm in names:
+        g = {k.split("|")[1]: d[k] for k in d.files if k.startswith(nm + "|")}
+        cls = int(g["cls"])
+        ok = ~g["uninit"]
+        for tag, mode, lev in (("J_L0", "fixed", 0), ("J_L1", "fixed", 1), ("J_adaptive", "compat", 0)):
+            _, J, _, _ = run(api, g["V"], g["C"], cls, g["pairs"], mode, lev)
+            assert rel_rows(J[ok], g[tag][ok]).max() < 1e-11, (nm, tag)
+
+
+@pytest.mark.parametrize("level", [0, 2, 3])
+def test_potential_and_deep_levels_match_oracle(api, level):
+    from integrator2_gb300 import meshes, pairs as P
+    from oracle import oracle as O
+    V, C = meshes.jittered_icosphere(2, 0.15, 9)
+    pl = P.build_pairs(V, C)
+    oracle_set_rule(10, 8, 3)
+    try:
+        for cls in (0, 1, 2):
+            pr = pl.by_class(cls)[:600]
+            raw, J, Pg, _ = run(api, V, C, cls, pr, "fixed", level)
+            oraw, oJ, oP, _ = O.integrate(cls, pr, V, C, mode=O.FIXED, level=level)
+            assert rel_rows(J, oJ).max() < TOL, (cls, level)
+            assert (np.abs(Pg - oP) / np.abs(oP)).max() < TOL, (cls, level)
+    finally:
+        oracle_set_rule(40, 32, 3)
+
+
+def test_adjacent_potential_against_high_order(api):
+    """product Duffy rule (10 x 8, grading 3) vs the oracle's 40 x 32 rule: <= 1e-6"""
+    from integrator2_gb300 import meshes, pairs as P
+    from oracle import oracle as O
+    V, C = meshes.jittered_icosphere(3, 0.15, 4)
+    pl = P.build_pairs(V, C)
+    for cls in (0, 1):
+        pr = pl.by_class(cls)[::7]
+        _, _, Pg, _ = run(api, V, C, cls, pr, "fixed", 0)
+        _, _, oP, _ = O.integrate(cls, pr, V, C, mode=O.FIXED, level=0)
+        assert (np.abs(Pg - oP) / np.abs(oP)).max() < 1e-6, cls
+
+
+@pytest.mark.parametrize("sign", [0, 1, -1])
+def test_self_class(api, sign):
+    from integrator2_gb300 import meshes
+    from oracle import oracle as O
+    V, C = meshes.jittered_icosphere(2, 0.2, 3)
+    pairs = np.stack([np.arange(len(C)), np.arange(len(C))], 1)
+    raw, J, Pg, _ = run(api, V, C, 3, pairs, "fixed", 0, self_sign=sign)
+    oraw, oJ, oP, _ = O.integrate(3, pairs, V, C, mode=O.FIXED, self_sign=sign)
+    assert np.abs(J - oJ).max() <= 1e-15 * max(1.0, np.abs(oJ).max())
+    assert (np.abs(Pg - oP) / oP).max() < 1e-9
+
+
+def test_relative_mode_matches_oracle(api):
+    from integrator2_gb300 import meshes, pairs as P
+    from oracle import oracle as O
+    V, C = meshes.jittered_icosphere(3, 0.15, 2)
+    pl = P.build_pairs(V, C)
+    oracle_set_rule(10, 8, 3)
+    try:
+        for cls in (0, 1, 2):
+            pr = pl.by_class(cls)[::5]
+            _, J, Pg, lev = run(api, V, C, cls, pr, "relative", tol=1e-6)
+            _, oJ, oP, olev = O.integrate(cls, pr, V, C, mode=O.ADAPTIVE_RELATIVE, tol=1e-6)
+            same = lev == olev
+            assert same.mean() > 0.999, cls
+            assert rel_rows(J[same], oJ[same]).max() < TOL
+            assert (np.abs(Pg[same] - oP[same]) / np.abs(oP[same])).max() < TOL
+    finally:
+        oracle_set_rule(40, 32, 3)
+
+
+def test_run_all_pairs_and_antisymmetry(api):
+    """runAllPairs(check=True): rows n..2n-1 are the reversed pairs; delta = |J_ij + J_ji| / max
+    is the reference's built-in correctness check (evaluator3d.cu:45-57)."""
+    from integrator2_gb300 import meshes
+    from oracle import oracle as O
+    V, C = meshes.icosphere(2)
+    m = api.Mesh3D()
+    m.setGeometry(V, C)
+    m.prepareMesh(3.0)
+    it = api.NumericalIntegrator3D(m, api.qf3D13)
+    it.setFixedRefinementLevel(1)
+    ev = api.EvaluatorJ3DK(m, it)
+    ev.runAllPairs(True)
+    for cls, lst in ((0, m.getSimpleNeighbors()), (1, m.getAttachedNeighbors()), (2, m.getNotNeighbors())):
+        J = ev.getResults(cls)
+        n = len(lst)
+        assert len(J) == 2 * n
+        err = ev.getErrors(cls)
+        assert err.max() < 0.05, cls
+        allp = np.concatenate([lst[:, :2], lst[:, 1::-1]])
+        _, oJ, _, _ = O.integrate(cls, allp, V, C, mode=O.FIXED, level=1)
+        assert rel_rows(J, oJ).max() < TOL
+    assert ev.resultCount(3) == len(C)
+
+
+def test_device_entry_point_and_edge_cases(api):
+    torch = pytest.importorskip("torch")
+    from integrator2_gb300 import meshes, pairs as P
+    V, C = meshes.jittered_icosphere(2, 0.15, 1)
+    pl = P.build_pairs(V, C)
+    m = api.Mesh3D()
+    m.setGeometry(V, C)
+    m.prepareMesh(3.0)
+    it = api.NumericalIntegrator3D(m, api.qf3D13)
+    it.setErrorControl(api.RELATIVE_ERROR_CONTROL, 1e-7, 5)
+    ev = api.EvaluatorJ3DK(m, it)
+    pr = pl.far
+    ev.runClass(2, pr)
+    J_host = ev.getResults(2)
+    d_pairs = torch.from_numpy(np.ascontiguousarray(pr)).cuda()
+    d_J = torch.zeros(len(pr), 3, dtype=torch.float64, device="cuda")
+    d_P = torch.zeros(len(pr), dtype=torch.float64, device="cuda")
+    ev.setStream(torch.cuda.current_stream().cuda_stream)
+    ev.runClassDevice(2, d_pairs.data_ptr(), len(pr), 0, d_J.data_ptr(), d_P.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(d_J.cpu().numpy(), J_host)
+    # empty list
+    ev.runClass(0, np.zeros((0, 2), np.int32))
+    assert ev.resultCount(0) == 0
+    # out-of-range index is rejected before any launch
+    with pytest.raises(Exception):
+        ev.runClass(2, np.array([[0, len(C)]], np.int32))
+    # the evaluator is still usable afterwards
+    ev.runClass(2, pr[:10])
+    assert np.array_equal(ev.getResults(2), J_host[:10])
