@@ -126,21 +126,18 @@ def cpu_run(V, C, lists, frac, tol, nthreads=0):
     """the oracle on a seeded sample (fraction frac of every class) with the product's rules;
     returns (pairs, seconds, threads)"""
     from oracle import oracle as O
-    L = O.lib()
-    L.o_set_potential_rule.argtypes = [ctypes.c_int] * 3
-    L.o_set_potential_rule(10, 8, 3)
     rng = np.random.default_rng(1)
     n = 0
-    t0 = time.perf_counter()
-    for cls in CLASSES:
-        pr = lists[cls]
-        k = max(1, int(len(pr) * frac))
-        sub = pr[np.sort(rng.choice(len(pr), k, replace=False))]
-        O.integrate(cls, sub, V, C, mode=O.ADAPTIVE_RELATIVE, tol=tol, nthreads=nthreads)
-        n += k
-    dt = time.perf_counter() - t0
-    L.o_set_potential_rule(40, 32, 3)
-    return n, dt, (nthreads or L.o_max_threads())
+    with O.potential_rule(10, 8, 3, adaptive=1e-8, depth=12):
+        t0 = time.perf_counter()
+        for cls in CLASSES:
+            pr = lists[cls]
+            k = max(1, int(len(pr) * frac))
+            sub = pr[np.sort(rng.choice(len(pr), k, replace=False))]
+            O.integrate(cls, sub, V, C, mode=O.ADAPTIVE_RELATIVE, tol=tol, nthreads=nthreads)
+            n += k
+        dt = time.perf_counter() - t0
+    return n, dt, (nthreads or O.lib().o_max_threads())
 
 
 def reference_arm(args):

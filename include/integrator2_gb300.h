@@ -129,6 +129,10 @@ i2_status i2_integrator_set_precision(i2_integrator_t *it, i2_precision precisio
  * piece, radial grading exponent) and of self pairs (n_self points per edge) */
 i2_status i2_integrator_set_potential_rule(i2_integrator_t *it, int32_t n_radial, int32_t n_angular, int32_t grading,
                                            int32_t n_self);
+/* relative tolerance of the locally adaptive potential rule used for hard common-edge /
+ * common-vertex pairs (folded: normals more than 60 degrees apart, or a cell with an angle
+ * below 10 degrees); 0 keeps the plain Duffy rule for them too.  Default 1e-8. */
+i2_status i2_integrator_set_hard_pair_tolerance(i2_integrator_t *it, double rel_tol);
 /* self-class normal convention: 0 principal value (J = 0), +1 / -1 one-sided limit */
 i2_status i2_integrator_set_self_convention(i2_integrator_t *it, int32_t sign);
 

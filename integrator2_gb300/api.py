@@ -156,6 +156,10 @@ class NumericalIntegrator3D:
     def setPotentialRule(self, n_radial=10, n_angular=8, grading=3, n_self=16) -> None:
         call("i2_integrator_set_potential_rule", self._h, n_radial, n_angular, grading, n_self)
 
+    def setHardPairTolerance(self, rel_tol: float) -> None:
+        """adaptive potential of folded / sliver adjacent pairs (0 disables)"""
+        call("i2_integrator_set_hard_pair_tolerance", self._h, float(rel_tol))
+
     def setSelfConvention(self, sign: int) -> None:
         call("i2_integrator_set_self_convention", self._h, int(sign))
 

@@ -310,7 +310,7 @@ struct ClassResult {
 
 struct Workspace {
     DevBuf<double> cur, fin_a, fin_b, sing, padj;
-    DevBuf<int> stop, act_a, act_b, cnt, maxlev;
+    DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list;
     DevBuf<int2> pairs;
 };
 
@@ -509,13 +509,15 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         W.act_a.reserve(n);
         W.act_b.reserve(n);
     }
-    W.cnt.reserve(8);
+    W.cnt.reserve(16);
     W.maxlev.reserve(1);
     if (cls == I2_SIMPLE_NEIGHBORS || cls == I2_ATTACHED_NEIGHBORS) {
         W.sing.reserve(4 * n);
         W.padj.reserve(n);
+        W.hard_list.reserve(n);
     }
-    I2_CHECK_CUDA(cudaMemsetAsync(W.cnt.ptr, 0, 8 * sizeof(int), ev->stream));
+    // cnt[0..7] active counts per level, cnt[8] hard pairs, cnt[9] adaptive-potential stack overflows
+    I2_CHECK_CUDA(cudaMemsetAsync(W.cnt.ptr, 0, 16 * sizeof(int), ev->stream));
     I2_CHECK_CUDA(cudaMemsetAsync(W.maxlev.ptr, 0, sizeof(int), ev->stream));
     i2::ClassArgs A;
     A.n = (int)n;
@@ -532,6 +534,11 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
     A.maxlev = W.maxlev.ptr;
     A.sing = W.sing.ptr;
     A.padj = W.padj.ptr;
+    if (cls == I2_SIMPLE_NEIGHBORS || cls == I2_ATTACHED_NEIGHBORS) {
+        A.hard_list = W.hard_list.ptr;
+        A.hard_cnt = W.cnt.ptr + 8;
+        A.hard_overflow = W.cnt.ptr + 9;
+    }
     A.raw4 = out_raw;
     A.J3 = out_J;
     A.P = out_P;
@@ -778,6 +785,16 @@ i2_status i2_integrator_set_potential_rule(i2_integrator_t *it, int32_t n_radial
         it->pot_nv = n_angular;
         it->pot_grade = grading;
         it->pot_nself = n_self;
+    });
+}
+
+i2_status i2_integrator_set_hard_pair_tolerance(i2_integrator_t *it, double rel_tol)
+{
+    return guarded([&] {
+        I2_REQUIRE(it, I2_ERR_INVALID_ARGUMENT, "null integrator");
+        I2_REQUIRE(rel_tol == 0.0 || (rel_tol >= 1e-13 && rel_tol < 1e-2), I2_ERR_INVALID_ARGUMENT,
+                   "hard-pair tolerance must be 0 or in [1e-13, 1e-2)");
+        it->cfg.hard_tol = rel_tol;
     });
 }
 

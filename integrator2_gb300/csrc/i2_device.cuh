@@ -211,9 +211,11 @@ __device__ __forceinline__ double edge_log_fp64(double l_from, double q_from, do
     return log((l_from + q_from) / (l_to + q_to));
 }
 
-__device__ __forceinline__ void far_integrand(d3 x, const PanelJ &K, const FarCtx &F, d3 &psi, double &th, double &pot)
+// from the point-to-vertex offsets oa = x - A, ob = x - B, oc = x - C (callers that know a point
+// only relative to a nearby vertex form these offsets without cancellation)
+__device__ __forceinline__ void far_integrand_o(d3 oa, d3 ob, d3 oc, const PanelJ &K, const FarCtx &F, d3 &psi, double &th,
+                                                double &pot)
 {
-    const d3 oa = x - K.A, ob = x - K.B, oc = x - K.C;
     const double la = norm(oa), lb = norm(ob), lc = norm(oc);
     const double Lc = edge_log_fp64(la, dot(oa, K.tc), lb, dot(ob, K.tc));  // A -> B
     const double La = edge_log_fp64(lb, dot(ob, K.ta), lc, dot(oc, K.ta));  // B -> C
@@ -223,7 +225,14 @@ __device__ __forceinline__ void far_integrand(d3 x, const PanelJ &K, const FarCt
     const double num = 2.0 * K.S * d;
     const double den = la * lb * lc + dot(oa, ob) * lc + dot(ob, oc) * la + dot(oc, oa) * lb;
     th = 2.0 * atan2(num, den);
-    pot = -dot(F.ma, ob) * La - dot(F.mb, oc) * Lb - dot(F.mc, oa) * Lc - d * th;
+    // t_e L_e -> 0 on the line of edge e even where L_e itself overflows
+    const double ta_ = -dot(F.ma, ob), tb_ = -dot(F.mb, oc), tc_ = -dot(F.mc, oa);
+    pot = (ta_ == 0.0 ? 0.0 : ta_ * La) + (tb_ == 0.0 ? 0.0 : tb_ * Lb) + (tc_ == 0.0 ? 0.0 : tc_ * Lc) - d * th;
+}
+
+__device__ __forceinline__ void far_integrand(d3 x, const PanelJ &K, const FarCtx &F, d3 &psi, double &th, double &pot)
+{
+    far_integrand_o(x - K.A, x - K.B, x - K.C, K, F, psi, th, pot);
 }
 
 // ------------------------------------------------------------------ a2: common-edge regular part

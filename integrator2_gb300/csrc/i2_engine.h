@@ -20,6 +20,7 @@ struct RunConfig {
     int max_level = kMaxLevel;
     double tol = 1e-6;    // relative tolerance of the adaptive relative mode
     int self_sign = 0;    // self-class normal convention
+    double hard_tol = 1e-8;  // relative tolerance of the adaptive potential of hard adjacent pairs (0: off)
 };
 
 // everything a class's kernel chain reads and writes (device pointers)
@@ -38,6 +39,8 @@ struct ClassArgs {
     int *maxlev = nullptr;
     double *sing = nullptr;                   // closed-form singular part (Psi, Theta)
     double *padj = nullptr;                   // potential of adjacent pairs
+    int *hard_list = nullptr, *hard_cnt = nullptr;  // adjacent pairs whose potential is refined adaptively
+    int *hard_overflow = nullptr;             // stack-capacity events of the adaptive potential (diagnostic)
     // outputs
     double *raw4 = nullptr, *J3 = nullptr, *P = nullptr;
     int *level_out = nullptr;

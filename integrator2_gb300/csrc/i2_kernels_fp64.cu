@@ -31,10 +31,12 @@ __global__ void k_prepare_panels(int nc, const double *__restrict__ V, const int
     const double la = norm(ea), lb = norm(eb), lc = norm(ec);
     const d3 ta = unit(ea), tb = unit(eb), tc = unit(ec);
     const d3 ctr = 0.3333333333333333 * (A + B + Cc);
+    // largest cosine of the cell's three angles (a sliver has one close to 1)
+    const double cmax = fmax(dot(tc, -1.0 * tb), fmax(dot(ta, -1.0 * tc), dot(tb, -1.0 * ta)));
     Panel p;
     p.v[0] = make_double4_32a(A.x, A.y, A.z, S);
     p.v[1] = make_double4_32a(B.x, B.y, B.z, 2.0 * S);
-    p.v[2] = make_double4_32a(Cc.x, Cc.y, Cc.z, 0.0);
+    p.v[2] = make_double4_32a(Cc.x, Cc.y, Cc.z, cmax);
     p.v[3] = make_double4_32a(n.x, n.y, n.z, 0.0);
     p.v[4] = make_double4_32a(ta.x, ta.y, ta.z, la);
     p.v[5] = make_double4_32a(tb.x, tb.y, tb.z, lb);
@@ -273,6 +275,176 @@ __global__ void __launch_bounds__(128) k_singular(ClassArgs A, QuadTables Q)
         total += area2 * acc;
     }
     A.padj[t] = kInv4Pi * total;
+    // hard pair: folded (normals more than 60 degrees apart) or a cell with an angle below 10 degrees
+    if (A.hard_list) {
+        const double c10 = 0.98480775301220806;
+        if (dot(ni, K.n) < 0.5 || A.panels[pr.x].v[2].w > c10 || A.panels[pr.y].v[2].w > c10) {
+            const int pos = atomicAdd(A.hard_cnt, 1);
+            A.hard_list[pos] = t;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ hard adjacent pairs: adaptive potential
+// One warp per pair.  A cell is compared with the sum of its four children and split again where
+// they differ by more than tol |P| 2^-depth; cells that hold a shared vertex (always in slot 1
+// of a corner child) use the graded Duffy rule with that vertex as apex, all others the 13-point
+// rule.  Point offsets to K_j's vertices are formed from vertex differences, so cells far below
+// the mesh scale keep full relative precision.  Work items live in a per-warp shared-memory
+// stack of (path, depth, corner, value); every loop pops at least one item and depth is bounded,
+// so the loop ends.
+constexpr int kHardWarps = 2;
+constexpr int kHardCap = 768;
+constexpr int kHardMaxDepth = 12;
+
+struct HardItem {
+    unsigned long long path;
+    double val;
+    int depth, corner;
+};
+
+template <int CLS>
+__device__ double pot_cell(const Tri &T, int corner, const PanelJ &K, const FarCtx &F, const PotEdge &pe, const QuadTables &Q)
+{
+    double acc = 0.0;
+    if (corner >= 0) {
+        const d3 Vx = corner == 0 ? T.a : (corner == 1 ? T.b : T.c);
+        const d3 B = corner == 0 ? T.b : (corner == 1 ? T.c : T.a);
+        const d3 Cc = corner == 0 ? T.c : (corner == 1 ? T.a : T.b);
+        const d3 eB = B - Vx, eC = Cc - Vx, dA = Vx - K.A, dB = Vx - K.B, dC = Vx - K.C;
+        const double area2 = norm(cross(eB, eC));
+        for (int a = 0; a < Q.nu; ++a) {
+            const double u = Q.du_u[a];
+            double row = 0.0;
+            for (int b = 0; b < Q.nv; ++b) {
+                const double v = Q.dv_v[b];
+                const d3 w = u * ((1.0 - v) * eB + v * eC);
+                d3 psi;
+                double th, g;
+                far_integrand_o(dA + w, dB + w, dC + w, K, F, psi, th, g);
+                if (CLS == kEdge) g -= pot_edge_sigma(Vx + w, pe);
+                row += Q.dv_w[b] * g;
+            }
+            acc += Q.du_w[a] * u * row;
+        }
+        return area2 * acc;
+    }
+    const d3 aA = T.a - K.A, bA = T.b - K.A, cA = T.c - K.A;
+    const d3 aB = T.a - K.B, bB = T.b - K.B, cB = T.c - K.B;
+    const d3 aC = T.a - K.C, bC = T.b - K.C, cC = T.c - K.C;
+    for (int g = 0; g < Q.npts; ++g) {
+        const d3 oa = Q.L1[g] * aA + Q.L2[g] * bA + Q.L3[g] * cA;
+        const d3 ob = Q.L1[g] * aB + Q.L2[g] * bB + Q.L3[g] * cB;
+        const d3 oc = Q.L1[g] * aC + Q.L2[g] * bC + Q.L3[g] * cC;
+        d3 psi;
+        double th, gx;
+        far_integrand_o(oa, ob, oc, K, F, psi, th, gx);
+        if (CLS == kEdge) gx -= pot_edge_sigma(oa + K.A, pe);
+        acc += Q.w[g] * gx;
+    }
+    return 0.5 * norm(cross(T.b - T.a, T.c - T.a)) * acc;
+}
+
+// corner slot of child k when the parent's corner is in slot c (the shared vertex moves to slot 1)
+__device__ __forceinline__ int child_corner(int parent_corner, int k)
+{
+    if (parent_corner < 0 || k == 3) return -1;
+    const int want = parent_corner == 1 ? 0 : (parent_corner == 2 ? 1 : 2);
+    return k == want ? 1 : -1;
+}
+
+template <int CLS>
+__global__ void __launch_bounds__(32 * kHardWarps) k_pot_hard(ClassArgs A, QuadTables Q, double tol)
+{
+    __shared__ HardItem stack[kHardWarps][kHardCap];
+    __shared__ int top[kHardWarps];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int count = *A.hard_cnt;
+    for (int h = blockIdx.x * kHardWarps + w; h < count; h += gridDim.x * kHardWarps) {
+        const int t = A.hard_list[h];
+        const int2 pr = A.pairs[t];
+        const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
+        const PanelJ K = load_panel(A.panels, pr.y);
+        const Tri Ti = load_tri(A.panels, pr.x);
+        const FarCtx F = make_far_ctx(K);
+        const double Si = A.panels[pr.x].v[0].w;
+        int si, sj;
+        if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
+        else shifts_vertex(ci, cj, si, sj);
+        PotEdge pe;
+        double sig_int = 0.0;
+        if (CLS == kEdge) {
+            const Tri Tj = rotate(Tri{K.A, K.B, K.C}, sj), Tr = rotate(Ti, si);
+            const d3 tau = unit(Tj.c - Tj.b), m = cross(tau, K.n), wv = Tr.a - Tj.b;
+            const d3 perp = wv - dot(wv, tau) * tau;
+            pe.P1 = Tj.b;
+            pe.h = norm(perp);
+            pe.m_in = (1.0 / pe.h) * perp;
+            pe.c = -dot(m, pe.m_in);
+            sig_int = (5.0 / 9.0) * pe.c * Si * pe.h;
+        }
+        // shared slots of K_i: the root's children 0, 1, 2 hold slots b, c, a
+        const int ia[3] = {ci.x, ci.y, ci.z};
+        bool shared[3];
+        for (int k = 0; k < 3; ++k) shared[k] = (ia[k] == cj.x || ia[k] == cj.y || ia[k] == cj.z);
+        const double root = A.padj[t] * (4.0 * kPi) - sig_int;  // Duffy value of the regular part
+        const double tol_abs = tol * fabs(A.padj[t] * (4.0 * kPi));
+        double acc = 0.0;
+        if (lane == 0) top[w] = 0;
+        __syncwarp();
+        // level 1: the root's four children, one per lane
+        double v1 = 0.0;
+        int c1 = -1;
+        if (lane < 4) {
+            c1 = lane == 3 ? -1 : (shared[lane == 0 ? 1 : (lane == 1 ? 2 : 0)] ? 1 : -1);
+            v1 = pot_cell<CLS>(child(Ti, lane), c1, K, F, pe, Q);
+        }
+        (void)root;  // the root is always split once; each child then adapts on its own
+        if (lane < 4) {
+            stack[w][lane] = HardItem{(unsigned long long)lane, v1, 1, c1};
+            if (lane == 0) top[w] = 4;
+        }
+        __syncwarp();
+        for (int guard = 0; guard < 1 << 20; ++guard) {
+            const int n = top[w];
+            if (n == 0) break;
+            const int take = n < 32 ? n : 32;
+            HardItem it;
+            const bool has = lane < take;
+            if (has) it = stack[w][n - take + lane];
+            __syncwarp();
+            if (lane == 0) top[w] = n - take;
+            __syncwarp();
+            if (has) {
+                const Tri T = subcell(Ti, it.depth, (int)it.path);
+                double v[4], sum = 0.0;
+                for (int k = 0; k < 4; ++k) {
+                    v[k] = pot_cell<CLS>(child(T, k), child_corner(it.corner, k), K, F, pe, Q);
+                    sum += v[k];
+                }
+                const double lim = ldexp(tol_abs, -it.depth);
+                bool accept = fabs(sum - it.val) <= lim || it.depth >= kHardMaxDepth;
+                int pos = 0;
+                if (!accept) {
+                    pos = atomicAdd(&top[w], 4);
+                    if (pos + 4 > kHardCap) {
+                        atomicSub(&top[w], 4);
+                        atomicAdd(A.hard_overflow, 1);
+                        accept = true;
+                    }
+                }
+                if (accept) acc += sum;
+                else
+                    for (int k = 0; k < 4; ++k)
+                        stack[w][pos + k] = HardItem{(it.path << 2) | (unsigned long long)k, v[k], it.depth + 1,
+                                                     child_corner(it.corner, k)};
+            }
+            __syncwarp();
+        }
+        for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+        if (lane == 0) A.padj[t] = kInv4Pi * (acc + sig_int);
+        __syncwarp();
+    }
 }
 
 // ------------------------------------------------------------------ self pairs
@@ -399,10 +571,12 @@ void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const R
         break;
     case kEdge:
         k_singular<kEdge><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q);
+        if (A.hard_list && cfg.hard_tol > 0) k_pot_hard<kEdge><<<persistent_blocks / 4, 32 * kHardWarps, 0, s>>>(A, Q, cfg.hard_tol);
         level_chain<kEdge>(A, Q, cfg, persistent_blocks, s);
         break;
     case kVertex:
         k_singular<kVertex><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q);
+        if (A.hard_list && cfg.hard_tol > 0) k_pot_hard<kVertex><<<persistent_blocks / 4, 32 * kHardWarps, 0, s>>>(A, Q, cfg.hard_tol);
         level_chain<kVertex>(A, Q, cfg, persistent_blocks, s);
         break;
     default:

@@ -109,10 +109,10 @@ typedef struct {
     double L[3]; /* line integrals of 1/R along edges BC (a), CA (b), AB (c) */
 } tp_full;
 
-static tp_full theta_psi_full(v3 x, v3 A, v3 B, v3 C)
+/* theta/psi from the point-to-vertex offsets oa = x - A, ob = x - B, oc = x - C */
+static tp_full theta_psi_offsets(v3 oa, v3 ob, v3 oc, v3 A, v3 B, v3 C)
 {
     tp_full out;
-    v3 oa = sub(x, A), ob = sub(x, B), oc = sub(x, C);
     double la = len(oa), lb = len(ob), lc = len(oc);
     oa = dvd(oa, la); ob = dvd(ob, lb); oc = dvd(oc, lc);
     v3 ta = unit(sub(C, B)), tb = unit(sub(A, C)), tc = unit(sub(B, A));
@@ -129,6 +129,11 @@ static tp_full theta_psi_full(v3 x, v3 A, v3 B, v3 C)
     return out;
 }
 
+static tp_full theta_psi_full(v3 x, v3 A, v3 B, v3 C)
+{
+    return theta_psi_offsets(sub(x, A), sub(x, B), sub(x, C), A, B, C);
+}
+
 void o_theta_psi(const double *x, const double *A, const double *B, const double *C, double *out4)
 {
     tp_full t = theta_psi_full(ld(x), ld(A), ld(B), ld(C));
@@ -139,15 +144,22 @@ void o_theta_psi(const double *x, const double *A, const double *B, const double
  * t_e the signed in-plane distance from x to edge e (positive inside), L_e the edge line
  * integral of 1/R (the same logs as Psi), d the height of x over the plane (Theta has the
  * sign of d, so d*Theta = |d||Omega|).  No counterpart in the reference. */
-static double potential_from(v3 x, v3 A, v3 B, v3 C, const tp_full *t)
+static double potential_offsets(v3 oa, v3 ob, v3 oc, v3 A, v3 B, v3 C, const tp_full *t)
 {
     v3 n = unit(crs(sub(B, A), sub(C, A)));
     v3 ta = unit(sub(C, B)), tb = unit(sub(A, C)), tc = unit(sub(B, A));
-    double sa = dot(crs(ta, n), sub(B, x));
-    double sb = dot(crs(tb, n), sub(C, x));
-    double sc = dot(crs(tc, n), sub(A, x));
-    double d = dot(n, sub(x, A));
-    return sa * t->L[0] + sb * t->L[1] + sc * t->L[2] - d * t->tp.v[3];
+    double sa = -dot(crs(ta, n), ob);
+    double sb = -dot(crs(tb, n), oc);
+    double sc = -dot(crs(tc, n), oa);
+    double d = dot(n, oa);
+    /* t_e L_e -> 0 on the edge's line even where L_e overflows */
+    double pa = sa == 0.0 ? 0.0 : sa * t->L[0], pb = sb == 0.0 ? 0.0 : sb * t->L[1], pc = sc == 0.0 ? 0.0 : sc * t->L[2];
+    return pa + pb + pc - d * t->tp.v[3];
+}
+
+static double potential_from(v3 x, v3 A, v3 B, v3 C, const tp_full *t)
+{
+    return potential_offsets(sub(x, A), sub(x, B), sub(x, C), A, B, C, t);
 }
 
 double o_potential_inner(const double *x, const double *A, const double *B, const double *C)
@@ -637,14 +649,101 @@ static double duffy_piece(v3 Vx, v3 B, v3 Cc, v3 JA, v3 JB, v3 JC, const pot_edg
         double u = pow(t, g_pot_grade), du = g_pot_grade * pow(t, g_pot_grade - 1) * wt;
         for (int b = 0; b < g_pot_nv; ++b) {
             double v = 0.5 * (tv[b] + 1.0), wvv = 0.5 * wv[b];
-            v3 x = add(Vx, scl(u, add(scl(1.0 - v, sub(B, Vx)), scl(v, sub(Cc, Vx)))));
-            tp_full f = theta_psi_full(x, JA, JB, JC);
-            double g = potential_from(x, JA, JB, JC, &f);
-            if (pe) g -= pot_edge_sigma(x, pe);
+            v3 w = scl(u, add(scl(1.0 - v, sub(B, Vx)), scl(v, sub(Cc, Vx))));
+            v3 oa = add(sub(Vx, JA), w), ob = add(sub(Vx, JB), w), oc = add(sub(Vx, JC), w);
+            tp_full f = theta_psi_offsets(oa, ob, oc, JA, JB, JC);
+            double g = potential_offsets(oa, ob, oc, JA, JB, JC, &f);
+            if (pe) g -= pot_edge_sigma(add(Vx, w), pe);
             acc += du * wvv * area2 * u * g;
         }
     }
     return acc;
+}
+
+/* Hard adjacent pairs (folded: n_i.n_j < 0.5, or a cell with an angle below 10 degrees) get a
+ * locally adaptive rule: a cell is compared with the sum of its four children and split again
+ * where they differ by more than tol x |P| x 2^-depth; cells holding a shared vertex use the
+ * Duffy rule with that vertex as apex, all others the 13-point rule. */
+static double g_pot_adapt_tol = 1e-10;   /* 0 disables the adaptive route */
+static int g_pot_adapt_depth = 18;
+
+void o_set_potential_adaptive(double tol) { g_pot_adapt_tol = tol; }
+void o_set_potential_adaptive_depth(int d) { g_pot_adapt_depth = d; }
+
+static const double Q13[13][3] = {
+    {0.333333333333333, 0.333333333333333, -0.149570044467670},
+    {0.479308067841923, 0.260345966079038, 0.175615257433204}, {0.260345966079038, 0.479308067841923, 0.175615257433204},
+    {0.260345966079038, 0.260345966079038, 0.175615257433204},
+    {0.869739794195598, 0.065130102902216, 0.053347235608839}, {0.065130102902216, 0.869739794195598, 0.053347235608839},
+    {0.065130102902216, 0.065130102902216, 0.053347235608839},
+    {0.638444188569809, 0.312865496004875, 0.077113760890257}, {0.312865496004875, 0.638444188569809, 0.077113760890257},
+    {0.638444188569809, 0.048690315425316, 0.077113760890257}, {0.048690315425316, 0.638444188569809, 0.077113760890257},
+    {0.312865496004875, 0.048690315425316, 0.077113760890257}, {0.048690315425316, 0.312865496004875, 0.077113760890257}};
+
+typedef struct { v3 JA, JB, JC; const pot_edge_ctx *pe; } pot_ctx;
+
+static double pot_cell(const pot_ctx *c, v3 a, v3 b, v3 cc, int corner)
+{
+    if (corner >= 0) { /* apex at the shared vertex, held in slot 'corner' */
+        v3 t[3] = {a, b, cc};
+        return duffy_piece(t[corner], t[(corner + 1) % 3], t[(corner + 2) % 3], c->JA, c->JB, c->JC, c->pe);
+    }
+    double acc = 0.0;
+    for (int g = 0; g < 13; ++g) {
+        double l3 = 1.0 - Q13[g][0] - Q13[g][1];
+        v3 oa = add(add(scl(Q13[g][0], sub(a, c->JA)), scl(Q13[g][1], sub(b, c->JA))), scl(l3, sub(cc, c->JA)));
+        v3 ob = add(add(scl(Q13[g][0], sub(a, c->JB)), scl(Q13[g][1], sub(b, c->JB))), scl(l3, sub(cc, c->JB)));
+        v3 oc = add(add(scl(Q13[g][0], sub(a, c->JC)), scl(Q13[g][1], sub(b, c->JC))), scl(l3, sub(cc, c->JC)));
+        tp_full f = theta_psi_offsets(oa, ob, oc, c->JA, c->JB, c->JC);
+        double gx = potential_offsets(oa, ob, oc, c->JA, c->JB, c->JC, &f);
+        if (c->pe) gx -= pot_edge_sigma(add(oa, c->JA), c->pe);
+        acc += Q13[g][2] * gx;
+    }
+    return 0.5 * len(crs(sub(b, a), sub(cc, a))) * acc;
+}
+
+/* children in the reference's split order; a parent corner in slot k moves to child
+ * (k==1 ? 0 : k==2 ? 1 : 2) at slot 1 */
+static double pot_adapt(const pot_ctx *c, v3 a, v3 b, v3 cc, int corner, double val, double tol_abs, int depth)
+{
+    v3 mbc = scl(0.5, add(b, cc)), mca = scl(0.5, add(cc, a)), mab = scl(0.5, add(a, b));
+    v3 ch[4][3] = {{mab, b, mbc}, {mbc, cc, mca}, {mca, a, mab}, {mbc, mca, mab}};
+    int cc_[4] = {-1, -1, -1, -1};
+    if (corner == 1) cc_[0] = 1;
+    else if (corner == 2) cc_[1] = 1;
+    else if (corner == 0) cc_[2] = 1;
+    double v[4], sum = 0.0;
+    for (int k = 0; k < 4; ++k) { v[k] = pot_cell(c, ch[k][0], ch[k][1], ch[k][2], cc_[k]); sum += v[k]; }
+    if (fabs(sum - val) <= tol_abs || depth >= g_pot_adapt_depth) return sum;
+    double out = 0.0;
+    for (int k = 0; k < 4; ++k) out += pot_adapt(c, ch[k][0], ch[k][1], ch[k][2], cc_[k], v[k], 0.5 * tol_abs, depth + 1);
+    return out;
+}
+
+static int pair_is_hard(int i, int j, const double *V, const int *C, const double *N)
+{
+    if (dot(ld(N + 3 * i), ld(N + 3 * j)) < 0.5) return 1;
+    const double c10 = 0.98480775301220806; /* cos 10 degrees */
+    for (int q = 0; q < 2; ++q) {
+        v3 a, b, cc;
+        tri_of(V, C, q ? j : i, &a, &b, &cc);
+        v3 P[3] = {a, b, cc};
+        for (int k = 0; k < 3; ++k) {
+            v3 u = unit(sub(P[(k + 1) % 3], P[k])), w = unit(sub(P[(k + 2) % 3], P[k]));
+            if (dot(u, w) > c10) return 1;
+        }
+    }
+    return 0;
+}
+
+int o_pair_is_hard(int i, int j, const double *V, const int *C)
+{
+    int nc = (i > j ? i : j) + 1;
+    double *N = (double *)malloc(sizeof(double) * 3 * nc);
+    o_cell_geometry(nc, V, C, N, NULL, NULL);
+    int r = pair_is_hard(i, j, V, C, N);
+    free(N);
+    return r;
 }
 
 static double potential_adjacent(int cls, int i, int j, const double *V, const int *C, const double *N, const double *S)
@@ -655,7 +754,24 @@ static double potential_adjacent(int cls, int i, int j, const double *V, const i
         int si, sj, ri[3];
         shifts_vertex(C + 3 * i, C + 3 * j, &si, &sj);
         rotated(C + 3 * i, si, ri);
-        return O_INV_4PI * duffy_piece(ld(V + 3 * ri[0]), ld(V + 3 * ri[1]), ld(V + 3 * ri[2]), JA, JB, JC, NULL);
+        double acc = duffy_piece(ld(V + 3 * ri[0]), ld(V + 3 * ri[1]), ld(V + 3 * ri[2]), JA, JB, JC, NULL);
+        if (g_pot_adapt_tol > 0 && pair_is_hard(i, j, V, C, N)) {
+            pot_ctx c = {JA, JB, JC, NULL};
+            v3 a, b, cc;
+            tri_of(V, C, i, &a, &b, &cc);
+            /* shared vertex in slot si of K_i: it is corner (slot 1) of child 0 (b), 1 (c) or 2 (a) */
+            v3 mbc = scl(0.5, add(b, cc)), mca = scl(0.5, add(cc, a)), mab = scl(0.5, add(a, b));
+            v3 ch[4][3] = {{mab, b, mbc}, {mbc, cc, mca}, {mca, a, mab}, {mbc, mca, mab}};
+            int corner_of_child[4] = {si == 1 ? 1 : -1, si == 2 ? 1 : -1, si == 0 ? 1 : -1, -1};
+            double tol_abs = g_pot_adapt_tol * fabs(acc);
+            double sum = 0.0;
+            for (int k = 0; k < 4; ++k) {
+                double v = pot_cell(&c, ch[k][0], ch[k][1], ch[k][2], corner_of_child[k]);
+                sum += pot_adapt(&c, ch[k][0], ch[k][1], ch[k][2], corner_of_child[k], v, 0.5 * tol_abs, 1);
+            }
+            acc = sum;
+        }
+        return O_INV_4PI * acc;
     }
     int si, sj, ri[3];
     shifts_edge(C + 3 * i, C + 3 * j, &si, &sj);
@@ -664,6 +780,24 @@ static double potential_adjacent(int cls, int i, int j, const double *V, const i
     v3 M = scl(0.5, add(P1, P2));
     pot_edge_ctx pe = make_pot_edge_ctx(i, j, V, C, N, S);
     double acc = duffy_piece(P1, M, A, JA, JB, JC, &pe) + duffy_piece(P2, A, M, JA, JB, JC, &pe);
+    if (g_pot_adapt_tol > 0 && pair_is_hard(i, j, V, C, N)) {
+        pot_ctx c = {JA, JB, JC, &pe};
+        v3 a, b, cc;
+        tri_of(V, C, i, &a, &b, &cc);
+        /* root: both ends of the shared edge are corners; its value is the two-piece Duffy rule */
+        v3 mbc = scl(0.5, add(b, cc)), mca = scl(0.5, add(cc, a)), mab = scl(0.5, add(a, b));
+        v3 ch[4][3] = {{mab, b, mbc}, {mbc, cc, mca}, {mca, a, mab}, {mbc, mca, mab}};
+        int in_i[3];
+        for (int k = 0; k < 3; ++k) in_i[k] = (C[3 * i + k] == C[3 * j] || C[3 * i + k] == C[3 * j + 1] || C[3 * i + k] == C[3 * j + 2]);
+        int corner_of_child[4] = {in_i[1] ? 1 : -1, in_i[2] ? 1 : -1, in_i[0] ? 1 : -1, -1};
+        double tol_abs = g_pot_adapt_tol * fabs(acc + pot_edge_sigma_integral(&pe));
+        double sum = 0.0;
+        for (int k = 0; k < 4; ++k) {
+            double v = pot_cell(&c, ch[k][0], ch[k][1], ch[k][2], corner_of_child[k]);
+            sum += pot_adapt(&c, ch[k][0], ch[k][1], ch[k][2], corner_of_child[k], v, 0.5 * tol_abs, 1);
+        }
+        acc = sum;
+    }
     return O_INV_4PI * (acc + pot_edge_sigma_integral(&pe));
 }
 

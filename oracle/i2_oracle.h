@@ -54,6 +54,12 @@ void o_closed_vertex(int i, int j, const double *V, const int *C, const double *
  * default 40 x 32, grade 3 */
 void o_set_potential_rule(int nu, int nv, int grade);
 
+/* locally adaptive potential rule for hard common-edge / common-vertex pairs (folded, n_i.n_j <
+ * 0.5, or a cell with an angle below 10 degrees): relative tolerance, 0 disables (default 1e-10) */
+void o_set_potential_adaptive(double tol);
+void o_set_potential_adaptive_depth(int depth); /* default 18 */
+int o_pair_is_hard(int i, int j, const double *V, const int *C);
+
 /* potential of a self pair (1/4pi included) */
 double o_self_potential(const double *A, const double *B, const double *C, int nquad);
 

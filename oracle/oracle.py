@@ -63,6 +63,11 @@ def lib():
             L.o_closed_vertex.argtypes = [i, i, vp, vp, vp, vp, vp]
             L.o_cell_geometry.argtypes = [i, vp, vp, vp, vp, vp]
             L.o_max_threads.restype = i
+            L.o_set_potential_rule.argtypes = [i, i, i]
+            L.o_set_potential_adaptive.argtypes = [ctypes.c_double]
+            L.o_set_potential_adaptive_depth.argtypes = [i]
+            L.o_pair_is_hard.argtypes = [i, i, vp, vp]
+            L.o_pair_is_hard.restype = i
             _lib = L
     return _lib
 
@@ -128,3 +133,46 @@ def ref_integrate(cls, pairs, V, C, level=0, qf=QF13):
     if rc != 0:
         raise ValueError("reference driver rejected the arguments")
     return raw, J, it
+
+
+class potential_rule:
+    """context manager: the oracle's adjacent-pair potential rule (Duffy nu x nv, grading) and
+    adaptive hard-pair tolerance (0 = off); restores the high-order defaults on exit"""
+
+    def __init__(self, nu=40, nv=32, grade=3, adaptive=1e-10, depth=18):
+        self.args = (nu, nv, grade, adaptive, depth)
+
+    def __enter__(self):
+        L = lib()
+        nu, nv, g, a, d = self.args
+        L.o_set_potential_rule(nu, nv, g)
+        L.o_set_potential_adaptive(a)
+        L.o_set_potential_adaptive_depth(d)
+        return self
+
+    def __exit__(self, *exc):
+        L = lib()
+        L.o_set_potential_rule(40, 32, 3)
+        L.o_set_potential_adaptive(1e-10)
+        L.o_set_potential_adaptive_depth(18)
+
+
+def hard_pairs(pairs, V, C):
+    V = np.ascontiguousarray(V, np.float64); C = np.ascontiguousarray(C, np.int32)
+    L = lib()
+    return np.array([L.o_pair_is_hard(int(i), int(j), _p(V), _p(C)) for i, j in pairs], bool)
+
+
+def conditioning(cls, pairs, V, C, level=0, rel=1e-13, seed=0):
+    """per-pair sensitivity of J to relative input perturbations of size rel: the relative
+    change of J divided by rel (an estimate of the condition number)"""
+    V = np.ascontiguousarray(V, np.float64)
+    _, J0, _, _ = integrate(cls, pairs, V, C, mode=FIXED, level=level)
+    rng = np.random.default_rng(seed)
+    worst = np.zeros(len(pairs))
+    for _ in range(3):
+        Vp = V * (1.0 + rel * rng.standard_normal(V.shape))
+        _, J1, _, _ = integrate(cls, pairs, Vp, C, mode=FIXED, level=level)
+        scale = np.maximum(np.linalg.norm(J0, axis=1), 1e-300)
+        worst = np.maximum(worst, np.linalg.norm(J1 - J0, axis=1) / scale / rel)
+    return worst

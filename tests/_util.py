@@ -25,3 +25,18 @@ def rel_rows(a, b):
 def ensure_built():
     from integrator2_gb300.build import build
     return build()
+
+
+def parity_bar(kappa):
+    """per-pair FP64 parity bar: 1e-12 relative, widened to 1e-13 x kappa for pairs whose J is
+    ill-conditioned (kappa = measured relative sensitivity of J to relative input perturbations;
+    different math libraries then legitimately disagree in the trailing digits)"""
+    return np.maximum(1e-12, 1e-13 * np.asarray(kappa))
+
+
+def assert_parity(J, Jref, kappa, what=""):
+    r = rel_rows(J, Jref)
+    bar = parity_bar(kappa)
+    bad = r > bar
+    assert not bad.any(), f"{what}: {bad.sum()} pairs above the bar, worst {r.max():.3e} (bar {bar[r.argmax()]:.1e})"
+    return float(r.max())
