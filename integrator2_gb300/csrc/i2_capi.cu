@@ -287,6 +287,25 @@ struct i2_integrator {
             Q.dv_v[b] = x[b];
             Q.dv_w[b] = w[b];
         }
+        auto duffy_rule = [&](int nu, int nv, double *u, double *uw, double *v, double *vw) {
+            std::vector<double> gx, gw;
+            gauss_legendre01(nu, gx, gw);
+            for (int a = 0; a < nu; ++a) {
+                u[a] = std::pow(gx[a], pot_grade);
+                uw[a] = gw[a] * pot_grade * std::pow(gx[a], pot_grade - 1);
+            }
+            gauss_legendre01(nv, gx, gw);
+            for (int b = 0; b < nv; ++b) {
+                v[b] = gx[b];
+                vw[b] = gw[b];
+            }
+        };
+        Q.lo_nu = std::max(2, pot_nu - 2);
+        Q.lo_nv = std::max(2, pot_nv - 2);
+        duffy_rule(Q.lo_nu, Q.lo_nv, Q.lo_u, Q.lo_uw, Q.lo_v, Q.lo_vw);
+        Q.hi_nu = i2::kMaxDuffy;
+        Q.hi_nv = i2::kMaxDuffy;
+        duffy_rule(Q.hi_nu, Q.hi_nv, Q.hi_u, Q.hi_uw, Q.hi_v, Q.hi_vw);
         gauss_legendre01(pot_nself, x, w);
         Q.nself = pot_nself;
         for (int k = 0; k < pot_nself; ++k) {
@@ -310,7 +329,7 @@ struct ClassResult {
 
 struct Workspace {
     DevBuf<double> cur, fin_a, fin_b, sing, padj;
-    DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list;
+    DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list, tier2_list;
     DevBuf<int2> pairs;
 };
 
@@ -515,6 +534,7 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         W.sing.reserve(4 * n);
         W.padj.reserve(n);
         W.hard_list.reserve(n);
+        W.tier2_list.reserve(n);
     }
     // cnt[0..7] active counts per level, cnt[8] hard pairs, cnt[9] adaptive-potential stack overflows
     I2_CHECK_CUDA(cudaMemsetAsync(W.cnt.ptr, 0, 16 * sizeof(int), ev->stream));
@@ -534,10 +554,13 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
     A.maxlev = W.maxlev.ptr;
     A.sing = W.sing.ptr;
     A.padj = W.padj.ptr;
-    if (cls == I2_SIMPLE_NEIGHBORS || cls == I2_ATTACHED_NEIGHBORS) {
+    if ((cls == I2_SIMPLE_NEIGHBORS || cls == I2_ATTACHED_NEIGHBORS) && cfg.hard_tol > 0) {
         A.hard_list = W.hard_list.ptr;
         A.hard_cnt = W.cnt.ptr + 8;
         A.hard_overflow = W.cnt.ptr + 9;
+        A.tier2_list = W.tier2_list.ptr;
+        A.tier2_cnt = W.cnt.ptr + 10;
+        A.tier_tol = 10.0 * cfg.hard_tol;
     }
     A.raw4 = out_raw;
     A.J3 = out_J;

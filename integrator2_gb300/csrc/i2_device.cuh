@@ -140,6 +140,12 @@ struct QuadTables {
     double du_u[kMaxDuffy], du_w[kMaxDuffy];   // radial nodes u = t^g and weights g t^(g-1) w_t
     double dv_v[kMaxDuffy], dv_w[kMaxDuffy];   // angular Gauss-Legendre on [0,1]
     int nu, nv;
+    // two more Duffy rules of the tiered potential: a lower-order check (tier 1) and a
+    // higher-order rule (tier 2)
+    double lo_u[kMaxDuffy], lo_uw[kMaxDuffy], lo_v[kMaxDuffy], lo_vw[kMaxDuffy];
+    int lo_nu, lo_nv;
+    double hi_u[kMaxDuffy], hi_uw[kMaxDuffy], hi_v[kMaxDuffy], hi_vw[kMaxDuffy];
+    int hi_nu, hi_nv;
     // Gauss-Legendre on [0,1] for the self-pair potential (graded t^2(3-2t) map applied)
     double sx[kMaxSelf], sw[kMaxSelf];
     int nself;

@@ -40,7 +40,9 @@ struct ClassArgs {
     double *sing = nullptr;                   // closed-form singular part (Psi, Theta)
     double *padj = nullptr;                   // potential of adjacent pairs
     int *hard_list = nullptr, *hard_cnt = nullptr;  // adjacent pairs whose potential is refined adaptively
+    int *tier2_list = nullptr, *tier2_cnt = nullptr;  // pairs re-integrated with the higher-order Duffy rule
     int *hard_overflow = nullptr;             // stack-capacity events of the adaptive potential (diagnostic)
+    double tier_tol = 1e-7;                   // main/check (and main/higher-order) rule agreement bar
     // outputs
     double *raw4 = nullptr, *J3 = nullptr, *P = nullptr;
     int *level_out = nullptr;

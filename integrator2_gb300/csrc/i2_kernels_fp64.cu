@@ -204,6 +204,60 @@ __global__ void __launch_bounds__(128) k_level(ClassArgs A, QuadTables Q, int le
     }
 }
 
+// ------------------------------------------------------------------ potential of adjacent pairs
+// s ln s term along the shared edge (Ti, Tj rotated: Ti.a / Tj.a off the shared edge); returns
+// its integral over K_i, (5/9) c S_i h
+__device__ __forceinline__ double make_pot_edge(const Tri &Ti, const Tri &Tj, const PanelJ &K, double Si, PotEdge &pe)
+{
+    const d3 tau = unit(Tj.c - Tj.b), m = cross(tau, K.n), w = Ti.a - Tj.b;
+    const d3 perp = w - dot(w, tau) * tau;
+    pe.P1 = Tj.b;
+    pe.h = norm(perp);
+    pe.m_in = (1.0 / pe.h) * perp;
+    pe.c = -dot(m, pe.m_in);
+    return (5.0 / 9.0) * pe.c * Si * pe.h;
+}
+
+// graded Duffy rule over the pieces of K_i (Ti rotated): one piece with apex at the shared
+// vertex (vertex class) or two pieces with apexes at the ends of the shared edge (edge class);
+// the edge class integrates g - sigma
+template <int CLS>
+__device__ double duffy_total(const Tri &Ti, const PanelJ &K, const FarCtx &F, const PotEdge &pe, const double *uu,
+                              const double *uw, int nu, const double *vv, const double *vw, int nv)
+{
+    double total = 0.0;
+    const int npieces = CLS == kEdge ? 2 : 1;
+    for (int piece = 0; piece < npieces; ++piece) {
+        d3 Vx, B, Cc;
+        if (CLS == kVertex) { Vx = Ti.a; B = Ti.b; Cc = Ti.c; }
+        else {
+            const d3 M = 0.5 * (Ti.b + Ti.c);
+            if (piece == 0) { Vx = Ti.b; B = M; Cc = Ti.a; }
+            else { Vx = Ti.c; B = Ti.a; Cc = M; }
+        }
+        const d3 eB = B - Vx, eC = Cc - Vx, dA = Vx - K.A, dB = Vx - K.B, dC = Vx - K.C;
+        const double area2 = norm(cross(eB, eC));
+        double acc = 0.0;
+#pragma unroll 1
+        for (int a = 0; a < nu; ++a) {
+            const double u = uu[a];
+            double row = 0.0;
+#pragma unroll 1
+            for (int b = 0; b < nv; ++b) {
+                const d3 w = u * ((1.0 - vv[b]) * eB + vv[b] * eC);
+                d3 psi;
+                double th, g;
+                far_integrand_o(dA + w, dB + w, dC + w, K, F, psi, th, g);
+                if (CLS == kEdge) g -= pot_edge_sigma(Vx + w, pe);
+                row += vw[b] * g;
+            }
+            acc += uw[a] * u * row;
+        }
+        total += area2 * acc;
+    }
+    return total;
+}
+
 // ------------------------------------------------------------------ singular parts (edge/vertex)
 template <int CLS>
 __global__ void __launch_bounds__(128) k_singular(ClassArgs A, QuadTables Q)
@@ -229,59 +283,48 @@ __global__ void __launch_bounds__(128) k_singular(ClassArgs A, QuadTables Q)
     double *sg = A.sing + 4 * (long long)t;
     sg[0] = psi.x; sg[1] = psi.y; sg[2] = psi.z; sg[3] = th;
 
-    // potential: graded Duffy rule around the shared vertex (vertex class) or around each end
-    // of the shared edge after subtracting the s ln s term along it (edge class)
+    // potential: tier 1 of the tiered rule (graded Duffy, main and lower-order check)
     const FarCtx F = make_far_ctx(K);
-    double total = 0.0;
-    const int npieces = CLS == kEdge ? 2 : 1;
     PotEdge pe;
-    if (CLS == kEdge) {
-        const d3 JB = Tj.b, JC = Tj.c;
-        const d3 tau = unit(JC - JB);
-        const d3 m = cross(tau, K.n);
-        const d3 w = Ti.a - JB;
-        const d3 perp = w - dot(w, tau) * tau;
-        pe.P1 = JB;
-        pe.h = norm(perp);
-        pe.m_in = (1.0 / pe.h) * perp;
-        pe.c = -dot(m, pe.m_in);
-        total = (5.0 / 9.0) * pe.c * Si * pe.h;
-    }
-    for (int piece = 0; piece < npieces; ++piece) {
-        d3 Vx, B, Cc;
-        if (CLS == kVertex) { Vx = Ti.a; B = Ti.b; Cc = Ti.c; }
-        else {
-            const d3 M = 0.5 * (Ti.b + Ti.c);
-            if (piece == 0) { Vx = Ti.b; B = M; Cc = Ti.a; }
-            else { Vx = Ti.c; B = Ti.a; Cc = M; }
-        }
-        const d3 eB = B - Vx, eC = Cc - Vx;
-        const double area2 = norm(cross(eB, eC));
-        double acc = 0.0;
-#pragma unroll 1
-        for (int a = 0; a < Q.nu; ++a) {
-            const double u = Q.du_u[a];
-            double row = 0.0;
-#pragma unroll 1
-            for (int b = 0; b < Q.nv; ++b) {
-                const double v = Q.dv_v[b];
-                const d3 x = Vx + u * ((1.0 - v) * eB + v * eC);
-                double g = potential_inner(x, K, F);
-                if (CLS == kEdge) g -= pot_edge_sigma(x, pe);
-                row += Q.dv_w[b] * g;
-            }
-            acc += Q.du_w[a] * u * row;
-        }
-        total += area2 * acc;
-    }
-    A.padj[t] = kInv4Pi * total;
-    // hard pair: folded (normals more than 60 degrees apart) or a cell with an angle below 10 degrees
+    const double sig = CLS == kEdge ? make_pot_edge(Ti, Tj, K, Si, pe) : 0.0;
+    const double pm = duffy_total<CLS>(Ti, K, F, pe, Q.du_u, Q.du_w, Q.nu, Q.dv_v, Q.dv_w, Q.nv) + sig;
+    A.padj[t] = kInv4Pi * pm;
     if (A.hard_list) {
+        // hard pair (folded: normals more than 60 degrees apart, or a cell with an angle below 10
+        // degrees) -> adaptive rule; main and check rules disagree -> higher-order rule
         const double c10 = 0.98480775301220806;
         if (dot(ni, K.n) < 0.5 || A.panels[pr.x].v[2].w > c10 || A.panels[pr.y].v[2].w > c10) {
-            const int pos = atomicAdd(A.hard_cnt, 1);
-            A.hard_list[pos] = t;
+            A.hard_list[atomicAdd(A.hard_cnt, 1)] = t;
+        } else {
+            const double pl = duffy_total<CLS>(Ti, K, F, pe, Q.lo_u, Q.lo_uw, Q.lo_nu, Q.lo_v, Q.lo_vw, Q.lo_nv) + sig;
+            if (fabs(pm - pl) > A.tier_tol * fabs(pm)) A.tier2_list[atomicAdd(A.tier2_cnt, 1)] = t;
         }
+    }
+}
+
+// tier 2: higher-order Duffy rule; pairs where it still disagrees with the main rule go on to
+// the adaptive rule (tier 3)
+template <int CLS>
+__global__ void __launch_bounds__(128) k_pot_tier2(ClassArgs A, QuadTables Q)
+{
+    const int count = *A.tier2_cnt;
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < count; h += gridDim.x * blockDim.x) {
+        const int t = A.tier2_list[h];
+        const int2 pr = A.pairs[t];
+        const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
+        const PanelJ K = load_panel(A.panels, pr.y);
+        const double Si = A.panels[pr.x].v[0].w;
+        int si, sj;
+        if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
+        else shifts_vertex(ci, cj, si, sj);
+        const Tri Ti = rotate(load_tri(A.panels, pr.x), si), Tj = rotate(Tri{K.A, K.B, K.C}, sj);
+        const FarCtx F = make_far_ctx(K);
+        PotEdge pe;
+        const double sig = CLS == kEdge ? make_pot_edge(Ti, Tj, K, Si, pe) : 0.0;
+        const double ph = duffy_total<CLS>(Ti, K, F, pe, Q.hi_u, Q.hi_uw, Q.hi_nu, Q.hi_v, Q.hi_vw, Q.hi_nv) + sig;
+        const double pm = A.padj[t] * (4.0 * kPi);
+        A.padj[t] = kInv4Pi * ph;
+        if (fabs(ph - pm) > A.tier_tol * fabs(ph)) A.hard_list[atomicAdd(A.hard_cnt, 1)] = t;
     }
 }
 
@@ -372,17 +415,7 @@ __global__ void __launch_bounds__(32 * kHardWarps) k_pot_hard(ClassArgs A, QuadT
         if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
         else shifts_vertex(ci, cj, si, sj);
         PotEdge pe;
-        double sig_int = 0.0;
-        if (CLS == kEdge) {
-            const Tri Tj = rotate(Tri{K.A, K.B, K.C}, sj), Tr = rotate(Ti, si);
-            const d3 tau = unit(Tj.c - Tj.b), m = cross(tau, K.n), wv = Tr.a - Tj.b;
-            const d3 perp = wv - dot(wv, tau) * tau;
-            pe.P1 = Tj.b;
-            pe.h = norm(perp);
-            pe.m_in = (1.0 / pe.h) * perp;
-            pe.c = -dot(m, pe.m_in);
-            sig_int = (5.0 / 9.0) * pe.c * Si * pe.h;
-        }
+        const double sig_int = CLS == kEdge ? make_pot_edge(rotate(Ti, si), rotate(Tri{K.A, K.B, K.C}, sj), K, Si, pe) : 0.0;
         // shared slots of K_i: the root's children 0, 1, 2 hold slots b, c, a
         const int ia[3] = {ci.x, ci.y, ci.z};
         bool shared[3];
@@ -571,12 +604,18 @@ void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const R
         break;
     case kEdge:
         k_singular<kEdge><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q);
-        if (A.hard_list && cfg.hard_tol > 0) k_pot_hard<kEdge><<<persistent_blocks / 4, 32 * kHardWarps, 0, s>>>(A, Q, cfg.hard_tol);
+        if (A.hard_list) {
+            k_pot_tier2<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Q);
+            k_pot_hard<kEdge><<<persistent_blocks / 4, 32 * kHardWarps, 0, s>>>(A, Q, cfg.hard_tol);
+        }
         level_chain<kEdge>(A, Q, cfg, persistent_blocks, s);
         break;
     case kVertex:
         k_singular<kVertex><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q);
-        if (A.hard_list && cfg.hard_tol > 0) k_pot_hard<kVertex><<<persistent_blocks / 4, 32 * kHardWarps, 0, s>>>(A, Q, cfg.hard_tol);
+        if (A.hard_list) {
+            k_pot_tier2<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Q);
+            k_pot_hard<kVertex><<<persistent_blocks / 4, 32 * kHardWarps, 0, s>>>(A, Q, cfg.hard_tol);
+        }
         level_chain<kVertex>(A, Q, cfg, persistent_blocks, s);
         break;
     default:

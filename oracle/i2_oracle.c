@@ -637,17 +637,17 @@ void o_set_potential_rule(int nu, int nv, int grade)
     g_pot_grade = grade < 1 ? 1 : grade;
 }
 
-static double duffy_piece(v3 Vx, v3 B, v3 Cc, v3 JA, v3 JB, v3 JC, const pot_edge_ctx *pe)
+static double duffy_piece_rule(v3 Vx, v3 B, v3 Cc, v3 JA, v3 JB, v3 JC, const pot_edge_ctx *pe, int nu, int nv)
 {
     double tu[256], wu[256], tv[256], wv[256];
-    gauss_legendre(g_pot_nu, tu, wu);
-    gauss_legendre(g_pot_nv, tv, wv);
+    gauss_legendre(nu, tu, wu);
+    gauss_legendre(nv, tv, wv);
     double area2 = len(crs(sub(B, Vx), sub(Cc, Vx)));
     double acc = 0.0;
-    for (int a = 0; a < g_pot_nu; ++a) {
+    for (int a = 0; a < nu; ++a) {
         double t = 0.5 * (tu[a] + 1.0), wt = 0.5 * wu[a];
         double u = pow(t, g_pot_grade), du = g_pot_grade * pow(t, g_pot_grade - 1) * wt;
-        for (int b = 0; b < g_pot_nv; ++b) {
+        for (int b = 0; b < nv; ++b) {
             double v = 0.5 * (tv[b] + 1.0), wvv = 0.5 * wv[b];
             v3 w = scl(u, add(scl(1.0 - v, sub(B, Vx)), scl(v, sub(Cc, Vx))));
             v3 oa = add(sub(Vx, JA), w), ob = add(sub(Vx, JB), w), oc = add(sub(Vx, JC), w);
@@ -660,15 +660,24 @@ static double duffy_piece(v3 Vx, v3 B, v3 Cc, v3 JA, v3 JB, v3 JC, const pot_edg
     return acc;
 }
 
+static double duffy_piece(v3 Vx, v3 B, v3 Cc, v3 JA, v3 JB, v3 JC, const pot_edge_ctx *pe)
+{
+    return duffy_piece_rule(Vx, B, Cc, JA, JB, JC, pe, g_pot_nu, g_pot_nv);
+}
+
 /* Hard adjacent pairs (folded: n_i.n_j < 0.5, or a cell with an angle below 10 degrees) get a
  * locally adaptive rule: a cell is compared with the sum of its four children and split again
  * where they differ by more than tol x |P| x 2^-depth; cells holding a shared vertex use the
  * Duffy rule with that vertex as apex, all others the 13-point rule. */
 static double g_pot_adapt_tol = 1e-10;   /* 0 disables the adaptive route */
 static int g_pot_adapt_depth = 18;
+static int g_pot_adapt_all = 0;   /* 1: adaptive rule for every adjacent pair, not only hard ones */
+static double g_pot_tier_tol = 0;  /* > 0: tiered rule (main vs check, then 16x16, then adaptive) */
 
 void o_set_potential_adaptive(double tol) { g_pot_adapt_tol = tol; }
 void o_set_potential_adaptive_depth(int d) { g_pot_adapt_depth = d; }
+void o_set_potential_adaptive_all(int on) { g_pot_adapt_all = on; }
+void o_set_potential_tiered(double tol) { g_pot_tier_tol = tol; }
 
 static const double Q13[13][3] = {
     {0.333333333333333, 0.333333333333333, -0.149570044467670},
@@ -720,6 +729,21 @@ static double pot_adapt(const pot_ctx *c, v3 a, v3 b, v3 cc, int corner, double 
     return out;
 }
 
+/* tiered potential rule of the library: the main Duffy rule is kept when a lower-order check
+ * (two fewer nodes per direction) agrees within the tier tolerance; otherwise a 16 x 16 rule is
+ * kept when it agrees with the main rule; otherwise the adaptive rule runs.  Returns 1 when the
+ * adaptive rule must run, and stores the kept Duffy value in *acc otherwise. */
+static int tier_select(int npieces, const v3 P[2][3], v3 JA, v3 JB, v3 JC, const pot_edge_ctx *pe, double sig, double *acc)
+{
+    double lo = 0.0, hi = 0.0;
+    for (int k = 0; k < npieces; ++k)
+        lo += duffy_piece_rule(P[k][0], P[k][1], P[k][2], JA, JB, JC, pe, g_pot_nu > 4 ? g_pot_nu - 2 : 2, g_pot_nv > 4 ? g_pot_nv - 2 : 2);
+    if (fabs((*acc + sig) - (lo + sig)) <= g_pot_tier_tol * fabs(*acc + sig)) return 0;
+    for (int k = 0; k < npieces; ++k) hi += duffy_piece_rule(P[k][0], P[k][1], P[k][2], JA, JB, JC, pe, 16, 16);
+    if (fabs((hi + sig) - (*acc + sig)) <= g_pot_tier_tol * fabs(hi + sig)) { *acc = hi; return 0; }
+    return 1;
+}
+
 static int pair_is_hard(int i, int j, const double *V, const int *C, const double *N)
 {
     if (dot(ld(N + 3 * i), ld(N + 3 * j)) < 0.5) return 1;
@@ -755,7 +779,12 @@ static double potential_adjacent(int cls, int i, int j, const double *V, const i
         shifts_vertex(C + 3 * i, C + 3 * j, &si, &sj);
         rotated(C + 3 * i, si, ri);
         double acc = duffy_piece(ld(V + 3 * ri[0]), ld(V + 3 * ri[1]), ld(V + 3 * ri[2]), JA, JB, JC, NULL);
-        if (g_pot_adapt_tol > 0 && pair_is_hard(i, j, V, C, N)) {
+        int go_adapt = g_pot_adapt_tol > 0 && (g_pot_adapt_all || pair_is_hard(i, j, V, C, N));
+        if (!go_adapt && g_pot_tier_tol > 0) {
+            const v3 P[2][3] = {{ld(V + 3 * ri[0]), ld(V + 3 * ri[1]), ld(V + 3 * ri[2])}, {ld(V), ld(V), ld(V)}};
+            go_adapt = tier_select(1, P, JA, JB, JC, NULL, 0.0, &acc);
+        }
+        if (go_adapt) {
             pot_ctx c = {JA, JB, JC, NULL};
             v3 a, b, cc;
             tri_of(V, C, i, &a, &b, &cc);
@@ -780,7 +809,12 @@ static double potential_adjacent(int cls, int i, int j, const double *V, const i
     v3 M = scl(0.5, add(P1, P2));
     pot_edge_ctx pe = make_pot_edge_ctx(i, j, V, C, N, S);
     double acc = duffy_piece(P1, M, A, JA, JB, JC, &pe) + duffy_piece(P2, A, M, JA, JB, JC, &pe);
-    if (g_pot_adapt_tol > 0 && pair_is_hard(i, j, V, C, N)) {
+    int go_adapt = g_pot_adapt_tol > 0 && (g_pot_adapt_all || pair_is_hard(i, j, V, C, N));
+    if (!go_adapt && g_pot_tier_tol > 0) {
+        const v3 P[2][3] = {{P1, M, A}, {P2, A, M}};
+        go_adapt = tier_select(2, P, JA, JB, JC, &pe, pot_edge_sigma_integral(&pe), &acc);
+    }
+    if (go_adapt) {
         pot_ctx c = {JA, JB, JC, &pe};
         v3 a, b, cc;
         tri_of(V, C, i, &a, &b, &cc);

@@ -58,6 +58,9 @@ void o_set_potential_rule(int nu, int nv, int grade);
  * 0.5, or a cell with an angle below 10 degrees): relative tolerance, 0 disables (default 1e-10) */
 void o_set_potential_adaptive(double tol);
 void o_set_potential_adaptive_depth(int depth); /* default 18 */
+void o_set_potential_adaptive_all(int on);     /* 1: adaptive rule for every adjacent pair */
+/* > 0: the library's tiered rule (Duffy main vs check, then 16 x 16, then adaptive); 0 off */
+void o_set_potential_tiered(double tier_tol);
 int o_pair_is_hard(int i, int j, const double *V, const int *C);
 
 /* potential of a self pair (1/4pi included) */

@@ -31,6 +31,8 @@ _QF13_COORDS = np.array([
 _QF13_W = np.array([-0.149570044467670] + [0.175615257433204] * 3 + [0.053347235608839] * 3 +
                    [0.077113760890257] * 6)
 QF13 = (_QF13_COORDS, _QF13_W, 7)
+# the library's default potential rule, for CPU runs doing the library's work
+PRODUCT_RULE = dict(nu=10, nv=8, grade=3, adaptive=1e-8, depth=12, tiered=1e-7)
 
 _lock = threading.Lock()
 _lib = None
@@ -66,6 +68,8 @@ def lib():
             L.o_set_potential_rule.argtypes = [i, i, i]
             L.o_set_potential_adaptive.argtypes = [ctypes.c_double]
             L.o_set_potential_adaptive_depth.argtypes = [i]
+            L.o_set_potential_adaptive_all.argtypes = [i]
+            L.o_set_potential_tiered.argtypes = [ctypes.c_double]
             L.o_pair_is_hard.argtypes = [i, i, vp, vp]
             L.o_pair_is_hard.restype = i
             _lib = L
@@ -139,15 +143,17 @@ class potential_rule:
     """context manager: the oracle's adjacent-pair potential rule (Duffy nu x nv, grading) and
     adaptive hard-pair tolerance (0 = off); restores the high-order defaults on exit"""
 
-    def __init__(self, nu=40, nv=32, grade=3, adaptive=1e-10, depth=18):
-        self.args = (nu, nv, grade, adaptive, depth)
+    def __init__(self, nu=40, nv=32, grade=3, adaptive=1e-10, depth=18, every_pair=False, tiered=0.0):
+        self.args = (nu, nv, grade, adaptive, depth, every_pair, tiered)
 
     def __enter__(self):
         L = lib()
-        nu, nv, g, a, d = self.args
+        nu, nv, g, a, d, e, t = self.args
         L.o_set_potential_rule(nu, nv, g)
         L.o_set_potential_adaptive(a)
         L.o_set_potential_adaptive_depth(d)
+        L.o_set_potential_adaptive_all(1 if e else 0)
+        L.o_set_potential_tiered(t)
         return self
 
     def __exit__(self, *exc):
@@ -155,6 +161,8 @@ class potential_rule:
         L.o_set_potential_rule(40, 32, 3)
         L.o_set_potential_adaptive(1e-10)
         L.o_set_potential_adaptive_depth(18)
+        L.o_set_potential_adaptive_all(0)
+        L.o_set_potential_tiered(0.0)
 
 
 def hard_pairs(pairs, V, C):
