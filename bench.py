@@ -190,6 +190,44 @@ def accuracy(V, C, lists, J, P, levels, nsample=400):
     return out
 
 
+def run_form(ev, lists, d_pairs, d_J, d_P, stream, flush, steps, warmup):
+    """times `steps` device-resident steps (L2 flushed between steps); returns the total device
+    time in ms and the mean per-class time"""
+    import torch
+    with torch.cuda.stream(stream):
+        for _ in range(max(warmup, 3)):
+            for c in CLASSES:
+                ev.runClassDevice(c, d_pairs[c].data_ptr(), len(lists[c]), 0, d_J[c].data_ptr(), d_P[c].data_ptr())
+        stream.synchronize()
+        ev_start = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ev_cls = [[torch.cuda.Event(enable_timing=True) for _ in CLASSES] for _ in range(steps)]
+        for s in range(steps):
+            flush.fill_(float(s))
+            ev_start[s].record(stream)
+            for k, c in enumerate(CLASSES):
+                ev.runClassDevice(c, d_pairs[c].data_ptr(), len(lists[c]), 0, d_J[c].data_ptr(), d_P[c].data_ptr())
+                ev_cls[s][k].record(stream)
+        torch.cuda.synchronize()
+    total = sum(ev_start[s].elapsed_time(ev_cls[s][-1]) for s in range(steps))
+    cls_ms = np.zeros(len(CLASSES))
+    for s in range(steps):
+        prev = ev_start[s]
+        for k in range(len(CLASSES)):
+            cls_ms[k] += prev.elapsed_time(ev_cls[s][k])
+            prev = ev_cls[s][k]
+    return total, cls_ms / steps
+
+
+# FP32 operation counts of the far-field integrand (same formulas, FP32 form): flops, sqrtf,
+# divide, log1pf, atan2f
+POINT_OPS_F32 = {"far": (211, 3, 3, 3, 1)}
+
+
+def point_flops_f32(cal):
+    a, sq, dv, lg, at = POINT_OPS_F32["far"]
+    return a + 2.0 * (sq * cal[8] + dv * cal[9] + lg * cal[10] + at * cal[11])
+
+
 def gpu_arm(args):
     import torch
     from integrator2_gb300 import api
@@ -205,72 +243,47 @@ def gpu_arm(args):
     V, C, lists = workload()
     total = sum(len(v) for v in lists.values())
 
-    cal = np.zeros(8)
+    cal = np.zeros(13)
     lib().i2_calibrate_pipes(cal.ctypes.data_as(ctypes.c_void_p))
     w = flop_weights(cal)
 
     m = api.Mesh3D()
     m.setGeometry(V, C)
     m.prepareMesh(NEAR)
-    it = api.NumericalIntegrator3D(m, api.qf3D13)
-    it.setErrorControl(api.RELATIVE_ERROR_CONTROL, args.tol, 5)
-    ev = api.EvaluatorJ3DK(m, it)
     stream = torch.cuda.Stream()
-    ev.setStream(stream.cuda_stream)
-
     d_pairs = {c: torch.from_numpy(lists[c]).to("cuda") for c in CLASSES}
     d_J = {c: torch.empty(len(lists[c]), 3, dtype=torch.float64, device="cuda") for c in CLASSES}
     d_P = {c: torch.empty(len(lists[c]), dtype=torch.float64, device="cuda") for c in CLASSES}
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    def step():
-        for c in CLASSES:
-            ev.runClassDevice(c, d_pairs[c].data_ptr(), len(lists[c]), 0, d_J[c].data_ptr(), d_P[c].data_ptr())
-
-    with torch.cuda.stream(stream):
-        for _ in range(max(args.warmup, 3)):
-            step()
-        stream.synchronize()
-        # per-class and whole-step device time
-        ev_start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-        ev_cls = [[torch.cuda.Event(enable_timing=True) for _ in CLASSES] for _ in range(args.steps)]
+    forms = {}
+    for name, prec in (("fp64", api.PRECISION_FP64), ("mixed", api.PRECISION_MIXED)):
+        it = api.NumericalIntegrator3D(m, api.qf3D13)
+        it.setErrorControl(api.RELATIVE_ERROR_CONTROL, args.tol, 5)
+        it.setPrecision(prec)
+        ev = api.EvaluatorJ3DK(m, it)
+        ev.setStream(stream.cuda_stream)
         if world > 1:
             torch.distributed.barrier()
-        torch.cuda.synchronize()
         with ClockSampler() as clk:
-            for s in range(args.steps):
-                flush.fill_(float(s))
-                ev_start[s].record(stream)
-                for k, c in enumerate(CLASSES):
-                    ev.runClassDevice(c, d_pairs[c].data_ptr(), len(lists[c]), 0, d_J[c].data_ptr(), d_P[c].data_ptr())
-                    ev_cls[s][k].record(stream)
-            torch.cuda.synchronize()
+            ms, cls_ms = run_form(ev, lists, d_pairs, d_J, d_P, stream, flush, args.steps, args.warmup)
         if world > 1:
-            torch.distributed.barrier()
-        step_ms = [ev_start[s].elapsed_time(ev_cls[s][-1]) for s in range(args.steps)]
-        cls_ms = np.zeros(len(CLASSES))
-        for s in range(args.steps):
-            prev = ev_start[s]
-            for k in range(len(CLASSES)):
-                cls_ms[k] += prev.elapsed_time(ev_cls[s][k])
-                prev = ev_cls[s][k]
-        cls_ms /= args.steps
-    ms = float(np.sum(step_ms))
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = total * world * args.steps / (ms * 1e-3)
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        J = {c: d_J[c].cpu().numpy() for c in CLASSES}
+        P = {c: d_P[c].cpu().numpy() for c in CLASSES}
+        levels = {}
+        for c in CLASSES:
+            ev.runClass(c, lists[c])  # host entry point: same results, records the kept level per pair
+            levels[c] = ev.getLevels(c)
+            if not np.array_equal(ev.getResults(c), J[c]):
+                raise RuntimeError(f"{name}: host and device entry points disagree on class {c}")
+        forms[name] = dict(ev=ev, it=it, ms=ms, cls_ms=cls_ms, J=J, P=P, levels=levels, clocks=clk.summary(),
+                           value=total * world * args.steps / (ms * 1e-3))
 
-    # levels reached per class (work model) and results for the accuracy check
-    J = {c: d_J[c].cpu().numpy() for c in CLASSES}
-    P = {c: d_P[c].cpu().numpy() for c in CLASSES}
-    levels = {}
-    for c in CLASSES:
-        ev.runClass(c, lists[c])  # host path, same results, also records the level per pair
-        levels[c] = ev.getLevels(c)
-        assert np.array_equal(ev.getResults(c), J[c]), "host and device paths disagree"
-
+    head = forms["mixed"]
+    ev = head["ev"]
     # e2e: host lists (pinned) -> H2D, compute, D2H of J and P inside the timed region
     h_pairs = {c: torch.from_numpy(lists[c]).pin_memory() for c in CLASSES}
     h_J = {c: torch.empty(len(lists[c]), 3, dtype=torch.float64).pin_memory() for c in CLASSES}
@@ -291,44 +304,49 @@ def gpu_arm(args):
             stream.synchronize()
             e2e_ms.append(1e3 * (time.perf_counter() - t0))
     e2e_value = total * world / (np.median(e2e_ms) * 1e-3)
-
     if rank != 0:
         return
-    # roofline of the dominant chain: the near-field class (levels 0..5 of k_level<far>)
-    far = lists[2]
-    lev = levels[2]
-    # a pair that stopped at level L visited levels 0..L: count sub-cell evaluations of every visited level
-    evals = int(sum(np.sum(lev >= L) * 4 ** L for L in range(6)))
-    far_flops = evals * 13 * point_flops("far", w)
-    far_ms = cls_ms[2]
-    achieved = far_flops / (far_ms * 1e-3) / 1e12
-    peak = float(cal[0])
-    acc = accuracy(V, C, lists, J, P, levels)
+
+    def far_roofline(form, per_point, peak, unit_note):
+        lev = form["levels"][2]
+        evals = int(sum(np.sum(lev >= L) * 4 ** L for L in range(6)))
+        flops = evals * 13 * per_point
+        achieved = flops / (form["cls_ms"][2] * 1e-3) / 1e12
+        return {"achieved": achieved, "peak": peak, "frac": achieved / peak, "flops_per_point": per_point,
+                "point_evaluations": evals * 13, "note": unit_note}
+
+    roof_mixed = far_roofline(head, point_flops_f32(cal), float(cal[1]), "FP32 FMA peak measured live (i2_calibrate_pipes)")
+    roof_fp64 = far_roofline(forms["fp64"], point_flops("far", w), float(cal[0]), "FP64 FMA peak measured live")
+    acc = {name: accuracy(V, C, lists, f["J"], f["P"], f["levels"]) for name, f in forms.items()}
     n_cpu, dt_cpu, thr = cpu_run(V, C, lists, args.cpu_fraction, args.tol)
     launches_per_step = 10 + 10 + 7 + 1
     line = {
-        "metric": METRIC, "value": value, "unit": "pair-integrals/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "metric": METRIC, "value": head["value"], "unit": "pair-integrals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 bulk / f64 singular, estimator and hard pairs", "data": "synthetic",
         "config": {"workload": "jittered icosphere s5 (20480 triangles, sigma 0.15h, seed 2026): common-vertex, "
                                "common-edge, self and near-field (< 3h) ordered pairs",
-                   "pairs": total, "form": "plain FP64", "error_control": f"relative tol {args.tol}, levels 0..5",
-                   "rule": "qf3D13; adjacent potential: tiered graded Duffy 10x8 / 8x6 check / 16x16 / adaptive", "l2": "flushed (512 MiB write) between steps",
-                   "parallelism": f"replicas x{world}"},
+                   "pairs": total, "form": "mixed precision (per-class kernel chains)",
+                   "error_control": f"relative tol {args.tol}, levels 0..5",
+                   "rule": "qf3D13; adjacent potential: tiered graded Duffy 10x8 / 8x6 check / 16x16 / adaptive",
+                   "l2": "flushed (512 MiB write) between steps", "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "pair-integrals/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-        "roofline": {"bound": "fp64", "kernel": "k_level<far> chain (levels 0..5)", "achieved": achieved, "peak": peak,
-                     "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
-                     "peak_source": "measured live by i2_calibrate_pipes (FP64 FMA chains); MEASURED_PEAKS.json has no FP64 figure",
-                     "flops_per_far_point": point_flops("far", w)},
-        "class_ms": {n: float(t) for n, t in zip(("vertex", "edge", "near", "self"), cls_ms)},
-        "levels": {n: np.bincount(levels[c][levels[c] >= 0], minlength=6).tolist() for n, c in
+        "roofline": {"bound": "fp32", "kernel": "k_level_mixed<far> chain (levels 0..5)", "unit": "TFLOP/s", "traffic": None,
+                     **roof_mixed},
+        "plain_fp64": {"value": forms["fp64"]["value"], "ms_per_step": forms["fp64"]["ms"] / args.steps,
+                       "class_ms": dict(zip(("vertex", "edge", "near", "self"), map(float, forms["fp64"]["cls_ms"]))),
+                       "roofline": {"bound": "fp64", "unit": "TFLOP/s", **roof_fp64}},
+        "mixed_over_fp64": head["value"] / forms["fp64"]["value"],
+        "class_ms": dict(zip(("vertex", "edge", "near", "self"), map(float, head["cls_ms"]))),
+        "levels": {n: np.bincount(head["levels"][c][head["levels"][c] >= 0], minlength=6).tolist() for n, c in
                    zip(("vertex", "edge", "near"), (0, 1, 2))},
         "accuracy": acc,
         "calibration": {"fp64_tflops": float(cal[0]), "fp32_tflops": float(cal[1]),
-                        "fma_units": dict(zip(("sqrt", "div", "log", "atan2", "sincos", "acos"), map(float, cal[2:8])))},
+                        "fp64_fma_units": dict(zip(("sqrt", "div", "log", "atan2", "sincos", "acos"), map(float, cal[2:8]))),
+                        "fp32_fma_units": dict(zip(("sqrtf", "div", "log1pf", "atan2f", "logf"), map(float, cal[8:13])))},
         "cpu_baseline": {"value": n_cpu / dt_cpu, "unit": "pair-integrals/s", "cores": thr, "kind": "port",
                          "sample": f"{args.cpu_fraction:.3f} of every class ({n_cpu} pairs), oracle C restatement, OpenMP, same rules"},
-        "clocks": clk.summary(),
+        "clocks": head["clocks"],
         "gpu_launches": launches_per_step * args.steps,
     }
     print(json.dumps(line))

@@ -170,7 +170,8 @@ i2_status i2_evaluator_output_results(const i2_evaluator_t *ev, i2_pair_class cl
 /* ------------------------------------------------------------------ measurement */
 /* measured pipe peaks of the current GPU for the kernels' roofline (no reference counterpart):
  * out[0] FP64 FMA TFLOP/s, out[1] FP32 FMA TFLOP/s, out[2..7] time of one FP64 sqrt, divide,
- * log, atan2, sincos, acos in units of one FP64 FMA */
+ * log, atan2, sincos, acos in units of one FP64 FMA, out[8..12] time of one FP32 sqrtf,
+ * divide, log1pf, atan2f, logf in units of one FP32 FMA (out holds 13 doubles) */
 i2_status i2_calibrate_pipes(double *out);
 
 #if defined(__GNUC__)

@@ -153,7 +153,7 @@ class NumericalIntegrator3D:
     def setPrecision(self, precision: int) -> None:
         call("i2_integrator_set_precision", self._h, int(precision))
 
-    def setPotentialRule(self, n_radial=10, n_angular=8, grading=3, n_self=16) -> None:
+    def setPotentialRule(self, n_radial=10, n_angular=8, grading=3, n_self=24) -> None:
         call("i2_integrator_set_potential_rule", self._h, n_radial, n_angular, grading, n_self)
 
     def setHardPairTolerance(self, rel_tol: float) -> None:

@@ -63,6 +63,29 @@ __global__ void k_fn(int iters, double *sink)
     if (s == 1.2345) sink[0] = s;
 }
 
+// f = 0 sqrtf, 1 divide, 2 log1pf, 3 atan2f, 4 logf
+template <int F>
+__global__ void k_fnf(int iters, float *sink)
+{
+    float a[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a[k] = 0.3f + 1e-3f * (threadIdx.x + k);
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float x = a[k];
+            float y;
+            if (F == 0) y = sqrtf(x + 1.0f);
+            else if (F == 1) y = 1.0f / (x + 1.0f);
+            else if (F == 2) y = log1pf(x);
+            else if (F == 3) y = atan2f(x, 1.0f - 0.5f * x);
+            else y = logf(x + 1.0f);
+            a[k] = 0.5f * y + 0.25f;
+        }
+    const float s = a[0] + a[1] + a[2] + a[3];
+    if (s == 1.2345f) sink[0] = s;
+}
+
 template <class L>
 float time_launch(L launch, cudaStream_t st)
 {
@@ -86,7 +109,8 @@ float time_launch(L launch, cudaStream_t st)
 extern "C" {
 
 /* out[0] FP64 FMA TFLOP/s, out[1] FP32 FMA TFLOP/s, out[2..7] cost of one FP64 sqrt, divide,
- * log, atan2, sincos, acos in FP64-FMA time units (each counted as 2 flops) */
+ * log, atan2, sincos, acos in FP64-FMA time units, out[8..12] cost of one FP32 sqrtf, divide,
+ * log1pf, atan2f, logf in FP32-FMA time units (out must hold 13 doubles) */
 i2_status i2_calibrate_pipes(double *out)
 {
     if (!out) return I2_ERR_INVALID_ARGUMENT;
@@ -116,6 +140,16 @@ i2_status i2_calibrate_pipes(double *out)
     tf[4] = time_launch([&] { k_fn<4><<<blocks, tpb, 0, st>>>(itf, sink); }, st);
     tf[5] = time_launch([&] { k_fn<5><<<blocks, tpb, 0, st>>>(itf, sink); }, st);
     for (int f = 0; f < 6; ++f) out[2 + f] = tf[f] / (threads * itf * 4) / fma_ms;
+    // FP32: time of one sqrtf, divide, log1pf, atan2f, logf in units of one FP32 FMA
+    const int itf32 = 4096;
+    const double ffma_ms = t32 / (threads * (double)it32 * kChains);
+    float tg[5];
+    tg[0] = time_launch([&] { k_fnf<0><<<blocks, tpb, 0, st>>>(itf32, (float *)sink); }, st);
+    tg[1] = time_launch([&] { k_fnf<1><<<blocks, tpb, 0, st>>>(itf32, (float *)sink); }, st);
+    tg[2] = time_launch([&] { k_fnf<2><<<blocks, tpb, 0, st>>>(itf32, (float *)sink); }, st);
+    tg[3] = time_launch([&] { k_fnf<3><<<blocks, tpb, 0, st>>>(itf32, (float *)sink); }, st);
+    tg[4] = time_launch([&] { k_fnf<4><<<blocks, tpb, 0, st>>>(itf32, (float *)sink); }, st);
+    for (int f = 0; f < 5; ++f) out[8 + f] = tg[f] / (threads * (double)itf32 * 4) / ffma_ms;
     const cudaError_t e = cudaGetLastError();
     cudaFree(sink);
     cudaStreamDestroy(st);

@@ -250,6 +250,7 @@ struct i2_mesh {
     DevBuf<double> dV;
     DevBuf<int> dC;
     DevBuf<i2::Panel> dPanels;
+    DevBuf<i2::PanelF> dPanelsF;
     int nv() const { return (int)(V.size() / 3); }
     int nc() const { return (int)(C.size() / 3); }
 };
@@ -260,7 +261,7 @@ struct i2_integrator {
     int order = 7;
     i2::RunConfig cfg;
     int precision = I2_PRECISION_FP64;
-    int pot_nu = 10, pot_nv = 8, pot_grade = 3, pot_nself = 16;
+    int pot_nu = 10, pot_nv = 8, pot_grade = 3, pot_nself = 24;
     i2::QuadTables tables() const
     {
         i2::QuadTables Q;
@@ -329,6 +330,7 @@ struct ClassResult {
 
 struct Workspace {
     DevBuf<double> cur, fin_a, fin_b, sing, padj;
+    DevBuf<float> ctx_e;
     DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list, tier2_list;
     DevBuf<int2> pairs;
 };
@@ -486,10 +488,37 @@ void upload_mesh(i2_mesh &m)
     m.dPanels.reserve(m.nc());
     I2_CHECK_CUDA(cudaMemcpy(m.dV.ptr, m.V.data(), m.V.size() * sizeof(double), cudaMemcpyHostToDevice));
     I2_CHECK_CUDA(cudaMemcpy(m.dC.ptr, m.C.data(), m.C.size() * sizeof(int), cudaMemcpyHostToDevice));
+    m.dPanelsF.reserve(m.nc());
     i2::launch_prepare_panels(m.nc(), m.dV.ptr, m.dC.ptr, m.dPanels.ptr, 0);
+    i2::launch_prepare_panels_f32(m.nc(), m.dV.ptr, m.dC.ptr, m.dPanelsF.ptr, 0);
     I2_CHECK_CUDA(cudaGetLastError());
     I2_CHECK_CUDA(cudaDeviceSynchronize());
     m.on_device = true;
+}
+
+i2::QuadTablesF tables_f32(const i2::QuadTables &Q)
+{
+    i2::QuadTablesF F;
+    std::memset(&F, 0, sizeof F);
+    F.npts = Q.npts;
+    for (int g = 0; g < Q.npts; ++g) {
+        F.L1[g] = (float)Q.L1[g];
+        F.L2[g] = (float)Q.L2[g];
+        F.L3[g] = (float)Q.L3[g];
+        F.w[g] = (float)Q.w[g];
+    }
+    F.nu = Q.nu;
+    F.nv = Q.nv;
+    F.lo_nu = Q.lo_nu;
+    F.lo_nv = Q.lo_nv;
+    F.hi_nu = Q.hi_nu;
+    F.hi_nv = Q.hi_nv;
+    for (int k = 0; k < i2::kMaxDuffy; ++k) {
+        F.du_u[k] = (float)Q.du_u[k]; F.du_w[k] = (float)Q.du_w[k]; F.dv_v[k] = (float)Q.dv_v[k]; F.dv_w[k] = (float)Q.dv_w[k];
+        F.lo_u[k] = (float)Q.lo_u[k]; F.lo_uw[k] = (float)Q.lo_uw[k]; F.lo_v[k] = (float)Q.lo_v[k]; F.lo_vw[k] = (float)Q.lo_vw[k];
+        F.hi_u[k] = (float)Q.hi_u[k]; F.hi_uw[k] = (float)Q.hi_uw[k]; F.hi_v[k] = (float)Q.hi_v[k]; F.hi_vw[k] = (float)Q.hi_vw[k];
+    }
+    return F;
 }
 
 i2_pair_class checked_class(int cls)
@@ -507,7 +536,6 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
     if (!ev->mesh->on_device) upload_mesh(const_cast<i2_mesh &>(*ev->mesh));
     const i2_mesh &m = *ev->mesh;
     I2_REQUIRE(n >= 0 && n < (1LL << 31), I2_ERR_INVALID_ARGUMENT, "pair count out of range");
-    I2_REQUIRE(ev->integrator->precision == I2_PRECISION_FP64, I2_ERR_UNSUPPORTED, "mixed precision is not available in this build");
     ClassResult &R = ev->results[cls];
     R.n = n;
     R.errors.clear();
@@ -535,6 +563,7 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         W.padj.reserve(n);
         W.hard_list.reserve(n);
         W.tier2_list.reserve(n);
+        if (ev->integrator->precision == I2_PRECISION_MIXED) W.ctx_e.reserve(3 * n);
     }
     // cnt[0..7] active counts per level, cnt[8] hard pairs, cnt[9] adaptive-potential stack overflows
     I2_CHECK_CUDA(cudaMemsetAsync(W.cnt.ptr, 0, 16 * sizeof(int), ev->stream));
@@ -544,6 +573,8 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
     A.pairs = d_pairs;
     A.cells = reinterpret_cast<const int3 *>(m.dC.ptr);
     A.panels = m.dPanels.ptr;
+    A.panels_f = m.dPanelsF.ptr;
+    A.ctx_e = W.ctx_e.ptr;
     A.cur = W.cur.ptr;
     A.fin_a = W.fin_a.ptr;
     A.fin_b = W.fin_b.ptr;
@@ -561,6 +592,8 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         A.tier2_list = W.tier2_list.ptr;
         A.tier2_cnt = W.cnt.ptr + 10;
         A.tier_tol = 10.0 * cfg.hard_tol;
+        // FP32 rounding of the tier-1 Duffy sums is a few 1e-8 of |P|; keep the agreement bar above it
+        if (ev->integrator->precision == I2_PRECISION_MIXED) A.tier_tol = std::max(A.tier_tol, 2e-7);
     }
     A.raw4 = out_raw;
     A.J3 = out_J;
@@ -573,7 +606,12 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         ev->persistent_blocks = std::max(1, sms) * 8;
     }
     const i2::QuadTables Q = ev->integrator->tables();
-    i2::launch_class_fp64(cls, A, Q, cfg, ev->persistent_blocks, ev->stream);
+    if (ev->integrator->precision == I2_PRECISION_MIXED) {
+        const i2::QuadTablesF Qf = tables_f32(Q);
+        i2::launch_class_mixed(cls, A, Q, Qf, cfg, ev->persistent_blocks, ev->stream);
+    } else {
+        i2::launch_class_fp64(cls, A, Q, cfg, ev->persistent_blocks, ev->stream);
+    }
     I2_CHECK_CUDA(cudaGetLastError());
     if (cls == I2_SELF) I2_CHECK_CUDA(cudaMemsetAsync(R.level.ptr, 0xff, n * sizeof(int), ev->stream));
     // keep the evaluator's copies coherent when the caller supplied output buffers

@@ -1,0 +1,144 @@
+// i2_device_f32.cuh -- FP32 geometry and integrands of the mixed-precision form.
+//
+// Each cell gets a 160-byte FP32 panel record (10 x float4) written once from the FP64 mesh:
+//   [0] A_hi.xyz, S     [1] A_lo.xyz, 2S    [2] B_hi.xyz, |C-B|   [3] B_lo.xyz, |A-C|
+//   [4] C_hi.xyz, |B-A| [5] C_lo.xyz, -     [6] n.xyz, -          [7..9] ta, tb, tc (unit edges)
+// Vertices are stored as unevaluated float sums hi + lo (double-float), so the offset of a
+// point of K_i from a vertex of K_j is formed in FP32 as (a_hi - b_hi) + (a_lo - b_lo) without
+// FP64 work and without the cancellation of subtracting two rounded absolute coordinates.
+// Edge log terms use a log1p form whose argument is a ratio of sums of positive terms only
+// (q_P - q_Q equals the edge length exactly), so no term of the FP32 evaluation cancels.
+#pragma once
+
+#include "i2_device.cuh"
+
+namespace i2 {
+
+struct f3 {
+    float x, y, z;
+};
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return f3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return f3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator*(float s, f3 a) { return f3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ float dotf(f3 a, f3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
+__device__ __forceinline__ f3 crossf(f3 a, f3 b) { return f3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+__device__ __forceinline__ float normf(f3 a) { return sqrtf(dotf(a, a)); }
+__device__ __forceinline__ f3 xyzf(float4 v) { return f3{v.x, v.y, v.z}; }
+__device__ __forceinline__ f3 to_f3(d3 a) { return f3{(float)a.x, (float)a.y, (float)a.z}; }
+
+struct alignas(16) PanelF {
+    float4 v[10];
+};
+static_assert(sizeof(PanelF) == 160, "FP32 panel record is 160 bytes");
+
+// FP32 view of K_j: offsets are measured from vertex A; B - A and C - A as FP32 vectors
+struct PanelJf {
+    f3 AB, AC, n, ta, tb, tc;
+    float S, lenA, lenB, lenC;
+};
+
+__device__ __forceinline__ f3 df_sub(float4 ahi, float4 alo, float4 bhi, float4 blo)
+{
+    return f3{(ahi.x - bhi.x) + (alo.x - blo.x), (ahi.y - bhi.y) + (alo.y - blo.y), (ahi.z - bhi.z) + (alo.z - blo.z)};
+}
+
+// offsets of the three vertices of panel p (cell pi) from vertex k (0..2) of panel q
+__device__ __forceinline__ void df_offsets(const PanelF *__restrict__ P, int pi, int qj, int k, f3 &a, f3 &b, f3 &c)
+{
+    const float4 *u = P[pi].v, *w = P[qj].v;
+    const float4 rh = w[2 * k], rl = w[2 * k + 1];
+    a = df_sub(u[0], u[1], rh, rl);
+    b = df_sub(u[2], u[3], rh, rl);
+    c = df_sub(u[4], u[5], rh, rl);
+}
+
+// offset of vertex k of panel q from vertex m of panel q
+__device__ __forceinline__ f3 df_edge(const PanelF *__restrict__ P, int q, int k, int m)
+{
+    const float4 *w = P[q].v;
+    return df_sub(w[2 * k], w[2 * k + 1], w[2 * m], w[2 * m + 1]);
+}
+
+__device__ __forceinline__ PanelJf load_panel_f(const PanelF *__restrict__ P, int c)
+{
+    const float4 *w = P[c].v;
+    PanelJf r;
+    r.AB = df_sub(w[2], w[3], w[0], w[1]);
+    r.AC = df_sub(w[4], w[5], w[0], w[1]);
+    r.S = w[0].w;
+    r.lenA = w[2].w;
+    r.lenB = w[3].w;
+    r.lenC = w[4].w;
+    r.n = xyzf(w[6]);
+    r.ta = xyzf(w[7]);
+    r.tb = xyzf(w[8]);
+    r.tc = xyzf(w[9]);
+    return r;
+}
+
+// ln((l_P + q_P) / (l_Q + q_Q)) for the edge P -> Q of length L, q = (x - P).tau:
+// log1p(delta) with delta from positive sums only (q_P - q_Q = L)
+__device__ __forceinline__ float edge_log_f32(float lP, float qP, f3 oP, float lQ, float qQ, f3 tau, float L)
+{
+    const float s = lP + lQ;
+    float d;
+    if (qQ >= 0.0f) {
+        d = L * (s + qP + qQ) / (s * (lQ + qQ));
+    } else if (qP <= 0.0f) {
+        d = L * (s - qP - qQ) / (s * (lP - qP));
+    } else {
+        const f3 r = crossf(oP, tau);
+        d = (lP + qP) * L * (s - qP - qQ) / (s * dotf(r, r));
+    }
+    return log1pf(d);
+}
+
+struct FarCtxF {
+    f3 ma, mb, mc;
+};
+
+// theta/psi (a1) and the potential integrand from the offsets to K_j's vertices
+__device__ __forceinline__ void far_integrand_f(f3 oa, f3 ob, f3 oc, const PanelJf &K, const FarCtxF &F, f3 &psi, float &th,
+                                                float &pot)
+{
+    const float la = normf(oa), lb = normf(ob), lc = normf(oc);
+    const float Lc = edge_log_f32(la, dotf(oa, K.tc), oa, lb, dotf(ob, K.tc), K.tc, K.lenC);  // A -> B
+    const float La = edge_log_f32(lb, dotf(ob, K.ta), ob, lc, dotf(oc, K.ta), K.ta, K.lenA);  // B -> C
+    const float Lb = edge_log_f32(lc, dotf(oc, K.tb), oc, la, dotf(oa, K.tb), K.tb, K.lenB);  // C -> A
+    psi = Lc * K.tc + La * K.ta + Lb * K.tb;
+    const float d = dotf(K.n, oa);
+    const float den = la * lb * lc + dotf(oa, ob) * lc + dotf(ob, oc) * la + dotf(oc, oa) * lb;
+    th = 2.0f * atan2f(2.0f * K.S * d, den);
+    const float ta_ = -dotf(F.ma, ob), tb_ = -dotf(F.mb, oc), tc_ = -dotf(F.mc, oa);
+    pot = ta_ * La + tb_ * Lb + tc_ * Lc - d * th;
+}
+
+// Kahan-compensated FP32 accumulator of (Psi, Theta, potential)
+struct kahan5 {
+    float s[5], c[5];
+};
+__device__ __forceinline__ void kahan_zero(kahan5 &k)
+{
+#pragma unroll
+    for (int i = 0; i < 5; ++i) k.s[i] = k.c[i] = 0.0f;
+}
+__device__ __forceinline__ void kahan_add(kahan5 &k, int i, float v)
+{
+    const float y = v - k.c[i];
+    const float t = k.s[i] + y;
+    k.c[i] = (t - k.s[i]) - y;
+    k.s[i] = t;
+}
+
+struct QuadTablesF {
+    float L1[kMaxGauss], L2[kMaxGauss], L3[kMaxGauss], w[kMaxGauss];
+    int npts;
+    float du_u[kMaxDuffy], du_w[kMaxDuffy], dv_v[kMaxDuffy], dv_w[kMaxDuffy];
+    int nu, nv;
+    float lo_u[kMaxDuffy], lo_uw[kMaxDuffy], lo_v[kMaxDuffy], lo_vw[kMaxDuffy];
+    int lo_nu, lo_nv;
+    float hi_u[kMaxDuffy], hi_uw[kMaxDuffy], hi_v[kMaxDuffy], hi_vw[kMaxDuffy];
+    int hi_nu, hi_nv;
+};
+
+} // namespace i2

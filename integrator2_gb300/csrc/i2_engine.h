@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include "i2_device.cuh"
+#include "i2_device_f32.cuh"
 
 namespace i2 {
 
@@ -29,6 +30,8 @@ struct ClassArgs {
     const int2 *pairs = nullptr;  // (i, j) per pair
     const int3 *cells = nullptr;
     const Panel *panels = nullptr;
+    const PanelF *panels_f = nullptr;         // FP32 panel records (mixed precision)
+    float *ctx_e = nullptr;                   // per-pair direction e of common-vertex pairs (mixed precision)
     // per-pair state: regular-part sums (Psi, Theta, potential)
     double *cur = nullptr, *fin_a = nullptr, *fin_b = nullptr;
     int *stop = nullptr;
@@ -49,7 +52,14 @@ struct ClassArgs {
 };
 
 void launch_prepare_panels(int nc, const double *V, const int *C, Panel *out, cudaStream_t s);
+void launch_prepare_panels_f32(int nc, const double *V, const int *C, PanelF *out, cudaStream_t s);
 void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks,
                        cudaStream_t s);
+void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const QuadTablesF &Qf, const RunConfig &cfg,
+                        int persistent_blocks, cudaStream_t s);
+// kernels shared by both forms
+void launch_finalize(int cls, const ClassArgs &A, int mode, cudaStream_t s);
+void launch_self(const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, cudaStream_t s);
+void launch_pot_hard(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s);
 
 } // namespace i2

@@ -441,7 +441,11 @@ __global__ void __launch_bounds__(32 * kHardWarps) k_pot_hard(ClassArgs A, QuadT
         for (int guard = 0; guard < 1 << 20; ++guard) {
             const int n = top[w];
             if (n == 0) break;
-            const int take = n < 32 ? n : 32;
+            // each popped item may push 4: popping k items grows the stack by at most 3k, so
+            // k <= (capacity - n) / 3 keeps every push in bounds (n <= capacity - 3 always holds)
+            const int room = (kHardCap - n) / 3;
+            int take = n < 32 ? n : 32;
+            if (take > room) take = room > 1 ? room : 1;
             HardItem it;
             const bool has = lane < take;
             if (has) it = stack[w][n - take + lane];
@@ -460,7 +464,7 @@ __global__ void __launch_bounds__(32 * kHardWarps) k_pot_hard(ClassArgs A, QuadT
                 int pos = 0;
                 if (!accept) {
                     pos = atomicAdd(&top[w], 4);
-                    if (pos + 4 > kHardCap) {
+                    if (pos + 4 > kHardCap) {  // cannot happen with the throttle above; kept as a guard
                         atomicSub(&top[w], 4);
                         atomicAdd(A.hard_overflow, 1);
                         accept = true;
@@ -484,7 +488,8 @@ __global__ void __launch_bounds__(32 * kHardWarps) k_pot_hard(ClassArgs A, QuadT
 // J(K_i, K_i): tangential part 0 by antisymmetry; normal part 0 (principal value) or the
 // one-sided limit +-(1/4pi) 2 pi S_i n_i.  Potential: with d = 0 the inner potential is
 // sum_e t_e L_e; per edge, int_K t_e L_e dS = int_e dl_y int_0^pi sin(phi) R(phi,y)^2/2 dphi
-// with the phi integral in closed form on the two sides the ray can hit.
+// with the phi integral in closed form on the two sides the ray can hit and the edge integral
+// by graded Gauss-Legendre on the pieces on either side of the foot of the altitude.
 __device__ __forceinline__ double ray_side(double a, double alpha, double u1)
 {
     double sa, ca;
@@ -515,15 +520,25 @@ __global__ void __launch_bounds__(128) k_self(ClassArgs A, QuadTables Q, int sel
         const d3 tau = (1.0 / L) * (P2 - P1);
         const double al1 = angle_ref(P2 - P1, P3 - P1);
         const double al2 = angle_ref(P1 - P2, P3 - P2);
+        // split at the foot of the altitude from P3, where the angle to P3 swings fastest
+        const double foot = dot(P3 - P1, tau);
+        const bool split = foot > 1e-12 * L && foot < (1.0 - 1e-12) * L;
         double acc = 0.0;
 #pragma unroll 1
-        for (int k = 0; k < Q.nself; ++k) {
-            const double b = L * Q.sx[k], a = L - b;
-            const d3 y = P1 + b * tau;
-            const double phis = angle_ref(tau, P3 - y);
-            acc += Q.sw[k] * (ray_side(a, al2, phis + al2) + ray_side(b, al1, (kPi - phis) + al1));
+        for (int piece = 0; piece < (split ? 2 : 1); ++piece) {
+            const double lo = split && piece == 1 ? foot : 0.0;
+            const double span = split ? (piece == 0 ? foot : L - foot) : L;
+            double part = 0.0;
+#pragma unroll 1
+            for (int k = 0; k < Q.nself; ++k) {
+                const double b = lo + span * Q.sx[k], a = L - b;
+                const d3 y = P1 + b * tau;
+                const double phis = angle_ref(tau, P3 - y);
+                part += Q.sw[k] * (ray_side(a, al2, phis + al2) + ray_side(b, al1, (kPi - phis) + al1));
+            }
+            acc += span * part;
         }
-        total += L * acc;
+        total += acc;
     }
     A.P[t] = kInv4Pi * total;
 }
@@ -592,6 +607,25 @@ static void level_chain(const ClassArgs &A, const QuadTables &Q, const RunConfig
         k_level<CLS><<<persistent_blocks, tpb, 0, s>>>(B, Q, lev, cfg.mode, cfg.tol, cfg.max_level);
     }
     k_finalize<CLS><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, cfg.mode);
+}
+
+void launch_finalize(int cls, const ClassArgs &A, int mode, cudaStream_t s)
+{
+    const int tpb = 128;
+    if (cls == kEdge) k_finalize<kEdge><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, mode);
+    else if (cls == kVertex) k_finalize<kVertex><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, mode);
+    else k_finalize<kFar><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, mode);
+}
+
+void launch_self(const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, cudaStream_t s)
+{
+    k_self<<<blocks_for(A.n, 128), 128, 0, s>>>(A, Q, cfg.self_sign);
+}
+
+void launch_pot_hard(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s)
+{
+    if (cls == kEdge) k_pot_hard<kEdge><<<persistent_blocks / 4, 32 * kHardWarps, 0, s>>>(A, Q, cfg.hard_tol);
+    else k_pot_hard<kVertex><<<persistent_blocks / 4, 32 * kHardWarps, 0, s>>>(A, Q, cfg.hard_tol);
 }
 
 void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s)

@@ -1,0 +1,504 @@
+// i2_kernels_mixed.cu -- mixed-precision form of the pair-integral path (sm_103a).
+//
+// FP32: the regular-part quadrature of every class (the bulk of the work), with per-pair
+//       offsets formed from double-float vertices, cancellation-free edge logs and
+//       Kahan-compensated accumulation; the graded-Duffy potential of adjacent pairs (tiers 1-2).
+// FP64: the closed-form singular parts of common-edge / common-vertex pairs (once per pair),
+//       the refinement error estimator (convergence test on the compensated sums), hard
+//       (folded / sliver) adjacent pairs' adaptive potential, self pairs.
+// The kernel chain per class mirrors the FP64 form (i2_kernels_fp64.cu) and shares its
+// finalisation, self and adaptive-potential kernels.
+#include "i2_device_f32.cuh"
+#include "i2_engine.h"
+
+namespace i2 {
+
+__global__ void k_prepare_panels_f32(int nc, const double *__restrict__ V, const int *__restrict__ C, PanelF *__restrict__ out)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    d3 P[3];
+    for (int k = 0; k < 3; ++k) {
+        const int v = C[3 * c + k];
+        P[k] = mk(V[3 * v], V[3 * v + 1], V[3 * v + 2]);
+    }
+    const d3 cr = cross(P[1] - P[0], P[2] - P[0]);
+    const d3 n = unit(cr);
+    const double S = norm(cr) * 0.5;
+    const d3 ea = P[2] - P[1], eb = P[0] - P[2], ec = P[1] - P[0];
+    PanelF p;
+    const double lens[3] = {norm(ea), norm(eb), norm(ec)};
+    for (int k = 0; k < 3; ++k) {
+        const float hx = (float)P[k].x, hy = (float)P[k].y, hz = (float)P[k].z;
+        const float lx = (float)(P[k].x - hx), ly = (float)(P[k].y - hy), lz = (float)(P[k].z - hz);
+        p.v[2 * k] = make_float4(hx, hy, hz, k == 0 ? (float)S : (float)lens[k - 1]);
+        p.v[2 * k + 1] = make_float4(lx, ly, lz, k == 0 ? (float)(2.0 * S) : (k == 1 ? (float)lens[1] : 0.0f));
+    }
+    // [2].w = |C-B|, [3].w = |A-C|, [4].w = |B-A|
+    p.v[2].w = (float)lens[0];
+    p.v[3].w = (float)lens[1];
+    p.v[4].w = (float)lens[2];
+    p.v[6] = make_float4((float)n.x, (float)n.y, (float)n.z, 0.0f);
+    const d3 ta = unit(ea), tb = unit(eb), tc = unit(ec);
+    p.v[7] = make_float4((float)ta.x, (float)ta.y, (float)ta.z, 0.0f);
+    p.v[8] = make_float4((float)tb.x, (float)tb.y, (float)tb.z, 0.0f);
+    p.v[9] = make_float4((float)tc.x, (float)tc.y, (float)tc.z, 0.0f);
+    out[c] = p;
+}
+
+// ------------------------------------------------------------------ FP32 fused regular parts
+struct EdgeCtxF {
+    f3 AB, AC;       // JB - JA, JC - JA (offsets are taken from JA, the vertex off the shared edge)
+    f3 ta, tb, tc;   // unit(JA - JC), unit(JB - JA), unit(JC - JB)
+    float ilvc;
+};
+struct VertexCtxF {
+    f3 AB, AC;       // JB - JA, JC - JA (JA = shared vertex)
+    f3 ta, tb, tbc, e;
+    float inv_sqrt_si, lenBC;
+};
+
+__device__ __forceinline__ f3 unitf(f3 a)
+{
+    const float inv = 1.0f / normf(a);
+    return inv * a;
+}
+
+__device__ __forceinline__ void edge_integrand_f(f3 oA, f3 oB, f3 oC, const PanelJf &K, const EdgeCtxF &E, f3 &psi, float &th)
+{
+    const float lA = normf(oA), lB = normf(oB), lC = normf(oC);
+    const float l1 = logf((lA + dotf(oA, E.tb)) * E.ilvc);
+    const float l2 = logf((lA - dotf(oA, E.ta)) * E.ilvc);
+    psi = l1 * E.tb + l2 * E.ta;
+    const float den = lA * lB * lC + dotf(oA, oB) * lC + dotf(oB, oC) * lA + dotf(oC, oA) * lB;
+    const float s1 = atan2f(dotf(crossf(oB, E.tb), E.tc), dotf(E.tb - E.tc, lB * E.tb + oB));
+    const float s2 = atan2f(dotf(crossf(oC, E.ta), E.tc), dotf(E.ta - E.tc, lC * E.ta - oC));
+    th = 2.0f * atan2f(2.0f * K.S * dotf(K.n, oA), den) - 2.0f * (s1 - s2);
+}
+
+__device__ __forceinline__ void vertex_integrand_f(f3 oA, f3 oB, f3 oC, const PanelJf &K, const VertexCtxF &Vx, f3 &psi, float &th)
+{
+    const float lA = normf(oA), lB = normf(oB), lC = normf(oC);
+    const float Lbc = edge_log_f32(lB, dotf(oB, Vx.tbc), oB, lC, dotf(oC, Vx.tbc), Vx.tbc, Vx.lenBC);
+    const float l1 = logf((lC + dotf(oC, Vx.ta)) * Vx.inv_sqrt_si);
+    const float l2 = logf((lB - dotf(oB, Vx.tb)) * Vx.inv_sqrt_si);
+    psi = Lbc * Vx.tbc + l1 * Vx.ta + l2 * Vx.tb;
+    const float den = lA * lB * lC + dotf(oA, oB) * lC + dotf(oB, oC) * lA + dotf(oC, oA) * lB;
+    const float s1 = atan2f(dotf(crossf(oA, Vx.ta), Vx.e), dotf(lA * Vx.e - oA, Vx.e - Vx.ta));
+    const float s2 = atan2f(dotf(crossf(oA, Vx.tb), Vx.e), dotf(lA * Vx.e - oA, Vx.e + Vx.tb));
+    th = 2.0f * atan2f(2.0f * K.S * dotf(K.n, oA), den) - 2.0f * (s1 + s2);
+}
+
+struct TriF {
+    f3 a, b, c;
+};
+__device__ __forceinline__ TriF childf(const TriF &t, int k)
+{
+    const f3 mbc = 0.5f * (t.b + t.c), mca = 0.5f * (t.c + t.a), mab = 0.5f * (t.a + t.b);
+    switch (k) {
+    case 0: return TriF{mab, t.b, mbc};
+    case 1: return TriF{mbc, t.c, mca};
+    case 2: return TriF{mca, t.a, mab};
+    default: return TriF{mbc, mca, mab};
+    }
+}
+__device__ __forceinline__ TriF subcellf(TriF t, int level, int s)
+{
+    for (int l = level - 1; l >= 0; --l) t = childf(t, (s >> (2 * l)) & 3);
+    return t;
+}
+
+__device__ __forceinline__ acc5 shfl_xor5m(acc5 a, int off)
+{
+    acc5 r;
+    r.px = __shfl_xor_sync(0xffffffffu, a.px, off);
+    r.py = __shfl_xor_sync(0xffffffffu, a.py, off);
+    r.pz = __shfl_xor_sync(0xffffffffu, a.pz, off);
+    r.th = __shfl_xor_sync(0xffffffffu, a.th, off);
+    r.pot = __shfl_xor_sync(0xffffffffu, a.pot, off);
+    return r;
+}
+
+__device__ __forceinline__ d3 finalize_j_m(int cls, d3 psi, double th, d3 nj, double Si)
+{
+    if (cls == kVertex) {
+        int p = 0;
+        const double ref = kTwoPi * Si;
+        if (th > ref) p = -((int)trunc((th - ref) / (2.0 * ref)) + 1);
+        else if (th < -ref) p = ((int)trunc((-ref - th) / (2.0 * ref)) + 1);
+        th = th + 2.0 * p * ref;
+    }
+    return kInv4Pi * (th * nj + cross(psi, nj));
+}
+
+// one refinement level of the regular part, FP32 evaluation, FP64 bookkeeping (same contract
+// as k_level of the FP64 form)
+template <int CLS>
+__global__ void __launch_bounds__(256) k_level_mixed(ClassArgs A, QuadTablesF Qf, int level, int mode, double tol, int kmax)
+{
+    const int nsub = 1 << (2 * level);
+    const int G = nsub < 32 ? nsub : 32;
+    const int per_lane = nsub / G;
+    const bool listed = A.act_in != nullptr;
+    const int count = listed ? *A.cnt_in : A.n;
+    const long long total = (long long)count * G;
+    const long long total_r = (total + 31) & ~31LL;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const float sub_scale = ldexpf(1.0f, -2 * level);
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total_r; idx += stride) {
+        const bool valid = idx < total;
+        const int slot = (int)(idx / G);
+        const int lane_g = (int)(idx % G);
+        const int t = valid ? (listed ? A.act_in[slot] : slot) : 0;
+        acc5 acc = zero5();
+        int2 pr = make_int2(0, 0);
+        if (valid) {
+            pr = A.pairs[t];
+            const PanelJf K = load_panel_f(A.panels_f, pr.y);
+            const float Ssub = A.panels_f[pr.x].v[0].w * sub_scale;
+            int origin = 0;  // vertex of K_j the offsets are measured from
+            EdgeCtxF E;
+            VertexCtxF Vx;
+            FarCtxF F;
+            if (CLS == kFar) {
+                F = FarCtxF{crossf(K.ta, K.n), crossf(K.tb, K.n), crossf(K.tc, K.n)};
+            } else {
+                const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
+                int si, sj;
+                if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
+                else shifts_vertex(ci, cj, si, sj);
+                origin = sj;
+                const f3 AB = df_edge(A.panels_f, pr.y, (sj + 1) % 3, sj), AC = df_edge(A.panels_f, pr.y, (sj + 2) % 3, sj);
+                if (CLS == kEdge) {
+                    E.AB = AB;
+                    E.AC = AC;
+                    E.ta = unitf(-1.0f * AC);
+                    E.tb = unitf(AB);
+                    const f3 bc = AC - AB;
+                    E.ilvc = 1.0f / normf(bc);
+                    E.tc = E.ilvc * bc;
+                } else {
+                    Vx.AB = AB;
+                    Vx.AC = AC;
+                    Vx.ta = unitf(-1.0f * AC);
+                    Vx.tb = unitf(AB);
+                    const f3 bc = AC - AB;
+                    Vx.lenBC = normf(bc);
+                    Vx.tbc = (1.0f / Vx.lenBC) * bc;
+                    const float *e = A.ctx_e + 3 * (long long)t;
+                    Vx.e = f3{e[0], e[1], e[2]};
+                    Vx.inv_sqrt_si = rsqrtf(A.panels_f[pr.x].v[0].w);
+                }
+            }
+            // K_i's vertices as offsets from each vertex of K_j, in the (rotated) order the
+            // integrand expects: every point-to-vertex offset keeps full relative precision
+            TriF T0, T1, T2;
+            df_offsets(A.panels_f, pr.x, pr.y, origin, T0.a, T0.b, T0.c);
+            df_offsets(A.panels_f, pr.x, pr.y, (origin + 1) % 3, T1.a, T1.b, T1.c);
+            df_offsets(A.panels_f, pr.x, pr.y, (origin + 2) % 3, T2.a, T2.b, T2.c);
+            kahan5 ks;
+            kahan_zero(ks);
+            for (int s = lane_g * per_lane; s < (lane_g + 1) * per_lane; ++s) {
+                const TriF U0 = subcellf(T0, level, s), U1 = subcellf(T1, level, s), U2 = subcellf(T2, level, s);
+                float c0 = 0, c1 = 0, c2 = 0, c3 = 0, c4 = 0;
+#pragma unroll 1
+                for (int g = 0; g < Qf.npts; ++g) {
+                    const float l1 = Qf.L1[g], l2 = Qf.L2[g], l3 = Qf.L3[g];
+                    const f3 oA = l1 * U0.a + l2 * U0.b + l3 * U0.c;
+                    const f3 oB = l1 * U1.a + l2 * U1.b + l3 * U1.c;
+                    const f3 oC = l1 * U2.a + l2 * U2.b + l3 * U2.c;
+                    f3 psi;
+                    float th, pot = 0.0f;
+                    if (CLS == kFar) far_integrand_f(oA, oB, oC, K, F, psi, th, pot);
+                    else if (CLS == kEdge) edge_integrand_f(oA, oB, oC, K, E, psi, th);
+                    else vertex_integrand_f(oA, oB, oC, K, Vx, psi, th);
+                    const float w = Qf.w[g];
+                    c0 = fmaf(w, psi.x, c0);
+                    c1 = fmaf(w, psi.y, c1);
+                    c2 = fmaf(w, psi.z, c2);
+                    c3 = fmaf(w, th, c3);
+                    c4 = fmaf(w, pot, c4);
+                }
+                kahan_add(ks, 0, Ssub * c0);
+                kahan_add(ks, 1, Ssub * c1);
+                kahan_add(ks, 2, Ssub * c2);
+                kahan_add(ks, 3, Ssub * c3);
+                kahan_add(ks, 4, Ssub * c4);
+            }
+            acc.px = (double)ks.s[0] - (double)ks.c[0];
+            acc.py = (double)ks.s[1] - (double)ks.c[1];
+            acc.pz = (double)ks.s[2] - (double)ks.c[2];
+            acc.th = (double)ks.s[3] - (double)ks.c[3];
+            acc.pot = (double)ks.s[4] - (double)ks.c[4];
+        }
+        for (int off = 1; off < G; off <<= 1) {
+            const acc5 o = shfl_xor5m(acc, off);
+            acc.px += o.px; acc.py += o.py; acc.pz += o.pz; acc.th += o.th; acc.pot += o.pot;
+        }
+        if (!valid || lane_g != 0) continue;
+        double *cur = A.cur + 5 * (long long)t;
+        if (mode == kFixed || level == 0) {
+            cur[0] = acc.px; cur[1] = acc.py; cur[2] = acc.pz; cur[3] = acc.th; cur[4] = acc.pot;
+            continue;
+        }
+        const acc5 prev = acc5{cur[0], cur[1], cur[2], cur[3], cur[4]};
+        cur[0] = acc.px; cur[1] = acc.py; cur[2] = acc.pz; cur[3] = acc.th; cur[4] = acc.pot;
+        // FP64 error estimator (relative change of J and of the near-field potential)
+        const double4_32a nj4 = A.panels[pr.y].v[3];
+        const d3 nj = mk(nj4.x, nj4.y, nj4.z);
+        const double Si = A.panels[pr.x].v[0].w;
+        d3 spsi = mk(0, 0, 0);
+        double sth = 0.0;
+        if (CLS != kFar) {
+            const double *sg = A.sing + 4 * (long long)t;
+            spsi = mk(sg[0], sg[1], sg[2]);
+            sth = sg[3];
+        }
+        const d3 Jc = finalize_j_m(CLS, mk(acc.px, acc.py, acc.pz) + spsi, acc.th + sth, nj, Si);
+        const d3 dJ = kInv4Pi * ((acc.th - prev.th) * nj + cross(mk(acc.px - prev.px, acc.py - prev.py, acc.pz - prev.pz), nj));
+        bool unconv = norm(dJ) > tol * norm(Jc);
+        if (CLS == kFar) unconv = unconv || fabs(acc.pot - prev.pot) > tol * fabs(acc.pot);
+        atomicMax(A.maxlev, level);
+        if (!unconv || level >= kmax) {
+            A.stop[t] = level;
+            double *fa = A.fin_a + 5 * (long long)t, *fb = A.fin_b + 5 * (long long)t;
+            fa[0] = acc.px; fa[1] = acc.py; fa[2] = acc.pz; fa[3] = acc.th; fa[4] = acc.pot;
+            fb[0] = prev.px; fb[1] = prev.py; fb[2] = prev.pz; fb[3] = prev.th; fb[4] = prev.pot;
+        } else {
+            A.act_out[atomicAdd(A.cnt_out, 1)] = t;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ adjacent pairs: singular parts + FP32 Duffy potential
+// graded Duffy rule in FP32 over the pieces of K_i; point offsets to K_j's vertices are formed
+// as (apex - vertex) + w with the apex offsets exact in double-float, so graded points that sit
+// very close to a shared vertex keep their relative precision
+template <int CLS>
+__device__ float duffy_total_f(const PanelF *__restrict__ P, int pi, int pj, int si, const PanelJf &K, const FarCtxF &F,
+                               int p1_vertex, const f3 &m_in, float c, float h, const float *uu, const float *uw, int nu,
+                               const float *vv, const float *vw, int nv)
+{
+    f3 R0[3], R1[3], R2[3];  // K_i's vertices (rotated by si) as offsets from K_j's vertices 0, 1, 2
+    {
+        f3 a, b, cc;
+        df_offsets(P, pi, pj, 0, a, b, cc);
+        const f3 q0[3] = {a, b, cc};
+        df_offsets(P, pi, pj, 1, a, b, cc);
+        const f3 q1[3] = {a, b, cc};
+        df_offsets(P, pi, pj, 2, a, b, cc);
+        const f3 q2[3] = {a, b, cc};
+        for (int k = 0; k < 3; ++k) {
+            R0[k] = q0[(si + k) % 3];
+            R1[k] = q1[(si + k) % 3];
+            R2[k] = q2[(si + k) % 3];
+        }
+    }
+    float total = 0.0f;
+    const int npieces = CLS == kEdge ? 2 : 1;
+    for (int piece = 0; piece < npieces; ++piece) {
+        // apex slot and the two other corners of the piece, as offsets from K_j's vertex 0
+        int ap;
+        f3 B, Cc;
+        if (CLS == kVertex) { ap = 0; B = R0[1]; Cc = R0[2]; }
+        else {
+            const f3 M = 0.5f * (R0[1] + R0[2]);
+            if (piece == 0) { ap = 1; B = M; Cc = R0[0]; }
+            else { ap = 2; B = R0[0]; Cc = M; }
+        }
+        const f3 dA = R0[ap], dB = R1[ap], dC = R2[ap];
+        const f3 eB = B - dA, eC = Cc - dA;
+        const float area2 = normf(crossf(eB, eC));
+        const f3 dP1 = p1_vertex == 0 ? dA : (p1_vertex == 1 ? dB : dC);
+        float acc = 0.0f;
+#pragma unroll 1
+        for (int a = 0; a < nu; ++a) {
+            const float u = uu[a];
+            float row = 0.0f;
+#pragma unroll 1
+            for (int b = 0; b < nv; ++b) {
+                const f3 w = u * ((1.0f - vv[b]) * eB + vv[b] * eC);
+                f3 psi;
+                float th, g;
+                far_integrand_f(dA + w, dB + w, dC + w, K, F, psi, th, g);
+                if (CLS == kEdge) {
+                    const float sd = dotf(dP1 + w, m_in);
+                    if (sd > 0.0f) g += 2.0f * c * sd * logf(sd / h);
+                }
+                row = fmaf(vw[b], g, row);
+            }
+            acc = fmaf(uw[a] * u, row, acc);
+        }
+        total = fmaf(area2, acc, total);
+    }
+    return total;
+}
+
+// s ln s term along the shared edge of a common-edge pair, set up in FP64 once per pair
+__device__ __forceinline__ void edge_sigma_setup(const ClassArgs &A, int2 pr, int si, int sj, const PanelJf &Kf, double Si, f3 &m_in,
+                                                 float &c, float &h, double &sig)
+{
+    const PanelJ K = load_panel(A.panels, pr.y);
+    const Tri Ti0 = load_tri(A.panels, pr.x);
+    const d3 Pi[3] = {Ti0.a, Ti0.b, Ti0.c}, Pj[3] = {K.A, K.B, K.C};
+    const d3 JB = Pj[(sj + 1) % 3], JC = Pj[(sj + 2) % 3], IA = Pi[si];
+    const d3 tau = unit(JC - JB), m = cross(tau, K.n), w = IA - JB;
+    const d3 perp = w - dot(w, tau) * tau;
+    const double hd = norm(perp);
+    const d3 mi = (1.0 / hd) * perp;
+    const double cd = -dot(m, mi);
+    m_in = to_f3(mi);
+    c = (float)cd;
+    h = (float)hd;
+    sig = (5.0 / 9.0) * cd * Si * hd;
+    (void)Kf;
+}
+
+template <int CLS>
+__global__ void __launch_bounds__(128) k_singular_mixed(ClassArgs A, QuadTablesF Qf)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= A.n) return;
+    const int2 pr = A.pairs[t];
+    const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
+    const PanelJ Kd = load_panel(A.panels, pr.y);
+    const double4_32a ni4 = A.panels[pr.x].v[3];
+    const d3 ni = mk(ni4.x, ni4.y, ni4.z);
+    const double Si = A.panels[pr.x].v[0].w;
+    int si, sj;
+    if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
+    else shifts_vertex(ci, cj, si, sj);
+    // FP64: closed-form singular part (a4 / a5) and, for the vertex class, the direction e
+    {
+        const Tri Ti0 = load_tri(A.panels, pr.x);
+        const Tri T0[3] = {Ti0, Tri{Ti0.b, Ti0.c, Ti0.a}, Tri{Ti0.c, Ti0.a, Ti0.b}};
+        const Tri Tj0 = Tri{Kd.A, Kd.B, Kd.C};
+        const Tri J0[3] = {Tj0, Tri{Tj0.b, Tj0.c, Tj0.a}, Tri{Tj0.c, Tj0.a, Tj0.b}};
+        d3 psi;
+        double th;
+        if (CLS == kEdge) closed_edge(T0[si], J0[sj], ni, Kd.n, Si, psi, th);
+        else {
+            closed_vertex(T0[si], J0[sj], ni, Kd.n, Si, psi, th);
+            const d3 ta = unit(J0[sj].a - J0[sj].c), tb = unit(J0[sj].b - J0[sj].a);
+            double dA, dB;
+            const d3 e = vertex_direction(ni, Kd.n, ta, tb, dA, dB);
+            float *ce = A.ctx_e + 3 * (long long)t;
+            ce[0] = (float)e.x; ce[1] = (float)e.y; ce[2] = (float)e.z;
+        }
+        double *sg = A.sing + 4 * (long long)t;
+        sg[0] = psi.x; sg[1] = psi.y; sg[2] = psi.z; sg[3] = th;
+    }
+    // FP32: tier 1 of the potential (main and check Duffy rules)
+    const PanelJf K = load_panel_f(A.panels_f, pr.y);
+    const FarCtxF F{crossf(K.ta, K.n), crossf(K.tb, K.n), crossf(K.tc, K.n)};
+    f3 m_in = f3{0, 0, 0};
+    float c = 0.0f, h = 1.0f;
+    double sig = 0.0;
+    const int p1v = (sj + 1) % 3;  // JB, start of the shared edge in K_j's orientation
+    if (CLS == kEdge) edge_sigma_setup(A, pr, si, sj, K, Si, m_in, c, h, sig);
+    const float pm = duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, K, F, p1v, m_in, c, h, Qf.du_u, Qf.du_w, Qf.nu, Qf.dv_v, Qf.dv_w, Qf.nv);
+    const double pmd = (double)pm + sig;
+    A.padj[t] = kInv4Pi * pmd;
+    if (A.hard_list) {
+        const double c10 = 0.98480775301220806;
+        if (dot(ni, Kd.n) < 0.5 || A.panels[pr.x].v[2].w > c10 || A.panels[pr.y].v[2].w > c10) {
+            A.hard_list[atomicAdd(A.hard_cnt, 1)] = t;
+        } else {
+            const float pl = duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, K, F, p1v, m_in, c, h, Qf.lo_u, Qf.lo_uw, Qf.lo_nu, Qf.lo_v,
+                                                Qf.lo_vw, Qf.lo_nv);
+            if (fabs(pmd - ((double)pl + sig)) > A.tier_tol * fabs(pmd)) A.tier2_list[atomicAdd(A.tier2_cnt, 1)] = t;
+        }
+    }
+}
+
+template <int CLS>
+__global__ void __launch_bounds__(128) k_pot_tier2_mixed(ClassArgs A, QuadTablesF Qf)
+{
+    const int count = *A.tier2_cnt;
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < count; h += gridDim.x * blockDim.x) {
+        const int t = A.tier2_list[h];
+        const int2 pr = A.pairs[t];
+        const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
+        int si, sj;
+        if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
+        else shifts_vertex(ci, cj, si, sj);
+        const PanelJf K = load_panel_f(A.panels_f, pr.y);
+        const FarCtxF F{crossf(K.ta, K.n), crossf(K.tb, K.n), crossf(K.tc, K.n)};
+        const double Si = A.panels[pr.x].v[0].w;
+        f3 m_in = f3{0, 0, 0};
+        float c = 0.0f, hh = 1.0f;
+        double sig = 0.0;
+        const int p1v = (sj + 1) % 3;
+        if (CLS == kEdge) edge_sigma_setup(A, pr, si, sj, K, Si, m_in, c, hh, sig);
+        const double ph = (double)duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, K, F, p1v, m_in, c, hh, Qf.hi_u, Qf.hi_uw, Qf.hi_nu,
+                                                     Qf.hi_v, Qf.hi_vw, Qf.hi_nv) + sig;
+        const double pm = A.padj[t] * (4.0 * kPi);
+        A.padj[t] = kInv4Pi * ph;
+        if (fabs(ph - pm) > A.tier_tol * fabs(ph)) A.hard_list[atomicAdd(A.hard_cnt, 1)] = t;
+    }
+}
+
+// ------------------------------------------------------------------ launchers
+static int blocks_for_m(long long n, int tpb) { return (int)((n + tpb - 1) / tpb); }
+
+void launch_prepare_panels_f32(int nc, const double *V, const int *C, PanelF *out, cudaStream_t s)
+{
+    if (nc > 0) k_prepare_panels_f32<<<blocks_for_m(nc, 128), 128, 0, s>>>(nc, V, C, out);
+}
+
+template <int CLS>
+static void level_chain_mixed(const ClassArgs &A, const QuadTablesF &Qf, const RunConfig &cfg, int persistent_blocks,
+                              cudaStream_t s)
+{
+    const int tpb = 256;
+    if (cfg.mode == kFixed) {
+        const long long work = (long long)A.n * (cfg.level <= 2 ? (1 << (2 * cfg.level)) : 32);
+        k_level_mixed<CLS><<<std::max(1, std::min(blocks_for_m(work, tpb), persistent_blocks * 8)), tpb, 0, s>>>(A, Qf, cfg.level, cfg.mode, cfg.tol,
+                                                                                                        cfg.max_level);
+        launch_finalize(CLS, A, cfg.mode, s);
+        return;
+    }
+    k_level_mixed<CLS><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf, 0, cfg.mode, cfg.tol, cfg.max_level);
+    ClassArgs B = A;
+    for (int lev = 1; lev <= cfg.max_level; ++lev) {
+        B.act_in = lev == 1 ? nullptr : (lev % 2 ? A.act_b : A.act_a);
+        B.cnt_in = lev == 1 ? nullptr : A.cnt + (lev - 1);
+        B.act_out = lev % 2 ? A.act_a : A.act_b;
+        B.cnt_out = A.cnt + lev;
+        k_level_mixed<CLS><<<persistent_blocks, tpb, 0, s>>>(B, Qf, lev, cfg.mode, cfg.tol, cfg.max_level);
+    }
+    launch_finalize(CLS, A, cfg.mode, s);
+}
+
+void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const QuadTablesF &Qf, const RunConfig &cfg,
+                        int persistent_blocks, cudaStream_t s)
+{
+    if (A.n <= 0) return;
+    const int tpb = 128;
+    switch (cls) {
+    case kSelf:
+        launch_self(A, Q, cfg, s);
+        break;
+    case kEdge:
+        k_singular_mixed<kEdge><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
+        if (A.hard_list) {
+            k_pot_tier2_mixed<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Qf);
+            launch_pot_hard(kEdge, A, Q, cfg, persistent_blocks, s);
+        }
+        level_chain_mixed<kEdge>(A, Qf, cfg, persistent_blocks, s);
+        break;
+    case kVertex:
+        k_singular_mixed<kVertex><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
+        if (A.hard_list) {
+            k_pot_tier2_mixed<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Qf);
+            launch_pot_hard(kVertex, A, Q, cfg, persistent_blocks, s);
+        }
+        level_chain_mixed<kVertex>(A, Qf, cfg, persistent_blocks, s);
+        break;
+    default:
+        level_chain_mixed<kFar>(A, Qf, cfg, persistent_blocks, s);
+        break;
+    }
+}
+
+} // namespace i2

@@ -606,16 +606,24 @@ double o_self_potential(const double *Ap, const double *Bp, const double *Cp, in
         v3 tau = scl(1.0 / L, sub(P2, P1));
         double al1 = o_angle(sub(P2, P1), sub(P3, P1));
         double al2 = o_angle(sub(P1, P2), sub(P3, P2));
+        /* split at the foot of the altitude from P3 (the angle to P3 swings fastest there) */
+        double foot = dot(sub(P3, P1), tau);
+        double cuts[3] = {0.0, L, L};
+        int nseg = 1;
+        if (foot > 1e-12 * L && foot < (1.0 - 1e-12) * L) { cuts[1] = foot; cuts[2] = L; nseg = 2; }
         double acc = 0.0;
-        for (int k = 0; k < nquad; ++k) {
-            /* graded map t -> t^2(3-2t) clusters nodes at both edge ends */
-            double t = 0.5 * (gx[k] + 1.0), wt = 0.5 * gw[k];
-            double tt = t * t * (3.0 - 2.0 * t), jac = 6.0 * t * (1.0 - t);
-            double b = L * tt, a = L - b;      /* b from P1, a from P2 */
-            v3 y = add(P1, scl(b, tau));
-            double phis = o_angle(tau, sub(P3, y));
-            double f = ray_side(a, al2, phis + al2) + ray_side(b, al1, (O_PI - phis) + al1);
-            acc += wt * jac * L * f;
+        for (int sgi = 0; sgi < nseg; ++sgi) {
+            double lo = cuts[sgi], span = cuts[sgi + 1] - cuts[sgi];
+            for (int k = 0; k < nquad; ++k) {
+                /* graded map t -> t^2(3-2t) clusters nodes at both ends of the piece */
+                double t = 0.5 * (gx[k] + 1.0), wt = 0.5 * gw[k];
+                double tt = t * t * (3.0 - 2.0 * t), jac = 6.0 * t * (1.0 - t);
+                double b = lo + span * tt, a = L - b;      /* b from P1, a from P2 */
+                v3 y = add(P1, scl(b, tau));
+                double phis = o_angle(tau, sub(P3, y));
+                double f = ray_side(a, al2, phis + al2) + ray_side(b, al1, (O_PI - phis) + al1);
+                acc += wt * jac * span * f;
+            }
         }
         total += acc;
     }
@@ -1034,7 +1042,7 @@ int o_integrate_class(int cls, int ntasks, const int *ti, const int *tj,
             v3 J = finalize_j(O_FAR, r, nj, S[i]);
             if (raw4) memcpy(raw4 + 4 * t, r.v, sizeof r.v);
             if (J3) { J3[3 * t] = J.x; J3[3 * t + 1] = J.y; J3[3 * t + 2] = J.z; }
-            if (P) P[t] = o_self_potential(&a.x, &b.x, &c.x, 64);
+            if (P) P[t] = o_self_potential(&a.x, &b.x, &c.x, 96);
             if (levels) levels[t] = 0;
             continue;
         }

@@ -22,7 +22,7 @@ def api():
     return A
 
 
-def run(api, V, C, cls, pairs, mode="fixed", level=0, tol=1e-6, max_level=5, rule=(10, 8, 3, 16), self_sign=0,
+def run(api, V, C, cls, pairs, mode="fixed", level=0, tol=1e-6, max_level=5, rule=(10, 8, 3, 24), self_sign=0,
         hard_tol=1e-8):
     m = api.Mesh3D()
     m.setGeometry(V, C)
