@@ -167,6 +167,30 @@ i2_status i2_evaluator_copy_results(const i2_evaluator_t *ev, i2_pair_class cls,
 i2_status i2_evaluator_output_results(const i2_evaluator_t *ev, i2_pair_class cls, i2_output_format format,
                                       const char *path);
 
+/* ------------------------------------------------------------------ batched form */
+/* Many (mesh, pair class) segments integrated together (no reference counterpart): the
+ * refinement levels of all segments run in ONE persistent cooperative kernel, the whole run is
+ * captured into a CUDA graph on the first i2_batch_run and replayed afterwards.  Settings
+ * (rule, error control, potential rule) come from the integrator given at creation; the
+ * batched form computes in mixed precision (FP32 bulk, FP64 singular parts, estimator and hard
+ * pairs) whatever the integrator's precision. */
+typedef struct i2_batch i2_batch_t;
+i2_status i2_batch_create(const i2_integrator_t *settings, i2_batch_t **out);
+void i2_batch_destroy(i2_batch_t *batch);
+i2_status i2_batch_set_stream(i2_batch_t *batch, void *stream);
+/* adds one segment (host rows, stride 2 or 3 int32); returns its index in *segment */
+i2_status i2_batch_add(i2_batch_t *batch, const i2_mesh_t *mesh, i2_pair_class cls, const int32_t *rows, int64_t n,
+                       int32_t row_stride, int32_t *segment);
+/* times the candidate launch shapes (threads per block, resident blocks per SM, lanes per pair)
+ * on the batch and keeps the fastest; the chosen shape is returned in shape[3] (may be NULL) */
+i2_status i2_batch_autotune(i2_batch_t *batch, int32_t *shape);
+/* enqueues the batch on its stream (graph replay after the first call); asynchronous */
+i2_status i2_batch_run(i2_batch_t *batch);
+/* 1 if the last run replayed a CUDA graph, 0 if it used direct launches */
+i2_status i2_batch_uses_graph(const i2_batch_t *batch, int32_t *uses_graph);
+i2_status i2_batch_result_count(const i2_batch_t *batch, int32_t segment, int64_t *n);
+i2_status i2_batch_copy_results(const i2_batch_t *batch, int32_t segment, i2_channel channel, double *out, int64_t n);
+
 /* ------------------------------------------------------------------ measurement */
 /* measured pipe peaks of the current GPU for the kernels' roofline (no reference counterpart):
  * out[0] FP64 FMA TFLOP/s, out[1] FP32 FMA TFLOP/s, out[2..7] time of one FP64 sqrt, divide,

@@ -53,6 +53,15 @@ SIGNATURES = {
     "i2_evaluator_result_count": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
     "i2_evaluator_copy_results": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, _i64]),
     "i2_evaluator_output_results": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _cp]),
+    "i2_batch_create": (ctypes.c_int, [_vp, _pp]),
+    "i2_batch_destroy": (None, [_vp]),
+    "i2_batch_set_stream": (ctypes.c_int, [_vp, _vp]),
+    "i2_batch_add": (ctypes.c_int, [_vp, _vp, ctypes.c_int, _vp, _i64, _i32, _vp]),
+    "i2_batch_autotune": (ctypes.c_int, [_vp, _vp]),
+    "i2_batch_run": (ctypes.c_int, [_vp]),
+    "i2_batch_uses_graph": (ctypes.c_int, [_vp, _vp]),
+    "i2_batch_result_count": (ctypes.c_int, [_vp, _i32, _vp]),
+    "i2_batch_copy_results": (ctypes.c_int, [_vp, _i32, ctypes.c_int, _vp, _i64]),
     "i2_calibrate_pipes": (ctypes.c_int, [_vp]),
 }
 

@@ -250,5 +250,74 @@ class EvaluatorJ3DK:
         return self._lib.i2_evaluator_output_results(self._h, int(cls), int(outputFormat), path.encode()) == 0
 
 
+class BatchEvaluator:
+    """Batched form (no reference counterpart): many (mesh, pair class) segments integrated
+    together by one persistent cooperative kernel per refinement sweep, captured in a CUDA graph
+    on the first run and replayed afterwards.  Settings come from the integrator given here;
+    the batch computes in mixed precision."""
+
+    def __init__(self, numIntegrator: NumericalIntegrator3D):
+        h = ctypes.c_void_p()
+        call("i2_batch_create", numIntegrator._h, ctypes.byref(h))
+        self._h = h
+        self._lib = _lib.lib()
+        self._keep = []  # meshes must outlive the batch
+        self.integrator = numIntegrator
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.i2_batch_destroy(self._h)
+            self._h = None
+
+    def setStream(self, stream_handle: int) -> None:
+        call("i2_batch_set_stream", self._h, ctypes.c_void_p(stream_handle))
+
+    def add(self, mesh: Mesh3D, cls: int, pairs) -> int:
+        rows = np.ascontiguousarray(np.asarray(pairs, np.int32))
+        stride = rows.shape[1] if rows.ndim == 2 else 2
+        seg = ctypes.c_int32()
+        call("i2_batch_add", self._h, mesh._h, int(cls), _p(rows), len(rows), int(stride), ctypes.byref(seg))
+        self._keep.append(mesh)
+        return int(seg.value)
+
+    def autotune(self):
+        """times the candidate launch shapes; returns (threads, blocks per SM, lanes per pair)"""
+        shape = np.zeros(3, np.int32)
+        call("i2_batch_autotune", self._h, _p(shape))
+        return tuple(int(x) for x in shape)
+
+    def run(self) -> None:
+        call("i2_batch_run", self._h)
+
+    def usesGraph(self) -> bool:
+        g = ctypes.c_int32()
+        call("i2_batch_uses_graph", self._h, ctypes.byref(g))
+        return bool(g.value)
+
+    def resultCount(self, segment: int) -> int:
+        n = ctypes.c_int64()
+        call("i2_batch_result_count", self._h, int(segment), ctypes.byref(n))
+        return int(n.value)
+
+    def _channel(self, segment: int, ch: int, width: int) -> np.ndarray:
+        n = self.resultCount(segment)
+        out = np.zeros(n * width)
+        if n:
+            call("i2_batch_copy_results", self._h, int(segment), ch, _p(out), n)
+        return out.reshape(n, width) if width > 1 else out
+
+    def getResults(self, segment: int) -> np.ndarray:
+        return self._channel(segment, _CH_J, 3)
+
+    def getIntegrals(self, segment: int) -> np.ndarray:
+        return self._channel(segment, _CH_RAW, 4)
+
+    def getPotentials(self, segment: int) -> np.ndarray:
+        return self._channel(segment, _CH_P, 1)
+
+    def getLevels(self, segment: int) -> np.ndarray:
+        return self._channel(segment, _CH_LEVEL, 1).astype(np.int32)
+
+
 def lastError() -> str:
     return _lib.lib().i2_last_error().decode()

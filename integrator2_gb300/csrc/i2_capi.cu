@@ -639,6 +639,80 @@ void run_class_host(i2_evaluator *ev, int cls, const int32_t *rows, int64_t n, i
 
 } // namespace
 
+
+// ------------------------------------------------------------------ batched form
+namespace {
+
+struct BatchSegment {
+    const i2_mesh *mesh = nullptr;
+    int cls = 0;
+    int64_t n = 0;
+    DevBuf<int2> pairs;
+    DevBuf<double> raw4, J, P, cur, fin_a, fin_b, sing, padj;
+    DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list, tier2_list, level;
+    DevBuf<float> ctx_e;
+    i2::ClassArgs args;
+};
+
+} // namespace
+
+struct i2_batch {
+    i2::RunConfig cfg;
+    i2::QuadTables Q;
+    i2::QuadTablesF Qf;
+    std::vector<std::unique_ptr<BatchSegment>> segs;
+    DevBuf<i2::BatchSeg> d_segs;
+    bool dirty = true;
+    cudaStream_t stream = 0;
+    int threads = 256, blocks_per_sm = 0, g_cap = 32, sms = 0;
+    cudaGraphExec_t graph = nullptr;
+    bool graph_tried = false, graph_ok = false, last_graph = false;
+    ~i2_batch()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+    }
+};
+
+namespace {
+
+void batch_prepare(i2_batch *b)
+{
+    if (!b->dirty) return;
+    if (b->sms == 0) {
+        int dev = 0;
+        I2_CHECK_CUDA(cudaGetDevice(&dev));
+        I2_CHECK_CUDA(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev));
+    }
+    std::vector<i2::BatchSeg> hs;
+    for (auto &sp : b->segs) hs.push_back(i2::BatchSeg{sp->args, sp->cls});
+    b->d_segs.reserve(std::max<size_t>(hs.size(), 1));
+    if (!hs.empty()) I2_CHECK_CUDA(cudaMemcpy(b->d_segs.ptr, hs.data(), hs.size() * sizeof(i2::BatchSeg), cudaMemcpyHostToDevice));
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    b->graph_tried = false;
+    b->dirty = false;
+}
+
+// the whole batch on a stream: counter resets, per-segment preludes, one cooperative level sweep
+void batch_enqueue(i2_batch *b, cudaStream_t s, int threads, int bps, int gcap)
+{
+    const int persistent = std::max(1, b->sms) * 8;
+    for (auto &sp : b->segs) {
+        if (sp->n == 0) continue;
+        I2_CHECK_CUDA(cudaMemsetAsync(sp->cnt.ptr, 0, 16 * sizeof(int), s));
+        I2_CHECK_CUDA(cudaMemsetAsync(sp->maxlev.ptr, 0, sizeof(int), s));
+        i2::launch_batch_prelude(sp->args, sp->cls, b->Q, b->Qf, b->cfg, persistent, s);
+    }
+    const int maxb = i2::batch_max_blocks_per_sm(threads);
+    I2_REQUIRE(maxb > 0, I2_ERR_CUDA, "batch kernel cannot be resident with this block size");
+    const int blocks = std::max(1, b->sms) * std::max(1, std::min(bps > 0 ? bps : maxb, maxb));
+    I2_CHECK_CUDA(i2::launch_batch_levels(b->d_segs.ptr, (int)b->segs.size(), b->Qf, b->cfg, blocks, threads, gcap, s));
+}
+
+} // namespace
+
 // ------------------------------------------------------------------ C-ABI
 extern "C" {
 
@@ -1036,6 +1110,202 @@ i2_status i2_evaluator_output_results(const i2_evaluator_t *ev, i2_pair_class cl
             }
             f << "\n";
         }
+    });
+}
+
+i2_status i2_batch_create(const i2_integrator_t *settings, i2_batch_t **out)
+{
+    return guarded([&] {
+        I2_REQUIRE(settings && out, I2_ERR_INVALID_ARGUMENT, "null argument");
+        auto b = std::make_unique<i2_batch>();
+        b->cfg = settings->cfg;
+        b->Q = settings->tables();
+        b->Qf = tables_f32(b->Q);
+        *out = b.release();
+    });
+}
+
+void i2_batch_destroy(i2_batch_t *batch) { delete batch; }
+
+i2_status i2_batch_set_stream(i2_batch_t *batch, void *stream)
+{
+    return guarded([&] {
+        I2_REQUIRE(batch, I2_ERR_INVALID_ARGUMENT, "null batch");
+        batch->stream = (cudaStream_t)stream;
+        if (batch->graph) {
+            cudaGraphExecDestroy(batch->graph);
+            batch->graph = nullptr;
+        }
+        batch->graph_tried = false;
+    });
+}
+
+i2_status i2_batch_add(i2_batch_t *batch, const i2_mesh_t *mesh, i2_pair_class cls, const int32_t *rows, int64_t n,
+                       int32_t row_stride, int32_t *segment)
+{
+    return guarded([&] {
+        I2_REQUIRE(batch && mesh && (n == 0 || rows), I2_ERR_INVALID_ARGUMENT, "null argument");
+        I2_REQUIRE(row_stride == 2 || row_stride == 3, I2_ERR_INVALID_ARGUMENT, "row stride must be 2 or 3");
+        I2_REQUIRE(mesh->prepared, I2_ERR_STATE, "mesh not prepared");
+        I2_REQUIRE(n >= 0 && n < (1LL << 31), I2_ERR_INVALID_ARGUMENT, "pair count out of range");
+        const int c = checked_class(cls);
+        if (!mesh->on_device) upload_mesh(const_cast<i2_mesh &>(*mesh));
+        const int nc = mesh->nc();
+        std::vector<int2> pr(n);
+        for (int64_t k = 0; k < n; ++k) {
+            const int i = rows[row_stride * k], j = rows[row_stride * k + 1];
+            I2_REQUIRE(i >= 0 && i < nc && j >= 0 && j < nc, I2_ERR_INVALID_ARGUMENT, "pair index outside the mesh");
+            pr[k] = make_int2(i, j);
+        }
+        auto sp = std::make_unique<BatchSegment>();
+        sp->mesh = mesh;
+        sp->cls = c;
+        sp->n = n;
+        const size_t m = std::max<int64_t>(n, 1);
+        sp->pairs.reserve(m);
+        if (n) I2_CHECK_CUDA(cudaMemcpy(sp->pairs.ptr, pr.data(), n * sizeof(int2), cudaMemcpyHostToDevice));
+        sp->raw4.reserve(4 * m); sp->J.reserve(3 * m); sp->P.reserve(m); sp->level.reserve(m);
+        sp->cur.reserve(5 * m); sp->fin_a.reserve(5 * m); sp->fin_b.reserve(5 * m);
+        sp->stop.reserve(m); sp->act_a.reserve(m); sp->act_b.reserve(m);
+        sp->cnt.reserve(16); sp->maxlev.reserve(1);
+        const bool adj = c == I2_SIMPLE_NEIGHBORS || c == I2_ATTACHED_NEIGHBORS;
+        if (adj) {
+            sp->sing.reserve(4 * m); sp->padj.reserve(m); sp->hard_list.reserve(m); sp->tier2_list.reserve(m); sp->ctx_e.reserve(3 * m);
+        }
+        i2::ClassArgs &A = sp->args;
+        A.n = (int)n;
+        A.pairs = sp->pairs.ptr;
+        A.cells = reinterpret_cast<const int3 *>(mesh->dC.ptr);
+        A.panels = mesh->dPanels.ptr;
+        A.panels_f = mesh->dPanelsF.ptr;
+        A.ctx_e = sp->ctx_e.ptr;
+        A.cur = sp->cur.ptr; A.fin_a = sp->fin_a.ptr; A.fin_b = sp->fin_b.ptr; A.stop = sp->stop.ptr;
+        A.act_a = sp->act_a.ptr; A.act_b = sp->act_b.ptr; A.cnt = sp->cnt.ptr; A.maxlev = sp->maxlev.ptr;
+        A.sing = sp->sing.ptr; A.padj = sp->padj.ptr;
+        if (adj && batch->cfg.hard_tol > 0) {
+            A.hard_list = sp->hard_list.ptr; A.hard_cnt = sp->cnt.ptr + 8; A.hard_overflow = sp->cnt.ptr + 9;
+            A.tier2_list = sp->tier2_list.ptr; A.tier2_cnt = sp->cnt.ptr + 10;
+            A.tier_tol = std::max(10.0 * batch->cfg.hard_tol, 2e-7);
+        }
+        A.raw4 = sp->raw4.ptr; A.J3 = sp->J.ptr; A.P = sp->P.ptr; A.level_out = sp->level.ptr;
+        if (segment) *segment = (int32_t)batch->segs.size();
+        batch->segs.push_back(std::move(sp));
+        batch->dirty = true;
+    });
+}
+
+i2_status i2_batch_autotune(i2_batch_t *batch, int32_t *shape)
+{
+    return guarded([&] {
+        I2_REQUIRE(batch, I2_ERR_INVALID_ARGUMENT, "null batch");
+        batch_prepare(batch);
+        cudaEvent_t e0, e1;
+        I2_CHECK_CUDA(cudaEventCreate(&e0));
+        I2_CHECK_CUDA(cudaEventCreate(&e1));
+        float best = 1e30f;
+        int bt = batch->threads, bb = batch->blocks_per_sm, bg = batch->g_cap;
+        for (int threads : {128, 256}) {
+            const int maxb = i2::batch_max_blocks_per_sm(threads);
+            for (int bps : {maxb, std::max(1, maxb / 2)}) {
+                for (int gcap : {8, 16, 32}) {
+                    batch_enqueue(batch, batch->stream, threads, bps, gcap);  // warm-up
+                    I2_CHECK_CUDA(cudaEventRecord(e0, batch->stream));
+                    batch_enqueue(batch, batch->stream, threads, bps, gcap);
+                    I2_CHECK_CUDA(cudaEventRecord(e1, batch->stream));
+                    I2_CHECK_CUDA(cudaEventSynchronize(e1));
+                    float ms = 0;
+                    I2_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                    if (ms < best) { best = ms; bt = threads; bb = bps; bg = gcap; }
+                }
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        batch->threads = bt;
+        batch->blocks_per_sm = bb;
+        batch->g_cap = bg;
+        if (batch->graph) { cudaGraphExecDestroy(batch->graph); batch->graph = nullptr; }
+        batch->graph_tried = false;
+        if (shape) { shape[0] = bt; shape[1] = bb; shape[2] = bg; }
+    });
+}
+
+i2_status i2_batch_run(i2_batch_t *batch)
+{
+    return guarded([&] {
+        I2_REQUIRE(batch, I2_ERR_INVALID_ARGUMENT, "null batch");
+        batch_prepare(batch);
+        if (!batch->graph_tried) {
+            batch->graph_tried = true;
+            // capture the whole batch once; a stream that cannot capture it runs direct launches
+            cudaStream_t cs = batch->stream;
+            bool own = false;
+            if (cs == 0) {
+                I2_CHECK_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+                own = true;
+            }
+            cudaGraph_t g = nullptr;
+            bool ok = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+            if (ok) {
+                try {
+                    batch_enqueue(batch, cs, batch->threads, batch->blocks_per_sm, batch->g_cap);
+                } catch (const Failure &) {
+                    ok = false;
+                }
+                const cudaError_t e = cudaStreamEndCapture(cs, &g);
+                ok = ok && e == cudaSuccess && g;
+            }
+            if (ok) ok = cudaGraphInstantiate(&batch->graph, g, 0) == cudaSuccess;
+            if (g) cudaGraphDestroy(g);
+            if (own) cudaStreamDestroy(cs);
+            cudaGetLastError();  // a refused capture leaves a sticky-free error code behind
+            batch->graph_ok = ok;
+            if (!ok && batch->graph) { cudaGraphExecDestroy(batch->graph); batch->graph = nullptr; }
+        }
+        if (batch->graph_ok) {
+            I2_CHECK_CUDA(cudaGraphLaunch(batch->graph, batch->stream));
+            batch->last_graph = true;
+        } else {
+            batch_enqueue(batch, batch->stream, batch->threads, batch->blocks_per_sm, batch->g_cap);
+            batch->last_graph = false;
+        }
+    });
+}
+
+i2_status i2_batch_uses_graph(const i2_batch_t *batch, int32_t *uses_graph)
+{
+    return guarded([&] {
+        I2_REQUIRE(batch && uses_graph, I2_ERR_INVALID_ARGUMENT, "null argument");
+        *uses_graph = batch->last_graph ? 1 : 0;
+    });
+}
+
+i2_status i2_batch_result_count(const i2_batch_t *batch, int32_t segment, int64_t *n)
+{
+    return guarded([&] {
+        I2_REQUIRE(batch && n, I2_ERR_INVALID_ARGUMENT, "null argument");
+        I2_REQUIRE(segment >= 0 && segment < (int)batch->segs.size(), I2_ERR_INVALID_ARGUMENT, "no such segment");
+        *n = batch->segs[segment]->n;
+    });
+}
+
+i2_status i2_batch_copy_results(const i2_batch_t *batch, int32_t segment, i2_channel channel, double *out, int64_t n)
+{
+    return guarded([&] {
+        I2_REQUIRE(batch && (n == 0 || out), I2_ERR_INVALID_ARGUMENT, "null argument");
+        I2_REQUIRE(segment >= 0 && segment < (int)batch->segs.size(), I2_ERR_INVALID_ARGUMENT, "no such segment");
+        const BatchSegment &S = *batch->segs[segment];
+        I2_REQUIRE(n == S.n, I2_ERR_INVALID_ARGUMENT, "count does not match the segment");
+        if (n == 0) return;
+        I2_CHECK_CUDA(cudaStreamSynchronize(batch->stream));
+        if (channel == I2_CHANNEL_J) I2_CHECK_CUDA(cudaMemcpy(out, S.J.ptr, 3 * n * sizeof(double), cudaMemcpyDeviceToHost));
+        else if (channel == I2_CHANNEL_P) I2_CHECK_CUDA(cudaMemcpy(out, S.P.ptr, n * sizeof(double), cudaMemcpyDeviceToHost));
+        else if (channel == I2_CHANNEL_RAW) I2_CHECK_CUDA(cudaMemcpy(out, S.raw4.ptr, 4 * n * sizeof(double), cudaMemcpyDeviceToHost));
+        else if (channel == I2_CHANNEL_LEVEL) {
+            std::vector<int> lv(n);
+            I2_CHECK_CUDA(cudaMemcpy(lv.data(), S.level.ptr, n * sizeof(int), cudaMemcpyDeviceToHost));
+            for (int64_t k = 0; k < n; ++k) out[k] = S.cls == I2_SELF ? -1 : lv[k];
+        } else throw Failure{I2_ERR_INVALID_ARGUMENT, "channel not available for batch segments"};
     });
 }
 

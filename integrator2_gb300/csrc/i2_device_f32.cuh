@@ -76,21 +76,25 @@ __device__ __forceinline__ PanelJf load_panel_f(const PanelF *__restrict__ P, in
     return r;
 }
 
-// ln((l_P + q_P) / (l_Q + q_Q)) for the edge P -> Q of length L, q = (x - P).tau:
-// log1p(delta) with delta from positive sums only (q_P - q_Q = L)
-__device__ __forceinline__ float edge_log_f32(float lP, float qP, f3 oP, float lQ, float qQ, f3 tau, float L)
+// ln((l_P + q_P) / (l_Q + q_Q)) for the edge P -> Q of length L, q = (x - P).tau, from sums
+// and products of positive terms only (q_P - q_Q = L):
+//   x beyond Q (q_Q >= 0) or before P (q_P <= 0): log1p(delta) with a positive delta;
+//   x projecting inside the edge: the ratio is (l_P + q_P)(l_Q - q_Q) / h^2, h the distance
+//   to the edge line, with h^2 = |o x tau|^2 taken from the NEARER endpoint (o_P x tau =
+//   o_Q x tau; from the far endpoint the cross product of a long offset cancels down to the
+//   short distance).  Close to the line (ratio > 2) the log of that product is exact to a few
+//   ulps; farther out log1p of (ratio - 1) keeps small logs accurate.  A point on the line
+//   itself (h = 0, where the caller's factor t_e is 0 too) gets a large finite value.
+__device__ __forceinline__ float edge_log_f32(float lP, float qP, f3 oP, float lQ, float qQ, f3 oQ, f3 tau, float L)
 {
     const float s = lP + lQ;
-    float d;
-    if (qQ >= 0.0f) {
-        d = L * (s + qP + qQ) / (s * (lQ + qQ));
-    } else if (qP <= 0.0f) {
-        d = L * (s - qP - qQ) / (s * (lP - qP));
-    } else {
-        const f3 r = crossf(oP, tau);
-        d = (lP + qP) * L * (s - qP - qQ) / (s * dotf(r, r));
-    }
-    return log1pf(d);
+    if (qQ >= 0.0f) return log1pf(L * (s + qP + qQ) / (s * (lQ + qQ)));
+    if (qP <= 0.0f) return log1pf(L * (s - qP - qQ) / (s * (lP - qP)));
+    const f3 r = crossf(lP < lQ ? oP : oQ, tau);
+    const float h2 = dotf(r, r);
+    const float num = (lP + qP) * (lQ - qQ);
+    if (num > 2.0f * h2) return logf(fminf(num / h2, 3.0e38f));
+    return log1pf((lP + qP) * L * (s - qP - qQ) / (s * h2));
 }
 
 struct FarCtxF {
@@ -102,9 +106,9 @@ __device__ __forceinline__ void far_integrand_f(f3 oa, f3 ob, f3 oc, const Panel
                                                 float &pot)
 {
     const float la = normf(oa), lb = normf(ob), lc = normf(oc);
-    const float Lc = edge_log_f32(la, dotf(oa, K.tc), oa, lb, dotf(ob, K.tc), K.tc, K.lenC);  // A -> B
-    const float La = edge_log_f32(lb, dotf(ob, K.ta), ob, lc, dotf(oc, K.ta), K.ta, K.lenA);  // B -> C
-    const float Lb = edge_log_f32(lc, dotf(oc, K.tb), oc, la, dotf(oa, K.tb), K.tb, K.lenB);  // C -> A
+    const float Lc = edge_log_f32(la, dotf(oa, K.tc), oa, lb, dotf(ob, K.tc), ob, K.tc, K.lenC);  // A -> B
+    const float La = edge_log_f32(lb, dotf(ob, K.ta), ob, lc, dotf(oc, K.ta), oc, K.ta, K.lenA);  // B -> C
+    const float Lb = edge_log_f32(lc, dotf(oc, K.tb), oc, la, dotf(oa, K.tb), oa, K.tb, K.lenB);  // C -> A
     psi = Lc * K.tc + La * K.ta + Lb * K.tb;
     const float d = dotf(K.n, oa);
     const float den = la * lb * lc + dotf(oa, ob) * lc + dotf(ob, oc) * la + dotf(oc, oa) * lb;

@@ -57,6 +57,16 @@ void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const R
                        cudaStream_t s);
 void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const QuadTablesF &Qf, const RunConfig &cfg,
                         int persistent_blocks, cudaStream_t s);
+// batched form: one segment = the pairs of one class of one mesh
+struct BatchSeg {
+    ClassArgs A;
+    int cls;
+};
+int batch_max_blocks_per_sm(int threads);
+cudaError_t launch_batch_levels(const BatchSeg *segs, int nseg, const QuadTablesF &Qf, const RunConfig &cfg, int blocks,
+                                int threads, int G_cap, cudaStream_t s);
+void launch_batch_prelude(const ClassArgs &A, int cls, const QuadTables &Q, const QuadTablesF &Qf, const RunConfig &cfg,
+                          int persistent_blocks, cudaStream_t s);
 // kernels shared by both forms
 void launch_finalize(int cls, const ClassArgs &A, int mode, cudaStream_t s);
 void launch_self(const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, cudaStream_t s);

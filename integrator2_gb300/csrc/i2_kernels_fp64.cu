@@ -11,6 +11,7 @@
 //                              to the next level's active list (device-side counter)
 //   k_finalize<CLS>            kept level, singular part, J = (Theta n_j + Psi x n_j)/4pi
 #include "i2_engine.h"
+#include "i2_finalize.cuh"
 
 namespace i2 {
 
@@ -64,25 +65,7 @@ __device__ __forceinline__ acc5 shfl_xor5(acc5 a, int off)
     return r;
 }
 
-__device__ __forceinline__ void store5(double *p, const acc5 &a)
-{
-    p[0] = a.px; p[1] = a.py; p[2] = a.pz; p[3] = a.th; p[4] = a.pot;
-}
-__device__ __forceinline__ acc5 load5(const double *p) { return acc5{p[0], p[1], p[2], p[3], p[4]}; }
 
-// J = (Theta n_j + Psi x n_j)/4pi, with the p-fix of the common-vertex class
-// (evaluatorJ3DK.cu:224-264)
-__device__ __forceinline__ d3 finalize_j(int cls, d3 psi, double th, d3 nj, double Si)
-{
-    if (cls == kVertex) {
-        int p = 0;
-        const double ref = kTwoPi * Si;
-        if (th > ref) p = -((int)trunc((th - ref) / (2.0 * ref)) + 1);
-        else if (th < -ref) p = ((int)trunc((-ref - th) / (2.0 * ref)) + 1);
-        th = th + 2.0 * p * ref;
-    }
-    return kInv4Pi * (th * nj + cross(psi, nj));
-}
 
 // Runge criterion of the reference on the regular-part sums (evaluator3d.cu:76-99 with
 // divide()/norm1() of cuda_math.cuh:270-300)
@@ -544,39 +527,15 @@ __global__ void __launch_bounds__(128) k_self(ClassArgs A, QuadTables Q, int sel
 }
 
 // ------------------------------------------------------------------ finalisation
+
 template <int CLS>
 __global__ void __launch_bounds__(128) k_finalize(ClassArgs A, int mode)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= A.n) return;
-    const int2 pr = A.pairs[t];
-    acc5 v;
-    if (mode == kFixed) {
-        v = load5(A.cur + 5 * (long long)t);
-    } else {
-        // compat: the reference swaps two buffers per iteration and rewrites only unconverged
-        // entries (evaluatorJ3DK.cu:966-1011), so a pair that stopped at level L keeps I_L when
-        // the class-wide loop ran an even number of further iterations, else I_{L-1}
-        const int K = *A.maxlev, L = A.stop[t];
-        const bool older = (mode == kAdaptiveCompat) && ((K - L) & 1);
-        v = load5((older ? A.fin_b : A.fin_a) + 5 * (long long)t);
-    }
-    d3 psi = mk(v.px, v.py, v.pz);
-    double th = v.th;
-    if (CLS != kFar) {
-        const double *sg = A.sing + 4 * (long long)t;
-        psi = psi + mk(sg[0], sg[1], sg[2]);
-        th += sg[3];
-    }
-    const double4_32a nj4 = A.panels[pr.y].v[3];
-    const d3 J = finalize_j(CLS, psi, th, mk(nj4.x, nj4.y, nj4.z), A.panels[pr.x].v[0].w);
-    double *raw = A.raw4 + 4 * (long long)t;
-    raw[0] = psi.x; raw[1] = psi.y; raw[2] = psi.z; raw[3] = th;
-    double *Jo = A.J3 + 3 * (long long)t;
-    Jo[0] = J.x; Jo[1] = J.y; Jo[2] = J.z;
-    A.P[t] = CLS == kFar ? kInv4Pi * v.pot : A.padj[t];
-    if (A.level_out) A.level_out[t] = mode == kFixed ? -1 : A.stop[t];
+    if (t < A.n) finalize_item<CLS>(A, mode, t);
 }
+
+
 
 // ------------------------------------------------------------------ host-side launchers
 static int blocks_for(long long n, int tpb) { return (int)((n + tpb - 1) / tpb); }

@@ -10,6 +10,9 @@
 // finalisation, self and adaptive-potential kernels.
 #include "i2_device_f32.cuh"
 #include "i2_engine.h"
+#include "i2_finalize.cuh"
+
+#include <cooperative_groups.h>
 
 namespace i2 {
 
@@ -79,7 +82,7 @@ __device__ __forceinline__ void edge_integrand_f(f3 oA, f3 oB, f3 oC, const Pane
 __device__ __forceinline__ void vertex_integrand_f(f3 oA, f3 oB, f3 oC, const PanelJf &K, const VertexCtxF &Vx, f3 &psi, float &th)
 {
     const float lA = normf(oA), lB = normf(oB), lC = normf(oC);
-    const float Lbc = edge_log_f32(lB, dotf(oB, Vx.tbc), oB, lC, dotf(oC, Vx.tbc), Vx.tbc, Vx.lenBC);
+    const float Lbc = edge_log_f32(lB, dotf(oB, Vx.tbc), oB, lC, dotf(oC, Vx.tbc), oC, Vx.tbc, Vx.lenBC);
     const float l1 = logf((lC + dotf(oC, Vx.ta)) * Vx.inv_sqrt_si);
     const float l2 = logf((lB - dotf(oB, Vx.tb)) * Vx.inv_sqrt_si);
     psi = Lbc * Vx.tbc + l1 * Vx.ta + l2 * Vx.tb;
@@ -119,33 +122,24 @@ __device__ __forceinline__ acc5 shfl_xor5m(acc5 a, int off)
     return r;
 }
 
-__device__ __forceinline__ d3 finalize_j_m(int cls, d3 psi, double th, d3 nj, double Si)
-{
-    if (cls == kVertex) {
-        int p = 0;
-        const double ref = kTwoPi * Si;
-        if (th > ref) p = -((int)trunc((th - ref) / (2.0 * ref)) + 1);
-        else if (th < -ref) p = ((int)trunc((-ref - th) / (2.0 * ref)) + 1);
-        th = th + 2.0 * p * ref;
-    }
-    return kInv4Pi * (th * nj + cross(psi, nj));
-}
 
 // one refinement level of the regular part, FP32 evaluation, FP64 bookkeeping (same contract
-// as k_level of the FP64 form)
+// as k_level of the FP64 form).  Work items are (pair, lane of its lane group) over a grid-stride
+// loop starting at `first` with stride `stride` (multiples of 32), so the same body serves the
+// per-class kernels and the batched persistent kernel.
 template <int CLS>
-__global__ void __launch_bounds__(256) k_level_mixed(ClassArgs A, QuadTablesF Qf, int level, int mode, double tol, int kmax)
+__device__ void level_items_mixed(const ClassArgs &A, const QuadTablesF &Qf, int level, int mode, double tol, int kmax,
+                                  long long first, long long stride, int G_cap)
 {
     const int nsub = 1 << (2 * level);
-    const int G = nsub < 32 ? nsub : 32;
+    const int G = nsub < G_cap ? nsub : G_cap;
     const int per_lane = nsub / G;
     const bool listed = A.act_in != nullptr;
     const int count = listed ? *A.cnt_in : A.n;
     const long long total = (long long)count * G;
     const long long total_r = (total + 31) & ~31LL;
-    const long long stride = (long long)gridDim.x * blockDim.x;
     const float sub_scale = ldexpf(1.0f, -2 * level);
-    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total_r; idx += stride) {
+    for (long long idx = first; idx < total_r; idx += stride) {
         const bool valid = idx < total;
         const int slot = (int)(idx / G);
         const int lane_g = (int)(idx % G);
@@ -254,7 +248,7 @@ __global__ void __launch_bounds__(256) k_level_mixed(ClassArgs A, QuadTablesF Qf
             spsi = mk(sg[0], sg[1], sg[2]);
             sth = sg[3];
         }
-        const d3 Jc = finalize_j_m(CLS, mk(acc.px, acc.py, acc.pz) + spsi, acc.th + sth, nj, Si);
+        const d3 Jc = finalize_j(CLS, mk(acc.px, acc.py, acc.pz) + spsi, acc.th + sth, nj, Si);
         const d3 dJ = kInv4Pi * ((acc.th - prev.th) * nj + cross(mk(acc.px - prev.px, acc.py - prev.py, acc.pz - prev.pz), nj));
         bool unconv = norm(dJ) > tol * norm(Jc);
         if (CLS == kFar) unconv = unconv || fabs(acc.pot - prev.pot) > tol * fabs(acc.pot);
@@ -268,6 +262,13 @@ __global__ void __launch_bounds__(256) k_level_mixed(ClassArgs A, QuadTablesF Qf
             A.act_out[atomicAdd(A.cnt_out, 1)] = t;
         }
     }
+}
+
+template <int CLS>
+__global__ void __launch_bounds__(256) k_level_mixed(ClassArgs A, QuadTablesF Qf, int level, int mode, double tol, int kmax)
+{
+    level_items_mixed<CLS>(A, Qf, level, mode, tol, kmax, (long long)blockIdx.x * blockDim.x + threadIdx.x,
+                           (long long)gridDim.x * blockDim.x, 32);
 }
 
 // ------------------------------------------------------------------ adjacent pairs: singular parts + FP32 Duffy potential
@@ -498,6 +499,85 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
     default:
         level_chain_mixed<kFar>(A, Qf, cfg, persistent_blocks, s);
         break;
+    }
+}
+
+
+// ------------------------------------------------------------------ batched persistent kernel
+// One cooperative launch runs every refinement level of every (mesh, class) segment of a batch:
+// for each level, the whole grid sweeps the segments' active lists (grid-stride, lane groups of
+// min(4^L, G_cap) lanes per pair), then a grid-wide barrier; after the last level it finalises
+// every pair.  Converged pairs drop out of the lists, so the uneven work left by adaptive
+// refinement is spread over the whole GPU at every level, across meshes and classes.
+__global__ void __launch_bounds__(256) k_batch_levels(const BatchSeg *__restrict__ segs, int nseg, QuadTablesF Qf, int mode,
+                                                      int level_fixed, double tol, int kmax, int G_cap)
+{
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    const long long first = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const int lo = mode == kFixed ? level_fixed : 0, hi = mode == kFixed ? level_fixed : kmax;
+    for (int level = lo; level <= hi; ++level) {
+        for (int sgi = 0; sgi < nseg; ++sgi) {
+            const int cls = segs[sgi].cls;
+            if (cls == kSelf) continue;
+            ClassArgs A = segs[sgi].A;
+            if (A.n <= 0) continue;
+            if (mode != kFixed && level >= 1) {
+                A.act_in = level == 1 ? nullptr : (level % 2 ? A.act_b : A.act_a);
+                A.cnt_in = level == 1 ? nullptr : A.cnt + (level - 1);
+                A.act_out = level % 2 ? A.act_a : A.act_b;
+                A.cnt_out = A.cnt + level;
+            }
+            if (cls == kFar) level_items_mixed<kFar>(A, Qf, level, mode, tol, kmax, first, stride, G_cap);
+            else if (cls == kEdge) level_items_mixed<kEdge>(A, Qf, level, mode, tol, kmax, first, stride, G_cap);
+            else level_items_mixed<kVertex>(A, Qf, level, mode, tol, kmax, first, stride, G_cap);
+        }
+        grid.sync();
+    }
+    for (int sgi = 0; sgi < nseg; ++sgi) {
+        const int cls = segs[sgi].cls;
+        if (cls != kSelf) finalize_all(cls, segs[sgi].A, mode, first, stride);
+    }
+}
+
+int batch_max_blocks_per_sm(int threads)
+{
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_levels, threads, 0);
+    return nb;
+}
+
+cudaError_t launch_batch_levels(const BatchSeg *segs, int nseg, const QuadTablesF &Qf, const RunConfig &cfg, int blocks,
+                                int threads, int G_cap, cudaStream_t s)
+{
+    int mode = cfg.mode, level = cfg.level, kmax = cfg.max_level;
+    double tol = cfg.tol;
+    QuadTablesF q = Qf;
+    void *args[] = {(void *)&segs, (void *)&nseg, (void *)&q, (void *)&mode, (void *)&level, (void *)&tol, (void *)&kmax, (void *)&G_cap};
+    return cudaLaunchCooperativeKernel((const void *)k_batch_levels, dim3(blocks), dim3(threads), args, 0, s);
+}
+
+// the per-segment work that precedes the level sweep: singular parts, potential tiers, self pairs
+void launch_batch_prelude(const ClassArgs &A, int cls, const QuadTables &Q, const QuadTablesF &Qf, const RunConfig &cfg,
+                          int persistent_blocks, cudaStream_t s)
+{
+    if (A.n <= 0) return;
+    const int tpb = 128;
+    if (cls == kSelf) {
+        launch_self(A, Q, cfg, s);
+    } else if (cls == kEdge) {
+        k_singular_mixed<kEdge><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
+        if (A.hard_list) {
+            k_pot_tier2_mixed<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Qf);
+            launch_pot_hard(kEdge, A, Q, cfg, persistent_blocks, s);
+        }
+    } else if (cls == kVertex) {
+        k_singular_mixed<kVertex><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
+        if (A.hard_list) {
+            k_pot_tier2_mixed<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Qf);
+            launch_pot_hard(kVertex, A, Q, cfg, persistent_blocks, s);
+        }
     }
 }
 

@@ -1,0 +1,117 @@
+"""Batched form through the C-ABI: several meshes and every pair class in one batch (one
+persistent cooperative kernel for all refinement levels, CUDA graph replay) against the same
+segments run class by class in mixed precision, and against the oracle's high-order answer."""
+import numpy as np
+import pytest
+
+from tests._util import ensure_built, rel_rows
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def api():
+    ensure_built()
+    from integrator2_gb300 import api as A
+    return A
+
+
+def _meshes():
+    from integrator2_gb300 import meshes
+    return [meshes.jittered_icosphere(3, 0.15, 31),
+            meshes.sh_displaced_icosphere(2, 4, 0.1, 5),
+            meshes.torus(24, 8, 1.0, 0.3)]
+
+
+def _integrator(api, m, mode):
+    it = api.NumericalIntegrator3D(m, api.qf3D13)
+    if mode == "relative":
+        it.setErrorControl(api.RELATIVE_ERROR_CONTROL, 1e-6, 5)
+    else:
+        it.setFixedRefinementLevel(1)
+    it.setPrecision(api.PRECISION_MIXED)
+    return it
+
+
+@pytest.mark.parametrize("mode", ["fixed", "relative"])
+def test_batch_matches_per_class_runs(api, mode):
+    from integrator2_gb300 import pairs as P
+    meshes, segs = [], []
+    first = None
+    batch = None
+    for V, C in _meshes():
+        m = api.Mesh3D()
+        m.setGeometry(V, C)
+        m.prepareMesh(3.0)
+        meshes.append((m, V, C, P.build_pairs(V, C)))
+    it0 = _integrator(api, meshes[0][0], mode)
+    batch = api.BatchEvaluator(it0)
+    for m, V, C, pl in meshes:
+        for cls in (0, 1, 2, 3):
+            pr = pl.by_class(cls)
+            segs.append((m, cls, pr, batch.add(m, cls, pr)))
+    shape = batch.autotune()
+    assert shape[0] in (128, 256) and shape[2] in (8, 16, 32)
+    for rep in range(2):
+        batch.run()
+        got = [(batch.getResults(s), batch.getPotentials(s), batch.getLevels(s)) for _, _, _, s in segs]
+        if rep == 0:
+            first = got
+    # the replay (graph or direct) reproduces the first run exactly
+    for a, b in zip(first, got):
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    for (m, cls, pr, s), (J, Pb, lev) in zip(segs, got):
+        it = _integrator(api, m, mode)
+        ev = api.EvaluatorJ3DK(m, it)
+        ev.runClass(cls, pr)
+        J1, P1, l1 = ev.getResults(cls), ev.getPotentials(cls), ev.getLevels(cls)
+        assert len(J) == len(pr)
+        if cls == 3:
+            assert np.array_equal(J, J1) and np.array_equal(Pb, P1)
+            continue
+        # lane grouping may differ (autotuned), so the FP32 sums round differently
+        same = lev == l1
+        assert same.mean() > 0.995, (cls, same.mean())
+        assert rel_rows(J[same], J1[same]).max() < 1e-5, cls
+        assert (np.abs(Pb[same] - P1[same]) / np.abs(P1[same])).max() < 1e-5, cls
+
+
+def test_batch_accuracy_against_high_order(api):
+    from integrator2_gb300 import pairs as P
+    from oracle import oracle as O
+    V, C = _meshes()[1]
+    m = api.Mesh3D()
+    m.setGeometry(V, C)
+    m.prepareMesh(3.0)
+    pl = P.build_pairs(V, C)
+    batch = api.BatchEvaluator(_integrator(api, m, "relative"))
+    rng = np.random.default_rng(1)
+    picks = {}
+    for cls in (0, 1, 2):
+        pr = pl.by_class(cls)
+        pr = pr[np.sort(rng.choice(len(pr), min(200, len(pr)), replace=False))]
+        picks[cls] = (pr, batch.add(m, cls, pr))
+    batch.run()
+    for cls, (pr, s) in picks.items():
+        with O.potential_rule(10, 8, 3, adaptive=1e-11, depth=18, every_pair=True):
+            _, oJ, oP, _ = O.integrate(cls, pr, V, C, mode=O.FIXED, level=4)
+        eJ = rel_rows(batch.getResults(s), oJ)
+        eP = np.abs(batch.getPotentials(s) - oP) / np.abs(oP)
+        assert eJ.max() < 1e-5 and eP.max() < 1e-5, (cls, eJ.max(), eP.max())
+
+
+def test_batch_rejects_bad_input(api):
+    from integrator2_gb300 import meshes
+    V, C = meshes.icosphere(1)
+    m = api.Mesh3D()
+    m.setGeometry(V, C)
+    m.prepareMesh(3.0)
+    it = _integrator(api, m, "fixed")
+    batch = api.BatchEvaluator(it)
+    with pytest.raises(Exception):
+        batch.add(m, 2, np.array([[0, len(C)]], np.int32))
+    with pytest.raises(Exception):
+        batch.getResults(0)
+    s = batch.add(m, 2, np.zeros((0, 2), np.int32))
+    batch.run()
+    assert batch.resultCount(s) == 0

@@ -98,9 +98,11 @@ def test_potential_and_deep_levels_match_oracle(api, level):
 
 
 def test_adjacent_potential_against_high_order(api):
-    """product rule (Duffy 10 x 8 with grading 3; adaptive rule at 1e-8 for hard pairs) against
-    the oracle's high-order answer (Duffy 40 x 32; adaptive at 1e-10 for hard pairs): <= 1e-6.
-    sigma 0.3 jitter makes folded and sliver pairs."""
+    """product rule (tiered: Duffy 10 x 8 with grading 3, checked against 8 x 6 and 16 x 16,
+    adaptive rule at 1e-8 where they disagree or the pair is folded/sliver) against the oracle's
+    adaptive rule at 1e-11 on every pair: <= 1e-6.  sigma 0.3 jitter makes folded, sliver and
+    near-coplanar overlapping pairs; on the last kind a fixed Duffy rule converges erratically
+    (pair (229, 178): 40 x 32 is 9e-5 away from the converged value), so the truth is adaptive."""
     from integrator2_gb300 import meshes, pairs as P
     from oracle import oracle as O
     V, C = meshes.jittered_icosphere(3, 0.3, 4)
@@ -112,7 +114,8 @@ def test_adjacent_potential_against_high_order(api):
         nhard += hard.sum()
         sel = hard | (np.arange(len(pr)) % 7 == 0)
         _, _, Pg, _ = run(api, V, C, cls, pr[sel], "fixed", 0)
-        _, _, oP, _ = O.integrate(cls, pr[sel], V, C, mode=O.FIXED, level=0)
+        with O.potential_rule(10, 8, 3, adaptive=1e-11, depth=18, every_pair=True):
+            _, _, oP, _ = O.integrate(cls, pr[sel], V, C, mode=O.FIXED, level=0)
         err = np.abs(Pg - oP) / np.abs(oP)
         assert err.max() < 1e-6, (cls, err.max(), pr[sel][err.argmax()])
     assert nhard > 10
