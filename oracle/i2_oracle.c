@@ -721,8 +721,20 @@ static double pot_cell(const pot_ctx *c, v3 a, v3 b, v3 cc, int corner)
 
 /* children in the reference's split order; a parent corner in slot k moves to child
  * (k==1 ? 0 : k==2 ? 1 : 2) at slot 1 */
+/* cells split by the adaptive rule, per depth (work statistics for sizing the device queues) */
+static long long g_adapt_cells[32];
+void o_adapt_stats(long long *out32, int reset)
+{
+    for (int k = 0; k < 32; ++k) {
+        if (out32) out32[k] = g_adapt_cells[k];
+        if (reset) g_adapt_cells[k] = 0;
+    }
+}
+
 static double pot_adapt(const pot_ctx *c, v3 a, v3 b, v3 cc, int corner, double val, double tol_abs, int depth)
 {
+#pragma omp atomic
+    g_adapt_cells[depth < 31 ? depth : 31]++;
     v3 mbc = scl(0.5, add(b, cc)), mca = scl(0.5, add(cc, a)), mab = scl(0.5, add(a, b));
     v3 ch[4][3] = {{mab, b, mbc}, {mbc, cc, mca}, {mca, a, mab}, {mbc, mca, mab}};
     int cc_[4] = {-1, -1, -1, -1};

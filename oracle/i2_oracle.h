@@ -95,6 +95,8 @@ void o_task_integrand(int cls, int i, int j, const double *V, const int *C,
 double o_antisymmetry(const double *Jij, const double *Jji);
 
 int o_max_threads(void);
+/* cells visited by the adaptive potential rule per depth since the last reset */
+void o_adapt_stats(long long *out32, int reset);
 
 #ifdef __cplusplus
 }

@@ -72,6 +72,7 @@ def lib():
             L.o_set_potential_tiered.argtypes = [ctypes.c_double]
             L.o_pair_is_hard.argtypes = [i, i, vp, vp]
             L.o_pair_is_hard.restype = i
+            L.o_adapt_stats.argtypes = [vp, i]
             _lib = L
     return _lib
 
@@ -95,6 +96,13 @@ def ref_lib():
             R.refd_geometry.argtypes = [i, vp, i, vp, vp, vp]
             _ref = R
     return _ref
+
+
+def adapt_stats(reset=True):
+    """cells visited by the adaptive potential rule per depth since the last reset"""
+    out = np.zeros(32, np.int64)
+    lib().o_adapt_stats(_p(out), int(reset))
+    return out
 
 
 def cell_geometry(V, C):
