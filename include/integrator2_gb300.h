@@ -191,6 +191,25 @@ i2_status i2_batch_uses_graph(const i2_batch_t *batch, int32_t *uses_graph);
 i2_status i2_batch_result_count(const i2_batch_t *batch, int32_t segment, int64_t *n);
 i2_status i2_batch_copy_results(const i2_batch_t *batch, int32_t segment, i2_channel channel, double *out, int64_t n);
 
+/* ------------------------------------------------------------------ without allocation */
+/* No counterpart in the reference.  For callers that cannot allocate device memory (plugins in
+ * a host application that reserves the GPU's memory for its own pool; loops where cudaMalloc /
+ * cudaFree, which may synchronise the device, are not allowed): the disjoint class with
+ * relative error control and the 13-point rule, as i2_evaluator_run_class_device with
+ * I2_RELATIVE_ERROR_CONTROL, with every scratch buffer in one static device array of about
+ * 4.6 MB that each GPU loading the library holds until exit.  The caller passes device
+ * buffers: vertices (3 nv doubles), cells (3 nc int32, 0-based), pairs (2 n int32, 8-byte
+ * aligned, indices valid: they are read on the device only), J (3 n doubles) and P (n
+ * doubles).  Limits: nc <= I2_NOALLOC_MAX_CELLS, n <= I2_NOALLOC_MAX_PAIRS; larger inputs are
+ * rejected with I2_ERR_INVALID_ARGUMENT before any launch.  Asynchronous on `stream`.  The
+ * first call on a device looks up the array's device address (make it before any stream
+ * capture).  Every call shares the array: calls that overlap on the GPU race. */
+#define I2_NOALLOC_MAX_CELLS 8192
+#define I2_NOALLOC_MAX_PAIRS 16384
+i2_status i2_not_neighbors_noalloc(const double *d_vertices, int32_t nv, const int32_t *d_cells, int32_t nc,
+                                   const int32_t *d_pairs, int64_t n, double rel_tol, int32_t max_level, double *d_J,
+                                   double *d_P, void *stream);
+
 /* ------------------------------------------------------------------ measurement */
 /* measured pipe peaks of the current GPU for the kernels' roofline (no reference counterpart):
  * out[0] FP64 FMA TFLOP/s, out[1] FP32 FMA TFLOP/s, out[2..7] time of one FP64 sqrt, divide,

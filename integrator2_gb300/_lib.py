@@ -63,6 +63,7 @@ SIGNATURES = {
     "i2_batch_result_count": (ctypes.c_int, [_vp, _i32, _vp]),
     "i2_batch_copy_results": (ctypes.c_int, [_vp, _i32, ctypes.c_int, _vp, _i64]),
     "i2_calibrate_pipes": (ctypes.c_int, [_vp]),
+    "i2_not_neighbors_noalloc": (ctypes.c_int, [_vp, _i32, _vp, _i32, _vp, _i64, _d, _i32, _vp, _vp, _vp]),
 }
 
 _lock = threading.Lock()

@@ -713,6 +713,8 @@ void batch_enqueue(i2_batch *b, cudaStream_t s, int threads, int bps, int gcap)
 
 } // namespace
 
+void i2::set_last_error(const std::string &msg) { g_error = msg; }
+
 // ------------------------------------------------------------------ C-ABI
 extern "C" {
 

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string>
 
 #include "i2_device.cuh"
 #include "i2_device_f32.cuh"
@@ -67,6 +68,8 @@ cudaError_t launch_batch_levels(const BatchSeg *segs, int nseg, const QuadTables
                                 int threads, int G_cap, cudaStream_t s);
 void launch_batch_prelude(const ClassArgs &A, int cls, const QuadTables &Q, const QuadTablesF &Qf, const RunConfig &cfg,
                           int persistent_blocks, cudaStream_t s);
+// sets the thread's message returned by i2_last_error()
+void set_last_error(const std::string &msg);
 // kernels shared by both forms
 void launch_finalize(int cls, const ClassArgs &A, int mode, cudaStream_t s);
 void launch_self(const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, cudaStream_t s);
