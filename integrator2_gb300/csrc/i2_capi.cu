@@ -331,7 +331,9 @@ struct ClassResult {
 struct Workspace {
     DevBuf<double> cur, fin_a, fin_b, sing, padj;
     DevBuf<float> ctx_e;
-    DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list, tier2_list;
+    DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list, tier2_list, pot_qcnt;
+    DevBuf<i2::PotCellItem> pot_q_a, pot_q_b;
+    DevBuf<long long> pot_fx;
     DevBuf<int2> pairs;
 };
 
@@ -521,6 +523,11 @@ i2::QuadTablesF tables_f32(const i2::QuadTables &Q)
     return F;
 }
 
+// cells per depth list of the adaptive potential (24 bytes each): every hard pair seeds 4 cells
+// at depth 1; deeper lists hold a few tens of thousands of cells on the meshes measured (C2: at
+// most 27,516).  Capped at 2^26 cells (1.5 GB per list).
+size_t pot_queue_capacity(int64_t n) { return (size_t)std::min<int64_t>(std::max<int64_t>(4 * n, 1 << 18), 1 << 26); }
+
 i2_pair_class checked_class(int cls)
 {
     I2_REQUIRE(cls >= 0 && cls <= 3, I2_ERR_INVALID_ARGUMENT, "pair class must be 0..3");
@@ -563,7 +570,11 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         W.padj.reserve(n);
         W.hard_list.reserve(n);
         W.tier2_list.reserve(n);
-        if (ev->integrator->precision == I2_PRECISION_MIXED) W.ctx_e.reserve(3 * n);
+        W.pot_q_a.reserve(pot_queue_capacity(n));
+        W.pot_q_b.reserve(pot_queue_capacity(n));
+        W.pot_qcnt.reserve(16);
+        W.pot_fx.reserve(n);
+        if (ev->integrator->precision == I2_PRECISION_MIXED) W.ctx_e.reserve((size_t)i2::kVertexCtxFloats * n);
     }
     // cnt[0..7] active counts per level, cnt[8] hard pairs, cnt[9] adaptive-potential stack overflows
     I2_CHECK_CUDA(cudaMemsetAsync(W.cnt.ptr, 0, 16 * sizeof(int), ev->stream));
@@ -590,6 +601,11 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         A.hard_cnt = W.cnt.ptr + 8;
         A.hard_overflow = W.cnt.ptr + 9;
         A.tier2_list = W.tier2_list.ptr;
+        A.pot_q_a = W.pot_q_a.ptr;
+        A.pot_q_b = W.pot_q_b.ptr;
+        A.pot_qcap = (int)pot_queue_capacity(n);
+        A.pot_qcnt = W.pot_qcnt.ptr;
+        A.pot_fx = W.pot_fx.ptr;
         A.tier2_cnt = W.cnt.ptr + 10;
         A.tier_tol = 10.0 * cfg.hard_tol;
         // FP32 rounding of the tier-1 Duffy sums is a few 1e-8 of |P|; keep the agreement bar above it
@@ -649,7 +665,9 @@ struct BatchSegment {
     int64_t n = 0;
     DevBuf<int2> pairs;
     DevBuf<double> raw4, J, P, cur, fin_a, fin_b, sing, padj;
-    DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list, tier2_list, level;
+    DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list, tier2_list, level, pot_qcnt;
+    DevBuf<i2::PotCellItem> pot_q_a, pot_q_b;
+    DevBuf<long long> pot_fx;
     DevBuf<float> ctx_e;
     i2::ClassArgs args;
 };
@@ -1172,7 +1190,8 @@ i2_status i2_batch_add(i2_batch_t *batch, const i2_mesh_t *mesh, i2_pair_class c
         sp->cnt.reserve(16); sp->maxlev.reserve(1);
         const bool adj = c == I2_SIMPLE_NEIGHBORS || c == I2_ATTACHED_NEIGHBORS;
         if (adj) {
-            sp->sing.reserve(4 * m); sp->padj.reserve(m); sp->hard_list.reserve(m); sp->tier2_list.reserve(m); sp->ctx_e.reserve(3 * m);
+            sp->sing.reserve(4 * m); sp->padj.reserve(m); sp->hard_list.reserve(m); sp->tier2_list.reserve(m); sp->ctx_e.reserve((size_t)i2::kVertexCtxFloats * m);
+            sp->pot_q_a.reserve(pot_queue_capacity(m)); sp->pot_q_b.reserve(pot_queue_capacity(m)); sp->pot_qcnt.reserve(16); sp->pot_fx.reserve(m);
         }
         i2::ClassArgs &A = sp->args;
         A.n = (int)n;
@@ -1187,6 +1206,8 @@ i2_status i2_batch_add(i2_batch_t *batch, const i2_mesh_t *mesh, i2_pair_class c
         if (adj && batch->cfg.hard_tol > 0) {
             A.hard_list = sp->hard_list.ptr; A.hard_cnt = sp->cnt.ptr + 8; A.hard_overflow = sp->cnt.ptr + 9;
             A.tier2_list = sp->tier2_list.ptr; A.tier2_cnt = sp->cnt.ptr + 10;
+            A.pot_q_a = sp->pot_q_a.ptr; A.pot_q_b = sp->pot_q_b.ptr; A.pot_qcap = (int)pot_queue_capacity(m);
+            A.pot_qcnt = sp->pot_qcnt.ptr; A.pot_fx = sp->pot_fx.ptr;
             A.tier_tol = std::max(10.0 * batch->cfg.hard_tol, 2e-7);
         }
         A.raw4 = sp->raw4.ptr; A.J3 = sp->J.ptr; A.P = sp->P.ptr; A.level_out = sp->level.ptr;

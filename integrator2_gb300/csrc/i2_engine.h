@@ -13,6 +13,10 @@ namespace i2 {
 
 // pair classes (values of the reference's neighbour_type_enum, src/Mesh3d.cuh:18-23, plus self)
 enum { kVertex = 0, kEdge = 1, kFar = 2, kSelf = 3 };
+// depth cap of the adaptive potential rule (sub-cell paths of up to 24 bits)
+constexpr int kHardMaxDepth = 12;
+// floats per common-vertex pair in ClassArgs::ctx_e
+constexpr int kVertexCtxFloats = 16;
 // refinement / error-control modes
 enum { kFixed = 0, kAdaptiveCompat = 1, kAdaptiveRelative = 2 };
 
@@ -25,6 +29,15 @@ struct RunConfig {
     double hard_tol = 1e-8;  // relative tolerance of the adaptive potential of hard adjacent pairs (0: off)
 };
 
+// one cell of the breadth-first adaptive potential rule of hard adjacent pairs
+struct PotCellItem {
+    unsigned long long path;  // base-4 digits of the sub-cell of K_i, first split most significant
+    double val;               // the cell's integral by its own rule
+    int h;                    // slot in the hard-pair list (-1: empty slot left by a full list)
+    int corner;               // slot of the shared vertex in this cell, -1 if none
+};
+static_assert(sizeof(PotCellItem) == 24, "queue item is 24 bytes");
+
 // everything a class's kernel chain reads and writes (device pointers)
 struct ClassArgs {
     int n = 0;
@@ -32,7 +45,8 @@ struct ClassArgs {
     const int3 *cells = nullptr;
     const Panel *panels = nullptr;
     const PanelF *panels_f = nullptr;         // FP32 panel records (mixed precision)
-    float *ctx_e = nullptr;                   // per-pair direction e of common-vertex pairs (mixed precision)
+    float *ctx_e = nullptr;                   // per-pair asymptote constants of common-vertex pairs (mixed precision),
+                                              // kVertexCtxFloats floats per pair
     // per-pair state: regular-part sums (Psi, Theta, potential)
     double *cur = nullptr, *fin_a = nullptr, *fin_b = nullptr;
     int *stop = nullptr;
@@ -45,7 +59,11 @@ struct ClassArgs {
     double *padj = nullptr;                   // potential of adjacent pairs
     int *hard_list = nullptr, *hard_cnt = nullptr;  // adjacent pairs whose potential is refined adaptively
     int *tier2_list = nullptr, *tier2_cnt = nullptr;  // pairs re-integrated with the higher-order Duffy rule
-    int *hard_overflow = nullptr;             // stack-capacity events of the adaptive potential (diagnostic)
+    int *hard_overflow = nullptr;             // cells accepted early because a depth's list was full (diagnostic)
+    PotCellItem *pot_q_a = nullptr, *pot_q_b = nullptr;  // adaptive potential: cell lists of two successive depths
+    int pot_qcap = 0;                         // capacity of each list (>= 4 x hard pairs)
+    int *pot_qcnt = nullptr;                  // cells per depth (kHardMaxDepth + 2 ints)
+    long long *pot_fx = nullptr;              // per hard pair: accepted sums in 64-bit fixed point
     double tier_tol = 1e-7;                   // main/check (and main/higher-order) rule agreement bar
     // outputs
     double *raw4 = nullptr, *J3 = nullptr, *P = nullptr;

@@ -312,23 +312,15 @@ __global__ void __launch_bounds__(128) k_pot_tier2(ClassArgs A, QuadTables Q)
 }
 
 // ------------------------------------------------------------------ hard adjacent pairs: adaptive potential
-// One warp per pair.  A cell is compared with the sum of its four children and split again where
-// they differ by more than tol |P| 2^-depth; cells that hold a shared vertex (always in slot 1
-// of a corner child) use the graded Duffy rule with that vertex as apex, all others the 13-point
-// rule.  Point offsets to K_j's vertices are formed from vertex differences, so cells far below
-// the mesh scale keep full relative precision.  Work items live in a per-warp shared-memory
-// stack of (path, depth, corner, value); every loop pops at least one item and depth is bounded,
-// so the loop ends.
-constexpr int kHardWarps = 2;
-constexpr int kHardCap = 768;
-constexpr int kHardMaxDepth = 12;
-
-struct HardItem {
-    unsigned long long path;
-    double val;
-    int depth, corner;
-};
-
+// Breadth-first over the cells of ALL hard pairs at once: depth d holds a device list of cells
+// (hard-list slot, path, depth, corner slot, value); one thread takes one cell, integrates its
+// four children and either accepts their sum (|sum - value| <= tol |P| 2^-d, or d at the depth
+// cap) or appends the children to depth d + 1's list.  Cells that hold a shared vertex (always
+// in slot 1 of a corner child) use the graded Duffy rule with that vertex as apex, all others
+// the 13-point rule; point offsets to K_j's vertices are formed from vertex differences.  The
+// whole GPU works on every depth, so one pair that needs thousands of cells no longer runs
+// alone on one SM.  Accepted sums are added as 64-bit fixed point (2^40 units per |P| + |sigma
+// integral|), so the result does not depend on the order of the atomics.
 template <int CLS>
 __device__ double pot_cell(const Tri &T, int corner, const PanelJ &K, const FarCtx &F, const PotEdge &pe, const QuadTables &Q)
 {
@@ -379,94 +371,122 @@ __device__ __forceinline__ int child_corner(int parent_corner, int k)
     return k == want ? 1 : -1;
 }
 
+struct PotPairCtx {
+    Tri Ti;
+    PanelJ K;
+    FarCtx F;
+    PotEdge pe;
+    double sig_int, tol_abs, scale;
+};
+
 template <int CLS>
-__global__ void __launch_bounds__(32 * kHardWarps) k_pot_hard(ClassArgs A, QuadTables Q, double tol)
+__device__ __forceinline__ PotPairCtx pot_pair_ctx(const ClassArgs &A, int t, double tol)
 {
-    __shared__ HardItem stack[kHardWarps][kHardCap];
-    __shared__ int top[kHardWarps];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int count = *A.hard_cnt;
-    for (int h = blockIdx.x * kHardWarps + w; h < count; h += gridDim.x * kHardWarps) {
-        const int t = A.hard_list[h];
-        const int2 pr = A.pairs[t];
-        const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
-        const PanelJ K = load_panel(A.panels, pr.y);
-        const Tri Ti = load_tri(A.panels, pr.x);
-        const FarCtx F = make_far_ctx(K);
-        const double Si = A.panels[pr.x].v[0].w;
+    PotPairCtx c;
+    const int2 pr = A.pairs[t];
+    const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
+    c.K = load_panel(A.panels, pr.y);
+    c.Ti = load_tri(A.panels, pr.x);
+    c.F = make_far_ctx(c.K);
+    c.sig_int = 0.0;
+    c.pe = PotEdge{};
+    if (CLS == kEdge) {
         int si, sj;
-        if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
-        else shifts_vertex(ci, cj, si, sj);
-        PotEdge pe;
-        const double sig_int = CLS == kEdge ? make_pot_edge(rotate(Ti, si), rotate(Tri{K.A, K.B, K.C}, sj), K, Si, pe) : 0.0;
-        // shared slots of K_i: the root's children 0, 1, 2 hold slots b, c, a
+        shifts_edge(ci, cj, si, sj);
+        c.sig_int = make_pot_edge(rotate(c.Ti, si), rotate(Tri{c.K.A, c.K.B, c.K.C}, sj), c.K, A.panels[pr.x].v[0].w, c.pe);
+    }
+    const double p_root = A.padj[t] * (4.0 * kPi);  // tier 1/2 value (regular part + sigma integral)
+    c.tol_abs = tol * fabs(p_root);
+    const double base = fabs(p_root) + fabs(c.sig_int);
+    c.scale = base > 0.0 ? ldexp(1.0, 40) / base : 1.0;
+    return c;
+}
+
+// seed: the root of every hard pair is split once; its four children form depth 1.  Pairs
+// beyond a quarter of the list capacity keep their Duffy value and are counted as overflows.
+__device__ __forceinline__ int pot_seeded(const ClassArgs &A) { return min(*A.hard_cnt, A.pot_qcap / 4); }
+
+template <int CLS>
+__global__ void __launch_bounds__(128) k_pot_seed(ClassArgs A, QuadTables Q, double tol)
+{
+    const int count = pot_seeded(A);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        // depth 1 holds the roots' children; the deeper lists start empty (the depth kernels
+        // run after this one on the same stream)
+        A.pot_qcnt[1] = 4 * count;
+        for (int d = 2; d <= kHardMaxDepth + 1; ++d) A.pot_qcnt[d] = 0;
+        if (*A.hard_cnt > count) atomicAdd(A.hard_overflow, *A.hard_cnt - count);
+    }
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < count; h += gridDim.x * blockDim.x) {
+        const int t = A.hard_list[h];
+        const PotPairCtx c = pot_pair_ctx<CLS>(A, t, tol);
+        const int3 ci = A.cells[A.pairs[t].x], cj = A.cells[A.pairs[t].y];
         const int ia[3] = {ci.x, ci.y, ci.z};
         bool shared[3];
         for (int k = 0; k < 3; ++k) shared[k] = (ia[k] == cj.x || ia[k] == cj.y || ia[k] == cj.z);
-        const double root = A.padj[t] * (4.0 * kPi) - sig_int;  // Duffy value of the regular part
-        const double tol_abs = tol * fabs(A.padj[t] * (4.0 * kPi));
-        double acc = 0.0;
-        if (lane == 0) top[w] = 0;
-        __syncwarp();
-        // level 1: the root's four children, one per lane
-        double v1 = 0.0;
-        int c1 = -1;
-        if (lane < 4) {
-            c1 = lane == 3 ? -1 : (shared[lane == 0 ? 1 : (lane == 1 ? 2 : 0)] ? 1 : -1);
-            v1 = pot_cell<CLS>(child(Ti, lane), c1, K, F, pe, Q);
+        A.pot_fx[h] = 0;
+        // the root's children 0, 1, 2 hold K_i's slots b, c, a in their slot 1
+        for (int k = 0; k < 4; ++k) {
+            const int corner = k == 3 ? -1 : (shared[k == 0 ? 1 : (k == 1 ? 2 : 0)] ? 1 : -1);
+            const double v = pot_cell<CLS>(child(c.Ti, k), corner, c.K, c.F, c.pe, Q);
+            A.pot_q_a[4 * (long long)h + k] = PotCellItem{(unsigned long long)k, v, h, corner};
         }
-        (void)root;  // the root is always split once; each child then adapts on its own
-        if (lane < 4) {
-            stack[w][lane] = HardItem{(unsigned long long)lane, v1, 1, c1};
-            if (lane == 0) top[w] = 4;
-        }
-        __syncwarp();
-        for (int guard = 0; guard < 1 << 20; ++guard) {
-            const int n = top[w];
-            if (n == 0) break;
-            // each popped item may push 4: popping k items grows the stack by at most 3k, so
-            // k <= (capacity - n) / 3 keeps every push in bounds (n <= capacity - 3 always holds)
-            const int room = (kHardCap - n) / 3;
-            int take = n < 32 ? n : 32;
-            if (take > room) take = room > 1 ? room : 1;
-            HardItem it;
-            const bool has = lane < take;
-            if (has) it = stack[w][n - take + lane];
-            __syncwarp();
-            if (lane == 0) top[w] = n - take;
-            __syncwarp();
-            if (has) {
-                const Tri T = subcell(Ti, it.depth, (int)it.path);
-                double v[4], sum = 0.0;
-                for (int k = 0; k < 4; ++k) {
-                    v[k] = pot_cell<CLS>(child(T, k), child_corner(it.corner, k), K, F, pe, Q);
-                    sum += v[k];
-                }
-                const double lim = ldexp(tol_abs, -it.depth);
-                bool accept = fabs(sum - it.val) <= lim || it.depth >= kHardMaxDepth;
-                int pos = 0;
-                if (!accept) {
-                    pos = atomicAdd(&top[w], 4);
-                    if (pos + 4 > kHardCap) {  // cannot happen with the throttle above; kept as a guard
-                        atomicSub(&top[w], 4);
-                        atomicAdd(A.hard_overflow, 1);
-                        accept = true;
-                    }
-                }
-                if (accept) acc += sum;
-                else
-                    for (int k = 0; k < 4; ++k)
-                        stack[w][pos + k] = HardItem{(it.path << 2) | (unsigned long long)k, v[k], it.depth + 1,
-                                                     child_corner(it.corner, k)};
-            }
-            __syncwarp();
-        }
-        for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-        if (lane == 0) A.padj[t] = kInv4Pi * (acc + sig_int);
-        __syncwarp();
     }
 }
 
+template <int CLS>
+__global__ void __launch_bounds__(128) k_pot_depth(ClassArgs A, QuadTables Q, double tol, int depth, const PotCellItem *__restrict__ in,
+                                                   PotCellItem *__restrict__ out)
+{
+    const int count = min(A.pot_qcnt[depth], A.pot_qcap);
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < count; idx += gridDim.x * blockDim.x) {
+        const PotCellItem it = in[idx];
+        if (it.h < 0) continue;
+        const int t = A.hard_list[it.h];
+        const PotPairCtx c = pot_pair_ctx<CLS>(A, t, tol);
+        const Tri T = subcell(c.Ti, depth, (int)it.path);
+        double v[4], sum = 0.0;
+        for (int k = 0; k < 4; ++k) {
+            v[k] = pot_cell<CLS>(child(T, k), child_corner(it.corner, k), c.K, c.F, c.pe, Q);
+            sum += v[k];
+        }
+        bool accept = fabs(sum - it.val) <= ldexp(c.tol_abs, -depth) || depth >= kHardMaxDepth;
+        if (!accept) {
+            const int pos = atomicAdd(&A.pot_qcnt[depth + 1], 4);
+            if (pos + 4 <= A.pot_qcap) {
+                for (int k = 0; k < 4; ++k)
+                    out[pos + k] = PotCellItem{(it.path << 2) | (unsigned long long)k, v[k], it.h, child_corner(it.corner, k)};
+            } else {
+                // list full: keep this cell's sum (counted as an overflow) and blank the slots it
+                // was given below the capacity, so the next depth skips them
+                for (int k = pos; k < A.pot_qcap && k < pos + 4; ++k) out[k] = PotCellItem{0ull, 0.0, -1, -1};
+                atomicAdd(A.hard_overflow, 1);
+                accept = true;
+            }
+        }
+        if (accept) atomicAdd(reinterpret_cast<unsigned long long *>(&A.pot_fx[it.h]), (unsigned long long)llrint(sum * c.scale));
+    }
+}
+
+template <int CLS>
+__global__ void __launch_bounds__(128) k_pot_final(ClassArgs A, double tol)
+{
+    const int count = pot_seeded(A);
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < count; h += gridDim.x * blockDim.x) {
+        const int t = A.hard_list[h];
+        const PotPairCtx c = pot_pair_ctx<CLS>(A, t, tol);
+        A.padj[t] = kInv4Pi * ((double)A.pot_fx[h] / c.scale + c.sig_int);
+    }
+}
+
+template <int CLS>
+static void pot_adaptive_chain(const ClassArgs &A, const QuadTables &Q, double tol, int persistent_blocks, cudaStream_t s)
+{
+    k_pot_seed<CLS><<<persistent_blocks, 128, 0, s>>>(A, Q, tol);
+    for (int d = 1; d <= kHardMaxDepth; ++d)
+        k_pot_depth<CLS><<<persistent_blocks, 128, 0, s>>>(A, Q, tol, d, d % 2 ? A.pot_q_a : A.pot_q_b, d % 2 ? A.pot_q_b : A.pot_q_a);
+    k_pot_final<CLS><<<persistent_blocks, 128, 0, s>>>(A, tol);
+}
 // ------------------------------------------------------------------ self pairs
 // J(K_i, K_i): tangential part 0 by antisymmetry; normal part 0 (principal value) or the
 // one-sided limit +-(1/4pi) 2 pi S_i n_i.  Potential: with d = 0 the inner potential is
@@ -583,8 +603,8 @@ void launch_self(const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, 
 
 void launch_pot_hard(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s)
 {
-    if (cls == kEdge) k_pot_hard<kEdge><<<persistent_blocks / 4, 32 * kHardWarps, 0, s>>>(A, Q, cfg.hard_tol);
-    else k_pot_hard<kVertex><<<persistent_blocks / 4, 32 * kHardWarps, 0, s>>>(A, Q, cfg.hard_tol);
+    if (cls == kEdge) pot_adaptive_chain<kEdge>(A, Q, cfg.hard_tol, persistent_blocks, s);
+    else pot_adaptive_chain<kVertex>(A, Q, cfg.hard_tol, persistent_blocks, s);
 }
 
 void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s)
@@ -599,7 +619,7 @@ void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const R
         k_singular<kEdge><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q);
         if (A.hard_list) {
             k_pot_tier2<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Q);
-            k_pot_hard<kEdge><<<persistent_blocks / 4, 32 * kHardWarps, 0, s>>>(A, Q, cfg.hard_tol);
+            pot_adaptive_chain<kEdge>(A, Q, cfg.hard_tol, persistent_blocks, s);
         }
         level_chain<kEdge>(A, Q, cfg, persistent_blocks, s);
         break;
@@ -607,7 +627,7 @@ void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const R
         k_singular<kVertex><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q);
         if (A.hard_list) {
             k_pot_tier2<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Q);
-            k_pot_hard<kVertex><<<persistent_blocks / 4, 32 * kHardWarps, 0, s>>>(A, Q, cfg.hard_tol);
+            pot_adaptive_chain<kVertex>(A, Q, cfg.hard_tol, persistent_blocks, s);
         }
         level_chain<kVertex>(A, Q, cfg, persistent_blocks, s);
         break;

@@ -57,7 +57,12 @@ struct EdgeCtxF {
 };
 struct VertexCtxF {
     f3 AB, AC;       // JB - JA, JC - JA (JA = shared vertex)
-    f3 ta, tb, tbc, e;
+    f3 ta, tb, tbc;
+    // the asymptote's angle terms s1, s2 as atan2(o_A.w, l_A c - o_A.p) with w = tau x e,
+    // p = e -+ tau, c = |p|^2 / 2 formed in FP64 once per pair: when e is nearly parallel to
+    // +-tau, e -+ tau formed in FP32 would keep only a few digits
+    f3 w1, p1, w2, p2;
+    float c1, c2;
     float inv_sqrt_si, lenBC;
 };
 
@@ -87,8 +92,8 @@ __device__ __forceinline__ void vertex_integrand_f(f3 oA, f3 oB, f3 oC, const Pa
     const float l2 = logf((lB - dotf(oB, Vx.tb)) * Vx.inv_sqrt_si);
     psi = Lbc * Vx.tbc + l1 * Vx.ta + l2 * Vx.tb;
     const float den = lA * lB * lC + dotf(oA, oB) * lC + dotf(oB, oC) * lA + dotf(oC, oA) * lB;
-    const float s1 = atan2f(dotf(crossf(oA, Vx.ta), Vx.e), dotf(lA * Vx.e - oA, Vx.e - Vx.ta));
-    const float s2 = atan2f(dotf(crossf(oA, Vx.tb), Vx.e), dotf(lA * Vx.e - oA, Vx.e + Vx.tb));
+    const float s1 = atan2f(dotf(oA, Vx.w1), lA * Vx.c1 - dotf(oA, Vx.p1));
+    const float s2 = atan2f(dotf(oA, Vx.w2), lA * Vx.c2 - dotf(oA, Vx.p2));
     th = 2.0f * atan2f(2.0f * K.S * dotf(K.n, oA), den) - 2.0f * (s1 + s2);
 }
 
@@ -179,8 +184,14 @@ __device__ void level_items_mixed(const ClassArgs &A, const QuadTablesF &Qf, int
                     const f3 bc = AC - AB;
                     Vx.lenBC = normf(bc);
                     Vx.tbc = (1.0f / Vx.lenBC) * bc;
-                    const float *e = A.ctx_e + 3 * (long long)t;
-                    Vx.e = f3{e[0], e[1], e[2]};
+                    const float4 *ce = reinterpret_cast<const float4 *>(A.ctx_e + kVertexCtxFloats * (long long)t);
+                    const float4 q0 = ce[0], q1 = ce[1], q2 = ce[2], q3 = ce[3];
+                    Vx.w1 = xyzf(q0);
+                    Vx.c1 = q0.w;
+                    Vx.p1 = xyzf(q1);
+                    Vx.w2 = xyzf(q2);
+                    Vx.c2 = q2.w;
+                    Vx.p2 = xyzf(q3);
                     Vx.inv_sqrt_si = rsqrtf(A.panels_f[pr.x].v[0].w);
                 }
             }
@@ -369,7 +380,7 @@ __global__ void __launch_bounds__(128) k_singular_mixed(ClassArgs A, QuadTablesF
     int si, sj;
     if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
     else shifts_vertex(ci, cj, si, sj);
-    // FP64: closed-form singular part (a4 / a5) and, for the vertex class, the direction e
+    // FP64: closed-form singular part (a4 / a5) and, for the vertex class, the asymptote's constants
     {
         const Tri Ti0 = load_tri(A.panels, pr.x);
         const Tri T0[3] = {Ti0, Tri{Ti0.b, Ti0.c, Ti0.a}, Tri{Ti0.c, Ti0.a, Ti0.b}};
@@ -383,8 +394,12 @@ __global__ void __launch_bounds__(128) k_singular_mixed(ClassArgs A, QuadTablesF
             const d3 ta = unit(J0[sj].a - J0[sj].c), tb = unit(J0[sj].b - J0[sj].a);
             double dA, dB;
             const d3 e = vertex_direction(ni, Kd.n, ta, tb, dA, dB);
-            float *ce = A.ctx_e + 3 * (long long)t;
-            ce[0] = (float)e.x; ce[1] = (float)e.y; ce[2] = (float)e.z;
+            const d3 w1 = cross(ta, e), p1 = e - ta, w2 = cross(tb, e), p2 = e + tb;
+            float4 *ce = reinterpret_cast<float4 *>(A.ctx_e + kVertexCtxFloats * (long long)t);
+            ce[0] = make_float4((float)w1.x, (float)w1.y, (float)w1.z, (float)(0.5 * dot(p1, p1)));
+            ce[1] = make_float4((float)p1.x, (float)p1.y, (float)p1.z, 0.0f);
+            ce[2] = make_float4((float)w2.x, (float)w2.y, (float)w2.z, (float)(0.5 * dot(p2, p2)));
+            ce[3] = make_float4((float)p2.x, (float)p2.y, (float)p2.z, 0.0f);
         }
         double *sg = A.sing + 4 * (long long)t;
         sg[0] = psi.x; sg[1] = psi.y; sg[2] = psi.z; sg[3] = th;

@@ -32,8 +32,12 @@ def _run(api, V, C, cls, pairs, precision, mode="relative", level=0):
 
 
 def test_mixed_matches_fp64_at_fixed_level(api):
-    """same rule, same refinement: the difference is the FP32 rounding of the bulk"""
+    """same rule, same refinement: the difference is the FP32 rounding of the bulk.  FP32
+    rounding acts like a relative input perturbation of a few 1e-8, so the per-pair bar grows
+    with kappa, the pair's measured relative sensitivity to such perturbations:
+    max(1e-5, 1e-7 kappa); the rms over the class stays below 1e-6."""
     from integrator2_gb300 import meshes, pairs as P
+    from oracle import oracle as O
     V, C = meshes.jittered_icosphere(3, 0.15, 11)
     pl = P.build_pairs(V, C)
     worst = {}
@@ -43,9 +47,13 @@ def test_mixed_matches_fp64_at_fixed_level(api):
         J32, P32, _ = _run(api, V, C, cls, pr, api.PRECISION_MIXED, "fixed", 1)
         eJ = rel_rows(J32, J64) if cls != 3 else np.abs(J32 - J64).max(axis=1)
         eP = np.abs(P32 - P64) / np.abs(P64)
-        worst[cls] = (float(eJ.max()), float(eP.max()), float(np.sqrt(np.mean(eJ ** 2))))
-        assert eJ.max() < 1e-5 and eP.max() < 1e-5, (cls, worst[cls])
-    print("mixed vs fp64 (J max, P max, J rms):", worst)
+        kap = O.conditioning(cls, pr, V, C, 1) if cls != 3 else np.ones(len(pr))
+        bar = np.maximum(1e-5, 1e-7 * kap)
+        w = int(np.argmax(eJ / bar))
+        worst[cls] = (float(eJ.max()), float(eP.max()), float(np.sqrt(np.mean(eJ ** 2))), float(kap[w]), pr[w].tolist())
+        assert np.all(eJ <= bar) and eP.max() < 1e-5, (cls, worst[cls])
+        assert np.sqrt(np.mean(eJ ** 2)) < 1e-6 and np.sqrt(np.mean(eP ** 2)) < 1e-6, (cls, worst[cls])
+    print("mixed vs fp64 (J max, P max, J rms, kappa and pair of the worst):", worst)
 
 
 def test_mixed_accuracy_against_high_order(api):
