@@ -218,6 +218,25 @@ def run_form(ev, lists, d_pairs, d_J, d_P, stream, flush, steps, warmup):
     return total, cls_ms / steps
 
 
+def run_batch(batch, flush, stream, steps, warmup):
+    """times `steps` replays of the batched form (CUDA graph of the whole step; L2 flushed
+    between steps); returns the total device time in ms"""
+    import torch
+    with torch.cuda.stream(stream):
+        for _ in range(max(warmup, 3)):
+            batch.run()
+        stream.synchronize()
+        e0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        e1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        for s in range(steps):
+            flush.fill_(float(s))
+            e0[s].record(stream)
+            batch.run()
+            e1[s].record(stream)
+        torch.cuda.synchronize()
+    return sum(e0[s].elapsed_time(e1[s]) for s in range(steps))
+
+
 # FP32 operation counts of the far-field integrand (same formulas, FP32 form): flops, sqrtf,
 # divide, log1pf, atan2f
 POINT_OPS_F32 = {"far": (211, 3, 3, 3, 1)}
@@ -257,7 +276,10 @@ def gpu_arm(args):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     forms = {}
+    wanted = [f.strip() for f in args.forms.split(",") if f.strip()]
     for name, prec in (("fp64", api.PRECISION_FP64), ("mixed", api.PRECISION_MIXED)):
+        if name not in wanted and not (name == "mixed" and "batch" in wanted):
+            continue
         it = api.NumericalIntegrator3D(m, api.qf3D13)
         it.setErrorControl(api.RELATIVE_ERROR_CONTROL, args.tol, 5)
         it.setPrecision(prec)
@@ -282,8 +304,31 @@ def gpu_arm(args):
         forms[name] = dict(ev=ev, it=it, ms=ms, cls_ms=cls_ms, J=J, P=P, levels=levels, clocks=clk.summary(),
                            value=total * world * args.steps / (ms * 1e-3))
 
-    head = forms["mixed"]
-    ev = head["ev"]
+    if "batch" in wanted:
+        # batched form: the four classes as segments of one batch, one persistent cooperative
+        # kernel for every refinement level, the whole step replayed as a CUDA graph
+        it = forms["mixed"]["it"]
+        batch = api.BatchEvaluator(it)
+        batch.setStream(stream.cuda_stream)
+        segs = {c: batch.add(m, c, lists[c]) for c in CLASSES}
+        shape = batch.autotune()
+        if world > 1:
+            torch.distributed.barrier()
+        with ClockSampler() as clk:
+            ms = run_batch(batch, flush, stream, args.steps, args.warmup)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        J = {c: batch.getResults(segs[c]) for c in CLASSES}
+        P = {c: batch.getPotentials(segs[c]) for c in CLASSES}
+        levels = {c: batch.getLevels(segs[c]) for c in CLASSES}
+        forms["batch"] = dict(ms=ms, J=J, P=P, levels=levels, clocks=clk.summary(), shape=shape, graph=batch.usesGraph(),
+                              value=total * world * args.steps / (ms * 1e-3), cls_ms=forms["mixed"]["cls_ms"])
+
+    head = forms["batch"] if "batch" in forms else forms[wanted[0]]
+    per_class = forms["mixed"] if "mixed" in forms else forms[wanted[0]]
+    ev = per_class["ev"]
     # e2e: host lists (pinned) -> H2D, compute, D2H of J and P inside the timed region
     h_pairs = {c: torch.from_numpy(lists[c]).pin_memory() for c in CLASSES}
     h_J = {c: torch.empty(len(lists[c]), 3, dtype=torch.float64).pin_memory() for c in CLASSES}
@@ -315,40 +360,62 @@ def gpu_arm(args):
         return {"achieved": achieved, "peak": peak, "frac": achieved / peak, "flops_per_point": per_point,
                 "point_evaluations": evals * 13, "note": unit_note}
 
-    roof_mixed = far_roofline(head, point_flops_f32(cal), float(cal[1]), "FP32 FMA peak measured live (i2_calibrate_pipes)")
-    roof_fp64 = far_roofline(forms["fp64"], point_flops("far", w), float(cal[0]), "FP64 FMA peak measured live")
+    roof = {}
+    if "mixed" in forms:
+        roof["mixed"] = far_roofline(forms["mixed"], point_flops_f32(cal), float(cal[1]), "FP32 FMA peak measured live (i2_calibrate_pipes)")
+    if "fp64" in forms:
+        roof["fp64"] = far_roofline(forms["fp64"], point_flops("far", w), float(cal[0]), "FP64 FMA peak measured live")
     acc = {name: accuracy(V, C, lists, f["J"], f["P"], f["levels"]) for name, f in forms.items()}
     n_cpu, dt_cpu, thr = cpu_run(V, C, lists, args.cpu_fraction, args.tol)
-    launches_per_step = 10 + 10 + 7 + 1
+    # kernels per step: adjacent classes run singular + tier 2 + adaptive potential (seed, 12
+    # depths, final); per-class chains add levels 0..5 + finalize per class, self pairs 1
+    pot_chain = 3 + 12
+    launches = {"fp64": 2 * (1 + pot_chain + 7) + 7 + 1, "mixed": 2 * (1 + pot_chain + 7) + 7 + 1, "batch": 2 * (1 + pot_chain) + 1 + 1}
+    names4 = ("vertex", "edge", "near", "self")
+    form_desc = {"batch": "mixed precision, batched: 4 class segments, one persistent cooperative level kernel, CUDA graph replay",
+                 "mixed": "mixed precision, per-class kernel chains", "fp64": "plain FP64, per-class kernel chains"}
+    hname = "batch" if "batch" in forms else wanted[0]
     line = {
         "metric": METRIC, "value": head["value"], "unit": "pair-integrals/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": head["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 bulk / f64 singular, estimator and hard pairs", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f64" if hname == "fp64" else "f32 bulk / f64 singular, estimator and hard pairs",
+        "data": "synthetic",
         "config": {"workload": "jittered icosphere s5 (20480 triangles, sigma 0.15h, seed 2026): common-vertex, "
                                "common-edge, self and near-field (< 3h) ordered pairs",
-                   "pairs": total, "form": "mixed precision (per-class kernel chains)",
+                   "pairs": total, "form": form_desc[hname],
                    "error_control": f"relative tol {args.tol}, levels 0..5",
                    "rule": "qf3D13; adjacent potential: tiered graded Duffy 10x8 / 8x6 check / 16x16 / adaptive",
                    "l2": "flushed (512 MiB write) between steps", "parallelism": f"replicas x{world}"},
-        "e2e": {"value": e2e_value, "unit": "pair-integrals/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-        "roofline": {"bound": "fp32", "kernel": "k_level_mixed<far> chain (levels 0..5)", "unit": "TFLOP/s", "traffic": None,
-                     **roof_mixed},
-        "plain_fp64": {"value": forms["fp64"]["value"], "ms_per_step": forms["fp64"]["ms"] / args.steps,
-                       "class_ms": dict(zip(("vertex", "edge", "near", "self"), map(float, forms["fp64"]["cls_ms"]))),
-                       "roofline": {"bound": "fp64", "unit": "TFLOP/s", **roof_fp64}},
-        "mixed_over_fp64": head["value"] / forms["fp64"]["value"],
-        "class_ms": dict(zip(("vertex", "edge", "near", "self"), map(float, head["cls_ms"]))),
+        "e2e": {"value": e2e_value, "unit": "pair-integrals/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "path": "EvaluatorJ3DK device entry point per class (mixed precision), pinned host lists in, J and P out"},
+        "forms": {n: {"value": f["value"], "ms_per_step": f["ms"] / args.steps,
+                      "class_ms": dict(zip(names4, map(float, f["cls_ms"]))) if n != "batch" else None,
+                      "accuracy": acc[n], "gpu_launches_per_step": launches[n]} for n, f in forms.items()},
+        "accuracy": acc[hname],
         "levels": {n: np.bincount(head["levels"][c][head["levels"][c] >= 0], minlength=6).tolist() for n, c in
                    zip(("vertex", "edge", "near"), (0, 1, 2))},
-        "accuracy": acc,
         "calibration": {"fp64_tflops": float(cal[0]), "fp32_tflops": float(cal[1]),
                         "fp64_fma_units": dict(zip(("sqrt", "div", "log", "atan2", "sincos", "acos"), map(float, cal[2:8]))),
                         "fp32_fma_units": dict(zip(("sqrtf", "div", "log1pf", "atan2f", "logf"), map(float, cal[8:13])))},
         "cpu_baseline": {"value": n_cpu / dt_cpu, "unit": "pair-integrals/s", "cores": thr, "kind": "port",
                          "sample": f"{args.cpu_fraction:.3f} of every class ({n_cpu} pairs), oracle C restatement, OpenMP, same rules"},
         "clocks": head["clocks"],
-        "gpu_launches": launches_per_step * args.steps,
+        "gpu_launches": launches[hname] * args.steps,
     }
+    if "fp64" in forms:
+        line["speedup_over_plain_fp64"] = head["value"] / forms["fp64"]["value"]
+    if "batch" in forms:
+        line["batch"] = {"shape": {"threads": forms["batch"]["shape"][0], "blocks_per_sm": forms["batch"]["shape"][1],
+                                   "lanes_per_pair": forms["batch"]["shape"][2],
+                                   "registers": "capped at 128" if forms["batch"]["shape"][3] else "unconstrained"},
+                         "cuda_graph": forms["batch"]["graph"]}
+    rk = "mixed" if "mixed" in roof else ("fp64" if "fp64" in roof else None)
+    if rk:
+        line["roofline"] = {"bound": "fp32" if rk == "mixed" else "fp64",
+                            "kernel": ("k_level_mixed" if rk == "mixed" else "k_level") + "<far> chain (levels 0..5), per-class form",
+                            "unit": "TFLOP/s", "traffic": None, **roof[rk]}
+    if "fp64" in roof and rk != "fp64":
+        line["roofline_fp64"] = {"bound": "fp64", "unit": "TFLOP/s", **roof["fp64"]}
     print(json.dumps(line))
 
 
@@ -360,6 +427,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--cpu-fraction", type=float, default=0.02)
+    ap.add_argument("--forms", default="fp64,mixed,batch",
+                    help="forms to run: fp64, mixed (per-class chains), batch (headline when present)")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)

@@ -167,6 +167,18 @@ i2_status i2_evaluator_copy_results(const i2_evaluator_t *ev, i2_pair_class cls,
 i2_status i2_evaluator_output_results(const i2_evaluator_t *ev, i2_pair_class cls, i2_output_format format,
                                       const char *path);
 
+/* ------------------------------------------------------------------ adjoint */
+/* Backward pass of the pair integrals (no reference counterpart): adds to d_gradV (3 doubles
+ * per vertex, device) the vector-Jacobian product
+ *     sum_p d_gJ[p] . dJ_p/dV + d_gP[p] dP_p/dV
+ * for the pairs of one class, with the refinement the forward pass kept frozen (sub-cells are
+ * recomputed, not stored).  It must follow the forward run of the same class with the same device
+ * pairs on this evaluator (i2_evaluator_run_class / run_class_device).  d_gJ (3 per pair) or d_gP
+ * (1 per pair) may be NULL.  FP64 dual numbers after an FP64 forward, FP32 after a mixed one.
+ * Asynchronous on the evaluator's stream; accumulation uses atomics. */
+i2_status i2_evaluator_backward_class(i2_evaluator_t *ev, i2_pair_class cls, const int32_t *d_pairs, int64_t n,
+                                      const double *d_gJ, const double *d_gP, double *d_gradV);
+
 /* ------------------------------------------------------------------ batched form */
 /* Many (mesh, pair class) segments integrated together (no reference counterpart): the
  * refinement levels of all segments run in ONE persistent cooperative kernel, the whole run is
@@ -181,8 +193,9 @@ i2_status i2_batch_set_stream(i2_batch_t *batch, void *stream);
 /* adds one segment (host rows, stride 2 or 3 int32); returns its index in *segment */
 i2_status i2_batch_add(i2_batch_t *batch, const i2_mesh_t *mesh, i2_pair_class cls, const int32_t *rows, int64_t n,
                        int32_t row_stride, int32_t *segment);
-/* times the candidate launch shapes (threads per block, resident blocks per SM, lanes per pair)
- * on the batch and keeps the fastest; the chosen shape is returned in shape[3] (may be NULL) */
+/* times the candidate launch shapes (threads per block, resident blocks per SM, lanes per pair,
+ * register variant: 0 unconstrained, 1 capped at 128 per thread) on the batch and keeps the
+ * fastest; the chosen shape is returned in shape[4] (may be NULL) */
 i2_status i2_batch_autotune(i2_batch_t *batch, int32_t *shape);
 /* enqueues the batch on its stream (graph replay after the first call); asynchronous */
 i2_status i2_batch_run(i2_batch_t *batch);

@@ -49,6 +49,7 @@ SIGNATURES = {
     "i2_evaluator_run_pairs": (ctypes.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _i64]),
     "i2_evaluator_run_class": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _i64, _i32]),
     "i2_evaluator_run_class_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _i64, _vp, _vp, _vp]),
+    "i2_evaluator_backward_class": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _i64, _vp, _vp, _vp]),
     "i2_evaluator_synchronize": (ctypes.c_int, [_vp]),
     "i2_evaluator_result_count": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
     "i2_evaluator_copy_results": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, _i64]),

@@ -211,6 +211,12 @@ class EvaluatorJ3DK:
         call("i2_evaluator_run_class_device", self._h, int(cls), ctypes.c_void_p(d_pairs_ptr), int(n),
              ctypes.c_void_p(d_raw or None), ctypes.c_void_p(d_J or None), ctypes.c_void_p(d_P or None))
 
+    def backwardClass(self, cls: int, d_pairs_ptr: int, n: int, d_gJ=0, d_gP=0, d_gradV=0) -> None:
+        """Adjoint of the last runClassDevice / runClass of this class (same pairs): adds
+        gJ . dJ/dV + gP dP/dV to the device buffer d_gradV (3 doubles per vertex)."""
+        call("i2_evaluator_backward_class", self._h, int(cls), ctypes.c_void_p(d_pairs_ptr), int(n),
+             ctypes.c_void_p(d_gJ or None), ctypes.c_void_p(d_gP or None), ctypes.c_void_p(d_gradV))
+
     def synchronize(self) -> None:
         call("i2_evaluator_synchronize", self._h)
 
@@ -281,8 +287,9 @@ class BatchEvaluator:
         return int(seg.value)
 
     def autotune(self):
-        """times the candidate launch shapes; returns (threads, blocks per SM, lanes per pair)"""
-        shape = np.zeros(3, np.int32)
+        """times the candidate launch shapes; returns (threads, blocks per SM, lanes per pair,
+        register variant)"""
+        shape = np.zeros(4, np.int32)
         call("i2_batch_autotune", self._h, _p(shape))
         return tuple(int(x) for x in shape)
 

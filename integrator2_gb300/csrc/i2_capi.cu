@@ -325,6 +325,9 @@ struct ClassResult {
     std::vector<int2> host_pairs;  // rows of the last host-side run (for output_results)
     DevBuf<double> raw4, J, P;
     DevBuf<int> level;
+    DevBuf<int> maxlev;            // class-wide last refinement level of the last run (adjoint)
+    i2::RunConfig cfg;             // settings of the last run (adjoint)
+    i2_precision precision = I2_PRECISION_FP64;
     std::vector<double> errors;  // antisymmetry deltas (host)
 };
 
@@ -630,6 +633,10 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
     }
     I2_CHECK_CUDA(cudaGetLastError());
     if (cls == I2_SELF) I2_CHECK_CUDA(cudaMemsetAsync(R.level.ptr, 0xff, n * sizeof(int), ev->stream));
+    R.maxlev.reserve(1);
+    I2_CHECK_CUDA(cudaMemcpyAsync(R.maxlev.ptr, W.maxlev.ptr, sizeof(int), cudaMemcpyDeviceToDevice, ev->stream));
+    R.cfg = cfg;
+    R.precision = (i2_precision)ev->integrator->precision;
     // keep the evaluator's copies coherent when the caller supplied output buffers
     if (out_raw != R.raw4.ptr) { R.raw4.reserve(4 * n); I2_CHECK_CUDA(cudaMemcpyAsync(R.raw4.ptr, out_raw, 4 * n * sizeof(double), cudaMemcpyDeviceToDevice, ev->stream)); }
     if (out_J != R.J.ptr) { R.J.reserve(3 * n); I2_CHECK_CUDA(cudaMemcpyAsync(R.J.ptr, out_J, 3 * n * sizeof(double), cudaMemcpyDeviceToDevice, ev->stream)); }
@@ -682,7 +689,7 @@ struct i2_batch {
     DevBuf<i2::BatchSeg> d_segs;
     bool dirty = true;
     cudaStream_t stream = 0;
-    int threads = 256, blocks_per_sm = 0, g_cap = 32, sms = 0;
+    int threads = 256, blocks_per_sm = 0, g_cap = 32, variant = 0, sms = 0;
     cudaGraphExec_t graph = nullptr;
     bool graph_tried = false, graph_ok = false, last_graph = false;
     ~i2_batch()
@@ -714,7 +721,7 @@ void batch_prepare(i2_batch *b)
 }
 
 // the whole batch on a stream: counter resets, per-segment preludes, one cooperative level sweep
-void batch_enqueue(i2_batch *b, cudaStream_t s, int threads, int bps, int gcap)
+void batch_enqueue(i2_batch *b, cudaStream_t s, int threads, int bps, int gcap, int variant)
 {
     const int persistent = std::max(1, b->sms) * 8;
     for (auto &sp : b->segs) {
@@ -723,10 +730,10 @@ void batch_enqueue(i2_batch *b, cudaStream_t s, int threads, int bps, int gcap)
         I2_CHECK_CUDA(cudaMemsetAsync(sp->maxlev.ptr, 0, sizeof(int), s));
         i2::launch_batch_prelude(sp->args, sp->cls, b->Q, b->Qf, b->cfg, persistent, s);
     }
-    const int maxb = i2::batch_max_blocks_per_sm(threads);
+    const int maxb = i2::batch_max_blocks_per_sm(threads, variant);
     I2_REQUIRE(maxb > 0, I2_ERR_CUDA, "batch kernel cannot be resident with this block size");
     const int blocks = std::max(1, b->sms) * std::max(1, std::min(bps > 0 ? bps : maxb, maxb));
-    I2_CHECK_CUDA(i2::launch_batch_levels(b->d_segs.ptr, (int)b->segs.size(), b->Qf, b->cfg, blocks, threads, gcap, s));
+    I2_CHECK_CUDA(i2::launch_batch_levels(b->d_segs.ptr, (int)b->segs.size(), b->Qf, b->cfg, blocks, threads, gcap, variant, s));
 }
 
 } // namespace
@@ -1056,6 +1063,34 @@ i2_status i2_evaluator_run_class_device(i2_evaluator_t *ev, i2_pair_class cls, c
     });
 }
 
+i2_status i2_evaluator_backward_class(i2_evaluator_t *ev, i2_pair_class cls, const int32_t *d_pairs, int64_t n,
+                                      const double *d_gJ, const double *d_gP, double *d_gradV)
+{
+    return guarded([&] {
+        I2_REQUIRE(ev && d_gradV && (n == 0 || d_pairs), I2_ERR_INVALID_ARGUMENT, "null argument");
+        const int c = checked_class(cls);
+        const ClassResult &R = ev->results[c];
+        I2_REQUIRE(R.n == n, I2_ERR_STATE, "backward needs the forward run of this class with the same pairs just before");
+        if (n == 0) return;
+        const i2_mesh &m = *ev->mesh;
+        I2_REQUIRE(m.on_device, I2_ERR_STATE, "mesh not on the device");
+        i2::RunConfig cfg = R.cfg;
+        // the tier bar of the forward pass (run_class_device)
+        double tier_tol = 10.0 * cfg.hard_tol;
+        if (R.precision == I2_PRECISION_MIXED) tier_tol = std::max(tier_tol, 2e-7);
+        if (ev->persistent_blocks == 0) {
+            int dev = 0, sms = 0;
+            I2_CHECK_CUDA(cudaGetDevice(&dev));
+            I2_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            ev->persistent_blocks = std::max(1, sms) * 8;
+        }
+        i2::launch_adjoint(c, R.precision == I2_PRECISION_MIXED, reinterpret_cast<const int2 *>(d_pairs), (int)n,
+                           reinterpret_cast<const int3 *>(m.dC.ptr), m.dV.ptr, R.level.ptr, R.maxlev.ptr, cfg, tier_tol, d_gJ, d_gP,
+                           d_gradV, ev->integrator->tables(), ev->persistent_blocks, ev->stream);
+        I2_CHECK_CUDA(cudaGetLastError());
+    });
+}
+
 i2_status i2_evaluator_synchronize(i2_evaluator_t *ev)
 {
     return guarded([&] {
@@ -1226,19 +1261,22 @@ i2_status i2_batch_autotune(i2_batch_t *batch, int32_t *shape)
         I2_CHECK_CUDA(cudaEventCreate(&e0));
         I2_CHECK_CUDA(cudaEventCreate(&e1));
         float best = 1e30f;
-        int bt = batch->threads, bb = batch->blocks_per_sm, bg = batch->g_cap;
-        for (int threads : {128, 256}) {
-            const int maxb = i2::batch_max_blocks_per_sm(threads);
-            for (int bps : {maxb, std::max(1, maxb / 2)}) {
-                for (int gcap : {8, 16, 32}) {
-                    batch_enqueue(batch, batch->stream, threads, bps, gcap);  // warm-up
-                    I2_CHECK_CUDA(cudaEventRecord(e0, batch->stream));
-                    batch_enqueue(batch, batch->stream, threads, bps, gcap);
-                    I2_CHECK_CUDA(cudaEventRecord(e1, batch->stream));
-                    I2_CHECK_CUDA(cudaEventSynchronize(e1));
-                    float ms = 0;
-                    I2_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                    if (ms < best) { best = ms; bt = threads; bb = bps; bg = gcap; }
+        int bt = batch->threads, bb = batch->blocks_per_sm, bg = batch->g_cap, bv = batch->variant;
+        for (int variant : {0, 1}) {
+            for (int threads : {128, 256}) {
+                const int maxb = i2::batch_max_blocks_per_sm(threads, variant);
+                if (maxb <= 0) continue;
+                for (int bps : {maxb, std::max(1, maxb / 2)}) {
+                    for (int gcap : {8, 16, 32}) {
+                        batch_enqueue(batch, batch->stream, threads, bps, gcap, variant);  // warm-up
+                        I2_CHECK_CUDA(cudaEventRecord(e0, batch->stream));
+                        batch_enqueue(batch, batch->stream, threads, bps, gcap, variant);
+                        I2_CHECK_CUDA(cudaEventRecord(e1, batch->stream));
+                        I2_CHECK_CUDA(cudaEventSynchronize(e1));
+                        float ms = 0;
+                        I2_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                        if (ms < best) { best = ms; bt = threads; bb = bps; bg = gcap; bv = variant; }
+                    }
                 }
             }
         }
@@ -1247,9 +1285,10 @@ i2_status i2_batch_autotune(i2_batch_t *batch, int32_t *shape)
         batch->threads = bt;
         batch->blocks_per_sm = bb;
         batch->g_cap = bg;
+        batch->variant = bv;
         if (batch->graph) { cudaGraphExecDestroy(batch->graph); batch->graph = nullptr; }
         batch->graph_tried = false;
-        if (shape) { shape[0] = bt; shape[1] = bb; shape[2] = bg; }
+        if (shape) { shape[0] = bt; shape[1] = bb; shape[2] = bg; shape[3] = bv; }
     });
 }
 
@@ -1271,7 +1310,7 @@ i2_status i2_batch_run(i2_batch_t *batch)
             bool ok = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
             if (ok) {
                 try {
-                    batch_enqueue(batch, cs, batch->threads, batch->blocks_per_sm, batch->g_cap);
+                    batch_enqueue(batch, cs, batch->threads, batch->blocks_per_sm, batch->g_cap, batch->variant);
                 } catch (const Failure &) {
                     ok = false;
                 }
@@ -1289,7 +1328,7 @@ i2_status i2_batch_run(i2_batch_t *batch)
             I2_CHECK_CUDA(cudaGraphLaunch(batch->graph, batch->stream));
             batch->last_graph = true;
         } else {
-            batch_enqueue(batch, batch->stream, batch->threads, batch->blocks_per_sm, batch->g_cap);
+            batch_enqueue(batch, batch->stream, batch->threads, batch->blocks_per_sm, batch->g_cap, batch->variant);
             batch->last_graph = false;
         }
     });

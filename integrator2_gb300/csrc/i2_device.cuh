@@ -1,4 +1,4 @@
-// i2_device.cuh -- device-side geometry and FP64 integrands of the pair-integral path.
+// i2_device.cuh -- device-side geometry and integrands of the pair-integral path.
 //
 // Layout: every cell of a mesh has one 256-byte "panel" record (8 x 32-byte double4_32a,
 // loaded with 256-bit vector loads), written once by k_prepare_panels:
@@ -7,6 +7,14 @@
 //   [7] centroid.xyz, longest edge
 // Edge naming follows the reference (evaluatorJ3DK.cu:286-288): edge a = B->C, b = C->A,
 // c = A->B.
+//
+// The geometry and integrand functions are templates over the scalar type R.  The forward
+// kernels instantiate them with R = double (the names d3, PanelJ, Tri, ... below are those
+// instantiations); the adjoint kernels instantiate them with a dual number that carries the
+// derivatives with respect to one vertex's coordinates (i2_dual.cuh), so the backward pass
+// differentiates exactly the arithmetic of the forward pass.  Math functions are called
+// unqualified: for double they resolve to CUDA's, for dual numbers by argument-dependent
+// lookup to their own overloads.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -28,25 +36,59 @@ constexpr int kMaxGauss = 16;
 constexpr int kMaxDuffy = 16;
 constexpr int kMaxSelf = 32;
 
-// ------------------------------------------------------------------ small FP64 vectors
-struct d3 {
-    double x, y, z;
+// the value of a scalar (dual numbers provide their own overload)
+__host__ __device__ __forceinline__ double value_of(double x) { return x; }
+__host__ __device__ __forceinline__ float value_of(float x) { return x; }
+
+// ------------------------------------------------------------------ small vectors
+template <class R>
+struct V3 {
+    R x, y, z;
 };
+using d3 = V3<double>;
+
 __host__ __device__ __forceinline__ d3 mk(double x, double y, double z) { return d3{x, y, z}; }
-__host__ __device__ __forceinline__ d3 operator+(d3 a, d3 b) { return d3{a.x + b.x, a.y + b.y, a.z + b.z}; }
-__host__ __device__ __forceinline__ d3 operator-(d3 a, d3 b) { return d3{a.x - b.x, a.y - b.y, a.z - b.z}; }
-__host__ __device__ __forceinline__ d3 operator-(d3 a) { return d3{-a.x, -a.y, -a.z}; }
-__host__ __device__ __forceinline__ d3 operator*(double s, d3 a) { return d3{a.x * s, a.y * s, a.z * s}; }
-__host__ __device__ __forceinline__ double dot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__host__ __device__ __forceinline__ d3 cross(d3 a, d3 b)
+template <class R>
+__host__ __device__ __forceinline__ V3<R> operator+(V3<R> a, V3<R> b)
 {
-    return d3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+    return V3<R>{a.x + b.x, a.y + b.y, a.z + b.z};
 }
-__host__ __device__ __forceinline__ double norm(d3 a) { return sqrt(dot(a, a)); }
-__host__ __device__ __forceinline__ d3 unit(d3 a)
+template <class R>
+__host__ __device__ __forceinline__ V3<R> operator-(V3<R> a, V3<R> b)
 {
-    const double inv = 1.0 / norm(a);
-    return d3{a.x * inv, a.y * inv, a.z * inv};
+    return V3<R>{a.x - b.x, a.y - b.y, a.z - b.z};
+}
+template <class R>
+__host__ __device__ __forceinline__ V3<R> operator-(V3<R> a)
+{
+    return V3<R>{-a.x, -a.y, -a.z};
+}
+// scalar times vector; the result takes the type of the product (double x dual -> dual)
+template <class S, class R>
+__host__ __device__ __forceinline__ auto operator*(S s, V3<R> a) -> V3<decltype(a.x * s)>
+{
+    return V3<decltype(a.x * s)>{a.x * s, a.y * s, a.z * s};
+}
+template <class R>
+__host__ __device__ __forceinline__ R dot(V3<R> a, V3<R> b)
+{
+    return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+template <class R>
+__host__ __device__ __forceinline__ V3<R> cross(V3<R> a, V3<R> b)
+{
+    return V3<R>{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <class R>
+__host__ __device__ __forceinline__ R norm(V3<R> a)
+{
+    return sqrt(dot(a, a));
+}
+template <class R>
+__host__ __device__ __forceinline__ V3<R> unit(V3<R> a)
+{
+    const R inv = 1.0 / norm(a);
+    return V3<R>{a.x * inv, a.y * inv, a.z * inv};
 }
 __device__ __forceinline__ d3 xyz(const double4_32a &v) { return d3{v.x, v.y, v.z}; }
 
@@ -71,10 +113,12 @@ struct alignas(32) Panel {
 static_assert(sizeof(Panel) == 256, "panel record is 256 bytes");
 
 // a K_j panel held in registers
-struct PanelJ {
-    d3 A, B, C, n, ta, tb, tc;
-    double S, lenA, lenB, lenC;  // |C-B|, |A-C|, |B-A|
+template <class R>
+struct PanelJT {
+    V3<R> A, B, C, n, ta, tb, tc;
+    R S, lenA, lenB, lenC;  // |C-B|, |A-C|, |B-A|
 };
+using PanelJ = PanelJT<double>;
 
 __device__ __forceinline__ PanelJ load_panel(const Panel *__restrict__ p, int c)
 {
@@ -95,9 +139,32 @@ __device__ __forceinline__ PanelJ load_panel(const Panel *__restrict__ p, int c)
     return r;
 }
 
-struct Tri {
-    d3 a, b, c;
+// a K_j panel from its vertices (the same quantities k_prepare_panels stores)
+template <class R>
+__device__ __forceinline__ PanelJT<R> make_panel(V3<R> A, V3<R> B, V3<R> C)
+{
+    PanelJT<R> r;
+    r.A = A;
+    r.B = B;
+    r.C = C;
+    const V3<R> cr = cross(B - A, C - A);
+    r.n = unit(cr);
+    r.S = 0.5 * norm(cr);
+    const V3<R> ea = C - B, eb = A - C, ec = B - A;
+    r.lenA = norm(ea);
+    r.lenB = norm(eb);
+    r.lenC = norm(ec);
+    r.ta = unit(ea);
+    r.tb = unit(eb);
+    r.tc = unit(ec);
+    return r;
+}
+
+template <class R>
+struct TriT {
+    V3<R> a, b, c;
 };
+using Tri = TriT<double>;
 
 __device__ __forceinline__ Tri load_tri(const Panel *__restrict__ p, int c)
 {
@@ -107,26 +174,39 @@ __device__ __forceinline__ Tri load_tri(const Panel *__restrict__ p, int c)
 }
 
 // vertex k (0..2) of a panel in its stored order
-__device__ __forceinline__ d3 panel_vertex(const PanelJ &P, int k) { return k == 0 ? P.A : (k == 1 ? P.B : P.C); }
+template <class R>
+__device__ __forceinline__ V3<R> panel_vertex(const PanelJT<R> &P, int k)
+{
+    return k == 0 ? P.A : (k == 1 ? P.B : P.C);
+}
 
 // 1 -> 4 midpoint split in the reference's child order (NumericalIntegrator3d.cu:37-87):
 // child 0 = (m_ab, b, m_bc), 1 = (m_bc, c, m_ca), 2 = (m_ca, a, m_ab), 3 = (m_bc, m_ca, m_ab)
-__device__ __forceinline__ Tri child(const Tri &t, int k)
+template <class R>
+__device__ __forceinline__ TriT<R> child(const TriT<R> &t, int k)
 {
-    const d3 mbc = 0.5 * (t.b + t.c), mca = 0.5 * (t.c + t.a), mab = 0.5 * (t.a + t.b);
+    const V3<R> mbc = 0.5 * (t.b + t.c), mca = 0.5 * (t.c + t.a), mab = 0.5 * (t.a + t.b);
     switch (k) {
-    case 0: return Tri{mab, t.b, mbc};
-    case 1: return Tri{mbc, t.c, mca};
-    case 2: return Tri{mca, t.a, mab};
-    default: return Tri{mbc, mca, mab};
+    case 0: return TriT<R>{mab, t.b, mbc};
+    case 1: return TriT<R>{mbc, t.c, mca};
+    case 2: return TriT<R>{mca, t.a, mab};
+    default: return TriT<R>{mbc, mca, mab};
     }
 }
 
 // sub-cell s (base-4 digits, most significant = first split) of a level-L refinement
-__device__ __forceinline__ Tri subcell(Tri t, int level, int s)
+template <class R>
+__device__ __forceinline__ TriT<R> subcell(TriT<R> t, int level, int s)
 {
     for (int l = level - 1; l >= 0; --l) t = child(t, (s >> (2 * l)) & 3);
     return t;
+}
+
+// rotation so that vertex s comes first
+template <class R>
+__device__ __forceinline__ TriT<R> rotate(const TriT<R> &t, int s)
+{
+    return s == 0 ? t : (s == 1 ? TriT<R>{t.b, t.c, t.a} : TriT<R>{t.c, t.a, t.b});
 }
 
 // ------------------------------------------------------------------ quadrature tables
@@ -153,21 +233,28 @@ struct QuadTables {
 
 // ------------------------------------------------------------------ reference helpers
 // angle() with the reference's clamps (src/common/cuda_math.cu:14-26)
-__device__ __forceinline__ double angle_ref(d3 a, d3 b)
+template <class R>
+__device__ __forceinline__ R angle_ref(V3<R> a, V3<R> b)
 {
-    const double den = sqrt(dot(a, a) * dot(b, b));
-    if (den < kEps) return 0.0;
-    const double c = dot(a, b) / den;
-    if (c >= 1.0) return 0.0;
-    if (c <= -1.0) return kPi;
+    const R den = sqrt(dot(a, a) * dot(b, b));
+    if (den < kEps) return R(0.0);
+    const R c = dot(a, b) / den;
+    if (c >= 1.0) return R(0.0);
+    if (c <= -1.0) return R(kPi);
     return acos(c);
 }
-__device__ __forceinline__ double sign_ref(double x)
+// piecewise constants of the reference: their derivative is 0
+template <class R>
+__device__ __forceinline__ double sign_ref(R x)
 {
     if (fabs(x) < kDoubleMin) return 0.0;
     return x > kDoubleMin ? 1.0 : -1.0;
 }
-__device__ __forceinline__ double arg_ref(double x) { return x > kDoubleMin ? 0.0 : kPi; }
+template <class R>
+__device__ __forceinline__ double arg_ref(R x)
+{
+    return x > kDoubleMin ? 0.0 : kPi;
+}
 
 // ------------------------------------------------------------------ index shifts
 // position in each triangle of the single shared vertex (evaluatorJ3DK.cu:782-795)
@@ -202,15 +289,20 @@ __device__ __forceinline__ void shifts_edge(int3 ti, int3 tj, int &si, int &sj)
 // Van Oosterom-Strackee form with the triple product (x-A).((x-B)x(x-C)) = 2S n.(x-A).
 // The collinear fallback of the reference is kept.  The potential integrand
 // sum_e t_e L_e - d Theta rides on the same logs (t_e = m_e.(P_e - x), m_e = tau_e x n).
-struct FarCtx {
-    d3 ma, mb, mc;  // outward in-plane edge normals of K_j
+template <class R>
+struct FarCtxT {
+    V3<R> ma, mb, mc;  // outward in-plane edge normals of K_j
 };
-__device__ __forceinline__ FarCtx make_far_ctx(const PanelJ &K)
+using FarCtx = FarCtxT<double>;
+
+template <class R>
+__device__ __forceinline__ FarCtxT<R> make_far_ctx(const PanelJT<R> &K)
 {
-    return FarCtx{cross(K.ta, K.n), cross(K.tb, K.n), cross(K.tc, K.n)};
+    return FarCtxT<R>{cross(K.ta, K.n), cross(K.tb, K.n), cross(K.tc, K.n)};
 }
 
-__device__ __forceinline__ double edge_log_fp64(double l_from, double q_from, double l_to, double q_to)
+template <class R>
+__device__ __forceinline__ R edge_log_fp64(R l_from, R q_from, R l_to, R q_to)
 {
     // q = (x - P).tau ; reference: |1 + unit(x - P_to).tau| < eps^2/2 -> log(l_to / l_from)
     if (fabs(q_to + l_to) < 0.5 * kEpsPsi2 * l_to) return log(l_to / l_from);
@@ -219,26 +311,61 @@ __device__ __forceinline__ double edge_log_fp64(double l_from, double q_from, do
 
 // from the point-to-vertex offsets oa = x - A, ob = x - B, oc = x - C (callers that know a point
 // only relative to a nearby vertex form these offsets without cancellation)
-__device__ __forceinline__ void far_integrand_o(d3 oa, d3 ob, d3 oc, const PanelJ &K, const FarCtx &F, d3 &psi, double &th,
-                                                double &pot)
+template <class R>
+__device__ __forceinline__ void far_integrand_o(V3<R> oa, V3<R> ob, V3<R> oc, const PanelJT<R> &K, const FarCtxT<R> &F,
+                                                V3<R> &psi, R &th, R &pot)
 {
-    const double la = norm(oa), lb = norm(ob), lc = norm(oc);
-    const double Lc = edge_log_fp64(la, dot(oa, K.tc), lb, dot(ob, K.tc));  // A -> B
-    const double La = edge_log_fp64(lb, dot(ob, K.ta), lc, dot(oc, K.ta));  // B -> C
-    const double Lb = edge_log_fp64(lc, dot(oc, K.tb), la, dot(oa, K.tb));  // C -> A
+    const R la = norm(oa), lb = norm(ob), lc = norm(oc);
+    const R Lc = edge_log_fp64(la, dot(oa, K.tc), lb, dot(ob, K.tc));  // A -> B
+    const R La = edge_log_fp64(lb, dot(ob, K.ta), lc, dot(oc, K.ta));  // B -> C
+    const R Lb = edge_log_fp64(lc, dot(oc, K.tb), la, dot(oa, K.tb));  // C -> A
     psi = Lc * K.tc + La * K.ta + Lb * K.tb;
-    const double d = dot(K.n, oa);
-    const double num = 2.0 * K.S * d;
-    const double den = la * lb * lc + dot(oa, ob) * lc + dot(ob, oc) * la + dot(oc, oa) * lb;
+    const R d = dot(K.n, oa);
+    const R num = 2.0 * K.S * d;
+    const R den = la * lb * lc + dot(oa, ob) * lc + dot(ob, oc) * la + dot(oc, oa) * lb;
     th = 2.0 * atan2(num, den);
     // t_e L_e -> 0 on the line of edge e even where L_e itself overflows
-    const double ta_ = -dot(F.ma, ob), tb_ = -dot(F.mb, oc), tc_ = -dot(F.mc, oa);
-    pot = (ta_ == 0.0 ? 0.0 : ta_ * La) + (tb_ == 0.0 ? 0.0 : tb_ * Lb) + (tc_ == 0.0 ? 0.0 : tc_ * Lc) - d * th;
+    const R ta_ = -dot(F.ma, ob), tb_ = -dot(F.mb, oc), tc_ = -dot(F.mc, oa);
+    pot = (ta_ == 0.0 ? R(0.0) : ta_ * La) + (tb_ == 0.0 ? R(0.0) : tb_ * Lb) + (tc_ == 0.0 ? R(0.0) : tc_ * Lc) - d * th;
 }
 
-__device__ __forceinline__ void far_integrand(d3 x, const PanelJ &K, const FarCtx &F, d3 &psi, double &th, double &pot)
+template <class R>
+__device__ __forceinline__ void far_integrand(V3<R> x, const PanelJT<R> &K, const FarCtxT<R> &F, V3<R> &psi, R &th, R &pot)
 {
     far_integrand_o(x - K.A, x - K.B, x - K.C, K, F, psi, th, pot);
+}
+
+// ln((l_P + q_P) / (l_Q + q_Q)) for the edge P -> Q of length L from sums and products of
+// positive terms only (q_P - q_Q = L; the squared distance to the edge line is taken from the
+// nearer endpoint).  The same form as the FP32 bulk's edge_log_f32, for single-precision scalar
+// types (FP32 adjoint) where the reference's form cancels.
+template <class R>
+__device__ __forceinline__ R edge_log_pos(R lP, R qP, V3<R> oP, R lQ, R qQ, V3<R> oQ, V3<R> tau, R L)
+{
+    const R s = lP + lQ;
+    if (qQ >= 0.0) return log1p(L * (s + qP + qQ) / (s * (lQ + qQ)));
+    if (qP <= 0.0) return log1p(L * (s - qP - qQ) / (s * (lP - qP)));
+    const V3<R> r = cross(lP < lQ ? oP : oQ, tau);
+    const R h2 = dot(r, r);
+    const R num = (lP + qP) * (lQ - qQ);
+    if (num > 2.0 * h2) return log(num / h2);
+    return log1p((lP + qP) * L * (s - qP - qQ) / (s * h2));
+}
+
+// far_integrand_o with edge_log_pos (no collinear fallback needed: no term cancels)
+template <class R>
+__device__ __forceinline__ void far_integrand_pos(V3<R> x, const PanelJT<R> &K, const FarCtxT<R> &F, V3<R> &psi, R &th, R &pot)
+{
+    const V3<R> oa = x - K.A, ob = x - K.B, oc = x - K.C;
+    const R la = norm(oa), lb = norm(ob), lc = norm(oc);
+    const R Lc = edge_log_pos(la, dot(oa, K.tc), oa, lb, dot(ob, K.tc), ob, K.tc, K.lenC);  // A -> B
+    const R La = edge_log_pos(lb, dot(ob, K.ta), ob, lc, dot(oc, K.ta), oc, K.ta, K.lenA);  // B -> C
+    const R Lb = edge_log_pos(lc, dot(oc, K.tb), oc, la, dot(oa, K.tb), oa, K.tb, K.lenB);  // C -> A
+    psi = Lc * K.tc + La * K.ta + Lb * K.tb;
+    const R d = dot(K.n, oa);
+    const R den = la * lb * lc + dot(oa, ob) * lc + dot(ob, oc) * la + dot(oc, oa) * lb;
+    th = 2.0 * atan2(2.0 * K.S * d, den);
+    pot = -dot(F.ma, ob) * La - dot(F.mb, oc) * Lb - dot(F.mc, oa) * Lc - d * th;
 }
 
 // ------------------------------------------------------------------ a2: common-edge regular part
@@ -248,39 +375,43 @@ __device__ __forceinline__ void far_integrand(d3 x, const PanelJ &K, const FarCt
 // single well-conditioned log:
 //   Psi_reg = log((l_A + o_A.tb) / |BC|) tb + log((l_A - o_A.ta) / |BC|) ta,
 // tb = unit(JB-JA), ta = unit(JA-JC).  Theta_reg keeps the reference's three atan2 (branches).
-struct EdgeCtx {
-    d3 JA, JB, JC, ta, tb, tc;
-    double ilvc;
+template <class R>
+struct EdgeCtxT {
+    V3<R> JA, JB, JC, ta, tb, tc;
+    R ilvc;
     int sj;
 };
+using EdgeCtx = EdgeCtxT<double>;
 
-__device__ __forceinline__ EdgeCtx make_edge_ctx(const PanelJ &K, int sj)
+template <class R>
+__device__ __forceinline__ EdgeCtxT<R> make_edge_ctx(const PanelJT<R> &K, int sj)
 {
-    EdgeCtx e;
+    EdgeCtxT<R> e;
     e.sj = sj;
     e.JA = panel_vertex(K, sj);
     e.JB = panel_vertex(K, (sj + 1) % 3);
     e.JC = panel_vertex(K, (sj + 2) % 3);
     e.ta = unit(e.JA - e.JC);
     e.tb = unit(e.JB - e.JA);
-    const d3 c = e.JC - e.JB;
+    const V3<R> c = e.JC - e.JB;
     e.ilvc = 1.0 / norm(c);
     e.tc = e.ilvc * c;
     return e;
 }
 
-__device__ __forceinline__ void edge_integrand(d3 x, const PanelJ &K, const EdgeCtx &E, d3 &psi, double &th)
+template <class R>
+__device__ __forceinline__ void edge_integrand(V3<R> x, const PanelJT<R> &K, const EdgeCtxT<R> &E, V3<R> &psi, R &th)
 {
-    const d3 oA = x - E.JA, oB = x - E.JB, oC = x - E.JC;
-    const double lA = norm(oA), lB = norm(oB), lC = norm(oC);
-    const double l1 = log((lA + dot(oA, E.tb)) * E.ilvc);
-    const double l2 = log((lA - dot(oA, E.ta)) * E.ilvc);
+    const V3<R> oA = x - E.JA, oB = x - E.JB, oC = x - E.JC;
+    const R lA = norm(oA), lB = norm(oB), lC = norm(oC);
+    const R l1 = log((lA + dot(oA, E.tb)) * E.ilvc);
+    const R l2 = log((lA - dot(oA, E.ta)) * E.ilvc);
     psi = l1 * E.tb + l2 * E.ta;
     // full solid angle (rotation keeps orientation), minus the two asymptotic angles
-    const double num = 2.0 * K.S * dot(K.n, oA);
-    const double den = lA * lB * lC + dot(oA, oB) * lC + dot(oB, oC) * lA + dot(oC, oA) * lB;
-    const double s1 = atan2(dot(cross(oB, E.tb), E.tc), dot(E.tb - E.tc, lB * E.tb + oB));
-    const double s2 = atan2(dot(cross(oC, E.ta), E.tc), dot(E.ta - E.tc, lC * E.ta - oC));
+    const R num = 2.0 * K.S * dot(K.n, oA);
+    const R den = lA * lB * lC + dot(oA, oB) * lC + dot(oB, oC) * lA + dot(oC, oA) * lB;
+    const R s1 = atan2(dot(cross(oB, E.tb), E.tc), dot(E.tb - E.tc, lB * E.tb + oB));
+    const R s2 = atan2(dot(cross(oC, E.ta), E.tc), dot(E.ta - E.tc, lC * E.ta - oC));
     th = 2.0 * atan2(num, den) - 2.0 * (s1 - s2);
 }
 
@@ -289,21 +420,25 @@ __device__ __forceinline__ void edge_integrand(d3 x, const PanelJ &K, const Edge
 // vertex.  The per-pair direction e (with the reference's two sign flips) is computed once per
 // task.  Fused logs: the two edges at JA give log((l_C + o_C.ta) / sqrt(S_i)) ta and
 // log((l_B - o_B.tb) / sqrt(S_i)) tb, the opposite edge keeps its thetaPsi term.
-struct VertexCtx {
-    d3 JA, JB, JC, ta, tb, tbc, e;
-    double inv_sqrt_si;
+template <class R>
+struct VertexCtxT {
+    V3<R> JA, JB, JC, ta, tb, tbc, e;
+    R inv_sqrt_si;
 };
+using VertexCtx = VertexCtxT<double>;
 
-__device__ __forceinline__ void vertex_deltas(d3 ta, d3 tb, d3 nj, d3 e, double &dA, double &dB)
+template <class R>
+__device__ __forceinline__ void vertex_deltas(V3<R> ta, V3<R> tb, V3<R> nj, V3<R> e, R &dA, R &dB)
 {
     dA = atan2(dot(cross(ta, e), nj), -dot(e, ta));
     dB = atan2(dot(cross(e, tb), nj), dot(e, tb));
 }
 
 // intersection direction of the two planes with the reference's flips (:376-399 / :698-723)
-__device__ __forceinline__ d3 vertex_direction(d3 ni, d3 nj, d3 ta, d3 tb, double &dA, double &dB)
+template <class R>
+__device__ __forceinline__ V3<R> vertex_direction(V3<R> ni, V3<R> nj, V3<R> ta, V3<R> tb, R &dA, R &dB)
 {
-    d3 e = cross(ni, nj);
+    V3<R> e = cross(ni, nj);
     if (dot(e, e) < kEps2) e = tb;
     else e = unit(e);
     vertex_deltas(ta, tb, nj, e, dA, dB);
@@ -311,68 +446,76 @@ __device__ __forceinline__ d3 vertex_direction(d3 ni, d3 nj, d3 ta, d3 tb, doubl
         e = -1.0 * e;
         vertex_deltas(ta, tb, nj, e, dA, dB);
     }
-    if ((dA * dB < 0) && (fabs(dA - dB) > kPi)) {
+    if ((dA * dB < 0.0) && (fabs(dA - dB) > kPi)) {
         e = -1.0 * e;
         vertex_deltas(ta, tb, nj, e, dA, dB);
     }
     return e;
 }
 
-__device__ __forceinline__ VertexCtx make_vertex_ctx(const PanelJ &K, int sj, d3 ni, double Si)
+template <class R>
+__device__ __forceinline__ VertexCtxT<R> make_vertex_ctx(const PanelJT<R> &K, int sj, V3<R> ni, R Si)
 {
-    VertexCtx v;
+    VertexCtxT<R> v;
     v.JA = panel_vertex(K, sj);
     v.JB = panel_vertex(K, (sj + 1) % 3);
     v.JC = panel_vertex(K, (sj + 2) % 3);
     v.ta = unit(v.JA - v.JC);
     v.tb = unit(v.JB - v.JA);
     v.tbc = unit(v.JC - v.JB);
-    double dA, dB;
+    R dA, dB;
     v.e = vertex_direction(ni, K.n, v.ta, v.tb, dA, dB);
     v.inv_sqrt_si = 1.0 / sqrt(Si);
     return v;
 }
 
-__device__ __forceinline__ void vertex_integrand(d3 x, const PanelJ &K, const VertexCtx &V, d3 &psi, double &th)
+template <class R>
+__device__ __forceinline__ void vertex_integrand(V3<R> x, const PanelJT<R> &K, const VertexCtxT<R> &V, V3<R> &psi, R &th)
 {
-    const d3 oA = x - V.JA, oB = x - V.JB, oC = x - V.JC;
-    const double lA = norm(oA), lB = norm(oB), lC = norm(oC);
-    const double Lbc = edge_log_fp64(lB, dot(oB, V.tbc), lC, dot(oC, V.tbc));
-    const double l1 = log((lC + dot(oC, V.ta)) * V.inv_sqrt_si);
-    const double l2 = log((lB - dot(oB, V.tb)) * V.inv_sqrt_si);
+    const V3<R> oA = x - V.JA, oB = x - V.JB, oC = x - V.JC;
+    const R lA = norm(oA), lB = norm(oB), lC = norm(oC);
+    const R Lbc = edge_log_fp64(lB, dot(oB, V.tbc), lC, dot(oC, V.tbc));
+    const R l1 = log((lC + dot(oC, V.ta)) * V.inv_sqrt_si);
+    const R l2 = log((lB - dot(oB, V.tb)) * V.inv_sqrt_si);
     psi = Lbc * V.tbc + l1 * V.ta + l2 * V.tb;
-    const double num = 2.0 * K.S * dot(K.n, oA);
-    const double den = lA * lB * lC + dot(oA, oB) * lC + dot(oB, oC) * lA + dot(oC, oA) * lB;
-    const double s1 = atan2(dot(cross(oA, V.ta), V.e), dot(lA * V.e - oA, V.e - V.ta));
-    const double s2 = atan2(dot(cross(oA, V.tb), V.e), dot(lA * V.e - oA, V.e + V.tb));
+    const R num = 2.0 * K.S * dot(K.n, oA);
+    const R den = lA * lB * lC + dot(oA, oB) * lC + dot(oB, oC) * lA + dot(oC, oA) * lB;
+    const R s1 = atan2(dot(cross(oA, V.ta), V.e), dot(lA * V.e - oA, V.e - V.ta));
+    const R s2 = atan2(dot(cross(oA, V.tb), V.e), dot(lA * V.e - oA, V.e + V.tb));
     th = 2.0 * atan2(num, den) - 2.0 * (s1 + s2);
 }
 
 // ------------------------------------------------------------------ a4: common-edge closed form
-struct sc2 {
-    double s, c;
+template <class R>
+struct SC2 {
+    R s, c;
 };
-__device__ __forceinline__ sc2 sc_of(double a)
+using sc2 = SC2<double>;
+
+template <class R>
+__device__ __forceinline__ SC2<R> sc_of(R a)
 {
-    sc2 r;
+    SC2<R> r;
     sincos(a, &r.s, &r.c);
     return r;
 }
 
 // 2 atan2(sin xi sin a sin g, 1 - cos a + cos g + cos l)   (evaluatorJ3DK.cu:418-421)
-__device__ __forceinline__ double phi_fn(sc2 a, sc2 g, double sxi, double cl)
+template <class R>
+__device__ __forceinline__ R phi_fn(SC2<R> a, SC2<R> g, R sxi, R cl)
 {
     return 2.0 * atan2(sxi * a.s * g.s, 1.0 - a.c + g.c + cl);
 }
 
 // q_theta, q_psi of the common-edge closed form (:438-461) and its coplanar limit (:474-481;
 // the reference leaves q_theta unset there, its documented value is 0)
-__device__ inline void q_edge(sc2 a, sc2 b, sc2 g, sc2 n, sc2 xi, double cmu, double cla, double &qt, double &qp)
+template <class R>
+__device__ inline void q_edge(SC2<R> a, SC2<R> b, SC2<R> g, SC2<R> n, SC2<R> xi, R cmu, R cla, R &qt, R &qp)
 {
-    const sc2 am{a.s, -a.c}, gm{g.s, -g.c};
-    const double p1 = phi_fn(a, g, xi.s, cla);
-    const double p2 = phi_fn(am, gm, xi.s, cla);
-    const double k = 1.0 / (a.s * (1.0 - cmu * cmu));
+    const SC2<R> am{a.s, -a.c}, gm{g.s, -g.c};
+    const R p1 = phi_fn(a, g, xi.s, cla);
+    const R p2 = phi_fn(am, gm, xi.s, cla);
+    const R k = 1.0 / (a.s * (1.0 - cmu * cmu));
     qt = p1 + g.s * n.s * k *
                   ((b.c * g.s - xi.c * b.s * g.c) * p2 +
                    xi.s * b.s *
@@ -382,33 +525,35 @@ __device__ inline void q_edge(sc2 a, sc2 b, sc2 g, sc2 n, sc2 xi, double cmu, do
                     b.s * (1.0 - cmu) * (n.c - cla) * log(b.s / n.s) +
                     n.s * b.s * (b.s * g.c - xi.c * g.s * b.c) * log((1.0 - n.c) / (1.0 + b.c)) + p2 * xi.s * g.s * n.s * b.s);
 }
-__device__ inline void q_edge_coplanar(sc2 b, sc2 n, double sa, double &qt, double &qp)
+template <class R>
+__device__ inline void q_edge_coplanar(SC2<R> b, SC2<R> n, R sa, R &qt, R &qp)
 {
-    qt = 0.0;
+    qt = R(0.0);
     qp = 1.5 - (n.c * b.s * log(1.0 + n.c) + n.s * b.c * log(1.0 - b.c) + sa - b.s + n.s + b.s * n.c * log(b.s / n.s)) / sa;
 }
 
 // integrateSingularPartAttached (:603-672): closed-form integral over K_i of the common-edge
 // asymptote; Ti/Tj hold the vertices rotated so that the off-edge vertex comes first
-__device__ inline void closed_edge(Tri Ti, Tri Tj, d3 ni, d3 nj, double Si, d3 &psi, double &th)
+template <class R>
+__device__ inline void closed_edge(TriT<R> Ti, TriT<R> Tj, V3<R> ni, V3<R> nj, R Si, V3<R> &psi, R &th)
 {
-    const d3 IA = Ti.a, IB = Ti.b, IC = Ti.c, JA = Tj.a, JB = Tj.b, JC = Tj.c;
-    const d3 ta = unit(JA - JC), tb = unit(JB - JA), tc = unit(JC - JB);
-    const double al = angle_ref(IA - IC, IB - IC);
-    const double be = angle_ref(IC - IB, IA - IB);
-    const double ga = angle_ref(JC - JB, JA - JB);
-    const double de = angle_ref(JB - JC, JA - JC);
-    const double nu = kPi - al - be;
-    const double xi = atan2(dot(cross(ni, nj), tc), dot(ni, nj));
-    const sc2 sa = sc_of(al), sb = sc_of(be), sg = sc_of(ga), sd = sc_of(de), sx = sc_of(xi);
-    const sc2 sn{sa.s * sb.c + sa.c * sb.s, sa.s * sb.s - sa.c * sb.c};
-    const double csig = -(sa.c * sd.c + sx.c * sa.s * sd.s);
-    const double cmu = -(sb.c * sg.c + sx.c * sb.s * sg.s);
-    const double cla = -(sa.c * sg.c - sx.c * sa.s * sg.s);
-    const double cth = -(sb.c * sd.c - sx.c * sb.s * sd.s);
-    const double qab = sn.s * log(tan(0.5 * al) * tan(0.5 * nu)) / sb.s + sn.s * log(tan(0.5 * be) * tan(0.5 * nu)) / sa.s +
-                       log(tan(0.5 * al) * tan(0.5 * be));
-    double qAt, qAp, qBt, qBp;
+    const V3<R> IA = Ti.a, IB = Ti.b, IC = Ti.c, JA = Tj.a, JB = Tj.b, JC = Tj.c;
+    const V3<R> ta = unit(JA - JC), tb = unit(JB - JA), tc = unit(JC - JB);
+    const R al = angle_ref(IA - IC, IB - IC);
+    const R be = angle_ref(IC - IB, IA - IB);
+    const R ga = angle_ref(JC - JB, JA - JB);
+    const R de = angle_ref(JB - JC, JA - JC);
+    const R nu = kPi - al - be;
+    const R xi = atan2(dot(cross(ni, nj), tc), dot(ni, nj));
+    const SC2<R> sa = sc_of(al), sb = sc_of(be), sg = sc_of(ga), sd = sc_of(de), sx = sc_of(xi);
+    const SC2<R> sn{sa.s * sb.c + sa.c * sb.s, sa.s * sb.s - sa.c * sb.c};
+    const R csig = -(sa.c * sd.c + sx.c * sa.s * sd.s);
+    const R cmu = -(sb.c * sg.c + sx.c * sb.s * sg.s);
+    const R cla = -(sa.c * sg.c - sx.c * sa.s * sg.s);
+    const R cth = -(sb.c * sd.c - sx.c * sb.s * sd.s);
+    const R qab = sn.s * log(tan(0.5 * al) * tan(0.5 * nu)) / sb.s + sn.s * log(tan(0.5 * be) * tan(0.5 * nu)) / sa.s +
+                  log(tan(0.5 * al) * tan(0.5 * be));
+    R qAt, qAp, qBt, qBp;
     if (fabs(xi) < kEps && fabs(be - ga) < kEps) q_edge_coplanar(sb, sn, sa.s, qAt, qAp);
     else q_edge(sa, sb, sg, sn, sx, cmu, cla, qAt, qAp);
     if (fabs(xi) < kEps && fabs(al - de) < kEps) q_edge_coplanar(sa, sn, sb.s, qBt, qBp);
@@ -418,48 +563,49 @@ __device__ inline void closed_edge(Tri Ti, Tri Tj, d3 ni, d3 nj, double Si, d3 &
 }
 
 // ------------------------------------------------------------------ a5: common-vertex closed form
-struct VtxAngles {
-    sc2 xi, mu, nu, psi, nupsi, mupsi;
-    double mu_a, nu_a, psi_a, kappa, skappa, lsmu, lsnu;
+template <class R>
+struct VtxAnglesT {
+    SC2<R> xi, mu, nu, psi, nupsi, mupsi;
+    R mu_a, nu_a, psi_a, kappa, skappa, lsmu, lsnu;
 };
 
 // q_thetaPsi_cont (:511-601): general case plus the reference's four special branches
-__device__ inline void q_vertex(const VtxAngles &g, double delta, sc2 sd, double cla, double cth, double ceta, double csig,
-                                double cchi, double &qt, double &qp)
+template <class R>
+__device__ inline void q_vertex(const VtxAnglesT<R> &g, R delta, SC2<R> sd, R cla, R cth, R ceta, R csig, R cchi, R &qt, R &qp)
 {
-    const double mu = g.mu_a, nu = g.nu_a, ps = g.psi_a, sk = g.skappa;
-    const sc2 xi = g.xi, smu = g.mu, snu = g.nu, sps = g.psi;
-    const double lth = log(1.0 + cth), lla = log(1.0 + cla);
-    const double Lam1 = lla - lth + g.lsnu - g.lsmu;
-    const double Lam2 = log(tan(0.5 * nu) * tan(0.5 * mu));
-    const sc2 hd = sc_of(0.5 * delta);
-    const double thd = hd.s / hd.c;
-    const sc2 hmp = sc_of(0.5 * (mu - ps)), hnp = sc_of(0.5 * (nu + ps));
-    const double Amu = atan2(thd * hmp.c * xi.s, thd * hmp.c * xi.c + hmp.s);
-    const double Anu = atan2(thd * hnp.s * xi.s, thd * hnp.s * xi.c + hnp.c);
-    const sc2 t1 = sc_of(0.5 * (mu - ps) - 0.5 * (nu + ps)), t2 = sc_of(0.5 * g.kappa);
-    const double W = atan2(sd.s * t2.s * xi.s, t2.c + sd.s * t1.c * xi.c + sd.c * t1.s);
-    const sc2 t3 = sc_of(delta - ps);
-    const double D = 1.0 / (t3.s * t3.s + sd.s * sps.s * (1.0 - xi.c) * (t3.c + csig));
-    const double G = sps.c * (sd.s * csig * xi.c + sd.c * cchi - sd.s * sd.s / sps.s);
-    const double mpsi = sign_ref(xi.s * sps.s), mdel = sign_ref(xi.s * sd.s);
+    const R mu = g.mu_a, nu = g.nu_a, ps = g.psi_a, sk = g.skappa;
+    const SC2<R> xi = g.xi, smu = g.mu, snu = g.nu, sps = g.psi;
+    const R lth = log(1.0 + cth), lla = log(1.0 + cla);
+    const R Lam1 = lla - lth + g.lsnu - g.lsmu;
+    const R Lam2 = log(tan(0.5 * nu) * tan(0.5 * mu));
+    const SC2<R> hd = sc_of(R(0.5 * delta));
+    const R thd = hd.s / hd.c;
+    const SC2<R> hmp = sc_of(R(0.5 * (mu - ps))), hnp = sc_of(R(0.5 * (nu + ps)));
+    const R Amu = atan2(thd * hmp.c * xi.s, thd * hmp.c * xi.c + hmp.s);
+    const R Anu = atan2(thd * hnp.s * xi.s, thd * hnp.s * xi.c + hnp.c);
+    const SC2<R> t1 = sc_of(R(0.5 * (mu - ps) - 0.5 * (nu + ps))), t2 = sc_of(R(0.5 * g.kappa));
+    const R W = atan2(sd.s * t2.s * xi.s, t2.c + sd.s * t1.c * xi.c + sd.c * t1.s);
+    const SC2<R> t3 = sc_of(R(delta - ps));
+    const R D = 1.0 / (t3.s * t3.s + sd.s * sps.s * (1.0 - xi.c) * (t3.c + csig));
+    const R G = sps.c * (sd.s * csig * xi.c + sd.c * cchi - sd.s * sd.s / sps.s);
+    const double mpsi = sign_ref(R(xi.s * sps.s)), mdel = sign_ref(R(xi.s * sd.s));
     if (fabs(xi.s) < kEps && 1.0 - fabs(csig) < 0.5 * kEps2 && fabs(sps.s) > kEps) {
-        const double ara = arg_ref(sin(0.5 * (nu + ps)) * csig);
-        const double arb = arg_ref(cos(0.5 * (mu - ps)) * csig);
+        const double ara = arg_ref(R(sin(0.5 * (nu + ps)) * csig));
+        const double arb = arg_ref(R(cos(0.5 * (mu - ps)) * csig));
         qt = 2.0 * mpsi * csig * xi.c / (sk * sps.s) * (smu.s * g.nupsi.s * ara - snu.s * g.mupsi.s * arb);
         qp = 0.5 * (1.0 - log(2.0)) - 0.5 * log((1.0 - csig * smu.c) * (1.0 + csig * snu.c) / sk) +
              csig * (smu.s - snu.s + 0.5 * sin(mu - nu) * Lam2) / sk;
         return;
     }
-    const double gens = 0.5 * (3.0 - log(2.0)) +
-                        (smu.s * snu.s / sk) * ((lla - lth) * sps.c / sps.s +
-                                                D * (Lam1 * sd.s * ceta / sps.s + Lam2 * cchi - 2.0 * W * sd.s * xi.s -
-                                                     G * (g.lsnu - g.lsmu))) -
-                        (smu.c * snu.s * (lla - g.lsmu) + smu.s * snu.c * (lth - g.lsnu)) / sk - 0.5 * (g.lsmu + g.lsnu - log(sk));
+    const R gens = 0.5 * (3.0 - log(2.0)) +
+                   (smu.s * snu.s / sk) * ((lla - lth) * sps.c / sps.s +
+                                           D * (Lam1 * sd.s * ceta / sps.s + Lam2 * cchi - 2.0 * W * sd.s * xi.s -
+                                                G * (g.lsnu - g.lsmu))) -
+                   (smu.c * snu.s * (lla - g.lsmu) + smu.s * snu.c * (lth - g.lsnu)) / sk - 0.5 * (g.lsmu + g.lsnu - log(sk));
     if (fabs(xi.s) < kEps && fabs(sps.s) > kEps) {
-        const double are = arg_ref(sin(0.5 * (nu + mu)) + sin(0.5 * (mu - nu) - ps + delta * xi.c));
-        const double arc = arg_ref(1.0 / tan(0.5 * (nu + ps)) + tan(0.5 * delta) * xi.c);
-        const double ard = arg_ref(tan(0.5 * (mu - ps)) + tan(0.5 * delta) * xi.c);
+        const double are = arg_ref(R(sin(0.5 * (nu + mu)) + sin(0.5 * (mu - nu) - ps + delta * xi.c)));
+        const double arc = arg_ref(R(1.0 / tan(0.5 * (nu + ps)) + tan(0.5 * delta) * xi.c));
+        const double ard = arg_ref(R(tan(0.5 * (mu - ps)) + tan(0.5 * delta) * xi.c));
         qt = 2.0 * mdel * (sd.s * smu.s * snu.s / cchi * xi.c * are + smu.s * g.nupsi.s * arc - snu.s * g.mupsi.s * ard) /
              (sk * sps.s);
         qp = gens;
@@ -468,13 +614,13 @@ __device__ inline void q_vertex(const VtxAngles &g, double delta, sc2 sd, double
     if (fabs(sin(ps)) < kEps) {
         if (fabs(delta) > kEps) {
             qt = 2.0 * (smu.s * snu.s * (W * sd.c * xi.c - 0.5 * (Lam1 - Lam2 * csig) * xi.s) / sd.s +
-                        (Anu + mdel * arg_ref(sin(0.5 * (nu + ps)))) * smu.s * snu.c +
-                        (Amu + mdel * arg_ref(cos(0.5 * (mu - ps)))) * smu.c * snu.s) /
+                        (Anu + mdel * arg_ref(R(sin(0.5 * (nu + ps))))) * smu.s * snu.c +
+                        (Amu + mdel * arg_ref(R(cos(0.5 * (mu - ps))))) * smu.c * snu.s) /
                  sk;
             qp = 0.5 * (3.0 - log(2.0)) - 0.5 * (log((1.0 + cla) * (1.0 + cth) / sk) - sin(mu - nu) / sk * Lam1) -
                  smu.s * snu.s * ((Lam1 * sd.c - Lam2 * sps.c) * xi.c + 2.0 * W * xi.s) / (sk * sd.s);
         } else {
-            qt = 2.0 * arg_ref(sps.c);
+            qt = R(2.0 * arg_ref(sps.c));
             qp = 0.5 * (1.0 - log(2.0)) - 0.5 * log((1.0 - sps.c * smu.c) * (1.0 + sps.c * snu.c) / sk) +
                  (0.5 * sin(mu - nu) * Lam1 + sps.c * (smu.s - snu.s)) / sk;
         }
@@ -487,17 +633,18 @@ __device__ inline void q_vertex(const VtxAngles &g, double delta, sc2 sd, double
 }
 
 // integrateSingularPartSimple (:674-780); Ti/Tj rotated so that the shared vertex comes first
-__device__ inline void closed_vertex(Tri Ti, Tri Tj, d3 ni, d3 nj, double Si, d3 &psi, double &th)
+template <class R>
+__device__ inline void closed_vertex(TriT<R> Ti, TriT<R> Tj, V3<R> ni, V3<R> nj, R Si, V3<R> &psi, R &th)
 {
-    const d3 IA = Ti.a, IB = Ti.b, IC = Ti.c, JA = Tj.a, JB = Tj.b, JC = Tj.c;
-    const d3 ta = unit(JA - JC), tb = unit(JB - JA);
-    double dA, dB;
-    const d3 e = vertex_direction(ni, nj, ta, tb, dA, dB);
-    const double xi = atan2(dot(cross(ni, nj), e), dot(ni, nj));
-    const sc2 sdA = sc_of(dA), sdB = sc_of(dB);
-    VtxAngles g;
+    const V3<R> IA = Ti.a, IB = Ti.b, IC = Ti.c, JA = Tj.a, JB = Tj.b, JC = Tj.c;
+    const V3<R> ta = unit(JA - JC), tb = unit(JB - JA);
+    R dA, dB;
+    const V3<R> e = vertex_direction(ni, nj, ta, tb, dA, dB);
+    const R xi = atan2(dot(cross(ni, nj), e), dot(ni, nj));
+    const SC2<R> sdA = sc_of(dA), sdB = sc_of(dB);
+    VtxAnglesT<R> g;
     g.xi = sc_of(xi);
-    const d3 s = IC - IB;
+    const V3<R> s = IC - IB;
     g.nu_a = angle_ref(IA - IB, IC - IB);
     g.mu_a = angle_ref(IB - IC, IA - IC);
     g.kappa = angle_ref(IB - IA, IC - IA);
@@ -508,43 +655,48 @@ __device__ inline void closed_vertex(Tri Ti, Tri Tj, d3 ni, d3 nj, double Si, d3
     g.skappa = sin(g.kappa);
     g.psi_a = atan2(dot(cross(e, s), ni), dot(e, s));
     g.psi = sc_of(g.psi_a);
-    g.nupsi = sc_of(g.nu_a + g.psi_a);
-    g.mupsi = sc_of(g.mu_a - g.psi_a);
-    double q[2][2];
+    g.nupsi = sc_of(R(g.nu_a + g.psi_a));
+    g.mupsi = sc_of(R(g.mu_a - g.psi_a));
+    R q[2][2];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-        const sc2 d = h == 0 ? sdA : sdB;
-        const double csig = d.s * g.psi.s * g.xi.c + d.c * g.psi.c;
-        const double cchi = d.s * g.psi.c * g.xi.c - d.c * g.psi.s;
-        const double ceta = d.c * g.psi.s * g.xi.c - d.s * g.psi.c;
-        const double cth = d.s * g.nupsi.s * g.xi.c + d.c * g.nupsi.c;
-        const double cla = d.s * g.mupsi.s * g.xi.c - d.c * g.mupsi.c;
+        const SC2<R> d = h == 0 ? sdA : sdB;
+        const R csig = d.s * g.psi.s * g.xi.c + d.c * g.psi.c;
+        const R cchi = d.s * g.psi.c * g.xi.c - d.c * g.psi.s;
+        const R ceta = d.c * g.psi.s * g.xi.c - d.s * g.psi.c;
+        const R cth = d.s * g.nupsi.s * g.xi.c + d.c * g.nupsi.c;
+        const R cla = d.s * g.mupsi.s * g.xi.c - d.c * g.mupsi.c;
         q_vertex(g, h == 0 ? dA : dB, d, cla, cth, ceta, csig, cchi, q[h][0], q[h][1]);
     }
     psi = Si * (q[0][1] * ta + q[1][1] * tb);
-    th = (fabs(xi) < kEps) ? 0.0 : (Si * (q[0][0] - q[1][0]));
+    th = (fabs(xi) < kEps) ? R(0.0) : R(Si * (q[0][0] - q[1][0]));
 }
 
 // ------------------------------------------------------------------ potential helpers
 // potential of K_j seen from x (no 1/4pi): sum_e t_e L_e - d Theta
-__device__ __forceinline__ double potential_inner(d3 x, const PanelJ &K, const FarCtx &F)
+template <class R>
+__device__ __forceinline__ R potential_inner(V3<R> x, const PanelJT<R> &K, const FarCtxT<R> &F)
 {
-    d3 psi;
-    double th, pot;
+    V3<R> psi;
+    R th, pot;
     far_integrand(x, K, F, psi, th, pot);
     return pot;
 }
 
 // common-edge potential: subtracted s ln s term along the shared edge (sigma = -2 c s ln(s/h),
 // integral over K_i = (5/9) c S_i h)
-struct PotEdge {
-    d3 P1, m_in;
-    double c, h;
+template <class R>
+struct PotEdgeT {
+    V3<R> P1, m_in;
+    R c, h;
 };
-__device__ __forceinline__ double pot_edge_sigma(d3 x, const PotEdge &p)
+using PotEdge = PotEdgeT<double>;
+
+template <class R>
+__device__ __forceinline__ R pot_edge_sigma(V3<R> x, const PotEdgeT<R> &p)
 {
-    const double s = dot(x - p.P1, p.m_in);
-    return s > 0.0 ? -2.0 * p.c * s * log(s / p.h) : 0.0;
+    const R s = dot(x - p.P1, p.m_in);
+    return s > 0.0 ? R(-2.0 * p.c * s * log(s / p.h)) : R(0.0);
 }
 
 } // namespace i2

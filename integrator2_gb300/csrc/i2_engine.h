@@ -8,11 +8,10 @@
 
 #include "i2_device.cuh"
 #include "i2_device_f32.cuh"
+#include "i2_rules.cuh"
 
 namespace i2 {
 
-// pair classes (values of the reference's neighbour_type_enum, src/Mesh3d.cuh:18-23, plus self)
-enum { kVertex = 0, kEdge = 1, kFar = 2, kSelf = 3 };
 // depth cap of the adaptive potential rule (sub-cell paths of up to 24 bits)
 constexpr int kHardMaxDepth = 12;
 // floats per common-vertex pair in ClassArgs::ctx_e
@@ -81,11 +80,16 @@ struct BatchSeg {
     ClassArgs A;
     int cls;
 };
-int batch_max_blocks_per_sm(int threads);
+// variant 0: registers unconstrained; 1: capped at 128 per thread (two 256-thread blocks per SM)
+int batch_max_blocks_per_sm(int threads, int variant);
 cudaError_t launch_batch_levels(const BatchSeg *segs, int nseg, const QuadTablesF &Qf, const RunConfig &cfg, int blocks,
-                                int threads, int G_cap, cudaStream_t s);
+                                int threads, int G_cap, int variant, cudaStream_t s);
 void launch_batch_prelude(const ClassArgs &A, int cls, const QuadTables &Q, const QuadTablesF &Qf, const RunConfig &cfg,
                           int persistent_blocks, cudaStream_t s);
+// adjoint: dL/dV += gJ . dJ/dV + gP dP/dV over the pairs of one class (fp32: FP32 dual numbers)
+void launch_adjoint(int cls, bool fp32, const int2 *pairs, int n, const int3 *cells, const double *V, const int *stop,
+                    const int *maxlev, const RunConfig &cfg, double tier_tol, const double *gJ, const double *gP, double *gradV,
+                    const QuadTables &Q, int persistent_blocks, cudaStream_t s);
 // sets the thread's message returned by i2_last_error()
 void set_last_error(const std::string &msg);
 // kernels shared by both forms

@@ -11,20 +11,6 @@ __device__ __forceinline__ void store5(double *p, const acc5 &a)
 }
 __device__ __forceinline__ acc5 load5(const double *p) { return acc5{p[0], p[1], p[2], p[3], p[4]}; }
 
-// J = (Theta n_j + Psi x n_j)/4pi, with the p-fix of the common-vertex class
-// (evaluatorJ3DK.cu:224-264)
-__device__ __forceinline__ d3 finalize_j(int cls, d3 psi, double th, d3 nj, double Si)
-{
-    if (cls == kVertex) {
-        int p = 0;
-        const double ref = kTwoPi * Si;
-        if (th > ref) p = -((int)trunc((th - ref) / (2.0 * ref)) + 1);
-        else if (th < -ref) p = ((int)trunc((-ref - th) / (2.0 * ref)) + 1);
-        th = th + 2.0 * p * ref;
-    }
-    return kInv4Pi * (th * nj + cross(psi, nj));
-}
-
 template <int CLS>
 __device__ inline void finalize_item(const ClassArgs &A, int mode, int t)
 {

@@ -47,13 +47,6 @@ __global__ void k_prepare_panels(int nc, const double *__restrict__ V, const int
 }
 
 // ------------------------------------------------------------------ helpers
-__device__ __forceinline__ Tri rotate(Tri t, int s)
-{
-    if (s == 0) return t;
-    if (s == 1) return Tri{t.b, t.c, t.a};
-    return Tri{t.c, t.a, t.b};
-}
-
 __device__ __forceinline__ acc5 shfl_xor5(acc5 a, int off)
 {
     acc5 r;
@@ -188,59 +181,6 @@ __global__ void __launch_bounds__(128) k_level(ClassArgs A, QuadTables Q, int le
 }
 
 // ------------------------------------------------------------------ potential of adjacent pairs
-// s ln s term along the shared edge (Ti, Tj rotated: Ti.a / Tj.a off the shared edge); returns
-// its integral over K_i, (5/9) c S_i h
-__device__ __forceinline__ double make_pot_edge(const Tri &Ti, const Tri &Tj, const PanelJ &K, double Si, PotEdge &pe)
-{
-    const d3 tau = unit(Tj.c - Tj.b), m = cross(tau, K.n), w = Ti.a - Tj.b;
-    const d3 perp = w - dot(w, tau) * tau;
-    pe.P1 = Tj.b;
-    pe.h = norm(perp);
-    pe.m_in = (1.0 / pe.h) * perp;
-    pe.c = -dot(m, pe.m_in);
-    return (5.0 / 9.0) * pe.c * Si * pe.h;
-}
-
-// graded Duffy rule over the pieces of K_i (Ti rotated): one piece with apex at the shared
-// vertex (vertex class) or two pieces with apexes at the ends of the shared edge (edge class);
-// the edge class integrates g - sigma
-template <int CLS>
-__device__ double duffy_total(const Tri &Ti, const PanelJ &K, const FarCtx &F, const PotEdge &pe, const double *uu,
-                              const double *uw, int nu, const double *vv, const double *vw, int nv)
-{
-    double total = 0.0;
-    const int npieces = CLS == kEdge ? 2 : 1;
-    for (int piece = 0; piece < npieces; ++piece) {
-        d3 Vx, B, Cc;
-        if (CLS == kVertex) { Vx = Ti.a; B = Ti.b; Cc = Ti.c; }
-        else {
-            const d3 M = 0.5 * (Ti.b + Ti.c);
-            if (piece == 0) { Vx = Ti.b; B = M; Cc = Ti.a; }
-            else { Vx = Ti.c; B = Ti.a; Cc = M; }
-        }
-        const d3 eB = B - Vx, eC = Cc - Vx, dA = Vx - K.A, dB = Vx - K.B, dC = Vx - K.C;
-        const double area2 = norm(cross(eB, eC));
-        double acc = 0.0;
-#pragma unroll 1
-        for (int a = 0; a < nu; ++a) {
-            const double u = uu[a];
-            double row = 0.0;
-#pragma unroll 1
-            for (int b = 0; b < nv; ++b) {
-                const d3 w = u * ((1.0 - vv[b]) * eB + vv[b] * eC);
-                d3 psi;
-                double th, g;
-                far_integrand_o(dA + w, dB + w, dC + w, K, F, psi, th, g);
-                if (CLS == kEdge) g -= pot_edge_sigma(Vx + w, pe);
-                row += vw[b] * g;
-            }
-            acc += uw[a] * u * row;
-        }
-        total += area2 * acc;
-    }
-    return total;
-}
-
 // ------------------------------------------------------------------ singular parts (edge/vertex)
 template <int CLS>
 __global__ void __launch_bounds__(128) k_singular(ClassArgs A, QuadTables Q)
@@ -321,56 +261,6 @@ __global__ void __launch_bounds__(128) k_pot_tier2(ClassArgs A, QuadTables Q)
 // whole GPU works on every depth, so one pair that needs thousands of cells no longer runs
 // alone on one SM.  Accepted sums are added as 64-bit fixed point (2^40 units per |P| + |sigma
 // integral|), so the result does not depend on the order of the atomics.
-template <int CLS>
-__device__ double pot_cell(const Tri &T, int corner, const PanelJ &K, const FarCtx &F, const PotEdge &pe, const QuadTables &Q)
-{
-    double acc = 0.0;
-    if (corner >= 0) {
-        const d3 Vx = corner == 0 ? T.a : (corner == 1 ? T.b : T.c);
-        const d3 B = corner == 0 ? T.b : (corner == 1 ? T.c : T.a);
-        const d3 Cc = corner == 0 ? T.c : (corner == 1 ? T.a : T.b);
-        const d3 eB = B - Vx, eC = Cc - Vx, dA = Vx - K.A, dB = Vx - K.B, dC = Vx - K.C;
-        const double area2 = norm(cross(eB, eC));
-        for (int a = 0; a < Q.nu; ++a) {
-            const double u = Q.du_u[a];
-            double row = 0.0;
-            for (int b = 0; b < Q.nv; ++b) {
-                const double v = Q.dv_v[b];
-                const d3 w = u * ((1.0 - v) * eB + v * eC);
-                d3 psi;
-                double th, g;
-                far_integrand_o(dA + w, dB + w, dC + w, K, F, psi, th, g);
-                if (CLS == kEdge) g -= pot_edge_sigma(Vx + w, pe);
-                row += Q.dv_w[b] * g;
-            }
-            acc += Q.du_w[a] * u * row;
-        }
-        return area2 * acc;
-    }
-    const d3 aA = T.a - K.A, bA = T.b - K.A, cA = T.c - K.A;
-    const d3 aB = T.a - K.B, bB = T.b - K.B, cB = T.c - K.B;
-    const d3 aC = T.a - K.C, bC = T.b - K.C, cC = T.c - K.C;
-    for (int g = 0; g < Q.npts; ++g) {
-        const d3 oa = Q.L1[g] * aA + Q.L2[g] * bA + Q.L3[g] * cA;
-        const d3 ob = Q.L1[g] * aB + Q.L2[g] * bB + Q.L3[g] * cB;
-        const d3 oc = Q.L1[g] * aC + Q.L2[g] * bC + Q.L3[g] * cC;
-        d3 psi;
-        double th, gx;
-        far_integrand_o(oa, ob, oc, K, F, psi, th, gx);
-        if (CLS == kEdge) gx -= pot_edge_sigma(oa + K.A, pe);
-        acc += Q.w[g] * gx;
-    }
-    return 0.5 * norm(cross(T.b - T.a, T.c - T.a)) * acc;
-}
-
-// corner slot of child k when the parent's corner is in slot c (the shared vertex moves to slot 1)
-__device__ __forceinline__ int child_corner(int parent_corner, int k)
-{
-    if (parent_corner < 0 || k == 3) return -1;
-    const int want = parent_corner == 1 ? 0 : (parent_corner == 2 ? 1 : 2);
-    return k == want ? 1 : -1;
-}
-
 struct PotPairCtx {
     Tri Ti;
     PanelJ K;
@@ -402,8 +292,62 @@ __device__ __forceinline__ PotPairCtx pot_pair_ctx(const ClassArgs &A, int t, do
     return c;
 }
 
-// seed: the root of every hard pair is split once; its four children form depth 1.  Pairs
-// beyond a quarter of the list capacity keep their Duffy value and are counted as overflows.
+// the four children of cell T (corner slot of each in cc[]) integrated by one warp: the lanes
+// stride over the flattened (child, quadrature point) list -- the graded Duffy rule for a child
+// that holds the shared vertex, the 13-point rule otherwise -- and a butterfly leaves the four
+// sums in every lane.  A cell costs 52 to 300 point evaluations, so spreading them over the warp
+// is what keeps the GPU busy when a depth holds only a few thousand cells.
+template <int CLS>
+__device__ void pot_children_warp(const Tri &T, const int cc[4], const PotPairCtx &c, const QuadTables &Q, int lane, double v[4])
+{
+    const int nduffy = Q.nu * Q.nv;
+    int start[5];
+    start[0] = 0;
+    for (int k = 0; k < 4; ++k) start[k + 1] = start[k] + (cc[k] >= 0 ? nduffy : Q.npts);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int j = lane; j < start[4]; j += 32) {
+        const int k = j < start[1] ? 0 : (j < start[2] ? 1 : (j < start[3] ? 2 : 3));
+        const int p = j - start[k];
+        const Tri Tc = child(T, k);
+        double g;
+        if (cc[k] >= 0) {
+            const int corner = cc[k];
+            const d3 Vx = corner == 0 ? Tc.a : (corner == 1 ? Tc.b : Tc.c);
+            const d3 B = corner == 0 ? Tc.b : (corner == 1 ? Tc.c : Tc.a);
+            const d3 Cc = corner == 0 ? Tc.c : (corner == 1 ? Tc.a : Tc.b);
+            const d3 eB = B - Vx, eC = Cc - Vx;
+            const int a = p / Q.nv, b = p - a * Q.nv;
+            const double u = Q.du_u[a], vv = Q.dv_v[b];
+            const d3 w = u * ((1.0 - vv) * eB + vv * eC);
+            d3 psi;
+            double th;
+            far_integrand_o((Vx - c.K.A) + w, (Vx - c.K.B) + w, (Vx - c.K.C) + w, c.K, c.F, psi, th, g);
+            if (CLS == kEdge) g -= pot_edge_sigma(Vx + w, c.pe);
+            g *= Q.du_w[a] * u * Q.dv_w[b] * norm(cross(eB, eC));
+        } else {
+            const double l1 = Q.L1[p], l2 = Q.L2[p], l3 = Q.L3[p];
+            const d3 oa = l1 * (Tc.a - c.K.A) + l2 * (Tc.b - c.K.A) + l3 * (Tc.c - c.K.A);
+            const d3 ob = l1 * (Tc.a - c.K.B) + l2 * (Tc.b - c.K.B) + l3 * (Tc.c - c.K.B);
+            const d3 oc = l1 * (Tc.a - c.K.C) + l2 * (Tc.b - c.K.C) + l3 * (Tc.c - c.K.C);
+            d3 psi;
+            double th;
+            far_integrand_o(oa, ob, oc, c.K, c.F, psi, th, g);
+            if (CLS == kEdge) g -= pot_edge_sigma(oa + c.K.A, c.pe);
+            g *= Q.w[p] * 0.5 * norm(cross(Tc.b - Tc.a, Tc.c - Tc.a));
+        }
+        acc[k] += g;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        double x = acc[k];
+        for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+        v[k] = x;
+    }
+}
+
+// seed: the root of every hard pair is split once (one warp per pair); its four children form
+// depth 1.  Pairs beyond a quarter of the list capacity keep their Duffy value and are counted
+// as overflows.
 __device__ __forceinline__ int pot_seeded(const ClassArgs &A) { return min(*A.hard_cnt, A.pot_qcap / 4); }
 
 template <int CLS>
@@ -417,45 +361,51 @@ __global__ void __launch_bounds__(128) k_pot_seed(ClassArgs A, QuadTables Q, dou
         for (int d = 2; d <= kHardMaxDepth + 1; ++d) A.pot_qcnt[d] = 0;
         if (*A.hard_cnt > count) atomicAdd(A.hard_overflow, *A.hard_cnt - count);
     }
-    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < count; h += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < count; h += nwarps) {
         const int t = A.hard_list[h];
         const PotPairCtx c = pot_pair_ctx<CLS>(A, t, tol);
         const int3 ci = A.cells[A.pairs[t].x], cj = A.cells[A.pairs[t].y];
         const int ia[3] = {ci.x, ci.y, ci.z};
         bool shared[3];
         for (int k = 0; k < 3; ++k) shared[k] = (ia[k] == cj.x || ia[k] == cj.y || ia[k] == cj.z);
-        A.pot_fx[h] = 0;
         // the root's children 0, 1, 2 hold K_i's slots b, c, a in their slot 1
-        for (int k = 0; k < 4; ++k) {
-            const int corner = k == 3 ? -1 : (shared[k == 0 ? 1 : (k == 1 ? 2 : 0)] ? 1 : -1);
-            const double v = pot_cell<CLS>(child(c.Ti, k), corner, c.K, c.F, c.pe, Q);
-            A.pot_q_a[4 * (long long)h + k] = PotCellItem{(unsigned long long)k, v, h, corner};
-        }
+        int cc[4];
+        for (int k = 0; k < 4; ++k) cc[k] = k == 3 ? -1 : (shared[k == 0 ? 1 : (k == 1 ? 2 : 0)] ? 1 : -1);
+        double v[4];
+        pot_children_warp<CLS>(c.Ti, cc, c, Q, lane, v);
+        if (lane < 4) A.pot_q_a[4 * (long long)h + lane] = PotCellItem{(unsigned long long)lane, v[lane], h, cc[lane]};
+        if (lane == 0) A.pot_fx[h] = 0;
     }
 }
 
+// one depth: one warp per cell
 template <int CLS>
 __global__ void __launch_bounds__(128) k_pot_depth(ClassArgs A, QuadTables Q, double tol, int depth, const PotCellItem *__restrict__ in,
                                                    PotCellItem *__restrict__ out)
 {
     const int count = min(A.pot_qcnt[depth], A.pot_qcap);
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < count; idx += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < count; idx += nwarps) {
         const PotCellItem it = in[idx];
         if (it.h < 0) continue;
         const int t = A.hard_list[it.h];
         const PotPairCtx c = pot_pair_ctx<CLS>(A, t, tol);
         const Tri T = subcell(c.Ti, depth, (int)it.path);
-        double v[4], sum = 0.0;
-        for (int k = 0; k < 4; ++k) {
-            v[k] = pot_cell<CLS>(child(T, k), child_corner(it.corner, k), c.K, c.F, c.pe, Q);
-            sum += v[k];
-        }
+        int cc[4];
+        for (int k = 0; k < 4; ++k) cc[k] = child_corner(it.corner, k);
+        double v[4];
+        pot_children_warp<CLS>(T, cc, c, Q, lane, v);
+        if (lane != 0) continue;
+        const double sum = v[0] + v[1] + v[2] + v[3];
         bool accept = fabs(sum - it.val) <= ldexp(c.tol_abs, -depth) || depth >= kHardMaxDepth;
         if (!accept) {
             const int pos = atomicAdd(&A.pot_qcnt[depth + 1], 4);
             if (pos + 4 <= A.pot_qcap) {
                 for (int k = 0; k < 4; ++k)
-                    out[pos + k] = PotCellItem{(it.path << 2) | (unsigned long long)k, v[k], it.h, child_corner(it.corner, k)};
+                    out[pos + k] = PotCellItem{(it.path << 2) | (unsigned long long)k, v[k], it.h, cc[k]};
             } else {
                 // list full: keep this cell's sum (counted as an overflow) and blank the slots it
                 // was given below the capacity, so the next depth skips them
@@ -488,62 +438,32 @@ static void pot_adaptive_chain(const ClassArgs &A, const QuadTables &Q, double t
     k_pot_final<CLS><<<persistent_blocks, 128, 0, s>>>(A, tol);
 }
 // ------------------------------------------------------------------ self pairs
-// J(K_i, K_i): tangential part 0 by antisymmetry; normal part 0 (principal value) or the
-// one-sided limit +-(1/4pi) 2 pi S_i n_i.  Potential: with d = 0 the inner potential is
-// sum_e t_e L_e; per edge, int_K t_e L_e dS = int_e dl_y int_0^pi sin(phi) R(phi,y)^2/2 dphi
-// with the phi integral in closed form on the two sides the ray can hit and the edge integral
-// by graded Gauss-Legendre on the pieces on either side of the foot of the altitude.
-__device__ __forceinline__ double ray_side(double a, double alpha, double u1)
-{
-    double sa, ca;
-    sincos(alpha, &sa, &ca);
-    const double F1 = ca * log(tan(0.5 * u1)) + sa / sin(u1);
-    const double F0 = ca * log(tan(0.5 * alpha)) + 1.0;  // lower limit u = alpha
-    return 0.5 * a * a * sa * sa * (F1 - F0);
-}
-
+// J(K_i, K_i) by the chosen convention, potential by self_potential (i2_rules.cuh)
+// eight lanes per pair: lanes 0..5 take one (edge, piece) of the self-pair rule each, the group
+// sums them (an edge's pieces are integrated independently, so the pair's 6 x nself point
+// evaluations run in parallel)
 __global__ void __launch_bounds__(128) k_self(ClassArgs A, QuadTables Q, int self_sign)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= A.n) return;
-    const int i = A.pairs[t].x;
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int g = threadIdx.x & 7;
+    const long long t = gid >> 3;
+    const bool valid = t < A.n;
+    const int i = valid ? A.pairs[t].x : 0;
     const PanelJ K = load_panel(A.panels, i);
+    double part = 0.0;
+    if (valid && g < 6) {
+        const d3 P[3] = {K.A, K.B, K.C};
+        part = self_potential_piece(P, g >> 1, g & 1, Q);
+    }
+    for (int off = 1; off < 8; off <<= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    if (!valid || g != 0) return;
     const double th = self_sign == 0 ? 0.0 : (self_sign > 0 ? kTwoPi : -kTwoPi) * K.S;
     const d3 J = kInv4Pi * (th * K.n);
-    double *raw = A.raw4 + 4 * (long long)t;
+    double *raw = A.raw4 + 4 * t;
     raw[0] = 0.0; raw[1] = 0.0; raw[2] = 0.0; raw[3] = th;
-    double *Jo = A.J3 + 3 * (long long)t;
+    double *Jo = A.J3 + 3 * t;
     Jo[0] = J.x; Jo[1] = J.y; Jo[2] = J.z;
-    const d3 P[3] = {K.A, K.B, K.C};
-    double total = 0.0;
-#pragma unroll 1
-    for (int e = 0; e < 3; ++e) {
-        const d3 P1 = P[e], P2 = P[(e + 1) % 3], P3 = P[(e + 2) % 3];
-        const double L = norm(P2 - P1);
-        const d3 tau = (1.0 / L) * (P2 - P1);
-        const double al1 = angle_ref(P2 - P1, P3 - P1);
-        const double al2 = angle_ref(P1 - P2, P3 - P2);
-        // split at the foot of the altitude from P3, where the angle to P3 swings fastest
-        const double foot = dot(P3 - P1, tau);
-        const bool split = foot > 1e-12 * L && foot < (1.0 - 1e-12) * L;
-        double acc = 0.0;
-#pragma unroll 1
-        for (int piece = 0; piece < (split ? 2 : 1); ++piece) {
-            const double lo = split && piece == 1 ? foot : 0.0;
-            const double span = split ? (piece == 0 ? foot : L - foot) : L;
-            double part = 0.0;
-#pragma unroll 1
-            for (int k = 0; k < Q.nself; ++k) {
-                const double b = lo + span * Q.sx[k], a = L - b;
-                const d3 y = P1 + b * tau;
-                const double phis = angle_ref(tau, P3 - y);
-                part += Q.sw[k] * (ray_side(a, al2, phis + al2) + ray_side(b, al1, (kPi - phis) + al1));
-            }
-            acc += span * part;
-        }
-        total += acc;
-    }
-    A.P[t] = kInv4Pi * total;
+    A.P[t] = kInv4Pi * part;
 }
 
 // ------------------------------------------------------------------ finalisation
@@ -598,7 +518,7 @@ void launch_finalize(int cls, const ClassArgs &A, int mode, cudaStream_t s)
 
 void launch_self(const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, cudaStream_t s)
 {
-    k_self<<<blocks_for(A.n, 128), 128, 0, s>>>(A, Q, cfg.self_sign);
+    k_self<<<blocks_for(8LL * A.n, 128), 128, 0, s>>>(A, Q, cfg.self_sign);
 }
 
 void launch_pot_hard(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s)
@@ -613,7 +533,7 @@ void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const R
     const int tpb = 128;
     switch (cls) {
     case kSelf:
-        k_self<<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q, cfg.self_sign);
+        launch_self(A, Q, cfg, s);
         break;
     case kEdge:
         k_singular<kEdge><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q);

@@ -276,7 +276,7 @@ __device__ void level_items_mixed(const ClassArgs &A, const QuadTablesF &Qf, int
 }
 
 template <int CLS>
-__global__ void __launch_bounds__(256) k_level_mixed(ClassArgs A, QuadTablesF Qf, int level, int mode, double tol, int kmax)
+__global__ void __launch_bounds__(256, 2) k_level_mixed(ClassArgs A, QuadTablesF Qf, int level, int mode, double tol, int kmax)
 {
     level_items_mixed<CLS>(A, Qf, level, mode, tol, kmax, (long long)blockIdx.x * blockDim.x + threadIdx.x,
                            (long long)gridDim.x * blockDim.x, 32);
@@ -524,7 +524,10 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
 // min(4^L, G_cap) lanes per pair), then a grid-wide barrier; after the last level it finalises
 // every pair.  Converged pairs drop out of the lists, so the uneven work left by adaptive
 // refinement is spread over the whole GPU at every level, across meshes and classes.
-__global__ void __launch_bounds__(256) k_batch_levels(const BatchSeg *__restrict__ segs, int nseg, QuadTablesF Qf, int mode,
+// MINB = 1: registers unconstrained (fewer resident warps); MINB = 2: at most 128 registers per
+// thread so that two 256-thread blocks stay resident per SM (some spilling).  The autotuner picks.
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) k_batch_levels(const BatchSeg *__restrict__ segs, int nseg, QuadTablesF Qf, int mode,
                                                       int level_fixed, double tol, int kmax, int G_cap)
 {
     namespace cg = cooperative_groups;
@@ -556,21 +559,23 @@ __global__ void __launch_bounds__(256) k_batch_levels(const BatchSeg *__restrict
     }
 }
 
-int batch_max_blocks_per_sm(int threads)
+int batch_max_blocks_per_sm(int threads, int variant)
 {
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_levels, threads, 0);
+    if (variant == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_levels<1>, threads, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_levels<2>, threads, 0);
     return nb;
 }
 
 cudaError_t launch_batch_levels(const BatchSeg *segs, int nseg, const QuadTablesF &Qf, const RunConfig &cfg, int blocks,
-                                int threads, int G_cap, cudaStream_t s)
+                                int threads, int G_cap, int variant, cudaStream_t s)
 {
     int mode = cfg.mode, level = cfg.level, kmax = cfg.max_level;
     double tol = cfg.tol;
     QuadTablesF q = Qf;
     void *args[] = {(void *)&segs, (void *)&nseg, (void *)&q, (void *)&mode, (void *)&level, (void *)&tol, (void *)&kmax, (void *)&G_cap};
-    return cudaLaunchCooperativeKernel((const void *)k_batch_levels, dim3(blocks), dim3(threads), args, 0, s);
+    const void *fn = variant == 0 ? (const void *)k_batch_levels<1> : (const void *)k_batch_levels<2>;
+    return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(threads), args, 0, s);
 }
 
 // the per-segment work that precedes the level sweep: singular parts, potential tiers, self pairs

@@ -1,0 +1,193 @@
+// i2_rules.cuh -- per-pair integration rules shared by the forward kernels (R = double) and
+// the adjoint kernels (R = dual number): the potential of common-edge / common-vertex pairs
+// (graded Duffy rule, s ln s term of the shared edge, cells of the adaptive rule), the self-pair
+// potential and the finalisation J = (Theta n_j + Psi x n_j)/4pi.
+#pragma once
+
+#include "i2_device.cuh"
+
+namespace i2 {
+
+// pair classes (values of the reference's neighbour_type_enum, src/Mesh3d.cuh:18-23, plus self)
+enum { kVertex = 0, kEdge = 1, kFar = 2, kSelf = 3 };
+
+// ------------------------------------------------------------------ potential of adjacent pairs
+// s ln s term along the shared edge (Ti, Tj rotated: Ti.a / Tj.a off the shared edge); returns
+// its integral over K_i, (5/9) c S_i h
+template <class R>
+__device__ __forceinline__ R make_pot_edge(const TriT<R> &Ti, const TriT<R> &Tj, const PanelJT<R> &K, R Si, PotEdgeT<R> &pe)
+{
+    const V3<R> tau = unit(Tj.c - Tj.b), m = cross(tau, K.n), w = Ti.a - Tj.b;
+    const V3<R> perp = w - dot(w, tau) * tau;
+    pe.P1 = Tj.b;
+    pe.h = norm(perp);
+    pe.m_in = (1.0 / pe.h) * perp;
+    pe.c = -dot(m, pe.m_in);
+    return (5.0 / 9.0) * pe.c * Si * pe.h;
+}
+
+// graded Duffy rule over the pieces of K_i (Ti rotated): one piece with apex at the shared
+// vertex (vertex class) or two pieces with apexes at the ends of the shared edge (edge class);
+// the edge class integrates g - sigma
+template <int CLS, class R>
+__device__ R duffy_total(const TriT<R> &Ti, const PanelJT<R> &K, const FarCtxT<R> &F, const PotEdgeT<R> &pe, const double *uu,
+                         const double *uw, int nu, const double *vv, const double *vw, int nv)
+{
+    R total = 0.0;
+    const int npieces = CLS == kEdge ? 2 : 1;
+    for (int piece = 0; piece < npieces; ++piece) {
+        V3<R> Vx, B, Cc;
+        if (CLS == kVertex) { Vx = Ti.a; B = Ti.b; Cc = Ti.c; }
+        else {
+            const V3<R> M = 0.5 * (Ti.b + Ti.c);
+            if (piece == 0) { Vx = Ti.b; B = M; Cc = Ti.a; }
+            else { Vx = Ti.c; B = Ti.a; Cc = M; }
+        }
+        const V3<R> eB = B - Vx, eC = Cc - Vx, dA = Vx - K.A, dB = Vx - K.B, dC = Vx - K.C;
+        const R area2 = norm(cross(eB, eC));
+        R acc = 0.0;
+#pragma unroll 1
+        for (int a = 0; a < nu; ++a) {
+            const double u = uu[a];
+            R row = 0.0;
+#pragma unroll 1
+            for (int b = 0; b < nv; ++b) {
+                const V3<R> w = u * ((1.0 - vv[b]) * eB + vv[b] * eC);
+                V3<R> psi;
+                R th, g;
+                far_integrand_o(dA + w, dB + w, dC + w, K, F, psi, th, g);
+                if (CLS == kEdge) g -= pot_edge_sigma(Vx + w, pe);
+                row += vw[b] * g;
+            }
+            acc += uw[a] * u * row;
+        }
+        total += area2 * acc;
+    }
+    return total;
+}
+
+// one cell of the adaptive rule: graded Duffy with the shared vertex (in slot `corner`) as apex,
+// or the 13-point rule; offsets to K_j's vertices from vertex differences
+template <int CLS, class R>
+__device__ R pot_cell(const TriT<R> &T, int corner, const PanelJT<R> &K, const FarCtxT<R> &F, const PotEdgeT<R> &pe,
+                      const QuadTables &Q)
+{
+    R acc = 0.0;
+    if (corner >= 0) {
+        const V3<R> Vx = corner == 0 ? T.a : (corner == 1 ? T.b : T.c);
+        const V3<R> B = corner == 0 ? T.b : (corner == 1 ? T.c : T.a);
+        const V3<R> Cc = corner == 0 ? T.c : (corner == 1 ? T.a : T.b);
+        const V3<R> eB = B - Vx, eC = Cc - Vx, dA = Vx - K.A, dB = Vx - K.B, dC = Vx - K.C;
+        const R area2 = norm(cross(eB, eC));
+        for (int a = 0; a < Q.nu; ++a) {
+            const double u = Q.du_u[a];
+            R row = 0.0;
+            for (int b = 0; b < Q.nv; ++b) {
+                const double v = Q.dv_v[b];
+                const V3<R> w = u * ((1.0 - v) * eB + v * eC);
+                V3<R> psi;
+                R th, g;
+                far_integrand_o(dA + w, dB + w, dC + w, K, F, psi, th, g);
+                if (CLS == kEdge) g -= pot_edge_sigma(Vx + w, pe);
+                row += Q.dv_w[b] * g;
+            }
+            acc += Q.du_w[a] * u * row;
+        }
+        return area2 * acc;
+    }
+    const V3<R> aA = T.a - K.A, bA = T.b - K.A, cA = T.c - K.A;
+    const V3<R> aB = T.a - K.B, bB = T.b - K.B, cB = T.c - K.B;
+    const V3<R> aC = T.a - K.C, bC = T.b - K.C, cC = T.c - K.C;
+    for (int g = 0; g < Q.npts; ++g) {
+        const V3<R> oa = Q.L1[g] * aA + Q.L2[g] * bA + Q.L3[g] * cA;
+        const V3<R> ob = Q.L1[g] * aB + Q.L2[g] * bB + Q.L3[g] * cB;
+        const V3<R> oc = Q.L1[g] * aC + Q.L2[g] * bC + Q.L3[g] * cC;
+        V3<R> psi;
+        R th, gx;
+        far_integrand_o(oa, ob, oc, K, F, psi, th, gx);
+        if (CLS == kEdge) gx -= pot_edge_sigma(oa + K.A, pe);
+        acc += Q.w[g] * gx;
+    }
+    return 0.5 * norm(cross(T.b - T.a, T.c - T.a)) * acc;
+}
+
+// corner slot of child k when the parent's corner is in slot c (the shared vertex moves to slot 1)
+__device__ __forceinline__ int child_corner(int parent_corner, int k)
+{
+    if (parent_corner < 0 || k == 3) return -1;
+    const int want = parent_corner == 1 ? 0 : (parent_corner == 2 ? 1 : 2);
+    return k == want ? 1 : -1;
+}
+
+// ------------------------------------------------------------------ self pairs
+// J(K_i, K_i): tangential part 0 by antisymmetry; normal part 0 (principal value) or the
+// one-sided limit +-(1/4pi) 2 pi S_i n_i.  Potential: with d = 0 the inner potential is
+// sum_e t_e L_e; per edge, int_K t_e L_e dS = int_e dl_y int_0^pi sin(phi) R(phi,y)^2/2 dphi
+// with the phi integral in closed form on the two sides the ray can hit and the edge integral
+// by graded Gauss-Legendre on the pieces on either side of the foot of the altitude.
+template <class R>
+__device__ __forceinline__ R ray_side(R a, R alpha, R u1)
+{
+    R sa, ca;
+    sincos(alpha, &sa, &ca);
+    const R F1 = ca * log(tan(0.5 * u1)) + sa / sin(u1);
+    const R F0 = ca * log(tan(0.5 * alpha)) + 1.0;  // lower limit u = alpha
+    return 0.5 * a * a * sa * sa * (F1 - F0);
+}
+
+// piece `piece` (0 or 1) of edge e of the self-pair rule for the triangle P[0..2]: the edge
+// P[e] -> P[e+1] is split at the foot of the altitude from the third vertex (where the angle to it
+// swings fastest) when the foot lies inside the edge; otherwise piece 0 is the whole edge and
+// piece 1 is empty
+template <class R>
+__device__ R self_potential_piece(const V3<R> P[3], int e, int piece, const QuadTables &Q)
+{
+    const V3<R> P1 = P[e], P2 = P[(e + 1) % 3], P3 = P[(e + 2) % 3];
+    const R L = norm(P2 - P1);
+    const V3<R> tau = (1.0 / L) * (P2 - P1);
+    const R foot = dot(P3 - P1, tau);
+    const bool split = foot > 1e-12 * L && foot < (1.0 - 1e-12) * L;
+    if (piece == 1 && !split) return R(0.0);
+    const R al1 = angle_ref(P2 - P1, P3 - P1);
+    const R al2 = angle_ref(P1 - P2, P3 - P2);
+    const R lo = split && piece == 1 ? foot : R(0.0);
+    const R span = split ? (piece == 0 ? foot : R(L - foot)) : L;
+    R part = 0.0;
+#pragma unroll 1
+    for (int k = 0; k < Q.nself; ++k) {
+        const R b = lo + span * Q.sx[k], a = L - b;
+        const V3<R> y = P1 + b * tau;
+        const R phis = angle_ref(tau, P3 - y);
+        part += Q.sw[k] * (ray_side(a, al2, R(phis + al2)) + ray_side(b, al1, R((kPi - phis) + al1)));
+    }
+    return span * part;
+}
+
+// int_K int_K 1/|x - y| (no 1/4pi) of the triangle (P0, P1, P2)
+template <class R>
+__device__ R self_potential(V3<R> P0, V3<R> P1v, V3<R> P2v, const QuadTables &Q)
+{
+    const V3<R> P[3] = {P0, P1v, P2v};
+    R total = 0.0;
+#pragma unroll 1
+    for (int e = 0; e < 3; ++e) total += self_potential_piece(P, e, 0, Q) + self_potential_piece(P, e, 1, Q);
+    return total;
+}
+
+// ------------------------------------------------------------------ finalisation
+// J = (Theta n_j + Psi x n_j)/4pi, with the p-fix of the common-vertex class
+// (evaluatorJ3DK.cu:224-264); the shift 2 p 2 pi S_i is a piecewise constant in the geometry
+template <class R>
+__device__ __forceinline__ V3<R> finalize_j(int cls, V3<R> psi, R th, V3<R> nj, R Si)
+{
+    if (cls == kVertex) {
+        int p = 0;
+        const R ref = kTwoPi * Si;
+        if (th > ref) p = -((int)trunc(value_of((th - ref) / (2.0 * ref))) + 1);
+        else if (th < -ref) p = ((int)trunc(value_of((-ref - th) / (2.0 * ref))) + 1);
+        th = th + 2.0 * p * ref;
+    }
+    return kInv4Pi * (th * nj + cross(psi, nj));
+}
+
+} // namespace i2

@@ -592,6 +592,11 @@ static inline double ray_side(double a, double alpha, double u1)
     return 0.5 * a * a * sa * sa * (F1 - F0);
 }
 
+/* Gauss-Legendre points per piece of the self-pair rule used by o_integrate_class (default 96;
+ * the library's default is 24) */
+static int g_self_nquad = 96;
+void o_set_self_rule(int nquad) { g_self_nquad = nquad; }
+
 double o_self_potential(const double *Ap, const double *Bp, const double *Cp, int nquad)
 {
     v3 P[3] = {ld(Ap), ld(Bp), ld(Cp)};
@@ -1054,7 +1059,7 @@ int o_integrate_class(int cls, int ntasks, const int *ti, const int *tj,
             v3 J = finalize_j(O_FAR, r, nj, S[i]);
             if (raw4) memcpy(raw4 + 4 * t, r.v, sizeof r.v);
             if (J3) { J3[3 * t] = J.x; J3[3 * t + 1] = J.y; J3[3 * t + 2] = J.z; }
-            if (P) P[t] = o_self_potential(&a.x, &b.x, &c.x, 96);
+            if (P) P[t] = o_self_potential(&a.x, &b.x, &c.x, g_self_nquad);
             if (levels) levels[t] = 0;
             continue;
         }

@@ -95,6 +95,8 @@ void o_task_integrand(int cls, int i, int j, const double *V, const int *C,
 double o_antisymmetry(const double *Jij, const double *Jji);
 
 int o_max_threads(void);
+/* Gauss-Legendre points per piece of the self-pair potential in o_integrate_class (default 96) */
+void o_set_self_rule(int nquad);
 /* cells visited by the adaptive potential rule per depth since the last reset */
 void o_adapt_stats(long long *out32, int reset);
 

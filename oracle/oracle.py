@@ -73,6 +73,7 @@ def lib():
             L.o_pair_is_hard.argtypes = [i, i, vp, vp]
             L.o_pair_is_hard.restype = i
             L.o_adapt_stats.argtypes = [vp, i]
+            L.o_set_self_rule.argtypes = [i]
             _lib = L
     return _lib
 
@@ -149,14 +150,16 @@ def ref_integrate(cls, pairs, V, C, level=0, qf=QF13):
 
 class potential_rule:
     """context manager: the oracle's adjacent-pair potential rule (Duffy nu x nv, grading) and
-    adaptive hard-pair tolerance (0 = off); restores the high-order defaults on exit"""
+    adaptive hard-pair tolerance (0 = off) and the self-pair rule size; restores the high-order
+    defaults on exit"""
 
-    def __init__(self, nu=40, nv=32, grade=3, adaptive=1e-10, depth=18, every_pair=False, tiered=0.0):
-        self.args = (nu, nv, grade, adaptive, depth, every_pair, tiered)
+    def __init__(self, nu=40, nv=32, grade=3, adaptive=1e-10, depth=18, every_pair=False, tiered=0.0, self_n=96):
+        self.args = (nu, nv, grade, adaptive, depth, every_pair, tiered, self_n)
 
     def __enter__(self):
         L = lib()
-        nu, nv, g, a, d, e, t = self.args
+        nu, nv, g, a, d, e, t, sn = self.args
+        L.o_set_self_rule(sn)
         L.o_set_potential_rule(nu, nv, g)
         L.o_set_potential_adaptive(a)
         L.o_set_potential_adaptive_depth(d)
@@ -171,6 +174,7 @@ class potential_rule:
         L.o_set_potential_adaptive_depth(18)
         L.o_set_potential_adaptive_all(0)
         L.o_set_potential_tiered(0.0)
+        L.o_set_self_rule(96)
 
 
 def hard_pairs(pairs, V, C):
