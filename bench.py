@@ -237,6 +237,66 @@ def run_batch(batch, flush, stream, steps, warmup):
     return sum(e0[s].elapsed_time(e1[s]) for s in range(steps))
 
 
+def adjoint_section(args):
+    """C4 workload: 5,120-triangle sphere displaced radially by spherical harmonics of degree <= 6
+    (coefficients ~ N(0, 0.05^2), seed 4), all four pair classes (near < 3h).  Times forward +
+    backward of L = sum_p c_p (P_p + w . J_p) through the torch front-end (FP64 and FP32 adjoint)
+    and checks the FP64 gradient against central differences (h = 1e-6) on a few coordinates."""
+    import torch
+    from integrator2_gb300 import api, meshes, pairs
+    from integrator2_gb300.autograd import pair_integrals
+    V, C = meshes.sh_displaced_icosphere(4, 6, 0.05, 4)
+    pl = pairs.build_pairs(V, C, NEAR)
+    lists = [pl.vertex, pl.edge, pl.far, pl.self_]
+    rng = np.random.default_rng(11)
+    c = [torch.as_tensor(rng.standard_normal(len(l)), device="cuda") for l in lists]
+    w = torch.as_tensor(rng.standard_normal(3), device="cuda")
+    settings = dict(mode="fixed", level=1, hard_tol=0.0)
+
+    def loss(Vt, **kw):
+        outs = pair_integrals(Vt, C, lists, **kw)
+        return sum((ck * (P + J @ w)).sum() for (J, P), ck in zip(outs, c))
+
+    out = {"workload": "C4: sphere s4 (5120 triangles) with SH displacement l<=6, 4 classes, fixed level 1",
+           "pairs": int(sum(len(l) for l in lists))}
+    for name, prec in (("fp64", api.PRECISION_FP64), ("fp32", api.PRECISION_MIXED)):
+        kw = dict(settings, precision=prec)
+        times = []
+        for rep in range(3):
+            Vt = torch.tensor(V, dtype=torch.float64, device="cuda", requires_grad=True)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            L = loss(Vt, **kw)
+            t1 = time.perf_counter()
+            L.backward()
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            times.append((t1 - t0, t2 - t1))
+        fwd, bwd = np.median([t[0] for t in times]), np.median([t[1] for t in times])
+        out[name] = {"forward_ms": 1e3 * fwd, "backward_ms": 1e3 * bwd}
+        if name == "fp64":
+            g64 = Vt.grad.detach().cpu().numpy().reshape(-1)
+        else:
+            g32 = Vt.grad.detach().cpu().numpy().reshape(-1)
+    h, err = 1e-6, 0.0
+    for k in rng.choice(V.size, max(1, args.fd_coords), replace=False):
+        Vp, Vm = V.reshape(-1).copy(), V.reshape(-1).copy()
+        Vp[k] += h
+        Vm[k] -= h
+        with torch.no_grad():
+            fd = (float(loss(torch.tensor(Vp.reshape(-1, 3), device="cuda"), **settings)) -
+                  float(loss(torch.tensor(Vm.reshape(-1, 3), device="cuda"), **settings))) / (2 * h)
+        err = max(err, abs(fd - g64[k]) / np.abs(g64).max())
+    out["fd_check"] = {"coordinates": int(args.fd_coords), "h": h, "max_abs_err_over_max_grad": float(err)}
+    out["fp32_vs_fp64_max_rel"] = float(np.abs(g32 - g64).max() / np.abs(g64).max())
+    return out
+
+
+# DRAM bytes (read + write) of one run of the disjoint class's FP32 level chain (k_level_mixed<2>,
+# levels 0..5) on this workload, measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum
+# summed over the chain's six launches); the chain is compute-bound, this is mostly per-pair state
+FAR_CHAIN_DRAM_BYTES = 147407616 + 91512576
+
 # FP32 operation counts of the far-field integrand (same formulas, FP32 form): flops, sqrtf,
 # divide, log1pf, atan2f
 POINT_OPS_F32 = {"far": (211, 3, 3, 3, 1)}
@@ -404,6 +464,7 @@ def gpu_arm(args):
     }
     if "fp64" in forms:
         line["speedup_over_plain_fp64"] = head["value"] / forms["fp64"]["value"]
+    line["adjoint"] = adjoint_section(args)
     if "batch" in forms:
         line["batch"] = {"shape": {"threads": forms["batch"]["shape"][0], "blocks_per_sm": forms["batch"]["shape"][1],
                                    "lanes_per_pair": forms["batch"]["shape"][2],
@@ -413,7 +474,8 @@ def gpu_arm(args):
     if rk:
         line["roofline"] = {"bound": "fp32" if rk == "mixed" else "fp64",
                             "kernel": ("k_level_mixed" if rk == "mixed" else "k_level") + "<far> chain (levels 0..5), per-class form",
-                            "unit": "TFLOP/s", "traffic": None, **roof[rk]}
+                            "unit": "TFLOP/s", "traffic": FAR_CHAIN_DRAM_BYTES if rk == "mixed" else None,
+                            "traffic_unit": "bytes per chain run (ncu)", **roof[rk]}
     if "fp64" in roof and rk != "fp64":
         line["roofline_fp64"] = {"bound": "fp64", "unit": "TFLOP/s", **roof["fp64"]}
     print(json.dumps(line))
@@ -427,6 +489,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--cpu-fraction", type=float, default=0.02)
+    ap.add_argument("--fd-coords", type=int, default=10, help="adjoint section: coordinates checked by finite differences")
     ap.add_argument("--forms", default="fp64,mixed,batch",
                     help="forms to run: fp64, mixed (per-class chains), batch (headline when present)")
     args = ap.parse_args()

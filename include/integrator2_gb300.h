@@ -106,6 +106,9 @@ i2_status i2_mesh_pair_count(const i2_mesh_t *mesh, i2_pair_class cls, int64_t *
 i2_status i2_mesh_copy_pairs(const i2_mesh_t *mesh, i2_pair_class cls, int32_t *rows, int64_t n);
 /* Mesh3D::getCellNormals / getCellMeasures (src/Mesh3d.cuh:110-126); any pointer may be NULL */
 i2_status i2_mesh_copy_cell_data(const i2_mesh_t *mesh, double *normals, double *measures, double *centres);
+/* Mesh3D::getVertices / getCells (src/Mesh3d.cuh:70-126) as host copies: 3 nv doubles, 3 nc int32
+ * (0-based); either pointer may be NULL */
+i2_status i2_mesh_copy_geometry(const i2_mesh_t *mesh, double *vertices, int32_t *cells);
 
 /* ------------------------------------------------------------------ QuadratureFormula3D */
 /* the reference's built-in rules qf3D1, qf3D3, qf3D4, qf3D6, qf3D7, qf3D9, qf3D12, qf3D13

@@ -121,6 +121,23 @@ public:
         i2::check(i2_mesh_copy_cell_data(h_, nullptr, m.data(), nullptr), "i2_mesh_copy_cell_data");
         return m;
     }
+    // src/Mesh3d.cuh:70-126 (host copies)
+    std::vector<double> getVertices() const
+    {
+        int32_t nv = 0, nc = 0;
+        i2::check(i2_mesh_sizes(h_, &nv, &nc), "i2_mesh_sizes");
+        std::vector<double> v(3 * (size_t)nv);
+        i2::check(i2_mesh_copy_geometry(h_, v.data(), nullptr), "i2_mesh_copy_geometry");
+        return v;
+    }
+    std::vector<Int3> getCells() const
+    {
+        int32_t nv = 0, nc = 0;
+        i2::check(i2_mesh_sizes(h_, &nv, &nc), "i2_mesh_sizes");
+        std::vector<Int3> c(nc);
+        if (nc) i2::check(i2_mesh_copy_geometry(h_, nullptr, &c[0].x), "i2_mesh_copy_geometry");
+        return c;
+    }
     std::vector<double> getCellNormals() const
     {
         int32_t nv = 0, nc = 0;
@@ -218,6 +235,9 @@ public:
     std::vector<double> getResults(neighbour_type_enum type) const { return channel(type, I2_CHANNEL_J, 3); }
     std::vector<double> getIntegrals(neighbour_type_enum type) const { return channel(type, I2_CHANNEL_RAW, 4); }
     std::vector<double> getPotentials(neighbour_type_enum type) const { return channel(type, I2_CHANNEL_P, 1); }
+    // refinement level kept per pair (-1 in fixed mode) and the (i,j)/(j,i) check (after runAllPairs(true))
+    std::vector<double> getLevels(neighbour_type_enum type) const { return channel(type, I2_CHANNEL_LEVEL, 1); }
+    std::vector<double> getErrors(neighbour_type_enum type) const { return channel(type, I2_CHANNEL_ERROR, 1); }
 
 private:
     std::vector<double> channel(neighbour_type_enum type, i2_channel ch, int width) const

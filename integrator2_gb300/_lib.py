@@ -32,6 +32,7 @@ SIGNATURES = {
     "i2_mesh_pair_count": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),
     "i2_mesh_copy_pairs": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _i64]),
     "i2_mesh_copy_cell_data": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "i2_mesh_copy_geometry": (ctypes.c_int, [_vp, _vp, _vp]),
     "i2_quadrature_builtin": (ctypes.c_int, [_i32, _vp, _vp, _vp]),
     "i2_integrator_create": (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _pp]),
     "i2_integrator_destroy": (None, [_vp]),

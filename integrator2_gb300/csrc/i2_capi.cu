@@ -526,6 +526,12 @@ i2::QuadTablesF tables_f32(const i2::QuadTables &Q)
     return F;
 }
 
+// agreement bar of the tiered potential rule (main vs check Duffy rule, then main vs 16 x 16):
+// 2e-7 keeps the rule within 1e-6 of the converged potential on the 20,480-triangle jittered
+// sphere (largest error 6.5e-7 common vertex, 8.9e-7 common edge) and stays above the FP32
+// rounding of the mixed form's Duffy sums
+double tier_tolerance(const i2::RunConfig &cfg) { return std::max(10.0 * cfg.hard_tol, 2e-7); }
+
 // cells per depth list of the adaptive potential (24 bytes each): every hard pair seeds 4 cells
 // at depth 1; deeper lists hold a few tens of thousands of cells on the meshes measured (C2: at
 // most 27,516).  Capped at 2^26 cells (1.5 GB per list).
@@ -566,6 +572,8 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         W.act_a.reserve(n);
         W.act_b.reserve(n);
     }
+    // the mixed form gathers its needle-cell pairs for the FP64 fix-up into act_a
+    if (ev->integrator->precision == I2_PRECISION_MIXED) W.act_a.reserve(n);
     W.cnt.reserve(16);
     W.maxlev.reserve(1);
     if (cls == I2_SIMPLE_NEIGHBORS || cls == I2_ATTACHED_NEIGHBORS) {
@@ -610,9 +618,7 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         A.pot_qcnt = W.pot_qcnt.ptr;
         A.pot_fx = W.pot_fx.ptr;
         A.tier2_cnt = W.cnt.ptr + 10;
-        A.tier_tol = 10.0 * cfg.hard_tol;
-        // FP32 rounding of the tier-1 Duffy sums is a few 1e-8 of |P|; keep the agreement bar above it
-        if (ev->integrator->precision == I2_PRECISION_MIXED) A.tier_tol = std::max(A.tier_tol, 2e-7);
+        A.tier_tol = tier_tolerance(cfg);
     }
     A.raw4 = out_raw;
     A.J3 = out_J;
@@ -734,6 +740,8 @@ void batch_enqueue(i2_batch *b, cudaStream_t s, int threads, int bps, int gcap, 
     I2_REQUIRE(maxb > 0, I2_ERR_CUDA, "batch kernel cannot be resident with this block size");
     const int blocks = std::max(1, b->sms) * std::max(1, std::min(bps > 0 ? bps : maxb, maxb));
     I2_CHECK_CUDA(i2::launch_batch_levels(b->d_segs.ptr, (int)b->segs.size(), b->Qf, b->cfg, blocks, threads, gcap, variant, s));
+    for (auto &sp : b->segs)
+        if (sp->n > 0 && sp->cls != I2_SELF) i2::launch_fp64_fixup(sp->cls, sp->args, b->Q, b->cfg, persistent, s);
 }
 
 } // namespace
@@ -843,6 +851,15 @@ i2_status i2_mesh_copy_pairs(const i2_mesh_t *mesh, i2_pair_class cls, int32_t *
             rows[3 * k + 1] = l[2 * k + 1];
             rows[3 * k + 2] = (int32_t)k;
         }
+    });
+}
+
+i2_status i2_mesh_copy_geometry(const i2_mesh_t *mesh, double *vertices, int32_t *cells)
+{
+    return guarded([&] {
+        I2_REQUIRE(mesh, I2_ERR_INVALID_ARGUMENT, "null mesh");
+        if (vertices) std::memcpy(vertices, mesh->V.data(), mesh->V.size() * sizeof(double));
+        if (cells) std::memcpy(cells, mesh->C.data(), mesh->C.size() * sizeof(int32_t));
     });
 }
 
@@ -1076,8 +1093,7 @@ i2_status i2_evaluator_backward_class(i2_evaluator_t *ev, i2_pair_class cls, con
         I2_REQUIRE(m.on_device, I2_ERR_STATE, "mesh not on the device");
         i2::RunConfig cfg = R.cfg;
         // the tier bar of the forward pass (run_class_device)
-        double tier_tol = 10.0 * cfg.hard_tol;
-        if (R.precision == I2_PRECISION_MIXED) tier_tol = std::max(tier_tol, 2e-7);
+        const double tier_tol = tier_tolerance(cfg);
         if (ev->persistent_blocks == 0) {
             int dev = 0, sms = 0;
             I2_CHECK_CUDA(cudaGetDevice(&dev));
@@ -1243,7 +1259,7 @@ i2_status i2_batch_add(i2_batch_t *batch, const i2_mesh_t *mesh, i2_pair_class c
             A.tier2_list = sp->tier2_list.ptr; A.tier2_cnt = sp->cnt.ptr + 10;
             A.pot_q_a = sp->pot_q_a.ptr; A.pot_q_b = sp->pot_q_b.ptr; A.pot_qcap = (int)pot_queue_capacity(m);
             A.pot_qcnt = sp->pot_qcnt.ptr; A.pot_fx = sp->pot_fx.ptr;
-            A.tier_tol = std::max(10.0 * batch->cfg.hard_tol, 2e-7);
+            A.tier_tol = tier_tolerance(batch->cfg);
         }
         A.raw4 = sp->raw4.ptr; A.J3 = sp->J.ptr; A.P = sp->P.ptr; A.level_out = sp->level.ptr;
         if (segment) *segment = (int32_t)batch->segs.size();

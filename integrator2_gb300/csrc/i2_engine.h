@@ -90,6 +90,8 @@ void launch_batch_prelude(const ClassArgs &A, int cls, const QuadTables &Q, cons
 void launch_adjoint(int cls, bool fp32, const int2 *pairs, int n, const int3 *cells, const double *V, const int *stop,
                     const int *maxlev, const RunConfig &cfg, double tier_tol, const double *gJ, const double *gP, double *gradV,
                     const QuadTables &Q, int persistent_blocks, cudaStream_t s);
+// mixed form: FP64 recomputation of the pairs with a needle cell (corner below 3 degrees)
+void launch_fp64_fixup(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s);
 // sets the thread's message returned by i2_last_error()
 void set_last_error(const std::string &msg);
 // kernels shared by both forms

@@ -454,6 +454,171 @@ __global__ void __launch_bounds__(128) k_pot_tier2_mixed(ClassArgs A, QuadTables
     }
 }
 
+// ------------------------------------------------------------------ FP64 fix-up of ill-conditioned pairs
+// A pair that holds a needle cell (a corner angle below 3 degrees) is ill-conditioned: its J is
+// a small difference of large parts, and FP32 rounding of the bulk is amplified by a few thousand
+// there (measured: errors up to 1e-3 on the 20,480-triangle jittered sphere, whose two needles
+// have corners of 0.6 and 1.5 degrees).  After the mixed chain has finished, one warp per such
+// pair recomputes its regular part in FP64 -- one whole block per such pair, the threads striding
+// over the 4^L sub-cells, since a few pairs at level 5 would otherwise set the time -- and
+// finalises J (and the disjoint class's potential) again.  Other pairs cost two loads.
+template <int CLS>
+struct FixupPair {
+    PanelJ K;
+    Tri Ti;
+    double Si;
+    FarCtx F;
+    EdgeCtx E;
+    VertexCtx Vx;
+};
+
+// (Psi, Theta, potential) of the regular part at `level`, summed by the whole block (every thread
+// receives the sums); red holds 5 doubles per warp
+template <int CLS>
+__device__ acc5 fixup_level_sum(const FixupPair<CLS> &p, const QuadTables &Q, int level, double *red)
+{
+    const int nsub = 1 << (2 * level);
+    const double Ssub = p.Si * ldexp(1.0, -2 * level);
+    acc5 acc = zero5();
+    for (int sc = threadIdx.x; sc < nsub; sc += blockDim.x) {
+        const Tri T = subcell(p.Ti, level, sc);
+        acc5 cell = zero5();
+        for (int g = 0; g < Q.npts; ++g) {
+            const d3 x = Q.L1[g] * T.a + Q.L2[g] * T.b + Q.L3[g] * T.c;
+            d3 psi;
+            double th, pot = 0.0;
+            if (CLS == kFar) far_integrand(x, p.K, p.F, psi, th, pot);
+            else if (CLS == kEdge) edge_integrand(x, p.K, p.E, psi, th);
+            else vertex_integrand(x, p.K, p.Vx, psi, th);
+            axpy5(cell, Q.w[g], psi, th, pot);
+        }
+        acc.px += Ssub * cell.px; acc.py += Ssub * cell.py; acc.pz += Ssub * cell.pz;
+        acc.th += Ssub * cell.th; acc.pot += Ssub * cell.pot;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        acc.px += __shfl_xor_sync(0xffffffffu, acc.px, off);
+        acc.py += __shfl_xor_sync(0xffffffffu, acc.py, off);
+        acc.pz += __shfl_xor_sync(0xffffffffu, acc.pz, off);
+        acc.th += __shfl_xor_sync(0xffffffffu, acc.th, off);
+        acc.pot += __shfl_xor_sync(0xffffffffu, acc.pot, off);
+    }
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) store5(red + 5 * w, acc);
+    __syncthreads();
+    acc5 tot = zero5();
+    for (int k = 0; k < nw; ++k) {
+        const acc5 v = load5(red + 5 * k);
+        tot.px += v.px; tot.py += v.py; tot.pz += v.pz; tot.th += v.th; tot.pot += v.pot;
+    }
+    return tot;
+}
+
+// the pairs that hold a needle cell, gathered into list[0 .. *count) (the class's active-list
+// buffer, free once the level chain has finished)
+__global__ void __launch_bounds__(256) k_fixup_collect(ClassArgs A, int *list, int *count)
+{
+    const double c3 = 0.99862953475457387;  // cos 3 degrees
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < A.n; t += (long long)gridDim.x * blockDim.x) {
+        const int2 pr = A.pairs[t];
+        if (A.panels[pr.x].v[2].w > c3 || A.panels[pr.y].v[2].w > c3) list[atomicAdd(count, 1)] = (int)t;
+    }
+}
+
+template <int CLS>
+__global__ void __launch_bounds__(256) k_fp64_fixup(ClassArgs A, QuadTables Q, int mode, int fixed_level, double tol, int kmax,
+                                                    const int *__restrict__ list, const int *__restrict__ count)
+{
+    __shared__ double red[5 * 8];
+    const int nbad = *count;
+    {
+        // one block per gathered pair (grid-stride), so that a few pairs at level 5 spread over the GPU
+        for (int q = blockIdx.x; q < nbad; q += gridDim.x) {
+            const int t = list[q];
+            const int2 pr = A.pairs[t];
+            const double4_32a ni4 = A.panels[pr.x].v[3], nj4 = A.panels[pr.y].v[3];
+            const d3 ni = mk(ni4.x, ni4.y, ni4.z), nj = mk(nj4.x, nj4.y, nj4.z);
+            FixupPair<CLS> p;
+            p.K = load_panel(A.panels, pr.y);
+            p.Ti = load_tri(A.panels, pr.x);
+            p.Si = A.panels[pr.x].v[0].w;
+            if (CLS == kFar) p.F = make_far_ctx(p.K);
+            else {
+                const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
+                int si, sj;
+                if (CLS == kEdge) {
+                    shifts_edge(ci, cj, si, sj);
+                    p.E = make_edge_ctx(p.K, sj);
+                } else {
+                    shifts_vertex(ci, cj, si, sj);
+                    p.Vx = make_vertex_ctx(p.K, sj, ni, p.Si);
+                }
+            }
+            d3 spsi = mk(0, 0, 0);
+            double sth = 0.0;
+            if (CLS != kFar) {
+                const double *sg = A.sing + 4 * (long long)t;
+                spsi = mk(sg[0], sg[1], sg[2]);
+                sth = sg[3];
+            }
+            acc5 acc;
+            int kept;
+            if (mode == kAdaptiveRelative) {
+                // FP64 refinement with the relative criterion from level 0 (FP32 noise may have kept
+                // the mixed pass refining up to the last level); every thread holds the same sums,
+                // so the decision is uniform
+                acc = fixup_level_sum<CLS>(p, Q, 0, red);
+                kept = 0;
+                for (int L = 1; L <= kmax; ++L) {
+                    const acc5 nxt = fixup_level_sum<CLS>(p, Q, L, red);
+                    const d3 Jc = finalize_j(CLS, mk(nxt.px, nxt.py, nxt.pz) + spsi, nxt.th + sth, nj, p.Si);
+                    const d3 dJ = kInv4Pi * ((nxt.th - acc.th) * nj + cross(mk(nxt.px - acc.px, nxt.py - acc.py, nxt.pz - acc.pz), nj));
+                    bool unconv = norm(dJ) > tol * norm(Jc);
+                    if (CLS == kFar) unconv = unconv || fabs(nxt.pot - acc.pot) > tol * fabs(nxt.pot);
+                    acc = nxt;
+                    kept = L;
+                    if (!unconv) break;
+                }
+            } else {
+                kept = fixed_level;
+                if (mode != kFixed) {
+                    const int L = A.stop[t];
+                    kept = ((*A.maxlev - L) & 1) ? (L > 0 ? L - 1 : 0) : L;
+                }
+                acc = fixup_level_sum<CLS>(p, Q, kept, red);
+            }
+            if (threadIdx.x == 0) {
+                const d3 psi = mk(acc.px, acc.py, acc.pz) + spsi;
+                const double th = acc.th + sth;
+                const d3 J = finalize_j(CLS, psi, th, nj, p.Si);
+                double *raw = A.raw4 + 4 * (long long)t;
+                raw[0] = psi.x; raw[1] = psi.y; raw[2] = psi.z; raw[3] = th;
+                double *Jo = A.J3 + 3 * (long long)t;
+                Jo[0] = J.x; Jo[1] = J.y; Jo[2] = J.z;
+                if (CLS == kFar) A.P[t] = kInv4Pi * acc.pot;
+                if (mode == kAdaptiveRelative) {
+                    A.stop[t] = kept;
+                    if (A.level_out) A.level_out[t] = kept;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+void launch_fp64_fixup(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s)
+{
+    if (A.n <= 0) return;
+    // cnt[11] counts the gathered pairs (the counters are cleared before every run); the active-list
+    // buffer act_a is free after the level chain
+    int *list = A.act_a, *count = A.cnt + 11;
+    if (!list) return;  // fixed mode without active lists: nothing to gather into
+    k_fixup_collect<<<persistent_blocks, 256, 0, s>>>(A, list, count);
+    if (cls == kEdge) k_fp64_fixup<kEdge><<<persistent_blocks, 256, 0, s>>>(A, Q, cfg.mode, cfg.level, cfg.tol, cfg.max_level, list, count);
+    else if (cls == kVertex) k_fp64_fixup<kVertex><<<persistent_blocks, 256, 0, s>>>(A, Q, cfg.mode, cfg.level, cfg.tol, cfg.max_level, list, count);
+    else if (cls == kFar) k_fp64_fixup<kFar><<<persistent_blocks, 256, 0, s>>>(A, Q, cfg.mode, cfg.level, cfg.tol, cfg.max_level, list, count);
+}
+
 // ------------------------------------------------------------------ launchers
 static int blocks_for_m(long long n, int tpb) { return (int)((n + tpb - 1) / tpb); }
 
@@ -502,6 +667,7 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
             launch_pot_hard(kEdge, A, Q, cfg, persistent_blocks, s);
         }
         level_chain_mixed<kEdge>(A, Qf, cfg, persistent_blocks, s);
+        launch_fp64_fixup(kEdge, A, Q, cfg, persistent_blocks, s);
         break;
     case kVertex:
         k_singular_mixed<kVertex><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
@@ -510,9 +676,11 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
             launch_pot_hard(kVertex, A, Q, cfg, persistent_blocks, s);
         }
         level_chain_mixed<kVertex>(A, Qf, cfg, persistent_blocks, s);
+        launch_fp64_fixup(kVertex, A, Q, cfg, persistent_blocks, s);
         break;
     default:
         level_chain_mixed<kFar>(A, Qf, cfg, persistent_blocks, s);
+        launch_fp64_fixup(kFar, A, Q, cfg, persistent_blocks, s);
         break;
     }
 }

@@ -125,13 +125,21 @@ __device__ __forceinline__ int child_corner(int parent_corner, int k)
 // sum_e t_e L_e; per edge, int_K t_e L_e dS = int_e dl_y int_0^pi sin(phi) R(phi,y)^2/2 dphi
 // with the phi integral in closed form on the two sides the ray can hit and the edge integral
 // by graded Gauss-Legendre on the pieces on either side of the foot of the altitude.
+// ln tan(u/2) from sin u and cos u, in the form that does not cancel on either half of (0, pi)
 template <class R>
-__device__ __forceinline__ R ray_side(R a, R alpha, R u1)
+__device__ __forceinline__ R log_tan_half(R s, R c)
 {
-    R sa, ca;
-    sincos(alpha, &sa, &ca);
-    const R F1 = ca * log(tan(0.5 * u1)) + sa / sin(u1);
-    const R F0 = ca * log(tan(0.5 * alpha)) + 1.0;  // lower limit u = alpha
+    return c >= 0.0 ? R(log(s / (1.0 + c))) : R(log((1.0 - c) / s));
+}
+
+// one side of the phi integral, (a^2 sin^2(alpha) / 2) [cos(alpha) ln tan(u/2) + sin(alpha) / sin(u)]
+// from u = alpha to u1; sin, cos of alpha and the bracket's value at alpha (F0) come from the caller
+template <class R>
+__device__ __forceinline__ R ray_side(R a, R sa, R ca, R F0, R u1)
+{
+    R su, cu;
+    sincos(u1, &su, &cu);
+    const R F1 = ca * log_tan_half(su, cu) + sa / su;
     return 0.5 * a * a * sa * sa * (F1 - F0);
 }
 
@@ -150,6 +158,11 @@ __device__ R self_potential_piece(const V3<R> P[3], int e, int piece, const Quad
     if (piece == 1 && !split) return R(0.0);
     const R al1 = angle_ref(P2 - P1, P3 - P1);
     const R al2 = angle_ref(P1 - P2, P3 - P2);
+    // per-side constants of the phi integral (the lower limit u = alpha)
+    R s1, c1, s2, c2;
+    sincos(al1, &s1, &c1);
+    sincos(al2, &s2, &c2);
+    const R F01 = c1 * log_tan_half(s1, c1) + 1.0, F02 = c2 * log_tan_half(s2, c2) + 1.0;
     const R lo = split && piece == 1 ? foot : R(0.0);
     const R span = split ? (piece == 0 ? foot : R(L - foot)) : L;
     R part = 0.0;
@@ -158,7 +171,7 @@ __device__ R self_potential_piece(const V3<R> P[3], int e, int piece, const Quad
         const R b = lo + span * Q.sx[k], a = L - b;
         const V3<R> y = P1 + b * tau;
         const R phis = angle_ref(tau, P3 - y);
-        part += Q.sw[k] * (ray_side(a, al2, R(phis + al2)) + ray_side(b, al1, R((kPi - phis) + al1)));
+        part += Q.sw[k] * (ray_side(a, s2, c2, F02, R(phis + al2)) + ray_side(b, s1, c1, F01, R((kPi - phis) + al1)));
     }
     return span * part;
 }

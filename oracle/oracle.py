@@ -32,7 +32,7 @@ _QF13_W = np.array([-0.149570044467670] + [0.175615257433204] * 3 + [0.053347235
                    [0.077113760890257] * 6)
 QF13 = (_QF13_COORDS, _QF13_W, 7)
 # the library's default potential rule, for CPU runs doing the library's work
-PRODUCT_RULE = dict(nu=10, nv=8, grade=3, adaptive=1e-8, depth=12, tiered=1e-7)
+PRODUCT_RULE = dict(nu=10, nv=8, grade=3, adaptive=1e-8, depth=12, tiered=2e-7)
 
 _lock = threading.Lock()
 _lib = None
