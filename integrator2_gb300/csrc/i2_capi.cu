@@ -506,6 +506,7 @@ i2::QuadTablesF tables_f32(const i2::QuadTables &Q)
     i2::QuadTablesF F;
     std::memset(&F, 0, sizeof F);
     F.npts = Q.npts;
+    F.pow2p = Q.pow2p;
     for (int g = 0; g < Q.npts; ++g) {
         F.L1[g] = (float)Q.L1[g];
         F.L2[g] = (float)Q.L2[g];

@@ -137,6 +137,7 @@ __device__ __forceinline__ void kahan_add(kahan5 &k, int i, float v)
 struct QuadTablesF {
     float L1[kMaxGauss], L2[kMaxGauss], L3[kMaxGauss], w[kMaxGauss];
     int npts;
+    double pow2p;  // 2^order of the rule (the compat mode's Runge criterion)
     float du_u[kMaxDuffy], du_w[kMaxDuffy], dv_v[kMaxDuffy], dv_w[kMaxDuffy];
     int nu, nv;
     float lo_u[kMaxDuffy], lo_uw[kMaxDuffy], lo_v[kMaxDuffy], lo_vw[kMaxDuffy];

@@ -11,6 +11,21 @@ __device__ __forceinline__ void store5(double *p, const acc5 &a)
 }
 __device__ __forceinline__ acc5 load5(const double *p) { return acc5{p[0], p[1], p[2], p[3], p[4]}; }
 
+// the reference's Runge criterion (evaluator3d.cu:76-99, cuda_math.cuh:270-300): the 1-norm of
+// divide(I_L - I_{L-1}, 2^p I_{L-1} - I_L) with its small-value guards against EPS_INTEGRATION
+__device__ __forceinline__ bool runge_unconverged(const acc5 &cur, const acc5 &prev, double pow2p)
+{
+    const double c[4] = {cur.px, cur.py, cur.pz, cur.th}, p[4] = {prev.px, prev.py, prev.pz, prev.th};
+    double crit = 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const double num = c[k] - p[k], den = pow2p * p[k] - c[k];
+        const double lim = k < 3 ? kDoubleMin : kEps2;
+        crit += fabs((fabs(num) < lim && fabs(den) < lim) ? 0.0 : num / den);
+    }
+    return crit > kEpsRunge;
+}
+
 template <int CLS>
 __device__ inline void finalize_item(const ClassArgs &A, int mode, int t)
 {

@@ -60,21 +60,6 @@ __device__ __forceinline__ acc5 shfl_xor5(acc5 a, int off)
 
 
 
-// Runge criterion of the reference on the regular-part sums (evaluator3d.cu:76-99 with
-// divide()/norm1() of cuda_math.cuh:270-300)
-__device__ __forceinline__ bool runge_unconverged(const acc5 &cur, const acc5 &prev, double pow2p)
-{
-    const double c[4] = {cur.px, cur.py, cur.pz, cur.th}, p[4] = {prev.px, prev.py, prev.pz, prev.th};
-    double crit = 0.0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const double num = c[k] - p[k], den = pow2p * p[k] - c[k];
-        const double lim = k < 3 ? kDoubleMin : kEps2;
-        crit += fabs((fabs(num) < lim && fabs(den) < lim) ? 0.0 : num / den);
-    }
-    return crit > kEpsRunge;
-}
-
 // ------------------------------------------------------------------ regular part, one level
 template <int CLS>
 __global__ void __launch_bounds__(128) k_level(ClassArgs A, QuadTables Q, int level, int mode, double tol, int kmax)
@@ -172,7 +157,7 @@ __global__ void __launch_bounds__(128) k_level(ClassArgs A, QuadTables Q, int le
         if (!unconv || level >= kmax) {
             A.stop[t] = level;
             store5(A.fin_a + 5 * (long long)t, acc);
-            store5(A.fin_b + 5 * (long long)t, prev);
+            if (mode == kAdaptiveCompat) store5(A.fin_b + 5 * (long long)t, prev);  // read by compat parity only
         } else {
             const int pos = atomicAdd(A.cnt_out, 1);
             A.act_out[pos] = t;

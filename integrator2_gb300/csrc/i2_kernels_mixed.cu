@@ -248,27 +248,46 @@ __device__ void level_items_mixed(const ClassArgs &A, const QuadTablesF &Qf, int
         }
         const acc5 prev = acc5{cur[0], cur[1], cur[2], cur[3], cur[4]};
         cur[0] = acc.px; cur[1] = acc.py; cur[2] = acc.pz; cur[3] = acc.th; cur[4] = acc.pot;
-        // FP64 error estimator (relative change of J and of the near-field potential)
+        // error estimator: the differences of successive levels (where cancellation sits) and the
+        // singular part are formed in FP64; the norms of the resulting J and dJ are compared in FP32
+        // (squared, no square roots), which is ample for a 1e-6..1e-2 tolerance
         const double4_32a nj4 = A.panels[pr.y].v[3];
-        const d3 nj = mk(nj4.x, nj4.y, nj4.z);
-        const double Si = A.panels[pr.x].v[0].w;
-        d3 spsi = mk(0, 0, 0);
-        double sth = 0.0;
+        const f3 nf = f3{(float)nj4.x, (float)nj4.y, (float)nj4.z};
+        double spx = 0.0, spy = 0.0, spz = 0.0, sth = 0.0;
         if (CLS != kFar) {
             const double *sg = A.sing + 4 * (long long)t;
-            spsi = mk(sg[0], sg[1], sg[2]);
-            sth = sg[3];
+            spx = sg[0]; spy = sg[1]; spz = sg[2]; sth = sg[3];
         }
-        const d3 Jc = finalize_j(CLS, mk(acc.px, acc.py, acc.pz) + spsi, acc.th + sth, nj, Si);
-        const d3 dJ = kInv4Pi * ((acc.th - prev.th) * nj + cross(mk(acc.px - prev.px, acc.py - prev.py, acc.pz - prev.pz), nj));
-        bool unconv = norm(dJ) > tol * norm(Jc);
-        if (CLS == kFar) unconv = unconv || fabs(acc.pot - prev.pot) > tol * fabs(acc.pot);
+        double th_tot = acc.th + sth;
+        if (CLS == kVertex) {
+            // the p-fix of the common-vertex class (evaluatorJ3DK.cu:224-264)
+            const double ref = kTwoPi * A.panels[pr.x].v[0].w;
+            int pf = 0;
+            if (th_tot > ref) pf = -((int)trunc((th_tot - ref) / (2.0 * ref)) + 1);
+            else if (th_tot < -ref) pf = ((int)trunc((-ref - th_tot) / (2.0 * ref)) + 1);
+            th_tot += 2.0 * pf * ref;
+        }
+        const f3 psif = f3{(float)(acc.px + spx), (float)(acc.py + spy), (float)(acc.pz + spz)};
+        const f3 Jf = (float)th_tot * nf + crossf(psif, nf);
+        const f3 dpsif = f3{(float)(acc.px - prev.px), (float)(acc.py - prev.py), (float)(acc.pz - prev.pz)};
+        const f3 dJf = (float)(acc.th - prev.th) * nf + crossf(dpsif, nf);
+        const float tolf = (float)tol;
+        bool unconv;
+        if (mode == kAdaptiveCompat) {
+            unconv = runge_unconverged(acc, prev, Qf.pow2p);
+        } else {
+            unconv = dotf(dJf, dJf) > tolf * tolf * dotf(Jf, Jf);
+            if (CLS == kFar) unconv = unconv || fabsf((float)(acc.pot - prev.pot)) > tolf * fabsf((float)acc.pot);
+        }
         atomicMax(A.maxlev, level);
         if (!unconv || level >= kmax) {
             A.stop[t] = level;
-            double *fa = A.fin_a + 5 * (long long)t, *fb = A.fin_b + 5 * (long long)t;
+            double *fa = A.fin_a + 5 * (long long)t;
             fa[0] = acc.px; fa[1] = acc.py; fa[2] = acc.pz; fa[3] = acc.th; fa[4] = acc.pot;
-            fb[0] = prev.px; fb[1] = prev.py; fb[2] = prev.pz; fb[3] = prev.th; fb[4] = prev.pot;
+            if (mode == kAdaptiveCompat) {  // only the compat mode's buffer parity reads the previous level
+                double *fb = A.fin_b + 5 * (long long)t;
+                fb[0] = prev.px; fb[1] = prev.py; fb[2] = prev.pz; fb[3] = prev.th; fb[4] = prev.pot;
+            }
         } else {
             A.act_out[atomicAdd(A.cnt_out, 1)] = t;
         }
