@@ -28,7 +28,7 @@ struct AdjointArgs {
     int mode, fixed_level;
     const double *gJ, *gP;   // upstream gradients (either may be nullptr)
     double *gradV;           // 3 per vertex, accumulated
-    double hard_tol, tier_tol;
+    double hard_tol, tier_tol, top_tol;
     int self_sign;
 };
 
@@ -201,8 +201,13 @@ __global__ void __launch_bounds__(128) k_adjoint(AdjointArgs A, QuadTables Q)
                         const R pl = duffy_total<CLS>(Ti, K, F, pe, Q.lo_u, Q.lo_uw, Q.lo_nu, Q.lo_v, Q.lo_vw, Q.lo_nv) + sig;
                         if (fabs(value_of(pm) - value_of(pl)) > A.tier_tol * fabs(value_of(pm))) {
                             const R ph = duffy_total<CLS>(Ti, K, F, pe, Q.hi_u, Q.hi_uw, Q.hi_nu, Q.hi_v, Q.hi_vw, Q.hi_nv) + sig;
-                            adapt = fabs(value_of(ph) - value_of(pm)) > A.tier_tol * fabs(value_of(ph));
+                            const bool agree = fabs(value_of(ph) - value_of(pm)) <= A.tier_tol * fabs(value_of(ph));
                             pm = ph;
+                            if (!agree) {
+                                const R pt = duffy_total<CLS>(Ti, K, F, pe, Q.top_u, Q.top_uw, Q.top_nu, Q.top_v, Q.top_vw, Q.top_nv) + sig;
+                                adapt = fabs(value_of(pt) - value_of(ph)) > A.top_tol * fabs(value_of(pt));
+                                if (!adapt) pm = pt;
+                            }
                         }
                     }
                 }
@@ -236,7 +241,7 @@ static void launch_adjoint_t(int cls, const AdjointArgs &A, const QuadTables &Q,
 }
 
 void launch_adjoint(int cls, bool fp32, const int2 *pairs, int n, const int3 *cells, const double *V, const int *stop,
-                    const int *maxlev, const RunConfig &cfg, double tier_tol, const double *gJ, const double *gP, double *gradV,
+                    const int *maxlev, const RunConfig &cfg, double tier_tol, double top_tol, const double *gJ, const double *gP, double *gradV,
                     const QuadTables &Q, int persistent_blocks, cudaStream_t s)
 {
     if (n <= 0) return;
@@ -254,6 +259,7 @@ void launch_adjoint(int cls, bool fp32, const int2 *pairs, int n, const int3 *ce
     A.gradV = gradV;
     A.hard_tol = cfg.hard_tol;
     A.tier_tol = tier_tol;
+    A.top_tol = top_tol;
     A.self_sign = cfg.self_sign;
     const long long items = 6LL * n;
     const int blocks = (int)std::min<long long>((items + 127) / 128, (long long)persistent_blocks * 4);

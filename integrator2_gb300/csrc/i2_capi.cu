@@ -307,6 +307,9 @@ struct i2_integrator {
         Q.hi_nu = i2::kMaxDuffy;
         Q.hi_nv = i2::kMaxDuffy;
         duffy_rule(Q.hi_nu, Q.hi_nv, Q.hi_u, Q.hi_uw, Q.hi_v, Q.hi_vw);
+        Q.top_nu = i2::kDuffyTop;
+        Q.top_nv = i2::kDuffyTop;
+        duffy_rule(Q.top_nu, Q.top_nv, Q.top_u, Q.top_uw, Q.top_v, Q.top_vw);
         gauss_legendre01(pot_nself, x, w);
         Q.nself = pot_nself;
         for (int k = 0; k < pot_nself; ++k) {
@@ -518,6 +521,11 @@ i2::QuadTablesF tables_f32(const i2::QuadTables &Q)
     F.lo_nu = Q.lo_nu;
     F.lo_nv = Q.lo_nv;
     F.hi_nu = Q.hi_nu;
+    F.top_nu = Q.top_nu;
+    F.top_nv = Q.top_nv;
+    for (int k = 0; k < i2::kDuffyTop; ++k) {
+        F.top_u[k] = (float)Q.top_u[k]; F.top_uw[k] = (float)Q.top_uw[k]; F.top_v[k] = (float)Q.top_v[k]; F.top_vw[k] = (float)Q.top_vw[k];
+    }
     F.hi_nv = Q.hi_nv;
     for (int k = 0; k < i2::kMaxDuffy; ++k) {
         F.du_u[k] = (float)Q.du_u[k]; F.du_w[k] = (float)Q.du_w[k]; F.dv_v[k] = (float)Q.dv_v[k]; F.dv_w[k] = (float)Q.dv_w[k];
@@ -532,6 +540,10 @@ i2::QuadTablesF tables_f32(const i2::QuadTables &Q)
 // sphere (largest error 6.5e-7 common vertex, 8.9e-7 common edge) and stays above the FP32
 // rounding of the mixed form's Duffy sums
 double tier_tolerance(const i2::RunConfig &cfg) { return std::max(10.0 * cfg.hard_tol, 2e-7); }
+// agreement bar of tier 2b (16 x 16 against 24 x 24, FP64 in both forms): a tenth of the tier bar,
+// since two rules that agree only to the tier bar can share a bias of 1e-6 (a near-coplanar pair of
+// the sigma 0.3 jittered sphere)
+double top_tolerance(const i2::RunConfig &cfg, bool) { return tier_tolerance(cfg) / 10.0; }
 
 // cells per depth list of the adaptive potential (24 bytes each): every hard pair seeds 4 cells
 // at depth 1; deeper lists hold a few tens of thousands of cells on the meshes measured (C2: at
@@ -620,6 +632,7 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         A.pot_fx = W.pot_fx.ptr;
         A.tier2_cnt = W.cnt.ptr + 10;
         A.tier_tol = tier_tolerance(cfg);
+        A.top_tol = top_tolerance(cfg, ev->integrator->precision == I2_PRECISION_MIXED);
     }
     A.raw4 = out_raw;
     A.J3 = out_J;
@@ -1094,7 +1107,7 @@ i2_status i2_evaluator_backward_class(i2_evaluator_t *ev, i2_pair_class cls, con
         I2_REQUIRE(m.on_device, I2_ERR_STATE, "mesh not on the device");
         i2::RunConfig cfg = R.cfg;
         // the tier bar of the forward pass (run_class_device)
-        const double tier_tol = tier_tolerance(cfg);
+        const double tier_tol = tier_tolerance(cfg), top_tol = top_tolerance(cfg, R.precision == I2_PRECISION_MIXED);
         if (ev->persistent_blocks == 0) {
             int dev = 0, sms = 0;
             I2_CHECK_CUDA(cudaGetDevice(&dev));
@@ -1102,7 +1115,7 @@ i2_status i2_evaluator_backward_class(i2_evaluator_t *ev, i2_pair_class cls, con
             ev->persistent_blocks = std::max(1, sms) * 8;
         }
         i2::launch_adjoint(c, R.precision == I2_PRECISION_MIXED, reinterpret_cast<const int2 *>(d_pairs), (int)n,
-                           reinterpret_cast<const int3 *>(m.dC.ptr), m.dV.ptr, R.level.ptr, R.maxlev.ptr, cfg, tier_tol, d_gJ, d_gP,
+                           reinterpret_cast<const int3 *>(m.dC.ptr), m.dV.ptr, R.level.ptr, R.maxlev.ptr, cfg, tier_tol, top_tol, d_gJ, d_gP,
                            d_gradV, ev->integrator->tables(), ev->persistent_blocks, ev->stream);
         I2_CHECK_CUDA(cudaGetLastError());
     });
@@ -1261,6 +1274,7 @@ i2_status i2_batch_add(i2_batch_t *batch, const i2_mesh_t *mesh, i2_pair_class c
             A.pot_q_a = sp->pot_q_a.ptr; A.pot_q_b = sp->pot_q_b.ptr; A.pot_qcap = (int)pot_queue_capacity(m);
             A.pot_qcnt = sp->pot_qcnt.ptr; A.pot_fx = sp->pot_fx.ptr;
             A.tier_tol = tier_tolerance(batch->cfg);
+            A.top_tol = top_tolerance(batch->cfg, true);
         }
         A.raw4 = sp->raw4.ptr; A.J3 = sp->J.ptr; A.P = sp->P.ptr; A.level_out = sp->level.ptr;
         if (segment) *segment = (int32_t)batch->segs.size();

@@ -34,6 +34,7 @@ constexpr double kEpsRunge = 1e-5;
 constexpr int kMaxLevel = 5;
 constexpr int kMaxGauss = 16;
 constexpr int kMaxDuffy = 16;
+constexpr int kDuffyTop = 24;  // size of the top Duffy rule of the tiered potential
 constexpr int kMaxSelf = 32;
 
 // the value of a scalar (dual numbers provide their own overload)
@@ -226,6 +227,9 @@ struct QuadTables {
     int lo_nu, lo_nv;
     double hi_u[kMaxDuffy], hi_uw[kMaxDuffy], hi_v[kMaxDuffy], hi_vw[kMaxDuffy];
     int hi_nu, hi_nv;
+    // top rule (24 x 24), checked against the higher-order rule before the adaptive rule
+    double top_u[kDuffyTop], top_uw[kDuffyTop], top_v[kDuffyTop], top_vw[kDuffyTop];
+    int top_nu, top_nv;
     // Gauss-Legendre on [0,1] for the self-pair potential (graded t^2(3-2t) map applied)
     double sx[kMaxSelf], sw[kMaxSelf];
     int nself;

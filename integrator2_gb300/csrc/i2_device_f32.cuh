@@ -144,6 +144,8 @@ struct QuadTablesF {
     int lo_nu, lo_nv;
     float hi_u[kMaxDuffy], hi_uw[kMaxDuffy], hi_v[kMaxDuffy], hi_vw[kMaxDuffy];
     int hi_nu, hi_nv;
+    float top_u[kDuffyTop], top_uw[kDuffyTop], top_v[kDuffyTop], top_vw[kDuffyTop];
+    int top_nu, top_nv;
 };
 
 } // namespace i2

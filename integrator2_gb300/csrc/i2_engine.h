@@ -64,6 +64,7 @@ struct ClassArgs {
     int *pot_qcnt = nullptr;                  // cells per depth (kHardMaxDepth + 2 ints)
     long long *pot_fx = nullptr;              // per hard pair: accepted sums in 64-bit fixed point
     double tier_tol = 1e-7;                   // main/check (and main/higher-order) rule agreement bar
+    double top_tol = 1e-8;                    // 16 x 16 / 24 x 24 agreement bar (tier 2b)
     // outputs
     double *raw4 = nullptr, *J3 = nullptr, *P = nullptr;
     int *level_out = nullptr;
@@ -88,7 +89,7 @@ void launch_batch_prelude(const ClassArgs &A, int cls, const QuadTables &Q, cons
                           int persistent_blocks, cudaStream_t s);
 // adjoint: dL/dV += gJ . dJ/dV + gP dP/dV over the pairs of one class (fp32: FP32 dual numbers)
 void launch_adjoint(int cls, bool fp32, const int2 *pairs, int n, const int3 *cells, const double *V, const int *stop,
-                    const int *maxlev, const RunConfig &cfg, double tier_tol, const double *gJ, const double *gP, double *gradV,
+                    const int *maxlev, const RunConfig &cfg, double tier_tol, double top_tol, const double *gJ, const double *gP, double *gradV,
                     const QuadTables &Q, int persistent_blocks, cudaStream_t s);
 // mixed form: FP64 recomputation of the pairs with a needle cell (corner below 3 degrees)
 void launch_fp64_fixup(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s);

@@ -210,13 +210,24 @@ __global__ void __launch_bounds__(128) k_singular(ClassArgs A, QuadTables Q)
     }
 }
 
-// tier 2: higher-order Duffy rule; pairs where it still disagrees with the main rule go on to
-// the adaptive rule (tier 3)
+// tier 2: higher-order Duffy rule (16 x 16), kept when it agrees with the main rule; otherwise
+// tier 2b: the top rule (24 x 24), kept when it agrees with the 16 x 16 one; pairs where that
+// fails too go on to the adaptive rule (tier 3)
+__device__ __forceinline__ double warp_sum(double x)
+{
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    return x;
+}
+
 template <int CLS>
 __global__ void __launch_bounds__(128) k_pot_tier2(ClassArgs A, QuadTables Q)
 {
+    // one warp per listed pair: the lanes share each rule's points, so the FP64 work of the
+    // list spreads over every SM
     const int count = *A.tier2_cnt;
-    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < count; h += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < count; h += nwarps) {
         const int t = A.tier2_list[h];
         const int2 pr = A.pairs[t];
         const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
@@ -229,16 +240,28 @@ __global__ void __launch_bounds__(128) k_pot_tier2(ClassArgs A, QuadTables Q)
         const FarCtx F = make_far_ctx(K);
         PotEdge pe;
         const double sig = CLS == kEdge ? make_pot_edge(Ti, Tj, K, Si, pe) : 0.0;
-        const double ph = duffy_total<CLS>(Ti, K, F, pe, Q.hi_u, Q.hi_uw, Q.hi_nu, Q.hi_v, Q.hi_vw, Q.hi_nv) + sig;
+        const double ph = warp_sum(duffy_partial<CLS>(Ti, K, F, pe, Q.hi_u, Q.hi_uw, Q.hi_nu, Q.hi_v, Q.hi_vw, Q.hi_nv, lane, 32)) + sig;
         const double pm = A.padj[t] * (4.0 * kPi);
-        A.padj[t] = kInv4Pi * ph;
-        if (fabs(ph - pm) > A.tier_tol * fabs(ph)) A.hard_list[atomicAdd(A.hard_cnt, 1)] = t;
+        if (fabs(ph - pm) <= A.tier_tol * fabs(ph)) {
+            if (lane == 0) A.padj[t] = kInv4Pi * ph;
+            continue;
+        }
+        // tier 2b: the top rule against the higher-order one (when the main rule was the
+        // inaccurate one, the 16 x 16 and 24 x 24 rules agree and the pair needs no adaptive rule)
+        const double pt = warp_sum(duffy_partial<CLS>(Ti, K, F, pe, Q.top_u, Q.top_uw, Q.top_nu, Q.top_v, Q.top_vw, Q.top_nv, lane, 32)) + sig;
+        if (lane != 0) continue;
+        if (fabs(pt - ph) <= A.top_tol * fabs(pt)) {
+            A.padj[t] = kInv4Pi * pt;
+        } else {
+            A.padj[t] = kInv4Pi * ph;  // the adaptive rule's tolerance base
+            A.hard_list[atomicAdd(A.hard_cnt, 1)] = t;
+        }
     }
 }
 
 // ------------------------------------------------------------------ hard adjacent pairs: adaptive potential
 // Breadth-first over the cells of ALL hard pairs at once: depth d holds a device list of cells
-// (hard-list slot, path, depth, corner slot, value); one thread takes one cell, integrates its
+// (hard-list slot, path, depth, corner slot, value); one warp takes one cell, integrates its
 // four children and either accepts their sum (|sum - value| <= tol |P| 2^-d, or d at the depth
 // cap) or appends the children to depth d + 1's list.  Cells that hold a shared vertex (always
 // in slot 1 of a corner child) use the graded Duffy rule with that vertex as apex, all others

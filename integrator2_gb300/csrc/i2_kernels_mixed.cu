@@ -308,8 +308,10 @@ __global__ void __launch_bounds__(256, 2) k_level_mixed(ClassArgs A, QuadTablesF
 template <int CLS>
 __device__ float duffy_total_f(const PanelF *__restrict__ P, int pi, int pj, int si, const PanelJf &K, const FarCtxF &F,
                                int p1_vertex, const f3 &m_in, float c, float h, const float *uu, const float *uw, int nu,
-                               const float *vv, const float *vw, int nv)
+                               const float *vv, const float *vw, int nv, int first = 0, int step = 1)
 {
+    // first / step select the points p = first, first + step, ... of the flattened (piece, radial,
+    // angular) list, so that a warp can share one rule (step 32); the defaults sum all points
     f3 R0[3], R1[3], R2[3];  // K_i's vertices (rotated by si) as offsets from K_j's vertices 0, 1, 2
     {
         f3 a, b, cc;
@@ -325,9 +327,12 @@ __device__ float duffy_total_f(const PanelF *__restrict__ P, int pi, int pj, int
             R2[k] = q2[(si + k) % 3];
         }
     }
-    float total = 0.0f;
     const int npieces = CLS == kEdge ? 2 : 1;
-    for (int piece = 0; piece < npieces; ++piece) {
+    const int per = nu * nv;
+    float total = 0.0f, comp = 0.0f;  // compensated (Kahan) sum: the tier checks compare to 2e-7
+#pragma unroll 1
+    for (int p = first; p < npieces * per; p += step) {
+        const int piece = p / per, q = p - piece * per, a = q / nv, b = q - a * nv;
         // apex slot and the two other corners of the piece, as offsets from K_j's vertex 0
         int ap;
         f3 B, Cc;
@@ -339,28 +344,20 @@ __device__ float duffy_total_f(const PanelF *__restrict__ P, int pi, int pj, int
         }
         const f3 dA = R0[ap], dB = R1[ap], dC = R2[ap];
         const f3 eB = B - dA, eC = Cc - dA;
-        const float area2 = normf(crossf(eB, eC));
-        const f3 dP1 = p1_vertex == 0 ? dA : (p1_vertex == 1 ? dB : dC);
-        float acc = 0.0f;
-#pragma unroll 1
-        for (int a = 0; a < nu; ++a) {
-            const float u = uu[a];
-            float row = 0.0f;
-#pragma unroll 1
-            for (int b = 0; b < nv; ++b) {
-                const f3 w = u * ((1.0f - vv[b]) * eB + vv[b] * eC);
-                f3 psi;
-                float th, g;
-                far_integrand_f(dA + w, dB + w, dC + w, K, F, psi, th, g);
-                if (CLS == kEdge) {
-                    const float sd = dotf(dP1 + w, m_in);
-                    if (sd > 0.0f) g += 2.0f * c * sd * logf(sd / h);
-                }
-                row = fmaf(vw[b], g, row);
-            }
-            acc = fmaf(uw[a] * u, row, acc);
+        const float u = uu[a];
+        const f3 w = u * ((1.0f - vv[b]) * eB + vv[b] * eC);
+        f3 psi;
+        float th, g;
+        far_integrand_f(dA + w, dB + w, dC + w, K, F, psi, th, g);
+        if (CLS == kEdge) {
+            const f3 dP1 = p1_vertex == 0 ? dA : (p1_vertex == 1 ? dB : dC);
+            const float sd = dotf(dP1 + w, m_in);
+            if (sd > 0.0f) g += 2.0f * c * sd * logf(sd / h);
         }
-        total = fmaf(area2, acc, total);
+        const float y = normf(crossf(eB, eC)) * uw[a] * u * vw[b] * g - comp;
+        const float tt = total + y;
+        comp = (tt - total) - y;
+        total = tt;
     }
     return total;
 }
@@ -446,30 +443,64 @@ __global__ void __launch_bounds__(128) k_singular_mixed(ClassArgs A, QuadTablesF
     }
 }
 
+__device__ __forceinline__ float warp_sum_f(float x)
+{
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    return x;
+}
+
+// tier 2 in FP32 and, for the pairs it rejects, tier 2b in FP64, one warp per listed pair (the
+// lanes share each rule's points).  Tier 2b is FP64 because the FP32 rules can share a bias of a
+// few 1e-6 (a small, flat K_j beside a large K_i), and two biased rules agree with each other.
 template <int CLS>
-__global__ void __launch_bounds__(128) k_pot_tier2_mixed(ClassArgs A, QuadTablesF Qf)
+__global__ void __launch_bounds__(128) k_pot_tier2_mixed(ClassArgs A, QuadTablesF Qf, QuadTables Q)
 {
     const int count = *A.tier2_cnt;
-    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < count; h += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < count; h += nwarps) {
         const int t = A.tier2_list[h];
         const int2 pr = A.pairs[t];
         const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
         int si, sj;
         if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
         else shifts_vertex(ci, cj, si, sj);
-        const PanelJf K = load_panel_f(A.panels_f, pr.y);
-        const FarCtxF F{crossf(K.ta, K.n), crossf(K.tb, K.n), crossf(K.tc, K.n)};
+        const PanelJf Kf = load_panel_f(A.panels_f, pr.y);
+        const FarCtxF Ff{crossf(Kf.ta, Kf.n), crossf(Kf.tb, Kf.n), crossf(Kf.tc, Kf.n)};
         const double Si = A.panels[pr.x].v[0].w;
         f3 m_in = f3{0, 0, 0};
         float c = 0.0f, hh = 1.0f;
         double sig = 0.0;
         const int p1v = (sj + 1) % 3;
-        if (CLS == kEdge) edge_sigma_setup(A, pr, si, sj, K, Si, m_in, c, hh, sig);
-        const double ph = (double)duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, K, F, p1v, m_in, c, hh, Qf.hi_u, Qf.hi_uw, Qf.hi_nu,
-                                                     Qf.hi_v, Qf.hi_vw, Qf.hi_nv) + sig;
+        if (CLS == kEdge) edge_sigma_setup(A, pr, si, sj, Kf, Si, m_in, c, hh, sig);
+        const double ph = (double)warp_sum_f(duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, Kf, Ff, p1v, m_in, c, hh, Qf.hi_u, Qf.hi_uw,
+                                                                Qf.hi_nu, Qf.hi_v, Qf.hi_vw, Qf.hi_nv, lane, 32)) + sig;
         const double pm = A.padj[t] * (4.0 * kPi);
-        A.padj[t] = kInv4Pi * ph;
-        if (fabs(ph - pm) > A.tier_tol * fabs(ph)) A.hard_list[atomicAdd(A.hard_cnt, 1)] = t;
+        if (fabs(ph - pm) <= A.tier_tol * fabs(ph)) {
+            if (lane == 0) A.padj[t] = kInv4Pi * ph;
+            continue;
+        }
+        // tier 2b in FP64: 24 x 24 against 16 x 16
+        const PanelJ K = load_panel(A.panels, pr.y);
+        const Tri Ti = rotate(load_tri(A.panels, pr.x), si), Tj = rotate(Tri{K.A, K.B, K.C}, sj);
+        const FarCtx F = make_far_ctx(K);
+        PotEdge pe;
+        const double sg64 = CLS == kEdge ? make_pot_edge(Ti, Tj, K, Si, pe) : 0.0;
+        double ph64 = duffy_partial<CLS>(Ti, K, F, pe, Q.hi_u, Q.hi_uw, Q.hi_nu, Q.hi_v, Q.hi_vw, Q.hi_nv, lane, 32);
+        double pt64 = duffy_partial<CLS>(Ti, K, F, pe, Q.top_u, Q.top_uw, Q.top_nu, Q.top_v, Q.top_vw, Q.top_nv, lane, 32);
+        for (int off = 16; off > 0; off >>= 1) {
+            ph64 += __shfl_xor_sync(0xffffffffu, ph64, off);
+            pt64 += __shfl_xor_sync(0xffffffffu, pt64, off);
+        }
+        ph64 += sg64;
+        pt64 += sg64;
+        if (lane != 0) continue;
+        if (fabs(pt64 - ph64) <= A.top_tol * fabs(pt64)) {
+            A.padj[t] = kInv4Pi * pt64;
+        } else {
+            A.padj[t] = kInv4Pi * ph64;  // the adaptive rule's tolerance base
+            A.hard_list[atomicAdd(A.hard_cnt, 1)] = t;
+        }
     }
 }
 
@@ -682,7 +713,7 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
     case kEdge:
         k_singular_mixed<kEdge><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
         if (A.hard_list) {
-            k_pot_tier2_mixed<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Qf);
+            k_pot_tier2_mixed<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Qf, Q);
             launch_pot_hard(kEdge, A, Q, cfg, persistent_blocks, s);
         }
         level_chain_mixed<kEdge>(A, Qf, cfg, persistent_blocks, s);
@@ -691,7 +722,7 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
     case kVertex:
         k_singular_mixed<kVertex><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
         if (A.hard_list) {
-            k_pot_tier2_mixed<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Qf);
+            k_pot_tier2_mixed<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Qf, Q);
             launch_pot_hard(kVertex, A, Q, cfg, persistent_blocks, s);
         }
         level_chain_mixed<kVertex>(A, Qf, cfg, persistent_blocks, s);
@@ -776,13 +807,13 @@ void launch_batch_prelude(const ClassArgs &A, int cls, const QuadTables &Q, cons
     } else if (cls == kEdge) {
         k_singular_mixed<kEdge><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
         if (A.hard_list) {
-            k_pot_tier2_mixed<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Qf);
+            k_pot_tier2_mixed<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Qf, Q);
             launch_pot_hard(kEdge, A, Q, cfg, persistent_blocks, s);
         }
     } else if (cls == kVertex) {
         k_singular_mixed<kVertex><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
         if (A.hard_list) {
-            k_pot_tier2_mixed<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Qf);
+            k_pot_tier2_mixed<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Qf, Q);
             launch_pot_hard(kVertex, A, Q, cfg, persistent_blocks, s);
         }
     }

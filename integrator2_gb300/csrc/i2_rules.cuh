@@ -66,6 +66,37 @@ __device__ R duffy_total(const TriT<R> &Ti, const PanelJT<R> &K, const FarCtxT<R
     return total;
 }
 
+// the same rule's points p = first, first + step, ... of the flattened (piece, radial, angular)
+// list, so that a warp can share one rule (step 32)
+template <int CLS, class R>
+__device__ R duffy_partial(const TriT<R> &Ti, const PanelJT<R> &K, const FarCtxT<R> &F, const PotEdgeT<R> &pe, const double *uu,
+                           const double *uw, int nu, const double *vv, const double *vw, int nv, int first, int step)
+{
+    const int npieces = CLS == kEdge ? 2 : 1;
+    const int per = nu * nv;
+    R total = 0.0;
+#pragma unroll 1
+    for (int p = first; p < npieces * per; p += step) {
+        const int piece = p / per, q = p - piece * per, a = q / nv, b = q - a * nv;
+        V3<R> Vx, B, Cc;
+        if (CLS == kVertex) { Vx = Ti.a; B = Ti.b; Cc = Ti.c; }
+        else {
+            const V3<R> M = 0.5 * (Ti.b + Ti.c);
+            if (piece == 0) { Vx = Ti.b; B = M; Cc = Ti.a; }
+            else { Vx = Ti.c; B = Ti.a; Cc = M; }
+        }
+        const V3<R> eB = B - Vx, eC = Cc - Vx;
+        const double u = uu[a];
+        const V3<R> w = u * ((1.0 - vv[b]) * eB + vv[b] * eC);
+        V3<R> psi;
+        R th, g;
+        far_integrand_o((Vx - K.A) + w, (Vx - K.B) + w, (Vx - K.C) + w, K, F, psi, th, g);
+        if (CLS == kEdge) g -= pot_edge_sigma(Vx + w, pe);
+        total += (uw[a] * u * vw[b]) * norm(cross(eB, eC)) * g;
+    }
+    return total;
+}
+
 // one cell of the adaptive rule: graded Duffy with the shared vertex (in slot `corner`) as apex,
 // or the 13-point rule; offsets to K_j's vertices from vertex differences
 template <int CLS, class R>

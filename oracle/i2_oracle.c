@@ -756,8 +756,10 @@ static double pot_adapt(const pot_ctx *c, v3 a, v3 b, v3 cc, int corner, double 
 
 /* tiered potential rule of the library: the main Duffy rule is kept when a lower-order check
  * (two fewer nodes per direction) agrees within the tier tolerance; otherwise a 16 x 16 rule is
- * kept when it agrees with the main rule; otherwise the adaptive rule runs.  Returns 1 when the
- * adaptive rule must run, and stores the kept Duffy value in *acc otherwise. */
+ * kept when it agrees with the main rule; otherwise a 24 x 24 rule is kept when it agrees with the
+ * 16 x 16 one to a tenth of the tolerance; otherwise the adaptive rule runs.  Returns 1 when the adaptive rule must run (*acc
+ * then holds the 16 x 16 value, the adaptive rule's tolerance base), and stores the kept Duffy
+ * value in *acc otherwise. */
 static int tier_select(int npieces, const v3 P[2][3], v3 JA, v3 JB, v3 JC, const pot_edge_ctx *pe, double sig, double *acc)
 {
     double lo = 0.0, hi = 0.0;
@@ -766,6 +768,11 @@ static int tier_select(int npieces, const v3 P[2][3], v3 JA, v3 JB, v3 JC, const
     if (fabs((*acc + sig) - (lo + sig)) <= g_pot_tier_tol * fabs(*acc + sig)) return 0;
     for (int k = 0; k < npieces; ++k) hi += duffy_piece_rule(P[k][0], P[k][1], P[k][2], JA, JB, JC, pe, 16, 16);
     if (fabs((hi + sig) - (*acc + sig)) <= g_pot_tier_tol * fabs(hi + sig)) { *acc = hi; return 0; }
+    /* tier 2b: 24 x 24 against 16 x 16 (the main rule was the inaccurate one) */
+    double top = 0.0;
+    for (int k = 0; k < npieces; ++k) top += duffy_piece_rule(P[k][0], P[k][1], P[k][2], JA, JB, JC, pe, 24, 24);
+    if (fabs((top + sig) - (hi + sig)) <= 0.1 * g_pot_tier_tol * fabs(top + sig)) { *acc = top; return 0; }
+    *acc = hi;
     return 1;
 }
 
