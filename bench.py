@@ -245,6 +245,68 @@ def run_batch(batch, flush, stream, steps, warmup):
     return sum(e0[s].elapsed_time(e1[s]) for s in range(steps))
 
 
+def uneven_batch_section(args):
+    """Many-mesh workload: 48 seeded closed meshes of uneven size (500-6,000 triangles,
+    log-uniform) and scale (5e-4 .. 1e2): ellipsoids, tori, jittered spheres; all four pair classes
+    (near < 3h); relative 1e-6, mixed precision.  The batched form (every segment in one graph
+    replay) against the same meshes run class by class through their own evaluators, all on one
+    stream; CUDA events, 3 steps after 3 warm-up steps."""
+    import torch
+    from integrator2_gb300 import api, meshes, pairs
+    mset = meshes.uneven_mesh_set(2026, 48, 500, 6000)
+    stream = torch.cuda.Stream()
+    evs, segs_dev, total = [], [], 0
+    batch = None
+    for V, C, kind, scale in mset:
+        pl = pairs.build_pairs(V, C, NEAR)
+        m = api.Mesh3D()
+        m.setGeometry(V, C)
+        m.prepareMesh(NEAR)
+        it = api.NumericalIntegrator3D(m, api.qf3D13)
+        it.setErrorControl(api.RELATIVE_ERROR_CONTROL, args.tol, 5)
+        it.setPrecision(api.PRECISION_MIXED)
+        ev = api.EvaluatorJ3DK(m, it)
+        ev.setStream(stream.cuda_stream)
+        lists = [np.ascontiguousarray(pl.by_class(c)) for c in CLASSES]
+        dev = [(torch.from_numpy(l).to("cuda"), torch.empty(len(l), 3, dtype=torch.float64, device="cuda"),
+                torch.empty(len(l), dtype=torch.float64, device="cuda")) for l in lists]
+        if batch is None:
+            batch = api.BatchEvaluator(it)
+            batch.setStream(stream.cuda_stream)
+        for c, l in zip(CLASSES, lists):
+            batch.add(m, c, l)
+        evs.append((m, it, ev, dev))
+        total += sum(len(l) for l in lists)
+
+    def per_class_step():
+        for m, it, ev, dev in evs:
+            for c, (p, J, P) in zip(CLASSES, dev):
+                if len(p):
+                    ev.runClassDevice(c, p.data_ptr(), len(p), 0, J.data_ptr(), P.data_ptr())
+
+    def timed(fn):
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                fn()
+            stream.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(3):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 3
+
+    ms_per_class = timed(per_class_step)
+    shape = batch.autotune()
+    ms_batch = timed(batch.run)
+    return {"workload": "48 meshes (ellipsoids, tori, jittered spheres), 500-6000 triangles, scales 5e-4..1e2, near < 3h, relative 1e-6",
+            "triangles": int(sum(len(c) for _, c, _, _ in mset)), "pairs": int(total),
+            "batched": {"value": total / (ms_batch * 1e-3), "ms_per_step": ms_batch, "cuda_graph": batch.usesGraph(),
+                        "shape": [int(x) for x in shape]},
+            "per_class": {"value": total / (ms_per_class * 1e-3), "ms_per_step": ms_per_class, "launches": "4 class chains x 48 meshes"}}
+
+
 def adjoint_section(args):
     """C4 workload: 5,120-triangle sphere displaced radially by spherical harmonics of degree <= 6
     (coefficients ~ N(0, 0.05^2), seed 4), all four pair classes (near < 3h).  Times forward +
@@ -472,6 +534,7 @@ def gpu_arm(args):
     }
     if "fp64" in forms:
         line["speedup_over_plain_fp64"] = head["value"] / forms["fp64"]["value"]
+    line["uneven_batch"] = uneven_batch_section(args)
     line["adjoint"] = adjoint_section(args)
     if "batch" in forms:
         line["batch"] = {"shape": {"threads": forms["batch"]["shape"][0], "blocks_per_sm": forms["batch"]["shape"][1],

@@ -537,9 +537,10 @@ __device__ inline void q_edge_coplanar(SC2<R> b, SC2<R> n, R sa, R &qt, R &qp)
 }
 
 // integrateSingularPartAttached (:603-672): closed-form integral over K_i of the common-edge
-// asymptote; Ti/Tj hold the vertices rotated so that the off-edge vertex comes first
+// asymptote; Ti/Tj hold the vertices rotated so that the off-edge vertex comes first.  At the
+// scale it is given (see closed_edge for the scale-invariant entry point)
 template <class R>
-__device__ inline void closed_edge(TriT<R> Ti, TriT<R> Tj, V3<R> ni, V3<R> nj, R Si, V3<R> &psi, R &th)
+__device__ inline void closed_edge_unit(TriT<R> Ti, TriT<R> Tj, V3<R> ni, V3<R> nj, R Si, V3<R> &psi, R &th)
 {
     const V3<R> IA = Ti.a, IB = Ti.b, IC = Ti.c, JA = Tj.a, JB = Tj.b, JC = Tj.c;
     const V3<R> ta = unit(JA - JC), tb = unit(JB - JA), tc = unit(JC - JB);
@@ -636,9 +637,10 @@ __device__ inline void q_vertex(const VtxAnglesT<R> &g, R delta, SC2<R> sd, R cl
     qp = gens;
 }
 
-// integrateSingularPartSimple (:674-780); Ti/Tj rotated so that the shared vertex comes first
+// integrateSingularPartSimple (:674-780); Ti/Tj rotated so that the shared vertex comes first.
+// At the scale it is given (see closed_vertex for the scale-invariant entry point)
 template <class R>
-__device__ inline void closed_vertex(TriT<R> Ti, TriT<R> Tj, V3<R> ni, V3<R> nj, R Si, V3<R> &psi, R &th)
+__device__ inline void closed_vertex_unit(TriT<R> Ti, TriT<R> Tj, V3<R> ni, V3<R> nj, R Si, V3<R> &psi, R &th)
 {
     const V3<R> IA = Ti.a, IB = Ti.b, IC = Ti.c, JA = Tj.a, JB = Tj.b, JC = Tj.c;
     const V3<R> ta = unit(JA - JC), tb = unit(JB - JA);
@@ -674,6 +676,47 @@ __device__ inline void closed_vertex(TriT<R> Ti, TriT<R> Tj, V3<R> ni, V3<R> nj,
     }
     psi = Si * (q[0][1] * ta + q[1][1] * tb);
     th = (fabs(xi) < kEps) ? R(0.0) : R(Si * (q[0][0] - q[1][0]));
+}
+
+// ------------------------------------------------------------------ scale-invariant closed forms
+// The reference's tolerances are absolute (angle() returns 0 below |a||b| = 1e-6,
+// src/common/cuda_math.cu:14-26), so its closed forms collapse on meshes far below unit scale.
+// The entry points below scale the pair by the power of two 2^k that brings sqrt(S_i) into
+// [0.5, 1), evaluate there and scale back: Psi and Theta are S_i times dimensionless functions of
+// the angles, the angles of the scaled vertices are bit-identical to the unscaled ones, and a
+// power-of-two scaling is exact -- so at ordinary scales the result is unchanged to the last bit,
+// and far from unit scale the thresholds act as they do at unit scale.
+__device__ __forceinline__ double pow2_normaliser(double len)
+{
+    int e = 0;
+    frexp(len, &e);  // len = m 2^e, m in [0.5, 1)
+    return ldexp(1.0, -e);
+}
+
+template <class R>
+__device__ __forceinline__ TriT<R> scaled_tri(const TriT<R> &t, double s)
+{
+    return TriT<R>{s * t.a, s * t.b, s * t.c};
+}
+
+template <class R>
+__device__ inline void closed_edge(TriT<R> Ti, TriT<R> Tj, V3<R> ni, V3<R> nj, R Si, V3<R> &psi, R &th)
+{
+    const double s = pow2_normaliser(sqrt((double)value_of(Si)));
+    closed_edge_unit(scaled_tri(Ti, s), scaled_tri(Tj, s), ni, nj, R((s * s) * Si), psi, th);
+    const double inv = 1.0 / (s * s);
+    psi = inv * psi;
+    th = inv * th;
+}
+
+template <class R>
+__device__ inline void closed_vertex(TriT<R> Ti, TriT<R> Tj, V3<R> ni, V3<R> nj, R Si, V3<R> &psi, R &th)
+{
+    const double s = pow2_normaliser(sqrt((double)value_of(Si)));
+    closed_vertex_unit(scaled_tri(Ti, s), scaled_tri(Tj, s), ni, nj, R((s * s) * Si), psi, th);
+    const double inv = 1.0 / (s * s);
+    psi = inv * psi;
+    th = inv * th;
 }
 
 // ------------------------------------------------------------------ potential helpers

@@ -179,7 +179,7 @@ __device__ __forceinline__ R ray_side(R a, R sa, R ca, R F0, R u1)
 // swings fastest) when the foot lies inside the edge; otherwise piece 0 is the whole edge and
 // piece 1 is empty
 template <class R>
-__device__ R self_potential_piece(const V3<R> P[3], int e, int piece, const QuadTables &Q)
+__device__ R self_potential_piece_unit(const V3<R> P[3], int e, int piece, const QuadTables &Q)
 {
     const V3<R> P1 = P[e], P2 = P[(e + 1) % 3], P3 = P[(e + 2) % 3];
     const R L = norm(P2 - P1);
@@ -205,6 +205,19 @@ __device__ R self_potential_piece(const V3<R> P[3], int e, int piece, const Quad
         part += Q.sw[k] * (ray_side(a, s2, c2, F02, R(phis + al2)) + ray_side(b, s1, c1, F01, R((kPi - phis) + al1)));
     }
     return span * part;
+}
+
+// the same, scale-invariant: evaluated on the triangle scaled by the power of two 2^k that
+// brings its longest edge into [0.5, 1) (angle_ref's threshold is absolute), the result scaled
+// back by 2^-3k (the potential of a pair of areas is a length cubed); exact at ordinary scales
+template <class R>
+__device__ R self_potential_piece(const V3<R> P[3], int e, int piece, const QuadTables &Q)
+{
+    const double lmax = fmax(fmax((double)value_of(norm(P[1] - P[0])), (double)value_of(norm(P[2] - P[1]))),
+                             (double)value_of(norm(P[0] - P[2])));
+    const double s = pow2_normaliser(lmax);
+    const V3<R> Ps[3] = {s * P[0], s * P[1], s * P[2]};
+    return (1.0 / (s * s * s)) * self_potential_piece_unit(Ps, e, piece, Q);
 }
 
 // int_K int_K 1/|x - y| (no 1/4pi) of the triangle (P0, P1, P2)

@@ -154,6 +154,36 @@ def ellipsoid(n_theta: int, n_phi: int, axes=(1.0, 1.0, 1.0), scale: float = 1.0
     return scale * v, np.asarray(faces, dtype=np.int32)
 
 
+def uneven_mesh_set(seed: int, count: int = 48, tri_min: int = 500, tri_max: int = 60000):
+    """A seeded set of independent closed meshes of uneven size and scale (a many-mesh batch
+    workload): ellipsoids with semi-axes uniform in [0.3, 3] (stretched icospheres), tori with R/r
+    uniform in [2, 6] and jittered icospheres, in turn; triangle counts log-uniform in
+    [tri_min, tri_max] (the nearest grid or subdivision level); scales uniform in [5e-4, 1e2].
+    Returns [(V, C, kind, scale)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        target = float(np.exp(rng.uniform(np.log(tri_min), np.log(tri_max))))
+        scale = float(rng.uniform(5e-4, 1e2))
+        kind = ("ellipsoid", "torus", "icosphere")[k % 3]
+        if kind == "ellipsoid":
+            # an icosphere stretched along its axes (a latitude-longitude grid would add pole fans
+            # of needle triangles)
+            axes = rng.uniform(0.3, 3.0, size=3)
+            sub = int(np.clip(round(np.log(target / 20.0) / np.log(4.0)), 1, 6))
+            V, C = icosphere(sub, 1.0)
+            V = scale * V * axes
+        elif kind == "torus":
+            ratio = rng.uniform(2.0, 6.0)
+            n_minor = max(4, int(round(np.sqrt(target / (2.0 * ratio)))))
+            V, C = torus(int(round(ratio * n_minor)), n_minor, 1.0, 1.0 / ratio, scale)
+        else:
+            sub = int(np.clip(round(np.log(target / 20.0) / np.log(4.0)), 1, 6))
+            V, C = jittered_icosphere(sub, 0.15, int(rng.integers(1 << 30)), scale)
+        out.append((V, C.astype(np.int32), kind, scale))
+    return out
+
+
 def orient_outward(v: np.ndarray, f: np.ndarray) -> np.ndarray:
     """Flip cells whose normal points towards the centroid of the surface (star-shaped meshes)."""
     c = v.mean(axis=0)

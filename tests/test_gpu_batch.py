@@ -115,3 +115,60 @@ def test_batch_rejects_bad_input(api):
     s = batch.add(m, 2, np.zeros((0, 2), np.int32))
     batch.run()
     assert batch.resultCount(s) == 0
+
+
+def test_uneven_mesh_set_and_scale_invariance(api):
+    """a small many-mesh batch of uneven sizes and scales against per-class runs, and the
+    scale invariance of relative error control: the same mesh at scale 1 and 5e-4 keeps the same
+    refinement levels, with J scaling as s^2 and P as s^3"""
+    from integrator2_gb300 import meshes, pairs as P
+    mset = meshes.uneven_mesh_set(7, 6, 300, 2000)
+    V0, C0, _, _ = mset[2]
+    mset.append((V0 / np.abs(V0).max(), C0, "unit", 1.0))
+    mset.append((5e-4 * V0 / np.abs(V0).max(), C0, "small", 5e-4))
+    batch, segs, held = None, [], []
+    for V, C, kind, scale in mset:
+        m = api.Mesh3D()
+        m.setGeometry(V, C)
+        m.prepareMesh(3.0)
+        it = _integrator(api, m, "relative")
+        held.append((m, it))
+        if batch is None:
+            batch = api.BatchEvaluator(it)
+        pl = P.build_pairs(V, C)
+        for cls in (0, 1, 2, 3):
+            segs.append((m, it, cls, pl.by_class(cls), batch.add(m, cls, pl.by_class(cls))))
+    batch.run()
+    for m, it, cls, pr, s in segs:
+        ev = api.EvaluatorJ3DK(m, it)
+        ev.runClass(cls, pr)
+        J1, l1 = ev.getResults(cls), ev.getLevels(cls)
+        J, lev = batch.getResults(s), batch.getLevels(s)
+        if cls == 3:
+            assert np.array_equal(J, J1)
+            continue
+        same = lev == l1
+        assert same.mean() > 0.99 and rel_rows(J[same], J1[same]).max() < 1e-5
+    # scale invariance (FP64 form; the mixed form's convergence decisions also depend on FP32
+    # rounding, which is not scale-free in the last bits): the last two meshes are the same
+    # geometry at scale 1 and 5e-4
+    res = []
+    for (V, C, kind, scale), (m, it) in zip(mset[-2:], held[-2:]):
+        it64 = api.NumericalIntegrator3D(m, api.qf3D13)
+        it64.setErrorControl(api.RELATIVE_ERROR_CONTROL, 1e-6, 5)
+        ev = api.EvaluatorJ3DK(m, it64)
+        pl = P.build_pairs(V, C)
+        out = {}
+        for cls in (0, 1, 2, 3):
+            ev.runClass(cls, pl.by_class(cls))
+            out[cls] = (ev.getResults(cls), ev.getPotentials(cls), ev.getLevels(cls))
+        res.append(out)
+    for cls in (0, 1, 2, 3):
+        (Ja, Pa, La), (Jb, Pb, Lb) = res[0][cls], res[1][cls]
+        same = La == Lb
+        assert same.mean() > 0.995, (cls, same.mean())
+        if cls == 3:
+            assert np.abs(Jb / 5e-4 ** 2 - Ja).max() <= 1e-12 * max(1.0, np.abs(Ja).max())
+        else:
+            assert rel_rows(Jb[same] / 5e-4 ** 2, Ja[same]).max() < 1e-9, cls
+        assert (np.abs(Pb[same] / 5e-4 ** 3 - Pa[same]) / np.abs(Pa[same])).max() < 1e-9, cls
