@@ -245,6 +245,10 @@ def run_batch(batch, flush, stream, steps, warmup):
     return sum(e0[s].elapsed_time(e1[s]) for s in range(steps))
 
 
+# kernels of one batched step, whatever the number of segments
+BATCH_LAUNCHES = 1 + 1 + 1 + (2 + 12) + 1 + 1 + 2
+
+
 def uneven_batch_section(args):
     """Many-mesh workload: 48 seeded closed meshes of uneven size (500-6,000 triangles,
     log-uniform) and scale (5e-4 .. 1e2): ellipsoids, tori, jittered spheres; all four pair classes
@@ -303,7 +307,7 @@ def uneven_batch_section(args):
     return {"workload": "48 meshes (ellipsoids, tori, jittered spheres), 500-6000 triangles, scales 5e-4..1e2, near < 3h, relative 1e-6",
             "triangles": int(sum(len(c) for _, c, _, _ in mset)), "pairs": int(total),
             "batched": {"value": total / (ms_batch * 1e-3), "ms_per_step": ms_batch, "cuda_graph": batch.usesGraph(),
-                        "shape": [int(x) for x in shape]},
+                        "shape": [int(x) for x in shape], "launches": f"{BATCH_LAUNCHES} for all {4 * len(mset)} segments"},
             "per_class": {"value": total / (ms_per_class * 1e-3), "ms_per_step": ms_per_class, "launches": "4 class chains x 48 meshes"}}
 
 
@@ -498,9 +502,12 @@ def gpu_arm(args):
     acc = {name: accuracy(V, C, lists, f["J"], f["P"], f["levels"]) for name, f in forms.items()}
     n_cpu, dt_cpu, thr = cpu_run(V, C, lists, args.cpu_fraction, args.tol)
     # kernels per step: adjacent classes run singular + tier 2 + adaptive potential (seed, 12
-    # depths, final); per-class chains add levels 0..5 + finalize per class, self pairs 1
+    # depths, final); per-class chains add levels 0..5 + finalize per class, self pairs 1; the
+    # mixed chains add the needle fix-up (collect + FP64 pass) per non-self class.  The batched
+    # form runs each stage once for all segments: reset, singular, tier 2, seed, 12 depths,
+    # final, self, the cooperative level kernel, collect, fix-up.
     pot_chain = 3 + 12
-    launches = {"fp64": 2 * (1 + pot_chain + 7) + 7 + 1, "mixed": 2 * (1 + pot_chain + 7) + 7 + 1, "batch": 2 * (1 + pot_chain) + 1 + 1}
+    launches = {"fp64": 2 * (1 + pot_chain + 7) + 7 + 1, "mixed": 2 * (1 + pot_chain + 7) + 7 + 1 + 3 * 2, "batch": BATCH_LAUNCHES}
     names4 = ("vertex", "edge", "near", "self")
     form_desc = {"batch": "mixed precision, batched: 4 class segments, one persistent cooperative level kernel, CUDA graph replay",
                  "mixed": "mixed precision, per-class kernel chains", "fp64": "plain FP64, per-class kernel chains"}

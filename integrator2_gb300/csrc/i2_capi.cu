@@ -707,6 +707,7 @@ struct i2_batch {
     i2::QuadTablesF Qf;
     std::vector<std::unique_ptr<BatchSegment>> segs;
     DevBuf<i2::BatchSeg> d_segs;
+    i2::BatchTotals totals;
     bool dirty = true;
     cudaStream_t stream = 0;
     int threads = 256, blocks_per_sm = 0, g_cap = 32, variant = 0, sms = 0;
@@ -729,7 +730,19 @@ void batch_prepare(i2_batch *b)
         I2_CHECK_CUDA(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev));
     }
     std::vector<i2::BatchSeg> hs;
-    for (auto &sp : b->segs) hs.push_back(i2::BatchSeg{sp->args, sp->cls});
+    b->totals = i2::BatchTotals{};
+    for (auto &sp : b->segs) {
+        hs.push_back(i2::BatchSeg{sp->args, sp->cls});
+        if (sp->n == 0) continue;
+        if (sp->cls == I2_SELF) b->totals.self_pairs += sp->n;
+        else {
+            if (sp->cls != I2_NOT_NEIGHBORS) {
+                b->totals.adjacent_pairs += sp->n;
+                b->totals.hard_lists = b->totals.hard_lists || sp->args.hard_list != nullptr;
+            }
+            if (sp->args.act_a) b->totals.fixup_pairs += sp->n;
+        }
+    }
     b->d_segs.reserve(std::max<size_t>(hs.size(), 1));
     if (!hs.empty()) I2_CHECK_CUDA(cudaMemcpy(b->d_segs.ptr, hs.data(), hs.size() * sizeof(i2::BatchSeg), cudaMemcpyHostToDevice));
     if (b->graph) {
@@ -744,18 +757,15 @@ void batch_prepare(i2_batch *b)
 void batch_enqueue(i2_batch *b, cudaStream_t s, int threads, int bps, int gcap, int variant)
 {
     const int persistent = std::max(1, b->sms) * 8;
-    for (auto &sp : b->segs) {
-        if (sp->n == 0) continue;
-        I2_CHECK_CUDA(cudaMemsetAsync(sp->cnt.ptr, 0, 16 * sizeof(int), s));
-        I2_CHECK_CUDA(cudaMemsetAsync(sp->maxlev.ptr, 0, sizeof(int), s));
-        i2::launch_batch_prelude(sp->args, sp->cls, b->Q, b->Qf, b->cfg, persistent, s);
-    }
+    const int nseg = (int)b->segs.size();
+    if (nseg == 0) return;
+    i2::launch_batch_prelude(b->d_segs.ptr, nseg, b->totals, b->Q, b->Qf, b->cfg, persistent, s);
     const int maxb = i2::batch_max_blocks_per_sm(threads, variant);
     I2_REQUIRE(maxb > 0, I2_ERR_CUDA, "batch kernel cannot be resident with this block size");
     const int blocks = std::max(1, b->sms) * std::max(1, std::min(bps > 0 ? bps : maxb, maxb));
-    I2_CHECK_CUDA(i2::launch_batch_levels(b->d_segs.ptr, (int)b->segs.size(), b->Qf, b->cfg, blocks, threads, gcap, variant, s));
-    for (auto &sp : b->segs)
-        if (sp->n > 0 && sp->cls != I2_SELF) i2::launch_fp64_fixup(sp->cls, sp->args, b->Q, b->cfg, persistent, s);
+    I2_CHECK_CUDA(i2::launch_batch_levels(b->d_segs.ptr, nseg, b->Qf, b->cfg, blocks, threads, gcap, variant, s));
+    i2::launch_batch_fixup(b->d_segs.ptr, nseg, b->totals, b->Q, b->cfg, persistent, s);
+    I2_CHECK_CUDA(cudaGetLastError());
 }
 
 } // namespace

@@ -85,8 +85,23 @@ struct BatchSeg {
 int batch_max_blocks_per_sm(int threads, int variant);
 cudaError_t launch_batch_levels(const BatchSeg *segs, int nseg, const QuadTablesF &Qf, const RunConfig &cfg, int blocks,
                                 int threads, int G_cap, int variant, cudaStream_t s);
-void launch_batch_prelude(const ClassArgs &A, int cls, const QuadTables &Q, const QuadTablesF &Qf, const RunConfig &cfg,
-                          int persistent_blocks, cudaStream_t s);
+// sizes the host knows about a batch (launch shapes of the batched stages)
+struct BatchTotals {
+    long long adjacent_pairs = 0;  // pairs of common-edge and common-vertex segments
+    long long self_pairs = 0;
+    long long fixup_pairs = 0;     // pairs the FP64 fix-up screens (segments with an active list)
+    bool hard_lists = false;       // some adjacent segment has the potential's tier lists
+};
+// every segment's counter reset, tier 1 with the singular parts, tiers 2 / 2b, the adaptive
+// potential and the self pairs: one launch per stage for the whole batch
+void launch_batch_prelude(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTables &Q, const QuadTablesF &Qf,
+                          const RunConfig &cfg, int persistent_blocks, cudaStream_t s);
+// the adaptive potential of every segment's hard pairs (seed, depths, final sums)
+void launch_batch_pot_chain(const BatchSeg *segs, int nseg, const QuadTables &Q, double tol, int persistent_blocks, cudaStream_t s);
+void launch_batch_self(const BatchSeg *segs, int nseg, long long self_pairs, const QuadTables &Q, const RunConfig &cfg, cudaStream_t s);
+// the FP64 fix-up of needle pairs after the level sweep, for every segment
+void launch_batch_fixup(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTables &Q, const RunConfig &cfg,
+                        int persistent_blocks, cudaStream_t s);
 // adjoint: dL/dV += gJ . dJ/dV + gP dP/dV over the pairs of one class (fp32: FP32 dual numbers)
 void launch_adjoint(int cls, bool fp32, const int2 *pairs, int n, const int3 *cells, const double *V, const int *stop,
                     const int *maxlev, const RunConfig &cfg, double tier_tol, double top_tol, const double *gJ, const double *gP, double *gradV,

@@ -10,6 +10,7 @@
 //                              it also runs the convergence test and appends unconverged pairs
 //                              to the next level's active list (device-side counter)
 //   k_finalize<CLS>            kept level, singular part, J = (Theta n_j + Psi x n_j)/4pi
+#include "i2_batch.cuh"
 #include "i2_engine.h"
 #include "i2_finalize.cuh"
 
@@ -358,83 +359,104 @@ __device__ void pot_children_warp(const Tri &T, const int cc[4], const PotPairCt
 // as overflows.
 __device__ __forceinline__ int pot_seeded(const ClassArgs &A) { return min(*A.hard_cnt, A.pot_qcap / 4); }
 
+// the seed's bookkeeping, once per segment before any depth kernel runs: depth 1 holds the
+// roots' children, the deeper lists start empty
+__device__ __forceinline__ void pot_seed_init(const ClassArgs &A)
+{
+    const int count = pot_seeded(A);
+    A.pot_qcnt[1] = 4 * count;
+    for (int d = 2; d <= kHardMaxDepth + 1; ++d) A.pot_qcnt[d] = 0;
+    if (*A.hard_cnt > count) atomicAdd(A.hard_overflow, *A.hard_cnt - count);
+}
+
+template <int CLS>
+__device__ __forceinline__ void pot_seed_item(const ClassArgs &A, const QuadTables &Q, double tol, int h, int lane)
+{
+    const int t = A.hard_list[h];
+    const PotPairCtx c = pot_pair_ctx<CLS>(A, t, tol);
+    const int3 ci = A.cells[A.pairs[t].x], cj = A.cells[A.pairs[t].y];
+    const int ia[3] = {ci.x, ci.y, ci.z};
+    bool shared[3];
+    for (int k = 0; k < 3; ++k) shared[k] = (ia[k] == cj.x || ia[k] == cj.y || ia[k] == cj.z);
+    // the root's children 0, 1, 2 hold K_i's slots b, c, a in their slot 1
+    int cc[4];
+    for (int k = 0; k < 4; ++k) cc[k] = k == 3 ? -1 : (shared[k == 0 ? 1 : (k == 1 ? 2 : 0)] ? 1 : -1);
+    double v[4];
+    pot_children_warp<CLS>(c.Ti, cc, c, Q, lane, v);
+    if (lane < 4) A.pot_q_a[4 * (long long)h + lane] = PotCellItem{(unsigned long long)lane, v[lane], h, cc[lane]};
+    if (lane == 0) A.pot_fx[h] = 0;
+}
+
 template <int CLS>
 __global__ void __launch_bounds__(128) k_pot_seed(ClassArgs A, QuadTables Q, double tol)
 {
     const int count = pot_seeded(A);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        // depth 1 holds the roots' children; the deeper lists start empty (the depth kernels
-        // run after this one on the same stream)
-        A.pot_qcnt[1] = 4 * count;
-        for (int d = 2; d <= kHardMaxDepth + 1; ++d) A.pot_qcnt[d] = 0;
-        if (*A.hard_cnt > count) atomicAdd(A.hard_overflow, *A.hard_cnt - count);
-    }
+    // the depth kernels run after this one on the same stream
+    if (blockIdx.x == 0 && threadIdx.x == 0) pot_seed_init(A);
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < count; h += nwarps) {
-        const int t = A.hard_list[h];
-        const PotPairCtx c = pot_pair_ctx<CLS>(A, t, tol);
-        const int3 ci = A.cells[A.pairs[t].x], cj = A.cells[A.pairs[t].y];
-        const int ia[3] = {ci.x, ci.y, ci.z};
-        bool shared[3];
-        for (int k = 0; k < 3; ++k) shared[k] = (ia[k] == cj.x || ia[k] == cj.y || ia[k] == cj.z);
-        // the root's children 0, 1, 2 hold K_i's slots b, c, a in their slot 1
-        int cc[4];
-        for (int k = 0; k < 4; ++k) cc[k] = k == 3 ? -1 : (shared[k == 0 ? 1 : (k == 1 ? 2 : 0)] ? 1 : -1);
-        double v[4];
-        pot_children_warp<CLS>(c.Ti, cc, c, Q, lane, v);
-        if (lane < 4) A.pot_q_a[4 * (long long)h + lane] = PotCellItem{(unsigned long long)lane, v[lane], h, cc[lane]};
-        if (lane == 0) A.pot_fx[h] = 0;
-    }
+    for (int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < count; h += nwarps) pot_seed_item<CLS>(A, Q, tol, h, lane);
 }
+
+// one cell of one depth, by one warp
+template <int CLS>
+__device__ __forceinline__ void pot_depth_item(const ClassArgs &A, const QuadTables &Q, double tol, int depth,
+                                               const PotCellItem *__restrict__ in, PotCellItem *__restrict__ out, int idx, int lane)
+{
+    const PotCellItem it = in[idx];
+    if (it.h < 0) return;
+    const int t = A.hard_list[it.h];
+    const PotPairCtx c = pot_pair_ctx<CLS>(A, t, tol);
+    const Tri T = subcell(c.Ti, depth, (int)it.path);
+    int cc[4];
+    for (int k = 0; k < 4; ++k) cc[k] = child_corner(it.corner, k);
+    double v[4];
+    pot_children_warp<CLS>(T, cc, c, Q, lane, v);
+    if (lane != 0) return;
+    const double sum = v[0] + v[1] + v[2] + v[3];
+    bool accept = fabs(sum - it.val) <= ldexp(c.tol_abs, -depth) || depth >= kHardMaxDepth;
+    if (!accept) {
+        const int pos = atomicAdd(&A.pot_qcnt[depth + 1], 4);
+        if (pos + 4 <= A.pot_qcap) {
+            for (int k = 0; k < 4; ++k) out[pos + k] = PotCellItem{(it.path << 2) | (unsigned long long)k, v[k], it.h, cc[k]};
+        } else {
+            // list full: keep this cell's sum (counted as an overflow) and blank the slots it
+            // was given below the capacity, so the next depth skips them
+            for (int k = pos; k < A.pot_qcap && k < pos + 4; ++k) out[k] = PotCellItem{0ull, 0.0, -1, -1};
+            atomicAdd(A.hard_overflow, 1);
+            accept = true;
+        }
+    }
+    if (accept) atomicAdd(reinterpret_cast<unsigned long long *>(&A.pot_fx[it.h]), (unsigned long long)llrint(sum * c.scale));
+}
+
+__device__ __forceinline__ int pot_depth_count(const ClassArgs &A, int depth) { return min(A.pot_qcnt[depth], A.pot_qcap); }
 
 // one depth: one warp per cell
 template <int CLS>
 __global__ void __launch_bounds__(128) k_pot_depth(ClassArgs A, QuadTables Q, double tol, int depth, const PotCellItem *__restrict__ in,
                                                    PotCellItem *__restrict__ out)
 {
-    const int count = min(A.pot_qcnt[depth], A.pot_qcap);
+    const int count = pot_depth_count(A, depth);
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < count; idx += nwarps) {
-        const PotCellItem it = in[idx];
-        if (it.h < 0) continue;
-        const int t = A.hard_list[it.h];
-        const PotPairCtx c = pot_pair_ctx<CLS>(A, t, tol);
-        const Tri T = subcell(c.Ti, depth, (int)it.path);
-        int cc[4];
-        for (int k = 0; k < 4; ++k) cc[k] = child_corner(it.corner, k);
-        double v[4];
-        pot_children_warp<CLS>(T, cc, c, Q, lane, v);
-        if (lane != 0) continue;
-        const double sum = v[0] + v[1] + v[2] + v[3];
-        bool accept = fabs(sum - it.val) <= ldexp(c.tol_abs, -depth) || depth >= kHardMaxDepth;
-        if (!accept) {
-            const int pos = atomicAdd(&A.pot_qcnt[depth + 1], 4);
-            if (pos + 4 <= A.pot_qcap) {
-                for (int k = 0; k < 4; ++k)
-                    out[pos + k] = PotCellItem{(it.path << 2) | (unsigned long long)k, v[k], it.h, cc[k]};
-            } else {
-                // list full: keep this cell's sum (counted as an overflow) and blank the slots it
-                // was given below the capacity, so the next depth skips them
-                for (int k = pos; k < A.pot_qcap && k < pos + 4; ++k) out[k] = PotCellItem{0ull, 0.0, -1, -1};
-                atomicAdd(A.hard_overflow, 1);
-                accept = true;
-            }
-        }
-        if (accept) atomicAdd(reinterpret_cast<unsigned long long *>(&A.pot_fx[it.h]), (unsigned long long)llrint(sum * c.scale));
-    }
+    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < count; idx += nwarps)
+        pot_depth_item<CLS>(A, Q, tol, depth, in, out, idx, lane);
+}
+
+template <int CLS>
+__device__ __forceinline__ void pot_final_item(const ClassArgs &A, double tol, int h)
+{
+    const int t = A.hard_list[h];
+    const PotPairCtx c = pot_pair_ctx<CLS>(A, t, tol);
+    A.padj[t] = kInv4Pi * ((double)A.pot_fx[h] / c.scale + c.sig_int);
 }
 
 template <int CLS>
 __global__ void __launch_bounds__(128) k_pot_final(ClassArgs A, double tol)
 {
     const int count = pot_seeded(A);
-    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < count; h += gridDim.x * blockDim.x) {
-        const int t = A.hard_list[h];
-        const PotPairCtx c = pot_pair_ctx<CLS>(A, t, tol);
-        A.padj[t] = kInv4Pi * ((double)A.pot_fx[h] / c.scale + c.sig_int);
-    }
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < count; h += gridDim.x * blockDim.x) pot_final_item<CLS>(A, tol, h);
 }
 
 template <int CLS>
@@ -450,21 +472,20 @@ static void pot_adaptive_chain(const ClassArgs &A, const QuadTables &Q, double t
 // eight lanes per pair: lanes 0..5 take one (edge, piece) of the self-pair rule each, the group
 // sums them (an edge's pieces are integrated independently, so the pair's 6 x nself point
 // evaluations run in parallel)
-__global__ void __launch_bounds__(128) k_self(ClassArgs A, QuadTables Q, int self_sign)
+// item g (0..7) of self pair t; the eight items of a pair sit in eight consecutive lanes
+// (lanes 8k .. 8k+7) that call this together
+__device__ __forceinline__ void self_item(const ClassArgs &A, const QuadTables &Q, int self_sign, long long t, int g)
 {
-    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int g = threadIdx.x & 7;
-    const long long t = gid >> 3;
-    const bool valid = t < A.n;
-    const int i = valid ? A.pairs[t].x : 0;
+    const int i = A.pairs[t].x;
     const PanelJ K = load_panel(A.panels, i);
     double part = 0.0;
-    if (valid && g < 6) {
+    if (g < 6) {
         const d3 P[3] = {K.A, K.B, K.C};
         part = self_potential_piece(P, g >> 1, g & 1, Q);
     }
-    for (int off = 1; off < 8; off <<= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
-    if (!valid || g != 0) return;
+    const unsigned group = 0xffu << (threadIdx.x & 24);
+    for (int off = 1; off < 8; off <<= 1) part += __shfl_xor_sync(group, part, off, 8);
+    if (g != 0) return;
     const double th = self_sign == 0 ? 0.0 : (self_sign > 0 ? kTwoPi : -kTwoPi) * K.S;
     const d3 J = kInv4Pi * (th * K.n);
     double *raw = A.raw4 + 4 * t;
@@ -472,6 +493,83 @@ __global__ void __launch_bounds__(128) k_self(ClassArgs A, QuadTables Q, int sel
     double *Jo = A.J3 + 3 * t;
     Jo[0] = J.x; Jo[1] = J.y; Jo[2] = J.z;
     A.P[t] = kInv4Pi * part;
+}
+
+__global__ void __launch_bounds__(128) k_self(ClassArgs A, QuadTables Q, int self_sign)
+{
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if ((gid >> 3) < A.n) self_item(A, Q, self_sign, gid >> 3, threadIdx.x & 7);
+}
+
+// ------------------------------------------------------------------ batched stages
+// The stages above, each as one launch over every segment of a batch (i2_batch.cuh): the
+// adaptive potential's seed, depths and final sums, and the self pairs.  Segments are walked in
+// chunks of kBatchSegChunk; a chunk's prefix sums live in dynamic shared memory.
+__global__ void __launch_bounds__(128) k_batch_pot_seed(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q, double tol)
+{
+    extern __shared__ long long prefix[];
+    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
+        return seg_adjacent(S) && S.A.hard_list ? pot_seeded(S.A) : 0;
+    });
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid < nseg && seg_adjacent(segs[gid]) && segs[gid].A.hard_list) pot_seed_init(segs[gid].A);
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long g = gid >> 5; g < total; g += nwarps) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        const int h = (int)(g - prefix[sg]);
+        if (S.cls == kEdge) pot_seed_item<kEdge>(S.A, Q, tol, h, lane);
+        else pot_seed_item<kVertex>(S.A, Q, tol, h, lane);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_batch_pot_depth(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q, double tol, int depth)
+{
+    extern __shared__ long long prefix[];
+    const long long total = seg_prefix(segs, nseg, prefix, [depth](const BatchSeg &S) -> long long {
+        return seg_adjacent(S) && S.A.hard_list ? pot_depth_count(S.A, depth) : 0;
+    });
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < total; g += nwarps) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        const int idx = (int)(g - prefix[sg]);
+        const PotCellItem *in = depth % 2 ? S.A.pot_q_a : S.A.pot_q_b;
+        PotCellItem *out = depth % 2 ? S.A.pot_q_b : S.A.pot_q_a;
+        if (S.cls == kEdge) pot_depth_item<kEdge>(S.A, Q, tol, depth, in, out, idx, lane);
+        else pot_depth_item<kVertex>(S.A, Q, tol, depth, in, out, idx, lane);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_batch_pot_final(const BatchSeg *__restrict__ segs, int nseg, double tol)
+{
+    extern __shared__ long long prefix[];
+    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
+        return seg_adjacent(S) && S.A.hard_list ? pot_seeded(S.A) : 0;
+    });
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        if (S.cls == kEdge) pot_final_item<kEdge>(S.A, tol, (int)(g - prefix[sg]));
+        else pot_final_item<kVertex>(S.A, tol, (int)(g - prefix[sg]));
+    }
+}
+
+__global__ void __launch_bounds__(128) k_batch_self(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q, int self_sign)
+{
+    extern __shared__ long long prefix[];
+    // eight items per pair; every segment's item count is a multiple of 8, and so is the grid's
+    // thread count, so a pair's items land in one aligned group of eight lanes
+    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
+        return S.cls == kSelf && S.A.n > 0 ? 8LL * S.A.n : 0;
+    });
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+        const int sg = seg_find(prefix, nseg, g);
+        const long long loc = g - prefix[sg];
+        self_item(segs[sg].A, Q, self_sign, loc >> 3, (int)(loc & 7));
+    }
 }
 
 // ------------------------------------------------------------------ finalisation
@@ -533,6 +631,36 @@ void launch_pot_hard(int cls, const ClassArgs &A, const QuadTables &Q, const Run
 {
     if (cls == kEdge) pot_adaptive_chain<kEdge>(A, Q, cfg.hard_tol, persistent_blocks, s);
     else pot_adaptive_chain<kVertex>(A, Q, cfg.hard_tol, persistent_blocks, s);
+}
+
+static size_t seg_smem(int nseg) { return (size_t)(nseg + 1) * sizeof(long long); }
+
+void launch_batch_pot_chain(const BatchSeg *segs, int nseg, const QuadTables &Q, double tol, int persistent_blocks, cudaStream_t s)
+{
+    for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
+        const int nc = std::min(kBatchSegChunk, nseg - c0);
+        // the seed initialises every segment of the chunk: at least one thread per segment
+        k_batch_pot_seed<<<std::max(persistent_blocks, blocks_for(nc, 128)), 128, seg_smem(nc), s>>>(segs + c0, nc, Q, tol);
+    }
+    for (int d = 1; d <= kHardMaxDepth; ++d)
+        for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
+            const int nc = std::min(kBatchSegChunk, nseg - c0);
+            k_batch_pot_depth<<<persistent_blocks, 128, seg_smem(nc), s>>>(segs + c0, nc, Q, tol, d);
+        }
+    for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
+        const int nc = std::min(kBatchSegChunk, nseg - c0);
+        k_batch_pot_final<<<persistent_blocks, 128, seg_smem(nc), s>>>(segs + c0, nc, tol);
+    }
+}
+
+void launch_batch_self(const BatchSeg *segs, int nseg, long long self_pairs, const QuadTables &Q, const RunConfig &cfg, cudaStream_t s)
+{
+    if (self_pairs <= 0) return;
+    const int blocks = std::max(1, std::min(blocks_for(8 * self_pairs, 128), 1 << 16));
+    for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
+        const int nc = std::min(kBatchSegChunk, nseg - c0);
+        k_batch_self<<<blocks, 128, seg_smem(nc), s>>>(segs + c0, nc, Q, cfg.self_sign);
+    }
 }
 
 void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s)

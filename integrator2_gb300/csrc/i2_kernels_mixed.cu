@@ -9,6 +9,7 @@
 // The kernel chain per class mirrors the FP64 form (i2_kernels_fp64.cu) and shares its
 // finalisation, self and adaptive-potential kernels.
 #include "i2_device_f32.cuh"
+#include "i2_batch.cuh"
 #include "i2_engine.h"
 #include "i2_finalize.cuh"
 
@@ -383,10 +384,8 @@ __device__ __forceinline__ void edge_sigma_setup(const ClassArgs &A, int2 pr, in
 }
 
 template <int CLS>
-__global__ void __launch_bounds__(128) k_singular_mixed(ClassArgs A, QuadTablesF Qf)
+__device__ __forceinline__ void singular_mixed_item(const ClassArgs &A, const QuadTablesF &Qf, long long t)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= A.n) return;
     const int2 pr = A.pairs[t];
     const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
     const PanelJ Kd = load_panel(A.panels, pr.y);
@@ -434,13 +433,20 @@ __global__ void __launch_bounds__(128) k_singular_mixed(ClassArgs A, QuadTablesF
     if (A.hard_list) {
         const double c10 = 0.98480775301220806;
         if (dot(ni, Kd.n) < 0.5 || A.panels[pr.x].v[2].w > c10 || A.panels[pr.y].v[2].w > c10) {
-            A.hard_list[atomicAdd(A.hard_cnt, 1)] = t;
+            A.hard_list[atomicAdd(A.hard_cnt, 1)] = (int)t;
         } else {
             const float pl = duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, K, F, p1v, m_in, c, h, Qf.lo_u, Qf.lo_uw, Qf.lo_nu, Qf.lo_v,
                                                 Qf.lo_vw, Qf.lo_nv);
-            if (fabs(pmd - ((double)pl + sig)) > A.tier_tol * fabs(pmd)) A.tier2_list[atomicAdd(A.tier2_cnt, 1)] = t;
+            if (fabs(pmd - ((double)pl + sig)) > A.tier_tol * fabs(pmd)) A.tier2_list[atomicAdd(A.tier2_cnt, 1)] = (int)t;
         }
     }
+}
+
+template <int CLS>
+__global__ void __launch_bounds__(128) k_singular_mixed(ClassArgs A, QuadTablesF Qf)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < A.n) singular_mixed_item<CLS>(A, Qf, t);
 }
 
 __device__ __forceinline__ float warp_sum_f(float x)
@@ -453,55 +459,59 @@ __device__ __forceinline__ float warp_sum_f(float x)
 // lanes share each rule's points).  Tier 2b is FP64 because the FP32 rules can share a bias of a
 // few 1e-6 (a small, flat K_j beside a large K_i), and two biased rules agree with each other.
 template <int CLS>
+__device__ __forceinline__ void tier2_mixed_item(const ClassArgs &A, const QuadTablesF &Qf, const QuadTables &Q, int h, int lane)
+{
+    const int t = A.tier2_list[h];
+    const int2 pr = A.pairs[t];
+    const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
+    int si, sj;
+    if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
+    else shifts_vertex(ci, cj, si, sj);
+    const PanelJf Kf = load_panel_f(A.panels_f, pr.y);
+    const FarCtxF Ff{crossf(Kf.ta, Kf.n), crossf(Kf.tb, Kf.n), crossf(Kf.tc, Kf.n)};
+    const double Si = A.panels[pr.x].v[0].w;
+    f3 m_in = f3{0, 0, 0};
+    float c = 0.0f, hh = 1.0f;
+    double sig = 0.0;
+    const int p1v = (sj + 1) % 3;
+    if (CLS == kEdge) edge_sigma_setup(A, pr, si, sj, Kf, Si, m_in, c, hh, sig);
+    const double ph = (double)warp_sum_f(duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, Kf, Ff, p1v, m_in, c, hh, Qf.hi_u, Qf.hi_uw,
+                                                            Qf.hi_nu, Qf.hi_v, Qf.hi_vw, Qf.hi_nv, lane, 32)) + sig;
+    const double pm = A.padj[t] * (4.0 * kPi);
+    if (fabs(ph - pm) <= A.tier_tol * fabs(ph)) {
+        if (lane == 0) A.padj[t] = kInv4Pi * ph;
+        return;
+    }
+    // tier 2b in FP64: 24 x 24 against 16 x 16
+    const PanelJ K = load_panel(A.panels, pr.y);
+    const Tri Ti = rotate(load_tri(A.panels, pr.x), si), Tj = rotate(Tri{K.A, K.B, K.C}, sj);
+    const FarCtx F = make_far_ctx(K);
+    PotEdge pe;
+    const double sg64 = CLS == kEdge ? make_pot_edge(Ti, Tj, K, Si, pe) : 0.0;
+    double ph64 = duffy_partial<CLS>(Ti, K, F, pe, Q.hi_u, Q.hi_uw, Q.hi_nu, Q.hi_v, Q.hi_vw, Q.hi_nv, lane, 32);
+    double pt64 = duffy_partial<CLS>(Ti, K, F, pe, Q.top_u, Q.top_uw, Q.top_nu, Q.top_v, Q.top_vw, Q.top_nv, lane, 32);
+    for (int off = 16; off > 0; off >>= 1) {
+        ph64 += __shfl_xor_sync(0xffffffffu, ph64, off);
+        pt64 += __shfl_xor_sync(0xffffffffu, pt64, off);
+    }
+    ph64 += sg64;
+    pt64 += sg64;
+    if (lane != 0) return;
+    if (fabs(pt64 - ph64) <= A.top_tol * fabs(pt64)) {
+        A.padj[t] = kInv4Pi * pt64;
+    } else {
+        A.padj[t] = kInv4Pi * ph64;  // the adaptive rule's tolerance base
+        A.hard_list[atomicAdd(A.hard_cnt, 1)] = t;
+    }
+}
+
+template <int CLS>
 __global__ void __launch_bounds__(128) k_pot_tier2_mixed(ClassArgs A, QuadTablesF Qf, QuadTables Q)
 {
     const int count = *A.tier2_cnt;
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < count; h += nwarps) {
-        const int t = A.tier2_list[h];
-        const int2 pr = A.pairs[t];
-        const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
-        int si, sj;
-        if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
-        else shifts_vertex(ci, cj, si, sj);
-        const PanelJf Kf = load_panel_f(A.panels_f, pr.y);
-        const FarCtxF Ff{crossf(Kf.ta, Kf.n), crossf(Kf.tb, Kf.n), crossf(Kf.tc, Kf.n)};
-        const double Si = A.panels[pr.x].v[0].w;
-        f3 m_in = f3{0, 0, 0};
-        float c = 0.0f, hh = 1.0f;
-        double sig = 0.0;
-        const int p1v = (sj + 1) % 3;
-        if (CLS == kEdge) edge_sigma_setup(A, pr, si, sj, Kf, Si, m_in, c, hh, sig);
-        const double ph = (double)warp_sum_f(duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, Kf, Ff, p1v, m_in, c, hh, Qf.hi_u, Qf.hi_uw,
-                                                                Qf.hi_nu, Qf.hi_v, Qf.hi_vw, Qf.hi_nv, lane, 32)) + sig;
-        const double pm = A.padj[t] * (4.0 * kPi);
-        if (fabs(ph - pm) <= A.tier_tol * fabs(ph)) {
-            if (lane == 0) A.padj[t] = kInv4Pi * ph;
-            continue;
-        }
-        // tier 2b in FP64: 24 x 24 against 16 x 16
-        const PanelJ K = load_panel(A.panels, pr.y);
-        const Tri Ti = rotate(load_tri(A.panels, pr.x), si), Tj = rotate(Tri{K.A, K.B, K.C}, sj);
-        const FarCtx F = make_far_ctx(K);
-        PotEdge pe;
-        const double sg64 = CLS == kEdge ? make_pot_edge(Ti, Tj, K, Si, pe) : 0.0;
-        double ph64 = duffy_partial<CLS>(Ti, K, F, pe, Q.hi_u, Q.hi_uw, Q.hi_nu, Q.hi_v, Q.hi_vw, Q.hi_nv, lane, 32);
-        double pt64 = duffy_partial<CLS>(Ti, K, F, pe, Q.top_u, Q.top_uw, Q.top_nu, Q.top_v, Q.top_vw, Q.top_nv, lane, 32);
-        for (int off = 16; off > 0; off >>= 1) {
-            ph64 += __shfl_xor_sync(0xffffffffu, ph64, off);
-            pt64 += __shfl_xor_sync(0xffffffffu, pt64, off);
-        }
-        ph64 += sg64;
-        pt64 += sg64;
-        if (lane != 0) continue;
-        if (fabs(pt64 - ph64) <= A.top_tol * fabs(pt64)) {
-            A.padj[t] = kInv4Pi * pt64;
-        } else {
-            A.padj[t] = kInv4Pi * ph64;  // the adaptive rule's tolerance base
-            A.hard_list[atomicAdd(A.hard_cnt, 1)] = t;
-        }
-    }
+    for (int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < count; h += nwarps) tier2_mixed_item<CLS>(A, Qf, Q, h, lane);
 }
 
 // ------------------------------------------------------------------ FP64 fix-up of ill-conditioned pairs
@@ -566,13 +576,91 @@ __device__ acc5 fixup_level_sum(const FixupPair<CLS> &p, const QuadTables &Q, in
 
 // the pairs that hold a needle cell, gathered into list[0 .. *count) (the class's active-list
 // buffer, free once the level chain has finished)
-__global__ void __launch_bounds__(256) k_fixup_collect(ClassArgs A, int *list, int *count)
+__device__ __forceinline__ void fixup_collect_item(const ClassArgs &A, int *list, int *count, long long t)
 {
     const double c3 = 0.99862953475457387;  // cos 3 degrees
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < A.n; t += (long long)gridDim.x * blockDim.x) {
-        const int2 pr = A.pairs[t];
-        if (A.panels[pr.x].v[2].w > c3 || A.panels[pr.y].v[2].w > c3) list[atomicAdd(count, 1)] = (int)t;
+    const int2 pr = A.pairs[t];
+    if (A.panels[pr.x].v[2].w > c3 || A.panels[pr.y].v[2].w > c3) list[atomicAdd(count, 1)] = (int)t;
+}
+
+__global__ void __launch_bounds__(256) k_fixup_collect(ClassArgs A, int *list, int *count)
+{
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < A.n; t += (long long)gridDim.x * blockDim.x)
+        fixup_collect_item(A, list, count, t);
+}
+
+// pair t, by the whole block (red: 5 doubles per warp of shared memory)
+template <int CLS>
+__device__ void fp64_fixup_item(const ClassArgs &A, const QuadTables &Q, int mode, int fixed_level, double tol, int kmax, int t,
+                                double *red)
+{
+    const int2 pr = A.pairs[t];
+    const double4_32a ni4 = A.panels[pr.x].v[3], nj4 = A.panels[pr.y].v[3];
+    const d3 ni = mk(ni4.x, ni4.y, ni4.z), nj = mk(nj4.x, nj4.y, nj4.z);
+    FixupPair<CLS> p;
+    p.K = load_panel(A.panels, pr.y);
+    p.Ti = load_tri(A.panels, pr.x);
+    p.Si = A.panels[pr.x].v[0].w;
+    if (CLS == kFar) p.F = make_far_ctx(p.K);
+    else {
+        const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
+        int si, sj;
+        if (CLS == kEdge) {
+            shifts_edge(ci, cj, si, sj);
+            p.E = make_edge_ctx(p.K, sj);
+        } else {
+            shifts_vertex(ci, cj, si, sj);
+            p.Vx = make_vertex_ctx(p.K, sj, ni, p.Si);
+        }
     }
+    d3 spsi = mk(0, 0, 0);
+    double sth = 0.0;
+    if (CLS != kFar) {
+        const double *sg = A.sing + 4 * (long long)t;
+        spsi = mk(sg[0], sg[1], sg[2]);
+        sth = sg[3];
+    }
+    acc5 acc;
+    int kept;
+    if (mode == kAdaptiveRelative) {
+        // FP64 refinement with the relative criterion from level 0 (FP32 noise may have kept
+        // the mixed pass refining up to the last level); every thread holds the same sums,
+        // so the decision is uniform
+        acc = fixup_level_sum<CLS>(p, Q, 0, red);
+        kept = 0;
+        for (int L = 1; L <= kmax; ++L) {
+            const acc5 nxt = fixup_level_sum<CLS>(p, Q, L, red);
+            const d3 Jc = finalize_j(CLS, mk(nxt.px, nxt.py, nxt.pz) + spsi, nxt.th + sth, nj, p.Si);
+            const d3 dJ = kInv4Pi * ((nxt.th - acc.th) * nj + cross(mk(nxt.px - acc.px, nxt.py - acc.py, nxt.pz - acc.pz), nj));
+            bool unconv = norm(dJ) > tol * norm(Jc);
+            if (CLS == kFar) unconv = unconv || fabs(nxt.pot - acc.pot) > tol * fabs(nxt.pot);
+            acc = nxt;
+            kept = L;
+            if (!unconv) break;
+        }
+    } else {
+        kept = fixed_level;
+        if (mode != kFixed) {
+            const int L = A.stop[t];
+            kept = ((*A.maxlev - L) & 1) ? (L > 0 ? L - 1 : 0) : L;
+        }
+        acc = fixup_level_sum<CLS>(p, Q, kept, red);
+    }
+    if (threadIdx.x == 0) {
+        const d3 psi = mk(acc.px, acc.py, acc.pz) + spsi;
+        const double th = acc.th + sth;
+        const d3 J = finalize_j(CLS, psi, th, nj, p.Si);
+        double *raw = A.raw4 + 4 * (long long)t;
+        raw[0] = psi.x; raw[1] = psi.y; raw[2] = psi.z; raw[3] = th;
+        double *Jo = A.J3 + 3 * (long long)t;
+        Jo[0] = J.x; Jo[1] = J.y; Jo[2] = J.z;
+        if (CLS == kFar) A.P[t] = kInv4Pi * acc.pot;
+        if (mode == kAdaptiveRelative) {
+            A.stop[t] = kept;
+            if (A.level_out) A.level_out[t] = kept;
+        }
+    }
+    __syncthreads();
 }
 
 template <int CLS>
@@ -581,79 +669,8 @@ __global__ void __launch_bounds__(256) k_fp64_fixup(ClassArgs A, QuadTables Q, i
 {
     __shared__ double red[5 * 8];
     const int nbad = *count;
-    {
-        // one block per gathered pair (grid-stride), so that a few pairs at level 5 spread over the GPU
-        for (int q = blockIdx.x; q < nbad; q += gridDim.x) {
-            const int t = list[q];
-            const int2 pr = A.pairs[t];
-            const double4_32a ni4 = A.panels[pr.x].v[3], nj4 = A.panels[pr.y].v[3];
-            const d3 ni = mk(ni4.x, ni4.y, ni4.z), nj = mk(nj4.x, nj4.y, nj4.z);
-            FixupPair<CLS> p;
-            p.K = load_panel(A.panels, pr.y);
-            p.Ti = load_tri(A.panels, pr.x);
-            p.Si = A.panels[pr.x].v[0].w;
-            if (CLS == kFar) p.F = make_far_ctx(p.K);
-            else {
-                const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
-                int si, sj;
-                if (CLS == kEdge) {
-                    shifts_edge(ci, cj, si, sj);
-                    p.E = make_edge_ctx(p.K, sj);
-                } else {
-                    shifts_vertex(ci, cj, si, sj);
-                    p.Vx = make_vertex_ctx(p.K, sj, ni, p.Si);
-                }
-            }
-            d3 spsi = mk(0, 0, 0);
-            double sth = 0.0;
-            if (CLS != kFar) {
-                const double *sg = A.sing + 4 * (long long)t;
-                spsi = mk(sg[0], sg[1], sg[2]);
-                sth = sg[3];
-            }
-            acc5 acc;
-            int kept;
-            if (mode == kAdaptiveRelative) {
-                // FP64 refinement with the relative criterion from level 0 (FP32 noise may have kept
-                // the mixed pass refining up to the last level); every thread holds the same sums,
-                // so the decision is uniform
-                acc = fixup_level_sum<CLS>(p, Q, 0, red);
-                kept = 0;
-                for (int L = 1; L <= kmax; ++L) {
-                    const acc5 nxt = fixup_level_sum<CLS>(p, Q, L, red);
-                    const d3 Jc = finalize_j(CLS, mk(nxt.px, nxt.py, nxt.pz) + spsi, nxt.th + sth, nj, p.Si);
-                    const d3 dJ = kInv4Pi * ((nxt.th - acc.th) * nj + cross(mk(nxt.px - acc.px, nxt.py - acc.py, nxt.pz - acc.pz), nj));
-                    bool unconv = norm(dJ) > tol * norm(Jc);
-                    if (CLS == kFar) unconv = unconv || fabs(nxt.pot - acc.pot) > tol * fabs(nxt.pot);
-                    acc = nxt;
-                    kept = L;
-                    if (!unconv) break;
-                }
-            } else {
-                kept = fixed_level;
-                if (mode != kFixed) {
-                    const int L = A.stop[t];
-                    kept = ((*A.maxlev - L) & 1) ? (L > 0 ? L - 1 : 0) : L;
-                }
-                acc = fixup_level_sum<CLS>(p, Q, kept, red);
-            }
-            if (threadIdx.x == 0) {
-                const d3 psi = mk(acc.px, acc.py, acc.pz) + spsi;
-                const double th = acc.th + sth;
-                const d3 J = finalize_j(CLS, psi, th, nj, p.Si);
-                double *raw = A.raw4 + 4 * (long long)t;
-                raw[0] = psi.x; raw[1] = psi.y; raw[2] = psi.z; raw[3] = th;
-                double *Jo = A.J3 + 3 * (long long)t;
-                Jo[0] = J.x; Jo[1] = J.y; Jo[2] = J.z;
-                if (CLS == kFar) A.P[t] = kInv4Pi * acc.pot;
-                if (mode == kAdaptiveRelative) {
-                    A.stop[t] = kept;
-                    if (A.level_out) A.level_out[t] = kept;
-                }
-            }
-            __syncthreads();
-        }
-    }
+    // one block per gathered pair (grid-stride), so that a few pairs at level 5 spread over the GPU
+    for (int q = blockIdx.x; q < nbad; q += gridDim.x) fp64_fixup_item<CLS>(A, Q, mode, fixed_level, tol, kmax, list[q], red);
 }
 
 void launch_fp64_fixup(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s)
@@ -796,26 +813,113 @@ cudaError_t launch_batch_levels(const BatchSeg *segs, int nseg, const QuadTables
     return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(threads), args, 0, s);
 }
 
-// the per-segment work that precedes the level sweep: singular parts, potential tiers, self pairs
-void launch_batch_prelude(const ClassArgs &A, int cls, const QuadTables &Q, const QuadTablesF &Qf, const RunConfig &cfg,
-                          int persistent_blocks, cudaStream_t s)
+// ------------------------------------------------------------------ batched stages
+// The stages that precede and follow the level sweep, each as one launch over every segment of
+// the batch (flattened walks of i2_batch.cuh): counter reset, tier 1 with the singular parts,
+// tiers 2 / 2b, the adaptive potential (i2_kernels_fp64.cu), self pairs, and the FP64 fix-up.
+__global__ void k_batch_reset(const BatchSeg *__restrict__ segs, int nseg)
 {
-    if (A.n <= 0) return;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nseg || segs[s].A.n <= 0) return;
+    for (int k = 0; k < 16; ++k) segs[s].A.cnt[k] = 0;
+    *segs[s].A.maxlev = 0;
+}
+
+__global__ void __launch_bounds__(128) k_batch_singular(const BatchSeg *__restrict__ segs, int nseg, QuadTablesF Qf)
+{
+    extern __shared__ long long prefix[];
+    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long { return seg_adjacent(S) ? S.A.n : 0; });
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        if (S.cls == kEdge) singular_mixed_item<kEdge>(S.A, Qf, g - prefix[sg]);
+        else singular_mixed_item<kVertex>(S.A, Qf, g - prefix[sg]);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_batch_tier2(const BatchSeg *__restrict__ segs, int nseg, QuadTablesF Qf, QuadTables Q)
+{
+    extern __shared__ long long prefix[];
+    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
+        return seg_adjacent(S) && S.A.hard_list ? *S.A.tier2_cnt : 0;
+    });
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < total; g += nwarps) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        if (S.cls == kEdge) tier2_mixed_item<kEdge>(S.A, Qf, Q, (int)(g - prefix[sg]), lane);
+        else tier2_mixed_item<kVertex>(S.A, Qf, Q, (int)(g - prefix[sg]), lane);
+    }
+}
+
+// segments whose pairs the fix-up gathers (into act_a, counted in cnt[11])
+__device__ __forceinline__ bool seg_fixup(const BatchSeg &S) { return S.A.n > 0 && S.cls != kSelf && S.A.act_a; }
+
+__global__ void __launch_bounds__(256) k_batch_fixup_collect(const BatchSeg *__restrict__ segs, int nseg)
+{
+    extern __shared__ long long prefix[];
+    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long { return seg_fixup(S) ? S.A.n : 0; });
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+        const int sg = seg_find(prefix, nseg, g);
+        const ClassArgs &A = segs[sg].A;
+        fixup_collect_item(A, A.act_a, A.cnt + 11, g - prefix[sg]);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_batch_fp64_fixup(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q, int mode,
+                                                          int fixed_level, double tol, int kmax)
+{
+    extern __shared__ long long prefix[];
+    __shared__ double red[5 * 8];
+    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long { return seg_fixup(S) ? S.A.cnt[11] : 0; });
+    // one block per gathered pair
+    for (long long g = blockIdx.x; g < total; g += gridDim.x) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        const int t = S.A.act_a[g - prefix[sg]];
+        if (S.cls == kFar) fp64_fixup_item<kFar>(S.A, Q, mode, fixed_level, tol, kmax, t, red);
+        else if (S.cls == kEdge) fp64_fixup_item<kEdge>(S.A, Q, mode, fixed_level, tol, kmax, t, red);
+        else fp64_fixup_item<kVertex>(S.A, Q, mode, fixed_level, tol, kmax, t, red);
+    }
+}
+
+static size_t seg_smem(int nseg) { return (size_t)(nseg + 1) * sizeof(long long); }
+
+void launch_batch_prelude(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTables &Q, const QuadTablesF &Qf,
+                          const RunConfig &cfg, int persistent_blocks, cudaStream_t s)
+{
     const int tpb = 128;
-    if (cls == kSelf) {
-        launch_self(A, Q, cfg, s);
-    } else if (cls == kEdge) {
-        k_singular_mixed<kEdge><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
-        if (A.hard_list) {
-            k_pot_tier2_mixed<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Qf, Q);
-            launch_pot_hard(kEdge, A, Q, cfg, persistent_blocks, s);
+    for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
+        const int nc = std::min(kBatchSegChunk, nseg - c0);
+        k_batch_reset<<<blocks_for_m(nc, 128), 128, 0, s>>>(segs + c0, nc);
+    }
+    if (tot.adjacent_pairs > 0) {
+        const int blocks = std::max(1, std::min(blocks_for_m(tot.adjacent_pairs, tpb), 1 << 16));
+        for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
+            const int nc = std::min(kBatchSegChunk, nseg - c0);
+            k_batch_singular<<<blocks, tpb, seg_smem(nc), s>>>(segs + c0, nc, Qf);
         }
-    } else if (cls == kVertex) {
-        k_singular_mixed<kVertex><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
-        if (A.hard_list) {
-            k_pot_tier2_mixed<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Qf, Q);
-            launch_pot_hard(kVertex, A, Q, cfg, persistent_blocks, s);
+        if (tot.hard_lists) {
+            for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
+                const int nc = std::min(kBatchSegChunk, nseg - c0);
+                k_batch_tier2<<<persistent_blocks, tpb, seg_smem(nc), s>>>(segs + c0, nc, Qf, Q);
+            }
+            launch_batch_pot_chain(segs, nseg, Q, cfg.hard_tol, persistent_blocks, s);
         }
+    }
+    launch_batch_self(segs, nseg, tot.self_pairs, Q, cfg, s);
+}
+
+void launch_batch_fixup(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTables &Q, const RunConfig &cfg,
+                        int persistent_blocks, cudaStream_t s)
+{
+    if (tot.fixup_pairs <= 0) return;
+    const int blocks = std::max(1, std::min(blocks_for_m(tot.fixup_pairs, 256), 1 << 16));
+    for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
+        const int nc = std::min(kBatchSegChunk, nseg - c0);
+        k_batch_fixup_collect<<<blocks, 256, seg_smem(nc), s>>>(segs + c0, nc);
+        k_batch_fp64_fixup<<<persistent_blocks, 256, seg_smem(nc), s>>>(segs + c0, nc, Q, cfg.mode, cfg.level, cfg.tol, cfg.max_level);
     }
 }
 
