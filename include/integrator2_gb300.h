@@ -98,6 +98,17 @@ i2_status i2_mesh_set_geometry(i2_mesh_t *mesh, const double *vertices, int32_t 
  * reference's all-pairs classifier does.  Lists are built in O(N) (vertex incidence + a
  * uniform grid over centroids) instead of the reference's O(N^2) kernel. */
 i2_status i2_mesh_prepare(i2_mesh_t *mesh, double near_factor);
+/* Mesh3D::prepareMesh with the pair lists built on the GPU (the reference's prepareMesh
+ * classifies pairs on the GPU, src/Mesh3d.cu:93-142 and 243-262, by an O(N^2) shared-vertex
+ * count).  Same cell data and the same lists, in the same order, as i2_mesh_prepare: O(N)
+ * through vertex incidence and a sorted centroid grid.  Also uploads the mesh.  host_copy = 0
+ * keeps the lists on the device only (they are copied to the host the first time a host-side
+ * call needs them); i2_mesh_device_pairs hands them out.  Synchronises the device. */
+i2_status i2_mesh_prepare_device(i2_mesh_t *mesh, double near_factor, int32_t host_copy);
+/* device copy of a class's unordered list: *d_rows = n int2 (i, j) rows (i < j, sorted; the
+ * self class (i, i)), owned by the mesh and valid until it is prepared again or destroyed.  A
+ * mesh prepared on the host has its lists uploaded on the first call. */
+i2_status i2_mesh_device_pairs(const i2_mesh_t *mesh, i2_pair_class cls, const int32_t **d_rows, int64_t *n);
 i2_status i2_mesh_sizes(const i2_mesh_t *mesh, int32_t *nv, int32_t *nc);
 /* Mesh3D::getSimpleNeighbors / getAttachedNeighbors / getNotNeighbors ().size: unordered
  * (i < j) pairs of a class; the self class has nc entries */

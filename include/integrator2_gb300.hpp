@@ -108,6 +108,18 @@ public:
     }
     // src/Mesh3d.cuh:63; near_factor <= 0: every disjoint pair, as the reference
     void prepareMesh(double near_factor = 0.0) { i2::check(i2_mesh_prepare(h_, near_factor), "i2_mesh_prepare"); }
+    // prepareMesh with the lists built on the GPU (same lists, same order)
+    void prepareMeshDevice(double near_factor = 0.0, bool host_copy = true)
+    {
+        i2::check(i2_mesh_prepare_device(h_, near_factor, host_copy ? 1 : 0), "i2_mesh_prepare_device");
+    }
+    // device rows (i, j) of a class's unordered list (2 int32 per row), owned by the mesh
+    const int32_t *devicePairs(i2_pair_class cls, int64_t &n) const
+    {
+        const int32_t *p = nullptr;
+        i2::check(i2_mesh_device_pairs(h_, cls, &p, &n), "i2_mesh_device_pairs");
+        return p;
+    }
 
     std::vector<Int3> getSimpleNeighbors() const { return pairs(I2_SIMPLE_NEIGHBORS); }
     std::vector<Int3> getAttachedNeighbors() const { return pairs(I2_ATTACHED_NEIGHBORS); }

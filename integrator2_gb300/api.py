@@ -79,6 +79,18 @@ class Mesh3D:
         a number keeps disjoint pairs closer than near_factor x mean edge length."""
         call("i2_mesh_prepare", self._h, float(near_factor) if near_factor else 0.0)
 
+    def prepareMeshDevice(self, near_factor: Optional[float] = None, host_copy: bool = True) -> None:
+        """prepareMesh with the pair lists built on the GPU (O(N), the same lists in the same
+        order as prepareMesh).  host_copy=False keeps them on the device until a host-side call
+        needs them; devicePairs() hands them out."""
+        call("i2_mesh_prepare_device", self._h, float(near_factor) if near_factor else 0.0, 1 if host_copy else 0)
+
+    def devicePairs(self, cls: int):
+        """(device pointer, n) of a class's unordered int2 (i, j) rows, owned by the mesh."""
+        ptr, n = ctypes.c_void_p(), ctypes.c_int64()
+        call("i2_mesh_device_pairs", self._h, cls, ctypes.byref(ptr), ctypes.byref(n))
+        return int(ptr.value or 0), int(n.value)
+
     def _count(self, cls: int) -> int:
         n = ctypes.c_int64()
         call("i2_mesh_pair_count", self._h, cls, ctypes.byref(n))

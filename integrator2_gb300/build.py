@@ -17,9 +17,12 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libi2gb300.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["i2_capi.cu", "i2_kernels_fp64.cu", "i2_kernels_mixed.cu", "i2_calibrate.cu", "i2_noalloc.cu", "i2_adjoint.cu"]
+SOURCES = ["i2_capi.cu", "i2_kernels_fp64.cu", "i2_kernels_mixed.cu", "i2_calibrate.cu", "i2_noalloc.cu", "i2_adjoint.cu",
+           "i2_pairs.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+# host code is compiled without floating-point contraction (GCC fuses a*b+c on Arm by default),
+# so the host arithmetic the pair builders share rounds the same on every host
+FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden", "-Xcompiler", "-ffp-contract=off",
          "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 
 

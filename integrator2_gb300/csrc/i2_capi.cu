@@ -4,6 +4,8 @@
 // turned into an i2_status with a thread-local message; nothing calls exit().
 #include "integrator2_gb300.h"
 #include "i2_engine.h"
+#include "i2_host.h"
+#include "i2_pairs.h"
 
 #include <cmath>
 #include <cstdio>
@@ -18,26 +20,10 @@
 
 namespace {
 
+using i2::DevBuf;
+using i2::Failure;
+
 thread_local std::string g_error;
-
-struct Failure {
-    i2_status code;
-    std::string msg;
-};
-
-#define I2_CHECK_CUDA(call)                                                                                            \
-    do {                                                                                                               \
-        cudaError_t e_ = (call);                                                                                       \
-        if (e_ != cudaSuccess) {                                                                                       \
-            throw Failure{e_ == cudaErrorMemoryAllocation ? I2_ERR_OUT_OF_MEMORY : I2_ERR_CUDA,                        \
-                          std::string(#call) + ": " + cudaGetErrorString(e_)};                                         \
-        }                                                                                                              \
-    } while (0)
-
-#define I2_REQUIRE(cond, code, text)                                                                                   \
-    do {                                                                                                               \
-        if (!(cond)) throw Failure{code, text};                                                                        \
-    } while (0)
 
 template <class F>
 i2_status guarded(F &&f)
@@ -57,31 +43,6 @@ i2_status guarded(F &&f)
         return I2_ERR_INVALID_ARGUMENT;
     }
 }
-
-// device buffer owned by one handle
-template <class T>
-struct DevBuf {
-    T *ptr = nullptr;
-    size_t count = 0;
-    DevBuf() = default;
-    DevBuf(const DevBuf &) = delete;
-    DevBuf &operator=(const DevBuf &) = delete;
-    ~DevBuf() { release(); }
-    void release()
-    {
-        if (ptr) cudaFree(ptr);
-        ptr = nullptr;
-        count = 0;
-    }
-    void reserve(size_t n)
-    {
-        if (n <= count && ptr) return;
-        release();
-        if (n == 0) return;
-        I2_CHECK_CUDA(cudaMalloc(&ptr, n * sizeof(T)));
-        count = n;
-    }
-};
 
 // ------------------------------------------------------------------ quadrature
 struct Rule {
@@ -244,6 +205,9 @@ struct i2_mesh {
     std::vector<int> C;
     std::vector<double> normals, measures, centres;
     std::vector<int> lists[4];  // unordered (i < j) pairs per class, flattened (i, j)
+    bool host_lists = true;     // lists[] hold the current lists (a device build may skip the host copy)
+    i2::DevicePairLists dlists; // the same lists on the device
+    bool dlists_ok = false;     // dlists hold the current lists
     bool prepared = false;   // host geometry and pair lists ready
     bool on_device = false;  // vertices, cells and panels uploaded (first run)
     double near_factor = 3.0;
@@ -408,35 +372,12 @@ void build_pair_lists(i2_mesh &m, double near_factor)
                 if (!touching(i, j)) { far.push_back(i); far.push_back(j); }
         return;
     }
-    double hsum = 0.0;
-    long long hcnt = 0;
-    {
-        // mean length over unique edges
-        std::vector<std::pair<int, int>> edges;
-        edges.reserve(m.C.size());
-        for (int c = 0; c < nc; ++c)
-            for (int d = 0; d < 3; ++d) {
-                int a = m.C[3 * c + d], b = m.C[3 * c + (d + 1) % 3];
-                if (a > b) std::swap(a, b);
-                edges.emplace_back(a, b);
-            }
-        std::sort(edges.begin(), edges.end());
-        edges.erase(std::unique(edges.begin(), edges.end()), edges.end());
-        for (auto &e : edges) {
-            const double *p = &m.V[3 * e.first], *q = &m.V[3 * e.second];
-            hsum += std::sqrt((p[0] - q[0]) * (p[0] - q[0]) + (p[1] - q[1]) * (p[1] - q[1]) + (p[2] - q[2]) * (p[2] - q[2]));
-            ++hcnt;
-        }
-    }
-    const double r = near_factor * (hcnt ? hsum / hcnt : 0.0), r2 = r * r;
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int c = 0; c < nc; ++c)
-        for (int d = 0; d < 3; ++d) {
-            lo[d] = std::min(lo[d], m.centres[3 * c + d]);
-            hi[d] = std::max(hi[d], m.centres[3 * c + d]);
-        }
-    long long dims[3];
-    for (int d = 0; d < 3; ++d) dims[d] = std::max(1LL, std::min(1LL << 20, (long long)std::floor((hi[d] - lo[d]) / r) + 1));
+    const double r = near_factor * i2::mean_edge_length(m.V.data(), m.C.data(), nc);
+    if (!(r > 0.0)) return;
+    const i2::NearGrid g = i2::near_grid(m.centres.data(), nc, r);
+    const double r2 = g.r2;
+    const double *lo = g.lo;
+    const long long *dims = g.dims;
     auto key = [&](long long x, long long y, long long z) { return (x * dims[1] + y) * dims[2] + z; };
     std::unordered_map<long long, std::vector<int>> grid;
     grid.reserve(nc);
@@ -467,6 +408,39 @@ void build_pair_lists(i2_mesh &m, double near_factor)
             if (d2 < r2 && !touching(i, j)) { far.push_back(i); far.push_back(j); }
         }
     }
+}
+
+// the host copy of a class's list, fetched once from the device when the mesh was prepared
+// there without one
+const std::vector<int> &host_list(const i2_mesh &cm, int cls)
+{
+    i2_mesh &m = const_cast<i2_mesh &>(cm);
+    if (!m.host_lists) {
+        for (int c = 0; c < 4; ++c) {
+            m.lists[c].resize(2 * (size_t)m.dlists.n[c]);
+            if (m.dlists.n[c])
+                I2_CHECK_CUDA(cudaMemcpy(m.lists[c].data(), m.dlists.rows[c].ptr, m.dlists.n[c] * sizeof(int2), cudaMemcpyDeviceToHost));
+        }
+        m.host_lists = true;
+    }
+    return m.lists[cls];
+}
+
+int64_t list_size(const i2_mesh &m, int cls) { return m.host_lists ? (int64_t)m.lists[cls].size() / 2 : m.dlists.n[cls]; }
+
+// the device copy of the lists, uploaded once when the mesh was prepared on the host
+void device_lists(const i2_mesh &cm)
+{
+    i2_mesh &m = const_cast<i2_mesh &>(cm);
+    if (m.dlists_ok) return;
+    for (int c = 0; c < 4; ++c) {
+        const int64_t n = (int64_t)m.lists[c].size() / 2;
+        m.dlists.rows[c].release();
+        m.dlists.rows[c].reserve(std::max<int64_t>(n, 1));
+        if (n) I2_CHECK_CUDA(cudaMemcpy(m.dlists.rows[c].ptr, m.lists[c].data(), n * sizeof(int2), cudaMemcpyHostToDevice));
+        m.dlists.n[c] = n;
+    }
+    m.dlists_ok = true;
 }
 
 void host_cell_geometry(i2_mesh &m)
@@ -839,9 +813,47 @@ i2_status i2_mesh_prepare(i2_mesh_t *mesh, double near_factor)
             I2_REQUIRE(mesh->measures[c] > 0.0 && std::isfinite(mesh->measures[c]), I2_ERR_INVALID_ARGUMENT,
                        "degenerate cell " + std::to_string(c));
         build_pair_lists(*mesh, near_factor);
+        mesh->host_lists = true;
+        mesh->dlists_ok = false;
         mesh->near_factor = near_factor;
         mesh->on_device = false;
         mesh->prepared = true;
+    });
+}
+
+i2_status i2_mesh_prepare_device(i2_mesh_t *mesh, double near_factor, int32_t host_copy)
+{
+    return guarded([&] {
+        I2_REQUIRE(mesh, I2_ERR_INVALID_ARGUMENT, "null mesh");
+        I2_REQUIRE(mesh->nc() > 0, I2_ERR_STATE, "mesh has no cells");
+        mesh->prepared = false;
+        host_cell_geometry(*mesh);
+        for (int c = 0; c < mesh->nc(); ++c)
+            I2_REQUIRE(mesh->measures[c] > 0.0 && std::isfinite(mesh->measures[c]), I2_ERR_INVALID_ARGUMENT,
+                       "degenerate cell " + std::to_string(c));
+        upload_mesh(*mesh);
+        mesh->on_device = true;
+        for (auto &l : mesh->lists) std::vector<int>().swap(l);
+        mesh->host_lists = false;
+        mesh->dlists_ok = false;
+        i2::build_pair_lists_device(mesh->V.data(), mesh->C.data(), mesh->centres.data(), mesh->nv(), mesh->nc(), mesh->dV.ptr,
+                                    mesh->dC.ptr, near_factor, mesh->dlists, 0);
+        mesh->dlists_ok = true;
+        if (host_copy) host_list(*mesh, 0);
+        mesh->near_factor = near_factor;
+        mesh->prepared = true;
+    });
+}
+
+i2_status i2_mesh_device_pairs(const i2_mesh_t *mesh, i2_pair_class cls, const int32_t **d_rows, int64_t *n)
+{
+    return guarded([&] {
+        I2_REQUIRE(mesh && d_rows && n, I2_ERR_INVALID_ARGUMENT, "null argument");
+        I2_REQUIRE(mesh->prepared, I2_ERR_STATE, "mesh not prepared");
+        const int c = checked_class(cls);
+        device_lists(*mesh);
+        *d_rows = reinterpret_cast<const int32_t *>(mesh->dlists.rows[c].ptr);
+        *n = mesh->dlists.n[c];
     });
 }
 
@@ -859,7 +871,7 @@ i2_status i2_mesh_pair_count(const i2_mesh_t *mesh, i2_pair_class cls, int64_t *
     return guarded([&] {
         I2_REQUIRE(mesh && n, I2_ERR_INVALID_ARGUMENT, "null argument");
         I2_REQUIRE(mesh->prepared, I2_ERR_STATE, "mesh not prepared");
-        *n = (int64_t)mesh->lists[checked_class(cls)].size() / 2;
+        *n = list_size(*mesh, checked_class(cls));
     });
 }
 
@@ -868,7 +880,7 @@ i2_status i2_mesh_copy_pairs(const i2_mesh_t *mesh, i2_pair_class cls, int32_t *
     return guarded([&] {
         I2_REQUIRE(mesh && rows, I2_ERR_INVALID_ARGUMENT, "null argument");
         I2_REQUIRE(mesh->prepared, I2_ERR_STATE, "mesh not prepared");
-        const auto &l = mesh->lists[checked_class(cls)];
+        const auto &l = host_list(*mesh, checked_class(cls));
         I2_REQUIRE(n == (int64_t)l.size() / 2, I2_ERR_INVALID_ARGUMENT, "row count does not match the list");
         for (int64_t k = 0; k < n; ++k) {
             rows[3 * k] = l[2 * k];
@@ -1061,7 +1073,7 @@ i2_status i2_evaluator_run_all_pairs(i2_evaluator_t *ev, int32_t check_correctne
         const i2_mesh &m = *ev->mesh;
         I2_REQUIRE(m.prepared, I2_ERR_STATE, "mesh not prepared");
         for (int cls = 0; cls < 4; ++cls) {
-            const auto &l = m.lists[cls];
+            const auto &l = host_list(m, cls);
             const int64_t u = (int64_t)l.size() / 2;
             std::vector<int32_t> rows;
             if (cls == I2_SELF) {
