@@ -169,33 +169,121 @@ METRIC = "pair-integrals/s at <=1e-6 rel err"
 
 
 # ------------------------------------------------------------------ GPU arm
-def accuracy(V, C, lists, J, P, levels, nsample=400):
-    """relative error per class and channel on a seeded sample against the oracle's high-order
-    answer (fixed level 4 of the 13-point rule for J; for the potential of adjacent pairs the
-    adaptive rule at 1e-10 on every pair): the largest per-pair error, its 99th percentile and
-    rms, and the normwise error |dJ| / |J| over the sample"""
+CLASS_NAMES = {0: "vertex", 1: "edge", 2: "near", 3: "self"}
+
+
+def class_accuracy(V, C, cls, pr, j, p):
+    """relative error of one class's sampled rows pr (results j, p) against the oracle's
+    high-order answer (fixed level 4 of the 13-point rule for J; for the potential of adjacent
+    pairs the adaptive rule at 1e-10 on every pair): the largest per-pair error, its 99th
+    percentile and rms, and the normwise error |dJ| / |J| over the sample"""
     from oracle import oracle as O
+    with O.potential_rule(40, 32, 3, adaptive=1e-10, depth=18, every_pair=True):
+        _, oJ, oP, _ = O.integrate(cls, pr, V, C, mode=O.FIXED, level=4 if cls != 3 else 0)
+    if cls == 3:
+        return {"J_abs_max": float(np.abs(j - oJ).max()), "P": float((np.abs(p - oP) / np.abs(oP)).max()), "sample": int(len(pr))}
+    eJ = np.linalg.norm(j - oJ, axis=1) / np.maximum(np.linalg.norm(oJ, axis=1), 1e-300)
+    eP = np.abs(p - oP) / np.abs(oP)
+    return {"J": float(eJ.max()), "P": float(eP.max()),
+            "J_p99": float(np.percentile(eJ, 99)), "P_p99": float(np.percentile(eP, 99)),
+            "J_rms": float(np.sqrt(np.mean(eJ ** 2))), "P_rms": float(np.sqrt(np.mean(eP ** 2))),
+            "J_normwise": float(np.linalg.norm(j - oJ) / np.linalg.norm(oJ)),
+            "P_normwise": float(np.linalg.norm(p - oP) / np.linalg.norm(oP)), "sample": int(len(pr))}
+
+
+def accuracy(V, C, lists, J, P, levels, nsample=400):
+    """class_accuracy on a seeded sample of every class"""
     rng = np.random.default_rng(5)
     out = {}
-    names = {0: "vertex", 1: "edge", 2: "near", 3: "self"}
     for cls in CLASSES:
         pr = lists[cls]
         idx = np.sort(rng.choice(len(pr), min(nsample, len(pr)), replace=False))
-        with O.potential_rule(40, 32, 3, adaptive=1e-10, depth=18, every_pair=True):
-            _, oJ, oP, _ = O.integrate(cls, pr[idx], V, C, mode=O.FIXED, level=4 if cls != 3 else 0)
-        j, p = J[cls][idx], P[cls][idx]
-        if cls == 3:
-            out[names[cls]] = {"J_abs_max": float(np.abs(j - oJ).max()),
-                               "P": float((np.abs(p - oP) / np.abs(oP)).max()), "sample": int(len(idx))}
-            continue
-        eJ = np.linalg.norm(j - oJ, axis=1) / np.maximum(np.linalg.norm(oJ, axis=1), 1e-300)
-        eP = np.abs(p - oP) / np.abs(oP)
-        out[names[cls]] = {"J": float(eJ.max()), "P": float(eP.max()),
-                           "J_p99": float(np.percentile(eJ, 99)), "P_p99": float(np.percentile(eP, 99)),
-                           "J_rms": float(np.sqrt(np.mean(eJ ** 2))), "P_rms": float(np.sqrt(np.mean(eP ** 2))),
-                           "J_normwise": float(np.linalg.norm(j - oJ) / np.linalg.norm(oJ)),
-                           "P_normwise": float(np.linalg.norm(p - oP) / np.linalg.norm(oP)), "sample": int(len(idx))}
+        out[CLASS_NAMES[cls]] = class_accuracy(V, C, cls, pr[idx], J[cls][idx], P[cls][idx])
     return out
+
+
+class DeviceRows:
+    """a device int32 [n, 2] array owned by the library, seen by torch without a copy"""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n, 2), "typestr": "<i4", "data": (ptr, False), "version": 3}
+
+
+def c5_section(args):
+    """C5: torus R = 1, r = 0.1 on a 2000 x 500 grid (2 M triangles), scaled by 5e-4, normal jitter
+    0.05 x the local edge length (seed 2026).  The pair lists are built on the GPU
+    (i2_mesh_prepare_device; the host builder is timed beside it and must give the same lists),
+    then all four classes (near < 3h, ordered pairs) run in mixed precision with relative error
+    control 1e-6 through the device entry point, lists and results resident on the device: one
+    warm-up step, two timed steps, CUDA events.  Accuracy: 200 sampled pairs per class against the
+    oracle on the same geometry scaled by 2^20 (exact integrals scale as s^2 for J and s^3 for P;
+    at that scale the oracle's absolute thresholds are in their normal range)."""
+    import torch
+    from integrator2_gb300 import api, meshes
+    V, C = meshes.torus(2000, 500, 1.0, 0.1, scale=5e-4, jitter_rel=0.05, seed=SEED)
+    e = np.linalg.norm(V[C[:, [1, 2, 0]]] - V[C], axis=2)
+    aspect = e.max(axis=1) / e.min(axis=1)
+    m = api.Mesh3D()
+    m.setGeometry(V, C)
+    m.prepareMeshDevice(NEAR, host_copy=False)  # first call: allocations and module loading
+    t0 = time.perf_counter()
+    m.prepareMeshDevice(NEAR, host_copy=False)
+    t_dev = time.perf_counter() - t0
+    h = api.Mesh3D()
+    h.setGeometry(V, C)
+    t0 = time.perf_counter()
+    h.prepareMesh(NEAR)
+    t_host = time.perf_counter() - t0
+    rows, counts = {}, {}
+    for c in CLASSES:
+        ptr, n = m.devicePairs(c)
+        u = torch.as_tensor(DeviceRows(ptr, n), device="cuda")
+        if c != 3:
+            hp, hn = h.devicePairs(c)
+            if hn != n or not torch.equal(u, torch.as_tensor(DeviceRows(hp, hn), device="cuda")):
+                raise RuntimeError(f"C5: device and host pair builders disagree on class {c}")
+        rows[c] = u if c == 3 else torch.cat([u, u.flip(1)]).contiguous()
+        counts[CLASS_NAMES[c]] = int(len(rows[c]))
+    del h
+    total = sum(counts.values())
+    it = api.NumericalIntegrator3D(m, api.qf3D13)
+    it.setErrorControl(api.RELATIVE_ERROR_CONTROL, args.tol, 5)
+    it.setPrecision(api.PRECISION_MIXED)
+    stream = torch.cuda.Stream()
+    ev = api.EvaluatorJ3DK(m, it)
+    ev.setStream(stream.cuda_stream)
+    J = {c: torch.empty(len(rows[c]), 3, dtype=torch.float64, device="cuda") for c in CLASSES}
+    P = {c: torch.empty(len(rows[c]), dtype=torch.float64, device="cuda") for c in CLASSES}
+
+    def step():
+        for c in CLASSES:
+            ev.runClassDevice(c, rows[c].data_ptr(), len(rows[c]), 0, J[c].data_ptr(), P[c].data_ptr())
+
+    steps = 2
+    with torch.cuda.stream(stream):
+        step()
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler() as clk:
+            e0.record(stream)
+            for _ in range(steps):
+                step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    rng = np.random.default_rng(7)
+    acc = {}
+    s = 2.0 ** 20
+    for c in CLASSES:
+        idx = torch.as_tensor(np.sort(rng.choice(len(rows[c]), 200, replace=False)), device="cuda")
+        pr = rows[c][idx].cpu().numpy()
+        acc[CLASS_NAMES[c]] = class_accuracy(V * s, C, c, pr, J[c][idx].cpu().numpy() * s ** 2, P[c][idx].cpu().numpy() * s ** 3)
+    return {"workload": "C5: torus R=1, r=0.1, 2000 x 500 grid, x 5e-4, normal jitter 0.05 h, near < 3h, relative 1e-6, mixed",
+            "triangles": int(len(C)), "pairs": int(total), "pairs_by_class": counts,
+            "edge_length": [float(e.min()), float(e.max())], "aspect_ratio": {"mean": float(aspect.mean()), "max": float(aspect.max())},
+            "pair_builder_s": {"gpu": t_dev, "host": t_host, "same_lists": True},
+            "value": total / (ms * 1e-3), "unit": "pair-integrals/s", "ms_per_step": ms, "steps": steps, "warmup": 1,
+            "clocks": clk.summary(), "accuracy": acc}
 
 
 def run_form(ev, lists, d_pairs, d_J, d_P, stream, flush, steps, warmup):
@@ -542,6 +630,7 @@ def gpu_arm(args):
     if "fp64" in forms:
         line["speedup_over_plain_fp64"] = head["value"] / forms["fp64"]["value"]
     line["uneven_batch"] = uneven_batch_section(args)
+    line["c5"] = c5_section(args)
     line["adjoint"] = adjoint_section(args)
     if "batch" in forms:
         line["batch"] = {"shape": {"threads": forms["batch"]["shape"][0], "blocks_per_sm": forms["batch"]["shape"][1],

@@ -2,7 +2,8 @@
 //
 // Each cell gets a 160-byte FP32 panel record (10 x float4) written once from the FP64 mesh:
 //   [0] A_hi.xyz, S     [1] A_lo.xyz, 2S    [2] B_hi.xyz, |C-B|   [3] B_lo.xyz, |A-C|
-//   [4] C_hi.xyz, |B-A| [5] C_lo.xyz, -     [6] n.xyz, -          [7..9] ta, tb, tc (unit edges)
+//   [4] C_hi.xyz, |B-A| [5] C_lo.xyz, 1/sqrt(S)   [6] n.xyz, -
+//   [7..9] ta, tb, tc (unit edges C-B, A-C, B-A), each with 1/|edge|
 // Vertices are stored as unevaluated float sums hi + lo (double-float), so the offset of a
 // point of K_i from a vertex of K_j is formed in FP32 as (a_hi - b_hi) + (a_lo - b_lo) without
 // FP64 work and without the cancellation of subtracting two rounded absolute coordinates.

@@ -42,11 +42,15 @@ __global__ void k_prepare_panels_f32(int nc, const double *__restrict__ V, const
     p.v[2].w = (float)lens[0];
     p.v[3].w = (float)lens[1];
     p.v[4].w = (float)lens[2];
+    // constants that scale logs against the FP64 closed forms, rounded once from FP64: [5].w =
+    // 1/sqrt(S), [7..9].w = 1/|edge| (an FP32 rsqrtf or a quotient of FP32-rounded lengths would be
+    // off by up to a few ulps, a bias the log terms carry into every point)
+    p.v[5].w = (float)(1.0 / sqrt(S));
     p.v[6] = make_float4((float)n.x, (float)n.y, (float)n.z, 0.0f);
     const d3 ta = unit(ea), tb = unit(eb), tc = unit(ec);
-    p.v[7] = make_float4((float)ta.x, (float)ta.y, (float)ta.z, 0.0f);
-    p.v[8] = make_float4((float)tb.x, (float)tb.y, (float)tb.z, 0.0f);
-    p.v[9] = make_float4((float)tc.x, (float)tc.y, (float)tc.z, 0.0f);
+    p.v[7] = make_float4((float)ta.x, (float)ta.y, (float)ta.z, (float)(1.0 / lens[0]));
+    p.v[8] = make_float4((float)tb.x, (float)tb.y, (float)tb.z, (float)(1.0 / lens[1]));
+    p.v[9] = make_float4((float)tc.x, (float)tc.y, (float)tc.z, (float)(1.0 / lens[2]));
     out[c] = p;
 }
 
@@ -59,19 +63,13 @@ struct EdgeCtxF {
 struct VertexCtxF {
     f3 AB, AC;       // JB - JA, JC - JA (JA = shared vertex)
     f3 ta, tb, tbc;
-    // the asymptote's angle terms s1, s2 as atan2(o_A.w, l_A c - o_A.p) with w = tau x e,
-    // p = e -+ tau, c = |p|^2 / 2 formed in FP64 once per pair: when e is nearly parallel to
-    // +-tau, e -+ tau formed in FP32 would keep only a few digits
-    f3 w1, p1, w2, p2;
+    // the asymptote's direction e and, formed in FP64 once per pair, w = tau x e and
+    // c = |e -+ tau|^2 / 2 = 1 -+ e.tau for its two angle terms (when e is nearly parallel to
+    // +-tau, e -+ tau formed in FP32 would keep only a few digits)
+    f3 e, w1, w2;
     float c1, c2;
     float inv_sqrt_si, lenBC;
 };
-
-__device__ __forceinline__ f3 unitf(f3 a)
-{
-    const float inv = 1.0f / normf(a);
-    return inv * a;
-}
 
 __device__ __forceinline__ void edge_integrand_f(f3 oA, f3 oB, f3 oC, const PanelJf &K, const EdgeCtxF &E, f3 &psi, float &th)
 {
@@ -93,8 +91,23 @@ __device__ __forceinline__ void vertex_integrand_f(f3 oA, f3 oB, f3 oC, const Pa
     const float l2 = logf((lB - dotf(oB, Vx.tb)) * Vx.inv_sqrt_si);
     psi = Lbc * Vx.tbc + l1 * Vx.ta + l2 * Vx.tb;
     const float den = lA * lB * lC + dotf(oA, oB) * lC + dotf(oB, oC) * lA + dotf(oC, oA) * lB;
-    const float s1 = atan2f(dotf(oA, Vx.w1), lA * Vx.c1 - dotf(oA, Vx.p1));
-    const float s2 = atan2f(dotf(oA, Vx.w2), lA * Vx.c2 - dotf(oA, Vx.p2));
+    // The angle terms s1 = atan2(o_A.w1, l_A c1 - o_A.(e - ta)) and s2 = atan2(o_A.w2,
+    // l_A c2 - o_A.(e + tb)) are both singular on the ray A + t e (the planes' intersection
+    // line, which may cross K_i): there both arguments vanish, each angle depends on the
+    // direction of approach, and only their sum is smooth.  Near the ray FP32 rounding of o_A
+    // decides those directions independently for s1 and s2 (errors up to 0.04 in the sum were
+    // seen).  Both are therefore formed from one deviation r = o_A - (o_A.e) e (projected
+    // again onto the plane normal to e), with the exact identities
+    //   l_A c1 - o_A.(e - ta) = q c1 + r.ta,   l_A c2 - o_A.(e + tb) = q c2 - r.tb,
+    //   o_A.w = r.w,   q = l_A - o_A.e = |r|^2 / (l_A + o_A.e)  (cancellation-free for o_A.e > 0);
+    // a rounding error in r then moves the point the two angles are taken at, consistently, and
+    // their sum does not depend on the direction of r near the ray.
+    const float oe = dotf(oA, Vx.e);
+    f3 r = oA - oe * Vx.e;
+    r = r - dotf(r, Vx.e) * Vx.e;
+    const float q = oe > 0.0f ? dotf(r, r) / (lA + oe) : lA - oe;
+    const float s1 = atan2f(dotf(r, Vx.w1), q * Vx.c1 + dotf(r, Vx.ta));
+    const float s2 = atan2f(dotf(r, Vx.w2), q * Vx.c2 - dotf(r, Vx.tb));
     th = 2.0f * atan2f(2.0f * K.S * dotf(K.n, oA), den) - 2.0f * (s1 + s2);
 }
 
@@ -169,31 +182,33 @@ __device__ void level_items_mixed(const ClassArgs &A, const QuadTablesF &Qf, int
                 else shifts_vertex(ci, cj, si, sj);
                 origin = sj;
                 const f3 AB = df_edge(A.panels_f, pr.y, (sj + 1) % 3, sj), AC = df_edge(A.panels_f, pr.y, (sj + 2) % 3, sj);
+                // unit edges of K_j in the rotated order, rounded from FP64 (the panel's unit edge
+                // k is opposite vertex k): the closed forms subtract the asymptote along the same
+                // directions, so FP32-normalised edges would leave a bias of a few ulps at every point
+                const float4 *uj = A.panels_f[pr.y].v + 7;
+                const f3 t_a = xyzf(uj[(sj + 1) % 3]), t_b = xyzf(uj[(sj + 2) % 3]), t_bc = xyzf(uj[sj]);
                 if (CLS == kEdge) {
                     E.AB = AB;
                     E.AC = AC;
-                    E.ta = unitf(-1.0f * AC);
-                    E.tb = unitf(AB);
-                    const f3 bc = AC - AB;
-                    E.ilvc = 1.0f / normf(bc);
-                    E.tc = E.ilvc * bc;
+                    E.ta = t_a;
+                    E.tb = t_b;
+                    E.ilvc = uj[sj].w;  // 1 / |JC - JB|, the edge opposite JA
+                    E.tc = t_bc;
                 } else {
                     Vx.AB = AB;
                     Vx.AC = AC;
-                    Vx.ta = unitf(-1.0f * AC);
-                    Vx.tb = unitf(AB);
-                    const f3 bc = AC - AB;
-                    Vx.lenBC = normf(bc);
-                    Vx.tbc = (1.0f / Vx.lenBC) * bc;
+                    Vx.ta = t_a;
+                    Vx.tb = t_b;
+                    Vx.lenBC = A.panels_f[pr.y].v[2 + sj].w;  // |JC - JB|, the edge opposite JA
+                    Vx.tbc = t_bc;
                     const float4 *ce = reinterpret_cast<const float4 *>(A.ctx_e + kVertexCtxFloats * (long long)t);
-                    const float4 q0 = ce[0], q1 = ce[1], q2 = ce[2], q3 = ce[3];
+                    const float4 q0 = ce[0], q1 = ce[1], q2 = ce[2];
                     Vx.w1 = xyzf(q0);
                     Vx.c1 = q0.w;
-                    Vx.p1 = xyzf(q1);
+                    Vx.e = xyzf(q1);
                     Vx.w2 = xyzf(q2);
                     Vx.c2 = q2.w;
-                    Vx.p2 = xyzf(q3);
-                    Vx.inv_sqrt_si = rsqrtf(A.panels_f[pr.x].v[0].w);
+                    Vx.inv_sqrt_si = A.panels_f[pr.x].v[5].w;
                 }
             }
             // K_i's vertices as offsets from each vertex of K_j, in the (rotated) order the
@@ -412,9 +427,9 @@ __device__ __forceinline__ void singular_mixed_item(const ClassArgs &A, const Qu
             const d3 w1 = cross(ta, e), p1 = e - ta, w2 = cross(tb, e), p2 = e + tb;
             float4 *ce = reinterpret_cast<float4 *>(A.ctx_e + kVertexCtxFloats * (long long)t);
             ce[0] = make_float4((float)w1.x, (float)w1.y, (float)w1.z, (float)(0.5 * dot(p1, p1)));
-            ce[1] = make_float4((float)p1.x, (float)p1.y, (float)p1.z, 0.0f);
+            ce[1] = make_float4((float)e.x, (float)e.y, (float)e.z, 0.0f);
             ce[2] = make_float4((float)w2.x, (float)w2.y, (float)w2.z, (float)(0.5 * dot(p2, p2)));
-            ce[3] = make_float4((float)p2.x, (float)p2.y, (float)p2.z, 0.0f);
+            ce[3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         }
         double *sg = A.sing + 4 * (long long)t;
         sg[0] = psi.x; sg[1] = psi.y; sg[2] = psi.z; sg[3] = th;
