@@ -459,9 +459,9 @@ def adjoint_section(args):
 # summed over the chain's six launches); the chain is compute-bound, this is mostly per-pair state
 FAR_CHAIN_DRAM_BYTES = 147407616 + 91512576
 
-# FP32 operation counts of the far-field integrand (same formulas, FP32 form): flops, sqrtf,
-# divide, log1pf, atan2f
-POINT_OPS_F32 = {"far": (211, 3, 3, 3, 1)}
+# FP32 operation counts of the far-field integrand (far_field_integrand_f with the point's
+# offsets): flops, sqrtf, divide, log1pf, atan2f
+POINT_OPS_F32 = {"far": (203, 3, 6, 3, 1)}
 
 
 def point_flops_f32(cal):

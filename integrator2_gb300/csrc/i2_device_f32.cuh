@@ -99,7 +99,8 @@ __device__ __forceinline__ float edge_log_f32(float lP, float qP, f3 oP, float l
 }
 
 struct FarCtxF {
-    f3 ma, mb, mc;
+    f3 ma, mb, mc;  // unit in-plane edge normals tau_e x n (potential by distances to the edge lines)
+    f3 ea, eb;      // edge vectors C - B, A - C (the far-field form below)
 };
 
 // theta/psi (a1) and the potential integrand from the offsets to K_j's vertices
@@ -116,6 +117,31 @@ __device__ __forceinline__ void far_integrand_f(f3 oa, f3 ob, f3 oc, const Panel
     th = 2.0f * atan2f(2.0f * K.S * d, den);
     const float ta_ = -dotf(F.ma, ob), tb_ = -dotf(F.mb, oc), tc_ = -dotf(F.mc, oa);
     pot = ta_ * La + tb_ * Lb + tc_ * Lc - d * th;
+}
+
+// The same three quantities for a point away from K_j (the disjoint class), in a form whose FP32
+// errors do not add up into a bias.  With lambda_e = L_e / |e| (divided by the same rounded |e|
+// that scales L_e's argument, so that rounding cancels to first order) and e_a + e_b + e_c = 0:
+//   Psi = sum_e lambda_e e_e = (lambda_a - lambda_c) e_a + (lambda_b - lambda_c) e_b,
+// where the rounding of the edge vectors only multiplies differences of lambda (sum_e tau_e L_e
+// with rounded unit tangents cancels down to Psi and keeps their rounding at full size), and
+//   sum_e t_e L_e = -(Psi x n).o_A + 2 S lambda_a
+// (t_e = distance of the point's projection to edge e's line, e_a x n . (B - A) = 2S,
+// e_b x n . (C - A) = 0), whose terms are of the size of the potential instead of cancelling.
+// Near K_j's edges lambda grows like a log and the potential's second form would rebuild
+// t_e L_e -> 0 from large terms, so the adjacent classes keep far_integrand_f.
+__device__ __forceinline__ void far_field_integrand_f(f3 oa, f3 ob, f3 oc, const PanelJf &K, const FarCtxF &F, f3 &psi, float &th,
+                                                      float &pot)
+{
+    const float la = normf(oa), lb = normf(ob), lc = normf(oc);
+    const float lam_c = edge_log_f32(la, dotf(oa, K.tc), oa, lb, dotf(ob, K.tc), ob, K.tc, K.lenC) / K.lenC;  // A -> B
+    const float lam_a = edge_log_f32(lb, dotf(ob, K.ta), ob, lc, dotf(oc, K.ta), oc, K.ta, K.lenA) / K.lenA;  // B -> C
+    const float lam_b = edge_log_f32(lc, dotf(oc, K.tb), oc, la, dotf(oa, K.tb), oa, K.tb, K.lenB) / K.lenB;  // C -> A
+    psi = (lam_a - lam_c) * F.ea + (lam_b - lam_c) * F.eb;
+    const float d = dotf(K.n, oa);
+    const float den = la * lb * lc + dotf(oa, ob) * lc + dotf(ob, oc) * la + dotf(oc, oa) * lb;
+    th = 2.0f * atan2f(2.0f * K.S * d, den);
+    pot = 2.0f * K.S * lam_a - dotf(crossf(psi, K.n), oa) - d * th;
 }
 
 // Kahan-compensated FP32 accumulator of (Psi, Theta, potential)

@@ -174,7 +174,8 @@ __device__ void level_items_mixed(const ClassArgs &A, const QuadTablesF &Qf, int
             VertexCtxF Vx;
             FarCtxF F;
             if (CLS == kFar) {
-                F = FarCtxF{crossf(K.ta, K.n), crossf(K.tb, K.n), crossf(K.tc, K.n)};
+                F.ea = df_edge(A.panels_f, pr.y, 2, 1);  // C - B
+                F.eb = -1.0f * K.AC;                      // A - C
             } else {
                 const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
                 int si, sj;
@@ -230,7 +231,7 @@ __device__ void level_items_mixed(const ClassArgs &A, const QuadTablesF &Qf, int
                     const f3 oC = l1 * U2.a + l2 * U2.b + l3 * U2.c;
                     f3 psi;
                     float th, pot = 0.0f;
-                    if (CLS == kFar) far_integrand_f(oA, oB, oC, K, F, psi, th, pot);
+                    if (CLS == kFar) far_field_integrand_f(oA, oB, oC, K, F, psi, th, pot);
                     else if (CLS == kEdge) edge_integrand_f(oA, oB, oC, K, E, psi, th);
                     else vertex_integrand_f(oA, oB, oC, K, Vx, psi, th);
                     const float w = Qf.w[g];
