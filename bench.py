@@ -629,9 +629,13 @@ def gpu_arm(args):
     }
     if "fp64" in forms:
         line["speedup_over_plain_fp64"] = head["value"] / forms["fp64"]["value"]
-    line["uneven_batch"] = uneven_batch_section(args)
-    line["c5"] = c5_section(args)
-    line["adjoint"] = adjoint_section(args)
+    sections = {x.strip() for x in args.sections.split(",") if x.strip()}
+    if "uneven" in sections:
+        line["uneven_batch"] = uneven_batch_section(args)
+    if "c5" in sections:
+        line["c5"] = c5_section(args)
+    if "adjoint" in sections:
+        line["adjoint"] = adjoint_section(args)
     if "batch" in forms:
         line["batch"] = {"shape": {"threads": forms["batch"]["shape"][0], "blocks_per_sm": forms["batch"]["shape"][1],
                                    "lanes_per_pair": forms["batch"]["shape"][2],
@@ -659,6 +663,9 @@ def main():
     ap.add_argument("--fd-coords", type=int, default=10, help="adjoint section: coordinates checked by finite differences")
     ap.add_argument("--forms", default="fp64,mixed,batch",
                     help="forms to run: fp64, mixed (per-class chains), batch (headline when present)")
+    ap.add_argument("--sections", default="uneven,c5,adjoint",
+                    help="side sections after the C2 line: uneven (48 meshes, batched vs per class), c5 (2 M triangles), "
+                         "adjoint (C4); empty for the C2 line alone")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)

@@ -63,10 +63,10 @@ struct EdgeCtxF {
 struct VertexCtxF {
     f3 AB, AC;       // JB - JA, JC - JA (JA = shared vertex)
     f3 ta, tb, tbc;
-    // the asymptote's direction e and, formed in FP64 once per pair, w = tau x e and
-    // c = |e -+ tau|^2 / 2 = 1 -+ e.tau for its two angle terms (when e is nearly parallel to
-    // +-tau, e -+ tau formed in FP32 would keep only a few digits)
-    f3 e, w1, w2;
+    // the asymptote's direction e and, formed in FP64 once per pair, w = tau x e and p = e -+ tau
+    // for its two angle terms, c = |p|^2 / 2 = 1 -+ e.tau (when e is nearly parallel to +-tau, w
+    // and p are small vectors that FP32 arithmetic on e and tau would keep only a few digits of)
+    f3 e, w1, w2, p1, p2;
     float c1, c2;
     float inv_sqrt_si, lenBC;
 };
@@ -91,23 +91,24 @@ __device__ __forceinline__ void vertex_integrand_f(f3 oA, f3 oB, f3 oC, const Pa
     const float l2 = logf((lB - dotf(oB, Vx.tb)) * Vx.inv_sqrt_si);
     psi = Lbc * Vx.tbc + l1 * Vx.ta + l2 * Vx.tb;
     const float den = lA * lB * lC + dotf(oA, oB) * lC + dotf(oB, oC) * lA + dotf(oC, oA) * lB;
-    // The angle terms s1 = atan2(o_A.w1, l_A c1 - o_A.(e - ta)) and s2 = atan2(o_A.w2,
-    // l_A c2 - o_A.(e + tb)) are both singular on the ray A + t e (the planes' intersection
-    // line, which may cross K_i): there both arguments vanish, each angle depends on the
-    // direction of approach, and only their sum is smooth.  Near the ray FP32 rounding of o_A
-    // decides those directions independently for s1 and s2 (errors up to 0.04 in the sum were
-    // seen).  Both are therefore formed from one deviation r = o_A - (o_A.e) e (projected
-    // again onto the plane normal to e), with the exact identities
-    //   l_A c1 - o_A.(e - ta) = q c1 + r.ta,   l_A c2 - o_A.(e + tb) = q c2 - r.tb,
-    //   o_A.w = r.w,   q = l_A - o_A.e = |r|^2 / (l_A + o_A.e)  (cancellation-free for o_A.e > 0);
+    // The angle terms s1 = atan2(o_A.w1, l_A c1 - o_A.p1) and s2 = atan2(o_A.w2, l_A c2 - o_A.p2)
+    // are both singular on the ray A + t e (the planes' intersection line, which may cross K_i):
+    // there both arguments vanish, each angle depends on the direction of approach, and only
+    // their sum is smooth.  Near the ray FP32 rounding of o_A decides those directions
+    // independently for s1 and s2 (errors up to 0.04 in the sum were seen).  Both are therefore
+    // formed from one deviation r = o_A - (o_A.e) e (projected again onto the plane normal to e),
+    // with the exact identities (e.w = 0, |e| = 1)
+    //   l_A c - o_A.p = q c - r.p,   o_A.w = r.w,
+    //   q = l_A - o_A.e = |r|^2 / (l_A + o_A.e)  (cancellation-free for o_A.e > 0);
     // a rounding error in r then moves the point the two angles are taken at, consistently, and
-    // their sum does not depend on the direction of r near the ray.
+    // their sum does not depend on the direction of r near the ray.  r.p keeps the small FP64
+    // vector p (r.p = r.(+-tau) would cancel when e is nearly parallel to -+tau).
     const float oe = dotf(oA, Vx.e);
     f3 r = oA - oe * Vx.e;
     r = r - dotf(r, Vx.e) * Vx.e;
     const float q = oe > 0.0f ? dotf(r, r) / (lA + oe) : lA - oe;
-    const float s1 = atan2f(dotf(r, Vx.w1), q * Vx.c1 + dotf(r, Vx.ta));
-    const float s2 = atan2f(dotf(r, Vx.w2), q * Vx.c2 - dotf(r, Vx.tb));
+    const float s1 = atan2f(dotf(r, Vx.w1), q * Vx.c1 - dotf(r, Vx.p1));
+    const float s2 = atan2f(dotf(r, Vx.w2), q * Vx.c2 - dotf(r, Vx.p2));
     th = 2.0f * atan2f(2.0f * K.S * dotf(K.n, oA), den) - 2.0f * (s1 + s2);
 }
 
@@ -203,12 +204,14 @@ __device__ void level_items_mixed(const ClassArgs &A, const QuadTablesF &Qf, int
                     Vx.lenBC = A.panels_f[pr.y].v[2 + sj].w;  // |JC - JB|, the edge opposite JA
                     Vx.tbc = t_bc;
                     const float4 *ce = reinterpret_cast<const float4 *>(A.ctx_e + kVertexCtxFloats * (long long)t);
-                    const float4 q0 = ce[0], q1 = ce[1], q2 = ce[2];
+                    const float4 q0 = ce[0], q1 = ce[1], q2 = ce[2], q3 = ce[3];
                     Vx.w1 = xyzf(q0);
-                    Vx.c1 = q0.w;
-                    Vx.e = xyzf(q1);
-                    Vx.w2 = xyzf(q2);
-                    Vx.c2 = q2.w;
+                    Vx.p1 = f3{q0.w, q1.x, q1.y};
+                    Vx.w2 = f3{q1.z, q1.w, q2.x};
+                    Vx.p2 = f3{q2.y, q2.z, q2.w};
+                    Vx.e = xyzf(q3);
+                    Vx.c1 = 0.5f * dotf(Vx.p1, Vx.p1);
+                    Vx.c2 = 0.5f * dotf(Vx.p2, Vx.p2);
                     Vx.inv_sqrt_si = A.panels_f[pr.x].v[5].w;
                 }
             }
@@ -427,10 +430,11 @@ __device__ __forceinline__ void singular_mixed_item(const ClassArgs &A, const Qu
             const d3 e = vertex_direction(ni, Kd.n, ta, tb, dA, dB);
             const d3 w1 = cross(ta, e), p1 = e - ta, w2 = cross(tb, e), p2 = e + tb;
             float4 *ce = reinterpret_cast<float4 *>(A.ctx_e + kVertexCtxFloats * (long long)t);
-            ce[0] = make_float4((float)w1.x, (float)w1.y, (float)w1.z, (float)(0.5 * dot(p1, p1)));
-            ce[1] = make_float4((float)e.x, (float)e.y, (float)e.z, 0.0f);
-            ce[2] = make_float4((float)w2.x, (float)w2.y, (float)w2.z, (float)(0.5 * dot(p2, p2)));
-            ce[3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            // w1, p1, w2, p2 (12 floats), then e
+            ce[0] = make_float4((float)w1.x, (float)w1.y, (float)w1.z, (float)p1.x);
+            ce[1] = make_float4((float)p1.y, (float)p1.z, (float)w2.x, (float)w2.y);
+            ce[2] = make_float4((float)w2.z, (float)p2.x, (float)p2.y, (float)p2.z);
+            ce[3] = make_float4((float)e.x, (float)e.y, (float)e.z, 0.0f);
         }
         double *sg = A.sing + 4 * (long long)t;
         sg[0] = psi.x; sg[1] = psi.y; sg[2] = psi.z; sg[3] = th;
