@@ -74,3 +74,42 @@ def test_mixed_accuracy_against_high_order(api):
         report[cls] = (float(eJ.max()), float(eP.max()))
         assert eJ.max() < 1e-5 and eP.max() < 1e-5, (cls, report[cls])
     print("mixed vs high-order oracle (J max, P max):", report)
+
+
+def _two_cells(V, C, i, j):
+    """the pair (i, j) as a two-cell mesh: cells 0 and 1, the same coordinates"""
+    verts = sorted(set(C[i].tolist()) | set(C[j].tolist()))
+    remap = {v: k for k, v in enumerate(verts)}
+    cells = np.array([[remap[v] for v in C[i]], [remap[v] for v in C[j]]], np.int32)
+    return V[verts], cells
+
+
+@pytest.mark.parametrize("case", ["ray through K_i (C5 torus)", "e antiparallel to an edge (C2)", "e antiparallel, second pair (C2)"])
+def test_mixed_vertex_asymptote_hard_cases(api, case):
+    """common-vertex pairs whose asymptote angle terms are ill-conditioned in FP32: the planes'
+    intersection ray crosses K_i (errors up to 5e-5 before the angles were formed from one
+    deviation vector), and the ray nearly antiparallel to an edge of K_j (2.5e-3 before the
+    small vectors e -+ tau were kept from FP64); mixed against FP64, relative mode 1e-6"""
+    from integrator2_gb300 import meshes
+    if case.startswith("ray"):
+        V, C = meshes.torus(2000, 500, 1.0, 0.1, scale=5e-4, jitter_rel=0.05, seed=2026)
+        i, j = 1982008, 1982508
+    else:
+        V, C = meshes.jittered_icosphere(5, 0.15, 2026)
+        i, j = (20270, 13870) if "second" not in case else (10030, 4910)
+    v2, c2 = _two_cells(V, C, i, j)
+    m = api.Mesh3D()
+    m.setGeometry(v2, c2)
+    m.prepareMesh(3.0)
+    rows = np.array([[0, 1], [1, 0]], np.int32)
+    out = {}
+    for prec in (api.PRECISION_FP64, api.PRECISION_MIXED):
+        it = api.NumericalIntegrator3D(m, api.qf3D13)
+        it.setErrorControl(api.RELATIVE_ERROR_CONTROL, 1e-6, 5)
+        it.setPrecision(prec)
+        ev = api.EvaluatorJ3DK(m, it)
+        ev.runClass(0, rows)
+        out[prec] = (ev.getResults(0), ev.getLevels(0))
+    (J64, L64), (J32, L32) = out[api.PRECISION_FP64], out[api.PRECISION_MIXED]
+    assert rel_rows(J32, J64).max() < 2e-6, (case, rel_rows(J32, J64), L64, L32)
+    assert (L32 <= L64 + 1).all(), (L64, L32)
