@@ -334,7 +334,7 @@ def run_batch(batch, flush, stream, steps, warmup):
 
 
 # kernels of one batched step, whatever the number of segments
-BATCH_LAUNCHES = 1 + 1 + 1 + (2 + 12) + 1 + 1 + 2
+BATCH_LAUNCHES = 1 + 1 + 2 + (2 + 12) + 1 + 1 + 2
 
 
 def uneven_batch_section(args):
@@ -589,12 +589,12 @@ def gpu_arm(args):
         roof["fp64"] = far_roofline(forms["fp64"], point_flops("far", w), float(cal[0]), "FP64 FMA peak measured live")
     acc = {name: accuracy(V, C, lists, f["J"], f["P"], f["levels"]) for name, f in forms.items()}
     n_cpu, dt_cpu, thr = cpu_run(V, C, lists, args.cpu_fraction, args.tol)
-    # kernels per step: adjacent classes run singular + tier 2 + adaptive potential (seed, 12
-    # depths, final); per-class chains add levels 0..5 + finalize per class, self pairs 1; the
+    # kernels per step: adjacent classes run singular + tiers 2 and 2b + adaptive potential (seed,
+    # 12 depths, final); per-class chains add levels 0..5 + finalize per class, self pairs 1; the
     # mixed chains add the needle fix-up (collect + FP64 pass) per non-self class.  The batched
-    # form runs each stage once for all segments: reset, singular, tier 2, seed, 12 depths,
-    # final, self, the cooperative level kernel, collect, fix-up.
-    pot_chain = 3 + 12
+    # form runs each stage once for all segments: reset, singular, tiers 2 and 2b, seed, 12
+    # depths, final, self, the cooperative level kernel, collect, fix-up.
+    pot_chain = 4 + 12
     launches = {"fp64": 2 * (1 + pot_chain + 7) + 7 + 1, "mixed": 2 * (1 + pot_chain + 7) + 7 + 1 + 3 * 2, "batch": BATCH_LAUNCHES}
     names4 = ("vertex", "edge", "near", "self")
     form_desc = {"batch": "mixed precision, batched: 4 class segments, one persistent cooperative level kernel, CUDA graph replay",

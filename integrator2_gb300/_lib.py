@@ -29,6 +29,7 @@ SIGNATURES = {
     "i2_mesh_set_geometry": (ctypes.c_int, [_vp, _vp, _i32, _vp, _i32]),
     "i2_mesh_prepare": (ctypes.c_int, [_vp, _d]),
     "i2_mesh_prepare_device": (ctypes.c_int, [_vp, _d, ctypes.c_int32]),
+    "i2_evaluator_run_stats": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_int32]),
     "i2_mesh_device_pairs": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp]),
     "i2_mesh_sizes": (ctypes.c_int, [_vp, _vp, _vp]),
     "i2_mesh_pair_count": (ctypes.c_int, [_vp, ctypes.c_int, _vp]),

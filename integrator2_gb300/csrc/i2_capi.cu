@@ -293,6 +293,7 @@ struct ClassResult {
     DevBuf<double> raw4, J, P;
     DevBuf<int> level;
     DevBuf<int> maxlev;            // class-wide last refinement level of the last run (adjoint)
+    DevBuf<int> counters;          // the run's 16 counters (i2_evaluator_run_stats)
     i2::RunConfig cfg;             // settings of the last run (adjoint)
     i2_precision precision = I2_PRECISION_FP64;
     std::vector<double> errors;  // antisymmetry deltas (host)
@@ -301,7 +302,7 @@ struct ClassResult {
 struct Workspace {
     DevBuf<double> cur, fin_a, fin_b, sing, padj;
     DevBuf<float> ctx_e;
-    DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list, tier2_list, pot_qcnt;
+    DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list, tier2_list, tier2b_list, pot_qcnt;
     DevBuf<i2::PotCellItem> pot_q_a, pot_q_b;
     DevBuf<long long> pot_fx;
     DevBuf<int2> pairs;
@@ -568,13 +569,14 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         W.padj.reserve(n);
         W.hard_list.reserve(n);
         W.tier2_list.reserve(n);
+        W.tier2b_list.reserve(n);
         W.pot_q_a.reserve(pot_queue_capacity(n));
         W.pot_q_b.reserve(pot_queue_capacity(n));
         W.pot_qcnt.reserve(16);
         W.pot_fx.reserve(n);
         if (ev->integrator->precision == I2_PRECISION_MIXED) W.ctx_e.reserve((size_t)i2::kVertexCtxFloats * n);
     }
-    // cnt[0..7] active counts per level, cnt[8] hard pairs, cnt[9] adaptive-potential stack overflows
+    // the run's counters (layout: kCnt* in i2_engine.h)
     I2_CHECK_CUDA(cudaMemsetAsync(W.cnt.ptr, 0, 16 * sizeof(int), ev->stream));
     I2_CHECK_CUDA(cudaMemsetAsync(W.maxlev.ptr, 0, sizeof(int), ev->stream));
     i2::ClassArgs A;
@@ -596,15 +598,16 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
     A.padj = W.padj.ptr;
     if ((cls == I2_SIMPLE_NEIGHBORS || cls == I2_ATTACHED_NEIGHBORS) && cfg.hard_tol > 0) {
         A.hard_list = W.hard_list.ptr;
-        A.hard_cnt = W.cnt.ptr + 8;
-        A.hard_overflow = W.cnt.ptr + 9;
+        A.hard_cnt = W.cnt.ptr + i2::kCntHard;
+        A.hard_overflow = W.cnt.ptr + i2::kCntOverflow;
         A.tier2_list = W.tier2_list.ptr;
+        A.tier2b_list = W.tier2b_list.ptr;
         A.pot_q_a = W.pot_q_a.ptr;
         A.pot_q_b = W.pot_q_b.ptr;
         A.pot_qcap = (int)pot_queue_capacity(n);
         A.pot_qcnt = W.pot_qcnt.ptr;
         A.pot_fx = W.pot_fx.ptr;
-        A.tier2_cnt = W.cnt.ptr + 10;
+        A.tier2_cnt = W.cnt.ptr + i2::kCntTier2;
         A.tier_tol = tier_tolerance(cfg);
         A.top_tol = top_tolerance(cfg, ev->integrator->precision == I2_PRECISION_MIXED);
     }
@@ -629,6 +632,8 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
     if (cls == I2_SELF) I2_CHECK_CUDA(cudaMemsetAsync(R.level.ptr, 0xff, n * sizeof(int), ev->stream));
     R.maxlev.reserve(1);
     I2_CHECK_CUDA(cudaMemcpyAsync(R.maxlev.ptr, W.maxlev.ptr, sizeof(int), cudaMemcpyDeviceToDevice, ev->stream));
+    R.counters.reserve(16);
+    I2_CHECK_CUDA(cudaMemcpyAsync(R.counters.ptr, W.cnt.ptr, 16 * sizeof(int), cudaMemcpyDeviceToDevice, ev->stream));
     R.cfg = cfg;
     R.precision = (i2_precision)ev->integrator->precision;
     // keep the evaluator's copies coherent when the caller supplied output buffers
@@ -666,7 +671,7 @@ struct BatchSegment {
     int64_t n = 0;
     DevBuf<int2> pairs;
     DevBuf<double> raw4, J, P, cur, fin_a, fin_b, sing, padj;
-    DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list, tier2_list, level, pot_qcnt;
+    DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list, tier2_list, tier2b_list, level, pot_qcnt;
     DevBuf<i2::PotCellItem> pot_q_a, pot_q_b;
     DevBuf<long long> pot_fx;
     DevBuf<float> ctx_e;
@@ -1159,6 +1164,29 @@ i2_status i2_evaluator_result_count(const i2_evaluator_t *ev, i2_pair_class cls,
     });
 }
 
+i2_status i2_evaluator_run_stats(const i2_evaluator_t *ev, i2_pair_class cls, int64_t *out, int32_t n)
+{
+    return guarded([&] {
+        I2_REQUIRE(ev && out, I2_ERR_INVALID_ARGUMENT, "null argument");
+        I2_REQUIRE(n >= I2_RUN_STATS, I2_ERR_INVALID_ARGUMENT, "stats array too short");
+        const ClassResult &R = ev->results[checked_class(cls)];
+        for (int k = 0; k < I2_RUN_STATS; ++k) out[k] = 0;
+        out[0] = R.n;
+        if (R.n == 0 || !R.counters.ptr) return;
+        int c[16], maxlev = 0;
+        I2_CHECK_CUDA(cudaStreamSynchronize(ev->stream));
+        I2_CHECK_CUDA(cudaMemcpy(c, R.counters.ptr, sizeof c, cudaMemcpyDeviceToHost));
+        I2_CHECK_CUDA(cudaMemcpy(&maxlev, R.maxlev.ptr, sizeof maxlev, cudaMemcpyDeviceToHost));
+        out[1] = c[i2::kCntTier2];
+        out[2] = c[i2::kCntTier2b];
+        out[3] = c[i2::kCntHard];
+        out[4] = c[i2::kCntOverflow];
+        out[5] = c[i2::kCntFixup];
+        out[6] = maxlev;
+        for (int L = 1; L <= 7; ++L) out[6 + L] = R.cfg.mode == i2::kFixed ? 0 : c[L];
+    });
+}
+
 i2_status i2_evaluator_copy_results(const i2_evaluator_t *ev, i2_pair_class cls, i2_channel channel, double *out, int64_t n)
 {
     return guarded([&] {
@@ -1277,7 +1305,7 @@ i2_status i2_batch_add(i2_batch_t *batch, const i2_mesh_t *mesh, i2_pair_class c
         sp->cnt.reserve(16); sp->maxlev.reserve(1);
         const bool adj = c == I2_SIMPLE_NEIGHBORS || c == I2_ATTACHED_NEIGHBORS;
         if (adj) {
-            sp->sing.reserve(4 * m); sp->padj.reserve(m); sp->hard_list.reserve(m); sp->tier2_list.reserve(m); sp->ctx_e.reserve((size_t)i2::kVertexCtxFloats * m);
+            sp->sing.reserve(4 * m); sp->padj.reserve(m); sp->hard_list.reserve(m); sp->tier2_list.reserve(m); sp->tier2b_list.reserve(m); sp->ctx_e.reserve((size_t)i2::kVertexCtxFloats * m);
             sp->pot_q_a.reserve(pot_queue_capacity(m)); sp->pot_q_b.reserve(pot_queue_capacity(m)); sp->pot_qcnt.reserve(16); sp->pot_fx.reserve(m);
         }
         i2::ClassArgs &A = sp->args;
@@ -1291,8 +1319,8 @@ i2_status i2_batch_add(i2_batch_t *batch, const i2_mesh_t *mesh, i2_pair_class c
         A.act_a = sp->act_a.ptr; A.act_b = sp->act_b.ptr; A.cnt = sp->cnt.ptr; A.maxlev = sp->maxlev.ptr;
         A.sing = sp->sing.ptr; A.padj = sp->padj.ptr;
         if (adj && batch->cfg.hard_tol > 0) {
-            A.hard_list = sp->hard_list.ptr; A.hard_cnt = sp->cnt.ptr + 8; A.hard_overflow = sp->cnt.ptr + 9;
-            A.tier2_list = sp->tier2_list.ptr; A.tier2_cnt = sp->cnt.ptr + 10;
+            A.hard_list = sp->hard_list.ptr; A.hard_cnt = sp->cnt.ptr + i2::kCntHard; A.hard_overflow = sp->cnt.ptr + i2::kCntOverflow;
+            A.tier2_list = sp->tier2_list.ptr; A.tier2_cnt = sp->cnt.ptr + i2::kCntTier2; A.tier2b_list = sp->tier2b_list.ptr;
             A.pot_q_a = sp->pot_q_a.ptr; A.pot_q_b = sp->pot_q_b.ptr; A.pot_qcap = (int)pot_queue_capacity(m);
             A.pot_qcnt = sp->pot_qcnt.ptr; A.pot_fx = sp->pot_fx.ptr;
             A.tier_tol = tier_tolerance(batch->cfg);

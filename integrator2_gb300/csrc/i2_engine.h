@@ -16,6 +16,13 @@ namespace i2 {
 constexpr int kHardMaxDepth = 12;
 // floats per common-vertex pair in ClassArgs::ctx_e
 constexpr int kVertexCtxFloats = 16;
+// ClassArgs::cnt, 16 ints per class run: [L] pairs still active after level L (L = 1..7),
+// then the counters below
+constexpr int kCntHard = 8;       // pairs handed to the adaptive potential rule
+constexpr int kCntOverflow = 9;   // adaptive-rule cells kept because a depth's list was full
+constexpr int kCntTier2 = 10;     // pairs the tier-1 potential check rejected
+constexpr int kCntFixup = 11;     // needle pairs recomputed in FP64 (mixed form)
+constexpr int kCntTier2b = 12;    // pairs that reached tier 2b
 // refinement / error-control modes
 enum { kFixed = 0, kAdaptiveCompat = 1, kAdaptiveRelative = 2 };
 
@@ -58,6 +65,7 @@ struct ClassArgs {
     double *padj = nullptr;                   // potential of adjacent pairs
     int *hard_list = nullptr, *hard_cnt = nullptr;  // adjacent pairs whose potential is refined adaptively
     int *tier2_list = nullptr, *tier2_cnt = nullptr;  // pairs re-integrated with the higher-order Duffy rule
+    int *tier2b_list = nullptr;               // pairs tier 2 rejected (count in cnt[kCntTier2b])
     int *hard_overflow = nullptr;             // cells accepted early because a depth's list was full (diagnostic)
     PotCellItem *pot_q_a = nullptr, *pot_q_b = nullptr;  // adaptive potential: cell lists of two successive depths
     int pot_qcap = 0;                         // capacity of each list (>= 4 x hard pairs)

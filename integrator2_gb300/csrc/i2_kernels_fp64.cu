@@ -13,6 +13,7 @@
 #include "i2_batch.cuh"
 #include "i2_engine.h"
 #include "i2_finalize.cuh"
+#include "i2_tiers.cuh"
 
 namespace i2 {
 
@@ -212,13 +213,7 @@ __global__ void __launch_bounds__(128) k_singular(ClassArgs A, QuadTables Q)
 }
 
 // tier 2: higher-order Duffy rule (16 x 16), kept when it agrees with the main rule; otherwise
-// tier 2b: the top rule (24 x 24), kept when it agrees with the 16 x 16 one; pairs where that
-// fails too go on to the adaptive rule (tier 3)
-__device__ __forceinline__ double warp_sum(double x)
-{
-    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
-    return x;
-}
+// the pair is listed for tier 2b (i2_tiers.cuh) with its 16 x 16 value
 
 template <int CLS>
 __global__ void __launch_bounds__(128) k_pot_tier2(ClassArgs A, QuadTables Q)
@@ -243,19 +238,15 @@ __global__ void __launch_bounds__(128) k_pot_tier2(ClassArgs A, QuadTables Q)
         const double sig = CLS == kEdge ? make_pot_edge(Ti, Tj, K, Si, pe) : 0.0;
         const double ph = warp_sum(duffy_partial<CLS>(Ti, K, F, pe, Q.hi_u, Q.hi_uw, Q.hi_nu, Q.hi_v, Q.hi_vw, Q.hi_nv, lane, 32)) + sig;
         const double pm = A.padj[t] * (4.0 * kPi);
-        if (fabs(ph - pm) <= A.tier_tol * fabs(ph)) {
-            if (lane == 0) A.padj[t] = kInv4Pi * ph;
-            continue;
-        }
-        // tier 2b: the top rule against the higher-order one (when the main rule was the
-        // inaccurate one, the 16 x 16 and 24 x 24 rules agree and the pair needs no adaptive rule)
-        const double pt = warp_sum(duffy_partial<CLS>(Ti, K, F, pe, Q.top_u, Q.top_uw, Q.top_nu, Q.top_v, Q.top_vw, Q.top_nv, lane, 32)) + sig;
         if (lane != 0) continue;
-        if (fabs(pt - ph) <= A.top_tol * fabs(pt)) {
-            A.padj[t] = kInv4Pi * pt;
+        if (fabs(ph - pm) <= A.tier_tol * fabs(ph)) {
+            A.padj[t] = kInv4Pi * ph;
         } else {
-            A.padj[t] = kInv4Pi * ph;  // the adaptive rule's tolerance base
-            A.hard_list[atomicAdd(A.hard_cnt, 1)] = t;
+            // tier 2b next (the top rule against this one: when the main rule was the inaccurate
+            // one, the 16 x 16 and 24 x 24 rules agree and the pair needs no adaptive rule); padj
+            // carries the 16 x 16 value, unscaled, until then
+            A.padj[t] = ph;
+            A.tier2b_list[atomicAdd(A.cnt + kCntTier2b, 1)] = t;
         }
     }
 }
@@ -675,6 +666,7 @@ void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const R
         k_singular<kEdge><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q);
         if (A.hard_list) {
             k_pot_tier2<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Q);
+            k_pot_tier2b<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Q, 1);
             pot_adaptive_chain<kEdge>(A, Q, cfg.hard_tol, persistent_blocks, s);
         }
         level_chain<kEdge>(A, Q, cfg, persistent_blocks, s);
@@ -683,6 +675,7 @@ void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const R
         k_singular<kVertex><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q);
         if (A.hard_list) {
             k_pot_tier2<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Q);
+            k_pot_tier2b<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Q, 1);
             pot_adaptive_chain<kVertex>(A, Q, cfg.hard_tol, persistent_blocks, s);
         }
         level_chain<kVertex>(A, Q, cfg, persistent_blocks, s);

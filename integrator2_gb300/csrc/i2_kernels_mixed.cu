@@ -12,6 +12,7 @@
 #include "i2_batch.cuh"
 #include "i2_engine.h"
 #include "i2_finalize.cuh"
+#include "i2_tiers.cuh"
 
 #include <cooperative_groups.h>
 
@@ -475,9 +476,9 @@ __device__ __forceinline__ float warp_sum_f(float x)
     return x;
 }
 
-// tier 2 in FP32 and, for the pairs it rejects, tier 2b in FP64, one warp per listed pair (the
-// lanes share each rule's points).  Tier 2b is FP64 because the FP32 rules can share a bias of a
-// few 1e-6 (a small, flat K_j beside a large K_i), and two biased rules agree with each other.
+// tier 2 in FP32, one warp per listed pair (the lanes share each rule's points); the pairs it
+// rejects are listed for tier 2b, which runs in FP64 because the FP32 rules can share a bias of
+// a few 1e-6 (a small, flat K_j beside a large K_i), and two biased rules agree with each other.
 template <int CLS>
 __device__ __forceinline__ void tier2_mixed_item(const ClassArgs &A, const QuadTablesF &Qf, const QuadTables &Q, int h, int lane)
 {
@@ -498,31 +499,9 @@ __device__ __forceinline__ void tier2_mixed_item(const ClassArgs &A, const QuadT
     const double ph = (double)warp_sum_f(duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, Kf, Ff, p1v, m_in, c, hh, Qf.hi_u, Qf.hi_uw,
                                                             Qf.hi_nu, Qf.hi_v, Qf.hi_vw, Qf.hi_nv, lane, 32)) + sig;
     const double pm = A.padj[t] * (4.0 * kPi);
-    if (fabs(ph - pm) <= A.tier_tol * fabs(ph)) {
-        if (lane == 0) A.padj[t] = kInv4Pi * ph;
-        return;
-    }
-    // tier 2b in FP64: 24 x 24 against 16 x 16
-    const PanelJ K = load_panel(A.panels, pr.y);
-    const Tri Ti = rotate(load_tri(A.panels, pr.x), si), Tj = rotate(Tri{K.A, K.B, K.C}, sj);
-    const FarCtx F = make_far_ctx(K);
-    PotEdge pe;
-    const double sg64 = CLS == kEdge ? make_pot_edge(Ti, Tj, K, Si, pe) : 0.0;
-    double ph64 = duffy_partial<CLS>(Ti, K, F, pe, Q.hi_u, Q.hi_uw, Q.hi_nu, Q.hi_v, Q.hi_vw, Q.hi_nv, lane, 32);
-    double pt64 = duffy_partial<CLS>(Ti, K, F, pe, Q.top_u, Q.top_uw, Q.top_nu, Q.top_v, Q.top_vw, Q.top_nv, lane, 32);
-    for (int off = 16; off > 0; off >>= 1) {
-        ph64 += __shfl_xor_sync(0xffffffffu, ph64, off);
-        pt64 += __shfl_xor_sync(0xffffffffu, pt64, off);
-    }
-    ph64 += sg64;
-    pt64 += sg64;
     if (lane != 0) return;
-    if (fabs(pt64 - ph64) <= A.top_tol * fabs(pt64)) {
-        A.padj[t] = kInv4Pi * pt64;
-    } else {
-        A.padj[t] = kInv4Pi * ph64;  // the adaptive rule's tolerance base
-        A.hard_list[atomicAdd(A.hard_cnt, 1)] = t;
-    }
+    if (fabs(ph - pm) <= A.tier_tol * fabs(ph)) A.padj[t] = kInv4Pi * ph;
+    else A.tier2b_list[atomicAdd(A.cnt + kCntTier2b, 1)] = t;  // tier 2b next, in FP64 (i2_tiers.cuh)
 }
 
 template <int CLS>
@@ -696,9 +675,9 @@ __global__ void __launch_bounds__(256) k_fp64_fixup(ClassArgs A, QuadTables Q, i
 void launch_fp64_fixup(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s)
 {
     if (A.n <= 0) return;
-    // cnt[11] counts the gathered pairs (the counters are cleared before every run); the active-list
+    // cnt[kCntFixup] counts the gathered pairs (the counters are cleared before every run); the active-list
     // buffer act_a is free after the level chain
-    int *list = A.act_a, *count = A.cnt + 11;
+    int *list = A.act_a, *count = A.cnt + kCntFixup;
     if (!list) return;  // fixed mode without active lists: nothing to gather into
     k_fixup_collect<<<persistent_blocks, 256, 0, s>>>(A, list, count);
     if (cls == kEdge) k_fp64_fixup<kEdge><<<persistent_blocks, 256, 0, s>>>(A, Q, cfg.mode, cfg.level, cfg.tol, cfg.max_level, list, count);
@@ -751,6 +730,7 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
         k_singular_mixed<kEdge><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
         if (A.hard_list) {
             k_pot_tier2_mixed<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Qf, Q);
+            k_pot_tier2b<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Q, 0);
             launch_pot_hard(kEdge, A, Q, cfg, persistent_blocks, s);
         }
         level_chain_mixed<kEdge>(A, Qf, cfg, persistent_blocks, s);
@@ -760,6 +740,7 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
         k_singular_mixed<kVertex><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
         if (A.hard_list) {
             k_pot_tier2_mixed<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Qf, Q);
+            k_pot_tier2b<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Q, 0);
             launch_pot_hard(kVertex, A, Q, cfg, persistent_blocks, s);
         }
         level_chain_mixed<kVertex>(A, Qf, cfg, persistent_blocks, s);
@@ -873,7 +854,23 @@ __global__ void __launch_bounds__(128) k_batch_tier2(const BatchSeg *__restrict_
     }
 }
 
-// segments whose pairs the fix-up gathers (into act_a, counted in cnt[11])
+__global__ void __launch_bounds__(128) k_batch_tier2b(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q)
+{
+    extern __shared__ long long prefix[];
+    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
+        return seg_adjacent(S) && S.A.hard_list ? S.A.cnt[kCntTier2b] : 0;
+    });
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < total; g += nwarps) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        if (S.cls == kEdge) tier2b_item<kEdge>(S.A, Q, false, (int)(g - prefix[sg]), lane);
+        else tier2b_item<kVertex>(S.A, Q, false, (int)(g - prefix[sg]), lane);
+    }
+}
+
+// segments whose pairs the fix-up gathers (into act_a, counted in cnt[kCntFixup])
 __device__ __forceinline__ bool seg_fixup(const BatchSeg &S) { return S.A.n > 0 && S.cls != kSelf && S.A.act_a; }
 
 __global__ void __launch_bounds__(256) k_batch_fixup_collect(const BatchSeg *__restrict__ segs, int nseg)
@@ -883,7 +880,7 @@ __global__ void __launch_bounds__(256) k_batch_fixup_collect(const BatchSeg *__r
     for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
         const int sg = seg_find(prefix, nseg, g);
         const ClassArgs &A = segs[sg].A;
-        fixup_collect_item(A, A.act_a, A.cnt + 11, g - prefix[sg]);
+        fixup_collect_item(A, A.act_a, A.cnt + kCntFixup, g - prefix[sg]);
     }
 }
 
@@ -892,7 +889,7 @@ __global__ void __launch_bounds__(256) k_batch_fp64_fixup(const BatchSeg *__rest
 {
     extern __shared__ long long prefix[];
     __shared__ double red[5 * 8];
-    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long { return seg_fixup(S) ? S.A.cnt[11] : 0; });
+    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long { return seg_fixup(S) ? S.A.cnt[kCntFixup] : 0; });
     // one block per gathered pair
     for (long long g = blockIdx.x; g < total; g += gridDim.x) {
         const int sg = seg_find(prefix, nseg, g);
@@ -924,6 +921,10 @@ void launch_batch_prelude(const BatchSeg *segs, int nseg, const BatchTotals &tot
             for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
                 const int nc = std::min(kBatchSegChunk, nseg - c0);
                 k_batch_tier2<<<persistent_blocks, tpb, seg_smem(nc), s>>>(segs + c0, nc, Qf, Q);
+            }
+            for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
+                const int nc = std::min(kBatchSegChunk, nseg - c0);
+                k_batch_tier2b<<<persistent_blocks, tpb, seg_smem(nc), s>>>(segs + c0, nc, Q);
             }
             launch_batch_pot_chain(segs, nseg, Q, cfg.hard_tol, persistent_blocks, s);
         }
