@@ -83,19 +83,33 @@ __device__ __forceinline__ PanelJf load_panel_f(const PanelF *__restrict__ P, in
 //   x projecting inside the edge: the ratio is (l_P + q_P)(l_Q - q_Q) / h^2, h the distance
 //   to the edge line, with h^2 = |o x tau|^2 taken from the NEARER endpoint (o_P x tau =
 //   o_Q x tau; from the far endpoint the cross product of a long offset cancels down to the
-//   short distance).  Close to the line (ratio > 2) the log of that product is exact to a few
-//   ulps; farther out log1p of (ratio - 1) keeps small logs accurate.  A point on the line
-//   itself (h = 0, where the caller's factor t_e is 0 too) gets a large finite value.
+//   short distance).  Close to the line (ratio > 2) log1p(ratio - 1) with ratio - 1 formed as
+//   (product - h^2) / h^2 (no cancellation there); farther out log1p of (ratio - 1) from the
+//   positive terms keeps small logs accurate.  A point on the line itself (h = 0, where the
+//   caller's factor t_e is 0 too) gets a large finite value.
+// Every case is log1p(n / d): the cases only select n and d, so the lanes of a warp, which hold
+// points in different cases, share one division and one log1pf instead of running each case's.
 __device__ __forceinline__ float edge_log_f32(float lP, float qP, f3 oP, float lQ, float qQ, f3 oQ, f3 tau, float L)
 {
     const float s = lP + lQ;
-    if (qQ >= 0.0f) return log1pf(L * (s + qP + qQ) / (s * (lQ + qQ)));
-    if (qP <= 0.0f) return log1pf(L * (s - qP - qQ) / (s * (lP - qP)));
     const f3 r = crossf(lP < lQ ? oP : oQ, tau);
     const float h2 = dotf(r, r);
     const float num = (lP + qP) * (lQ - qQ);
-    if (num > 2.0f * h2) return logf(fminf(num / h2, 3.0e38f));
-    return log1pf((lP + qP) * L * (s - qP - qQ) / (s * h2));
+    float n, d;
+    if (qQ >= 0.0f) {
+        n = L * (s + qP + qQ);
+        d = s * (lQ + qQ);
+    } else if (qP <= 0.0f) {
+        n = L * (s - qP - qQ);
+        d = s * (lP - qP);
+    } else if (num > 2.0f * h2) {
+        n = num - h2;
+        d = h2;
+    } else {
+        n = (lP + qP) * L * (s - qP - qQ);
+        d = s * h2;
+    }
+    return log1pf(fminf(n / d, 3.0e38f));
 }
 
 struct FarCtxF {

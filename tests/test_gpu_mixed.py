@@ -113,3 +113,39 @@ def test_mixed_vertex_asymptote_hard_cases(api, case):
     (J64, L64), (J32, L32) = out[api.PRECISION_FP64], out[api.PRECISION_MIXED]
     assert rel_rows(J32, J64).max() < 2e-6, (case, rel_rows(J32, J64), L64, L32)
     assert (L32 <= L64 + 1).all(), (L64, L32)
+
+
+def test_run_stats_are_consistent(api):
+    """i2_evaluator_run_stats: the counters of a run agree with each other and with the levels
+    the run reports"""
+    from integrator2_gb300 import meshes, pairs as P
+    V, C = meshes.jittered_icosphere(3, 0.3, 4)
+    pl = P.build_pairs(V, C)
+    m = api.Mesh3D()
+    m.setGeometry(V, C)
+    m.prepareMesh(3.0)
+    for prec in (api.PRECISION_FP64, api.PRECISION_MIXED):
+        it = api.NumericalIntegrator3D(m, api.qf3D13)
+        it.setErrorControl(api.RELATIVE_ERROR_CONTROL, 1e-6, 5)
+        it.setPrecision(prec)
+        ev = api.EvaluatorJ3DK(m, it)
+        for cls in (0, 1, 2, 3):
+            ev.runClass(cls, pl.by_class(cls))
+            st = ev.getRunStats(cls)
+            assert st["pairs"] == len(pl.by_class(cls))
+            if cls == 3:
+                continue
+            lev = ev.getLevels(cls)
+            assert st["max_level"] == lev.max()
+            # the pairs still unconverged after level L (below the last) went on to level L + 1;
+            # in the mixed form the FP64 fix-up re-refines its needle pairs afterwards and keeps
+            # its own levels for them
+            for L in range(1, st["max_level"]):
+                diff = abs(st["unconverged_after_level"][L - 1] - int((lev > L).sum()))
+                assert diff <= st["fp64_fixup"], (prec, cls, L, diff)
+            if cls == 2:
+                assert st["tier2"] == st["tier2b"] == st["adaptive_potential"] == 0
+            else:
+                assert 0 < st["tier2b"] <= st["tier2"] < st["pairs"] and st["adaptive_potential"] > 0
+            if prec == api.PRECISION_FP64:
+                assert st["fp64_fixup"] == 0
