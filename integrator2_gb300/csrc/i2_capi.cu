@@ -294,7 +294,8 @@ struct ClassResult {
     DevBuf<int> level;
     DevBuf<int> maxlev;            // class-wide last refinement level of the last run (adjoint)
     DevBuf<int> counters;          // the run's 16 counters (i2_evaluator_run_stats)
-    i2::RunConfig cfg;             // settings of the last run (adjoint)
+    i2::RunConfig cfg;             // settings of the last run, adaptive-rule tolerance as applied (adjoint)
+    double tier_tol = 0.0, top_tol = 0.0;  // tier bars of the last run (adjoint)
     i2_precision precision = I2_PRECISION_FP64;
     std::vector<double> errors;  // antisymmetry deltas (host)
 };
@@ -519,6 +520,16 @@ double tier_tolerance(const i2::RunConfig &cfg) { return std::max(10.0 * cfg.har
 // since two rules that agree only to the tier bar can share a bias of 1e-6 (a near-coplanar pair of
 // the sigma 0.3 jittered sphere)
 double top_tolerance(const i2::RunConfig &cfg, bool) { return tier_tolerance(cfg) / 10.0; }
+// relative tolerance of the adaptive potential rule: in the mixed form the FP64 rule stops at
+// 1e-7, 10x below the tier bar and 100x below the form's 1e-6 target, whatever tighter value the
+// integrator holds.  On the 20,480-triangle jittered sphere 1e-7 and 1e-8 give the same largest and
+// 99th-percentile rule errors against a 1e-11 reference (3,000 pairs per adjacent class) with half
+// the cells, and the FP32 bulk's own rounding (a few 1e-7) dominates either way.
+constexpr double kMixedAdaptiveTol = 1e-7;
+double adaptive_tolerance(const i2::RunConfig &cfg, bool mixed)
+{
+    return mixed && cfg.hard_tol > 0 ? std::max(cfg.hard_tol, kMixedAdaptiveTol) : cfg.hard_tol;
+}
 
 // cells per depth list of the adaptive potential (24 bytes each): every hard pair seeds 4 cells
 // at depth 1; deeper lists hold a few tens of thousands of cells on the meshes measured (C2: at
@@ -549,7 +560,10 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
     if (!out_J) { R.J.reserve(3 * n); out_J = R.J.ptr; }
     if (!out_P) { R.P.reserve(n); out_P = R.P.ptr; }
     R.level.reserve(n);
-    const i2::RunConfig cfg = ev->integrator->cfg;
+    const bool mixed = ev->integrator->precision == I2_PRECISION_MIXED;
+    i2::RunConfig cfg = ev->integrator->cfg;
+    const double tier_tol = tier_tolerance(cfg), top_tol = top_tolerance(cfg, mixed);
+    cfg.hard_tol = adaptive_tolerance(cfg, mixed);
     Workspace &W = ev->ws;
     const bool adaptive = cfg.mode != i2::kFixed && cls != I2_SELF;
     W.cur.reserve(5 * n);
@@ -608,8 +622,8 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         A.pot_qcnt = W.pot_qcnt.ptr;
         A.pot_fx = W.pot_fx.ptr;
         A.tier2_cnt = W.cnt.ptr + i2::kCntTier2;
-        A.tier_tol = tier_tolerance(cfg);
-        A.top_tol = top_tolerance(cfg, ev->integrator->precision == I2_PRECISION_MIXED);
+        A.tier_tol = tier_tol;
+        A.top_tol = top_tol;
     }
     A.raw4 = out_raw;
     A.J3 = out_J;
@@ -635,6 +649,8 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
     R.counters.reserve(16);
     I2_CHECK_CUDA(cudaMemcpyAsync(R.counters.ptr, W.cnt.ptr, 16 * sizeof(int), cudaMemcpyDeviceToDevice, ev->stream));
     R.cfg = cfg;
+    R.tier_tol = tier_tol;
+    R.top_tol = top_tol;
     R.precision = (i2_precision)ev->integrator->precision;
     // keep the evaluator's copies coherent when the caller supplied output buffers
     if (out_raw != R.raw4.ptr) { R.raw4.reserve(4 * n); I2_CHECK_CUDA(cudaMemcpyAsync(R.raw4.ptr, out_raw, 4 * n * sizeof(double), cudaMemcpyDeviceToDevice, ev->stream)); }
@@ -738,7 +754,9 @@ void batch_enqueue(i2_batch *b, cudaStream_t s, int threads, int bps, int gcap, 
     const int persistent = std::max(1, b->sms) * 8;
     const int nseg = (int)b->segs.size();
     if (nseg == 0) return;
-    i2::launch_batch_prelude(b->d_segs.ptr, nseg, b->totals, b->Q, b->Qf, b->cfg, persistent, s);
+    i2::RunConfig cfg = b->cfg;
+    cfg.hard_tol = adaptive_tolerance(cfg, true);  // the batched form is mixed precision
+    i2::launch_batch_prelude(b->d_segs.ptr, nseg, b->totals, b->Q, b->Qf, cfg, persistent, s);
     const int maxb = i2::batch_max_blocks_per_sm(threads, variant);
     I2_REQUIRE(maxb > 0, I2_ERR_CUDA, "batch kernel cannot be resident with this block size");
     const int blocks = std::max(1, b->sms) * std::max(1, std::min(bps > 0 ? bps : maxb, maxb));
@@ -1132,9 +1150,9 @@ i2_status i2_evaluator_backward_class(i2_evaluator_t *ev, i2_pair_class cls, con
         if (n == 0) return;
         const i2_mesh &m = *ev->mesh;
         I2_REQUIRE(m.on_device, I2_ERR_STATE, "mesh not on the device");
+        // the settings and tier bars of the forward pass (run_class_device)
         i2::RunConfig cfg = R.cfg;
-        // the tier bar of the forward pass (run_class_device)
-        const double tier_tol = tier_tolerance(cfg), top_tol = top_tolerance(cfg, R.precision == I2_PRECISION_MIXED);
+        const double tier_tol = R.tier_tol, top_tol = R.top_tol;
         if (ev->persistent_blocks == 0) {
             int dev = 0, sms = 0;
             I2_CHECK_CUDA(cudaGetDevice(&dev));
