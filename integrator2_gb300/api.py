@@ -165,7 +165,9 @@ class NumericalIntegrator3D:
     def setPrecision(self, precision: int) -> None:
         call("i2_integrator_set_precision", self._h, int(precision))
 
-    def setPotentialRule(self, n_radial=10, n_angular=8, grading=3, n_self=24) -> None:
+    def setPotentialRule(self, n_radial=10, n_angular=8, grading=3, n_self=0) -> None:
+        """graded Duffy rule of adjacent pairs; n_self points per edge piece of the self-pair rule
+        (0: 24 in FP64, 12 in the mixed form)"""
         call("i2_integrator_set_potential_rule", self._h, n_radial, n_angular, grading, n_self)
 
     def setHardPairTolerance(self, rel_tol: float) -> None:

@@ -225,7 +225,12 @@ struct i2_integrator {
     int order = 7;
     i2::RunConfig cfg;
     int precision = I2_PRECISION_FP64;
-    int pot_nu = 10, pot_nv = 8, pot_grade = 3, pot_nself = 24;
+    int pot_nu = 10, pot_nv = 8, pot_grade = 3;
+    // points per edge piece of the self-pair rule; 0: by precision, 24 in FP64 (1e-12 of a 96-point
+    // rule on the 20,480-triangle jittered sphere, needle cells included) and 12 in the mixed form
+    // (4e-8 there, against its 1e-6 target)
+    int pot_nself = 0;
+    int self_points() const { return pot_nself > 0 ? pot_nself : (precision == I2_PRECISION_MIXED ? 12 : 24); }
     i2::QuadTables tables() const
     {
         i2::QuadTables Q;
@@ -274,9 +279,10 @@ struct i2_integrator {
         Q.top_nu = i2::kDuffyTop;
         Q.top_nv = i2::kDuffyTop;
         duffy_rule(Q.top_nu, Q.top_nv, Q.top_u, Q.top_uw, Q.top_v, Q.top_vw);
-        gauss_legendre01(pot_nself, x, w);
-        Q.nself = pot_nself;
-        for (int k = 0; k < pot_nself; ++k) {
+        const int nself = self_points();
+        gauss_legendre01(nself, x, w);
+        Q.nself = nself;
+        for (int k = 0; k < nself; ++k) {
             const double t = x[k];
             Q.sx[k] = t * t * (3.0 - 2.0 * t);
             Q.sw[k] = w[k] * 6.0 * t * (1.0 - t);
@@ -521,11 +527,12 @@ double tier_tolerance(const i2::RunConfig &cfg) { return std::max(10.0 * cfg.har
 // the sigma 0.3 jittered sphere)
 double top_tolerance(const i2::RunConfig &cfg, bool) { return tier_tolerance(cfg) / 10.0; }
 // relative tolerance of the adaptive potential rule: in the mixed form the FP64 rule stops at
-// 1e-7, 10x below the tier bar and 100x below the form's 1e-6 target, whatever tighter value the
-// integrator holds.  On the 20,480-triangle jittered sphere 1e-7 and 1e-8 give the same largest and
-// 99th-percentile rule errors against a 1e-11 reference (3,000 pairs per adjacent class) with half
-// the cells, and the FP32 bulk's own rounding (a few 1e-7) dominates either way.
-constexpr double kMixedAdaptiveTol = 1e-7;
+// 2e-8, whatever tighter value the integrator holds (the FP32 bulk's own rounding is a few 1e-7).
+// Over every common-edge pair and 60,000 common-vertex pairs of the 20,480-triangle jittered
+// sphere, 2e-8 stays within 1.6e-8 of the 1e-8 result with 17-20 % fewer cells; looser values let
+// the rule's local acceptance test pass cells that are off: 3e-8 gave 4.7e-7 on two common-edge
+// pairs, 1e-7 gave 4.2e-6 on one.
+constexpr double kMixedAdaptiveTol = 2e-8;
 double adaptive_tolerance(const i2::RunConfig &cfg, bool mixed)
 {
     return mixed && cfg.hard_tol > 0 ? std::max(cfg.hard_tol, kMixedAdaptiveTol) : cfg.hard_tol;
@@ -1018,7 +1025,7 @@ i2_status i2_integrator_set_potential_rule(i2_integrator_t *it, int32_t n_radial
         I2_REQUIRE(n_radial >= 2 && n_radial <= i2::kMaxDuffy && n_angular >= 2 && n_angular <= i2::kMaxDuffy,
                    I2_ERR_INVALID_ARGUMENT, "Duffy rule sizes must be 2..16");
         I2_REQUIRE(grading >= 1 && grading <= 6, I2_ERR_INVALID_ARGUMENT, "grading must be 1..6");
-        I2_REQUIRE(n_self >= 2 && n_self <= i2::kMaxSelf, I2_ERR_INVALID_ARGUMENT, "self rule size must be 2..32");
+        I2_REQUIRE(n_self == 0 || (n_self >= 2 && n_self <= i2::kMaxSelf), I2_ERR_INVALID_ARGUMENT, "self rule size must be 0 or 2..32");
         it->pot_nu = n_radial;
         it->pot_nv = n_angular;
         it->pot_grade = grading;

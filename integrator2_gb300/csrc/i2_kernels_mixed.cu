@@ -517,10 +517,10 @@ __global__ void __launch_bounds__(128) k_pot_tier2_mixed(ClassArgs A, QuadTables
 // A pair that holds a needle cell (a corner angle below 3 degrees) is ill-conditioned: its J is
 // a small difference of large parts, and FP32 rounding of the bulk is amplified by a few thousand
 // there (measured: errors up to 1e-3 on the 20,480-triangle jittered sphere, whose two needles
-// have corners of 0.6 and 1.5 degrees).  After the mixed chain has finished, one warp per such
-// pair recomputes its regular part in FP64 -- one whole block per such pair, the threads striding
-// over the 4^L sub-cells, since a few pairs at level 5 would otherwise set the time -- and
-// finalises J (and the disjoint class's potential) again.  Other pairs cost two loads.
+// have corners of 0.6 and 1.5 degrees).  After the mixed chain has finished, each such pair's
+// regular part is recomputed in FP64 by one whole block, the threads striding over the 4^L
+// sub-cells (a few pairs at level 5 would otherwise set the time), and J (and the disjoint
+// class's potential) is finalised again.  Other pairs cost two loads.
 template <int CLS>
 struct FixupPair {
     PanelJ K;
@@ -575,17 +575,23 @@ __device__ acc5 fixup_level_sum(const FixupPair<CLS> &p, const QuadTables &Q, in
 
 // the pairs that hold a needle cell, gathered into list[0 .. *count) (the class's active-list
 // buffer, free once the level chain has finished)
+// A disjoint pair needs it only when K_j, the cell integrated in closed form, is the needle: its
+// two long, nearly antiparallel edges make Psi a small difference of nearly equal edge terms.  A
+// needle K_i is only a small area the quadrature runs over.  Adjacent pairs share vertices with
+// both cells, so either cell's needle counts there.
+template <int CLS>
 __device__ __forceinline__ void fixup_collect_item(const ClassArgs &A, int *list, int *count, long long t)
 {
     const double c3 = 0.99862953475457387;  // cos 3 degrees
     const int2 pr = A.pairs[t];
-    if (A.panels[pr.x].v[2].w > c3 || A.panels[pr.y].v[2].w > c3) list[atomicAdd(count, 1)] = (int)t;
+    if ((CLS != kFar && A.panels[pr.x].v[2].w > c3) || A.panels[pr.y].v[2].w > c3) list[atomicAdd(count, 1)] = (int)t;
 }
 
+template <int CLS>
 __global__ void __launch_bounds__(256) k_fixup_collect(ClassArgs A, int *list, int *count)
 {
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < A.n; t += (long long)gridDim.x * blockDim.x)
-        fixup_collect_item(A, list, count, t);
+        fixup_collect_item<CLS>(A, list, count, t);
 }
 
 // pair t, by the whole block (red: 5 doubles per warp of shared memory)
@@ -679,7 +685,8 @@ void launch_fp64_fixup(int cls, const ClassArgs &A, const QuadTables &Q, const R
     // buffer act_a is free after the level chain
     int *list = A.act_a, *count = A.cnt + kCntFixup;
     if (!list) return;  // fixed mode without active lists: nothing to gather into
-    k_fixup_collect<<<persistent_blocks, 256, 0, s>>>(A, list, count);
+    if (cls == kFar) k_fixup_collect<kFar><<<persistent_blocks, 256, 0, s>>>(A, list, count);
+    else k_fixup_collect<kEdge><<<persistent_blocks, 256, 0, s>>>(A, list, count);
     if (cls == kEdge) k_fp64_fixup<kEdge><<<persistent_blocks, 256, 0, s>>>(A, Q, cfg.mode, cfg.level, cfg.tol, cfg.max_level, list, count);
     else if (cls == kVertex) k_fp64_fixup<kVertex><<<persistent_blocks, 256, 0, s>>>(A, Q, cfg.mode, cfg.level, cfg.tol, cfg.max_level, list, count);
     else if (cls == kFar) k_fp64_fixup<kFar><<<persistent_blocks, 256, 0, s>>>(A, Q, cfg.mode, cfg.level, cfg.tol, cfg.max_level, list, count);
@@ -880,7 +887,8 @@ __global__ void __launch_bounds__(256) k_batch_fixup_collect(const BatchSeg *__r
     for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
         const int sg = seg_find(prefix, nseg, g);
         const ClassArgs &A = segs[sg].A;
-        fixup_collect_item(A, A.act_a, A.cnt + kCntFixup, g - prefix[sg]);
+        if (segs[sg].cls == kFar) fixup_collect_item<kFar>(A, A.act_a, A.cnt + kCntFixup, g - prefix[sg]);
+        else fixup_collect_item<kEdge>(A, A.act_a, A.cnt + kCntFixup, g - prefix[sg]);
     }
 }
 
