@@ -338,28 +338,30 @@ BATCH_LAUNCHES = 1 + 1 + 2 + (2 + 12) + 1 + 1 + 2
 
 
 def uneven_batch_section(args):
-    """Many-mesh workload: 48 seeded closed meshes of uneven size (500-6,000 triangles,
+    """Many-mesh workload (C3): 48 seeded closed meshes of uneven size (500-60,000 triangles,
     log-uniform) and scale (5e-4 .. 1e2): ellipsoids, tori, jittered spheres; all four pair classes
-    (near < 3h); relative 1e-6, mixed precision.  The batched form (every segment in one graph
+    (near < 3h, lists built on the GPU, ordered as the reference's (i, j) rows followed by the
+    reversed rows); relative 1e-6, mixed precision.  The batched form (every segment in one graph
     replay) against the same meshes run class by class through their own evaluators, all on one
     stream; CUDA events, 3 steps after 3 warm-up steps."""
     import torch
-    from integrator2_gb300 import api, meshes, pairs
-    mset = meshes.uneven_mesh_set(2026, 48, 500, 6000)
+    from integrator2_gb300 import api, meshes
+    mset = meshes.uneven_mesh_set(2026, 48, 500, 60000)
     stream = torch.cuda.Stream()
     evs, segs_dev, total = [], [], 0
     batch = None
     for V, C, kind, scale in mset:
-        pl = pairs.build_pairs(V, C, NEAR)
         m = api.Mesh3D()
         m.setGeometry(V, C)
-        m.prepareMesh(NEAR)
+        m.prepareMeshDevice(NEAR)
         it = api.NumericalIntegrator3D(m, api.qf3D13)
         it.setErrorControl(api.RELATIVE_ERROR_CONTROL, args.tol, 5)
         it.setPrecision(api.PRECISION_MIXED)
         ev = api.EvaluatorJ3DK(m, it)
         ev.setStream(stream.cuda_stream)
-        lists = [np.ascontiguousarray(pl.by_class(c)) for c in CLASSES]
+        unordered = [m.getSimpleNeighbors()[:, :2], m.getAttachedNeighbors()[:, :2], m.getNotNeighbors()[:, :2]]
+        lists = [np.ascontiguousarray(np.concatenate([u, u[:, ::-1]])) for u in unordered]
+        lists.append(np.ascontiguousarray(m.getSelfPairs()[:, :2]))
         dev = [(torch.from_numpy(l).to("cuda"), torch.empty(len(l), 3, dtype=torch.float64, device="cuda"),
                 torch.empty(len(l), dtype=torch.float64, device="cuda")) for l in lists]
         if batch is None:
@@ -392,7 +394,7 @@ def uneven_batch_section(args):
     ms_per_class = timed(per_class_step)
     shape = batch.autotune()
     ms_batch = timed(batch.run)
-    return {"workload": "48 meshes (ellipsoids, tori, jittered spheres), 500-6000 triangles, scales 5e-4..1e2, near < 3h, relative 1e-6",
+    return {"workload": "C3: 48 meshes (ellipsoids, tori, jittered spheres), 500-60000 triangles, scales 5e-4..1e2, near < 3h, relative 1e-6",
             "triangles": int(sum(len(c) for _, c, _, _ in mset)), "pairs": int(total),
             "batched": {"value": total / (ms_batch * 1e-3), "ms_per_step": ms_batch, "cuda_graph": batch.usesGraph(),
                         "shape": [int(x) for x in shape], "launches": f"{BATCH_LAUNCHES} for all {4 * len(mset)} segments"},
