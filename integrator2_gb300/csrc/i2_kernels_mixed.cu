@@ -861,7 +861,8 @@ __global__ void __launch_bounds__(128) k_batch_tier2(const BatchSeg *__restrict_
     }
 }
 
-__global__ void __launch_bounds__(128) k_batch_tier2b(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q)
+// three blocks per SM, as k_pot_tier2b
+__global__ void __launch_bounds__(128, 3) k_batch_tier2b(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q)
 {
     extern __shared__ long long prefix[];
     const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {

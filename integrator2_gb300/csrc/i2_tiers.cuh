@@ -47,8 +47,10 @@ __device__ __forceinline__ void tier2b_item(const ClassArgs &A, const QuadTables
     }
 }
 
+// three 128-thread blocks per SM (at most 170 registers, a few spilled) rather than two at the
+// unconstrained 178: the pass is latency-bound at the 1/64 FP64 rate
 template <int CLS>
-__global__ void __launch_bounds__(128) k_pot_tier2b(ClassArgs A, QuadTables Q, int hi_known)
+__global__ void __launch_bounds__(128, 3) k_pot_tier2b(ClassArgs A, QuadTables Q, int hi_known)
 {
     const int count = A.cnt[kCntTier2b];
     const int lane = threadIdx.x & 31;
