@@ -309,9 +309,10 @@ struct ClassResult {
 struct Workspace {
     DevBuf<double> cur, fin_a, fin_b, sing, padj;
     DevBuf<float> ctx_e;
-    DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list, tier2_list, tier2b_list, pot_qcnt;
+    DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list, tier2_list, tier2b_list, pot_qcnt, fix_deep;
     DevBuf<i2::PotCellItem> pot_q_a, pot_q_b;
     DevBuf<long long> pot_fx;
+    DevBuf<double> fix_base, fix_part;
     DevBuf<int2> pairs;
 };
 
@@ -582,7 +583,12 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         W.act_b.reserve(n);
     }
     // the mixed form gathers its needle-cell pairs for the FP64 fix-up into act_a
-    if (ev->integrator->precision == I2_PRECISION_MIXED) W.act_a.reserve(n);
+    if (mixed) {
+        W.act_a.reserve(n);
+        W.fix_deep.reserve(i2::kFixDeepCap);
+        W.fix_base.reserve(5 * i2::kFixDeepCap);
+        W.fix_part.reserve(5 * i2::kFixDeepSlots * i2::kFixDeepCap);
+    }
     W.cnt.reserve(16);
     W.maxlev.reserve(1);
     if (cls == I2_SIMPLE_NEIGHBORS || cls == I2_ATTACHED_NEIGHBORS) {
@@ -617,6 +623,12 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
     A.maxlev = W.maxlev.ptr;
     A.sing = W.sing.ptr;
     A.padj = W.padj.ptr;
+    if (mixed) {
+        A.fix_deep = W.fix_deep.ptr;
+        A.fix_base = W.fix_base.ptr;
+        A.fix_part = W.fix_part.ptr;
+        A.fix_cap = i2::kFixDeepCap;
+    }
     if ((cls == I2_SIMPLE_NEIGHBORS || cls == I2_ATTACHED_NEIGHBORS) && cfg.hard_tol > 0) {
         A.hard_list = W.hard_list.ptr;
         A.hard_cnt = W.cnt.ptr + i2::kCntHard;
@@ -694,7 +706,8 @@ struct BatchSegment {
     int64_t n = 0;
     DevBuf<int2> pairs;
     DevBuf<double> raw4, J, P, cur, fin_a, fin_b, sing, padj;
-    DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list, tier2_list, tier2b_list, level, pot_qcnt;
+    DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list, tier2_list, tier2b_list, level, pot_qcnt, fix_deep;
+    DevBuf<double> fix_base, fix_part;
     DevBuf<i2::PotCellItem> pot_q_a, pot_q_b;
     DevBuf<long long> pot_fx;
     DevBuf<float> ctx_e;
@@ -1328,6 +1341,11 @@ i2_status i2_batch_add(i2_batch_t *batch, const i2_mesh_t *mesh, i2_pair_class c
         sp->cur.reserve(5 * m); sp->fin_a.reserve(5 * m); sp->fin_b.reserve(5 * m);
         sp->stop.reserve(m); sp->act_a.reserve(m); sp->act_b.reserve(m);
         sp->cnt.reserve(16); sp->maxlev.reserve(1);
+        if (c != I2_SELF && n > 0) {
+            // deep FP64 fix-up pairs of this segment (at most the segment's pairs)
+            const int cap = (int)std::min<int64_t>(n, i2::kFixDeepCap);
+            sp->fix_deep.reserve(cap); sp->fix_base.reserve(5 * (size_t)cap); sp->fix_part.reserve(5 * (size_t)i2::kFixDeepSlots * cap);
+        }
         const bool adj = c == I2_SIMPLE_NEIGHBORS || c == I2_ATTACHED_NEIGHBORS;
         if (adj) {
             sp->sing.reserve(4 * m); sp->padj.reserve(m); sp->hard_list.reserve(m); sp->tier2_list.reserve(m); sp->tier2b_list.reserve(m); sp->ctx_e.reserve((size_t)i2::kVertexCtxFloats * m);
@@ -1352,6 +1370,10 @@ i2_status i2_batch_add(i2_batch_t *batch, const i2_mesh_t *mesh, i2_pair_class c
             A.top_tol = top_tolerance(batch->cfg, true);
         }
         A.raw4 = sp->raw4.ptr; A.J3 = sp->J.ptr; A.P = sp->P.ptr; A.level_out = sp->level.ptr;
+        if (sp->fix_deep.ptr) {
+            A.fix_deep = sp->fix_deep.ptr; A.fix_base = sp->fix_base.ptr; A.fix_part = sp->fix_part.ptr;
+            A.fix_cap = (int)sp->fix_deep.count;
+        }
         if (segment) *segment = (int32_t)batch->segs.size();
         batch->segs.push_back(std::move(sp));
         batch->dirty = true;

@@ -23,6 +23,11 @@ constexpr int kCntOverflow = 9;   // adaptive-rule cells kept because a depth's 
 constexpr int kCntTier2 = 10;     // pairs the tier-1 potential check rejected
 constexpr int kCntFixup = 11;     // needle pairs recomputed in FP64 (mixed form)
 constexpr int kCntTier2b = 12;    // pairs that reached tier 2b
+constexpr int kCntFixDeep = 13;   // FP64 fix-up pairs whose deeper levels were spread over the GPU
+// FP64 fix-up pairs per class run whose levels 4..5 can be spread over the GPU (820 KB of chunk
+// sums); further deep pairs stay with their own block
+constexpr int kFixDeepCap = 1024;
+constexpr int kFixDeepSlots = 20;  // chunks of 64 sub-cells in levels 4 and 5
 // refinement / error-control modes
 enum { kFixed = 0, kAdaptiveCompat = 1, kAdaptiveRelative = 2 };
 
@@ -66,6 +71,11 @@ struct ClassArgs {
     int *hard_list = nullptr, *hard_cnt = nullptr;  // adjacent pairs whose potential is refined adaptively
     int *tier2_list = nullptr, *tier2_cnt = nullptr;  // pairs re-integrated with the higher-order Duffy rule
     int *tier2b_list = nullptr;               // pairs tier 2 rejected (count in cnt[kCntTier2b])
+    // FP64 fix-up pairs whose levels 4..5 run spread over the GPU: the pairs, their level-3 sums
+    // (5 doubles each), 20 chunk sums each (5 doubles), at most fix_cap pairs
+    int *fix_deep = nullptr;
+    double *fix_base = nullptr, *fix_part = nullptr;
+    int fix_cap = 0;
     int *hard_overflow = nullptr;             // cells accepted early because a depth's list was full (diagnostic)
     PotCellItem *pot_q_a = nullptr, *pot_q_b = nullptr;  // adaptive potential: cell lists of two successive depths
     int pot_qcap = 0;                         // capacity of each list (>= 4 x hard pairs)

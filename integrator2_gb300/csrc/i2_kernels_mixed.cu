@@ -596,12 +596,12 @@ __global__ void __launch_bounds__(256) k_fixup_collect(ClassArgs A, int *list, i
 
 // pair t, by the whole block (red: 5 doubles per warp of shared memory)
 template <int CLS>
-__device__ void fp64_fixup_item(const ClassArgs &A, const QuadTables &Q, int mode, int fixed_level, double tol, int kmax, int t,
-                                double *red)
+__device__ __forceinline__ FixupPair<CLS> fixup_pair(const ClassArgs &A, int t, d3 &nj, d3 &spsi, double &sth)
 {
     const int2 pr = A.pairs[t];
     const double4_32a ni4 = A.panels[pr.x].v[3], nj4 = A.panels[pr.y].v[3];
-    const d3 ni = mk(ni4.x, ni4.y, ni4.z), nj = mk(nj4.x, nj4.y, nj4.z);
+    const d3 ni = mk(ni4.x, ni4.y, ni4.z);
+    nj = mk(nj4.x, nj4.y, nj4.z);
     FixupPair<CLS> p;
     p.K = load_panel(A.panels, pr.y);
     p.Ti = load_tri(A.panels, pr.x);
@@ -618,13 +618,77 @@ __device__ void fp64_fixup_item(const ClassArgs &A, const QuadTables &Q, int mod
             p.Vx = make_vertex_ctx(p.K, sj, ni, p.Si);
         }
     }
-    d3 spsi = mk(0, 0, 0);
-    double sth = 0.0;
+    spsi = mk(0, 0, 0);
+    sth = 0.0;
     if (CLS != kFar) {
         const double *sg = A.sing + 4 * (long long)t;
         spsi = mk(sg[0], sg[1], sg[2]);
         sth = sg[3];
     }
+    return p;
+}
+
+// the relative criterion between successive levels' sums (J, and P for the disjoint class)
+template <int CLS>
+__device__ __forceinline__ bool fixup_unconverged(const acc5 &nxt, const acc5 &prev, const FixupPair<CLS> &p, d3 nj, d3 spsi, double sth,
+                                                  double tol)
+{
+    const d3 Jc = finalize_j(CLS, mk(nxt.px, nxt.py, nxt.pz) + spsi, nxt.th + sth, nj, p.Si);
+    const d3 dJ = kInv4Pi * ((nxt.th - prev.th) * nj + cross(mk(nxt.px - prev.px, nxt.py - prev.py, nxt.pz - prev.pz), nj));
+    bool unconv = norm(dJ) > tol * norm(Jc);
+    if (CLS == kFar) unconv = unconv || fabs(nxt.pot - prev.pot) > tol * fabs(nxt.pot);
+    return unconv;
+}
+
+// the kept level's sums plus the singular part, finalised into the pair's outputs
+template <int CLS>
+__device__ __forceinline__ void fixup_store(const ClassArgs &A, int t, const acc5 &acc, const FixupPair<CLS> &p, d3 nj, d3 spsi, double sth,
+                                            int kept, int mode)
+{
+    const d3 psi = mk(acc.px, acc.py, acc.pz) + spsi;
+    const double th = acc.th + sth;
+    const d3 J = finalize_j(CLS, psi, th, nj, p.Si);
+    double *raw = A.raw4 + 4 * (long long)t;
+    raw[0] = psi.x; raw[1] = psi.y; raw[2] = psi.z; raw[3] = th;
+    double *Jo = A.J3 + 3 * (long long)t;
+    Jo[0] = J.x; Jo[1] = J.y; Jo[2] = J.z;
+    if (CLS == kFar) A.P[t] = kInv4Pi * acc.pot;
+    if (mode == kAdaptiveRelative) {
+        A.stop[t] = kept;
+        if (A.level_out) A.level_out[t] = kept;
+    }
+}
+
+// the level the compat and fixed modes keep for pair t
+__device__ __forceinline__ int fixup_kept_level(const ClassArgs &A, int mode, int fixed_level, int t)
+{
+    if (mode == kFixed) return fixed_level;
+    const int L = A.stop[t];
+    return ((*A.maxlev - L) & 1) ? (L > 0 ? L - 1 : 0) : L;
+}
+
+// Levels deeper than kFixDirect are spread over the GPU: the block that owns a pair stops after
+// level kFixDirect, lists the pair (up to ClassArgs::fix_cap pairs; later ones stay in the block)
+// with its last sums, and k_fix_spread integrates levels kFixDirect+1..5 in chunks of kFixChunk
+// sub-cells, one block per chunk; k_fix_finish adds the chunks in order and decides.  A needle pair
+// refined to level 5 is 17.7 MFLOP of FP64, about 2 ms on one SM, which otherwise sets the length
+// of the whole pass.
+constexpr int kFixDirect = 3;
+constexpr int kFixChunk = 64;
+constexpr int kFixSlots = kFixDeepSlots;  // chunks of levels 4 and 5: 4 + 16
+static_assert(kFixSlots == 4 + 16 && kFixChunk * 4 == 256, "chunk layout of levels 4 and 5");
+__device__ __forceinline__ int fix_slot0(int L) { return L == 4 ? 0 : 4; }
+__device__ __forceinline__ int fix_chunks(int L) { return (1 << (2 * L)) / kFixChunk; }
+
+// pair t, by the whole block (red: 5 doubles per warp of shared memory)
+template <int CLS>
+__device__ void fp64_fixup_item(const ClassArgs &A, const QuadTables &Q, int mode, int fixed_level, double tol, int kmax, int t,
+                                double *red)
+{
+    __shared__ int deep_slot;
+    d3 nj, spsi;
+    double sth;
+    const FixupPair<CLS> p = fixup_pair<CLS>(A, t, nj, spsi, sth);
     acc5 acc;
     int kept;
     if (mode == kAdaptiveRelative) {
@@ -634,38 +698,143 @@ __device__ void fp64_fixup_item(const ClassArgs &A, const QuadTables &Q, int mod
         acc = fixup_level_sum<CLS>(p, Q, 0, red);
         kept = 0;
         for (int L = 1; L <= kmax; ++L) {
+            if (L > kFixDirect && A.fix_deep) {
+                if (threadIdx.x == 0) {
+                    const int k = atomicAdd(A.cnt + kCntFixDeep, 1);
+                    deep_slot = k < A.fix_cap ? k : -1;
+                    if (deep_slot >= 0) {
+                        A.fix_deep[k] = t;
+                        store5(A.fix_base + 5 * (long long)k, acc);
+                    }
+                }
+                __syncthreads();
+                const int k = deep_slot;
+                __syncthreads();
+                if (k >= 0) return;  // k_fix_spread and k_fix_finish take it from here
+            }
             const acc5 nxt = fixup_level_sum<CLS>(p, Q, L, red);
-            const d3 Jc = finalize_j(CLS, mk(nxt.px, nxt.py, nxt.pz) + spsi, nxt.th + sth, nj, p.Si);
-            const d3 dJ = kInv4Pi * ((nxt.th - acc.th) * nj + cross(mk(nxt.px - acc.px, nxt.py - acc.py, nxt.pz - acc.pz), nj));
-            bool unconv = norm(dJ) > tol * norm(Jc);
-            if (CLS == kFar) unconv = unconv || fabs(nxt.pot - acc.pot) > tol * fabs(nxt.pot);
+            const bool unconv = fixup_unconverged<CLS>(nxt, acc, p, nj, spsi, sth, tol);
             acc = nxt;
             kept = L;
             if (!unconv) break;
         }
     } else {
-        kept = fixed_level;
-        if (mode != kFixed) {
-            const int L = A.stop[t];
-            kept = ((*A.maxlev - L) & 1) ? (L > 0 ? L - 1 : 0) : L;
+        kept = fixup_kept_level(A, mode, fixed_level, t);
+        if (kept > kFixDirect && A.fix_deep) {
+            if (threadIdx.x == 0) {
+                const int k = atomicAdd(A.cnt + kCntFixDeep, 1);
+                deep_slot = k < A.fix_cap ? k : -1;
+                if (deep_slot >= 0) A.fix_deep[k] = t;
+            }
+            __syncthreads();
+            const int k = deep_slot;
+            __syncthreads();
+            if (k >= 0) return;
         }
         acc = fixup_level_sum<CLS>(p, Q, kept, red);
     }
+    if (threadIdx.x == 0) fixup_store<CLS>(A, t, acc, p, nj, spsi, sth, kept, mode);
+    __syncthreads();
+}
+
+// one chunk of one deep level of listed pair k, by the whole block (kFixChunk threads, one
+// sub-cell each); the chunk's sums go to their own slot, so the finish pass adds them in order
+template <int CLS>
+__device__ void fix_spread_item(const ClassArgs &A, const QuadTables &Q, int mode, int fixed_level, int kmax, int k, int slot, double *red)
+{
+    const int L = slot < 4 ? 4 : 5;
+    const int t = A.fix_deep[k];
+    const bool wanted = L <= kmax && (mode == kAdaptiveRelative || fixup_kept_level(A, mode, fixed_level, t) == L);
+    if (!wanted) return;  // uniform over the block
+    d3 nj, spsi;
+    double sth;
+    const FixupPair<CLS> p = fixup_pair<CLS>(A, t, nj, spsi, sth);
+    const int sc = (slot - fix_slot0(L)) * kFixChunk + threadIdx.x;
+    const Tri T = subcell(p.Ti, L, sc);
+    const double Ssub = p.Si * ldexp(1.0, -2 * L);
+    acc5 acc = zero5();
+    for (int g = 0; g < Q.npts; ++g) {
+        const d3 x = Q.L1[g] * T.a + Q.L2[g] * T.b + Q.L3[g] * T.c;
+        d3 psi;
+        double th, pot = 0.0;
+        if (CLS == kFar) far_integrand(x, p.K, p.F, psi, th, pot);
+        else if (CLS == kEdge) edge_integrand(x, p.K, p.E, psi, th);
+        else vertex_integrand(x, p.K, p.Vx, psi, th);
+        axpy5(acc, Q.w[g], psi, th, pot);
+    }
+    acc.px *= Ssub; acc.py *= Ssub; acc.pz *= Ssub; acc.th *= Ssub; acc.pot *= Ssub;
+    for (int off = 16; off > 0; off >>= 1) {
+        acc.px += __shfl_xor_sync(0xffffffffu, acc.px, off);
+        acc.py += __shfl_xor_sync(0xffffffffu, acc.py, off);
+        acc.pz += __shfl_xor_sync(0xffffffffu, acc.pz, off);
+        acc.th += __shfl_xor_sync(0xffffffffu, acc.th, off);
+        acc.pot += __shfl_xor_sync(0xffffffffu, acc.pot, off);
+    }
+    if ((threadIdx.x & 31) == 0) store5(red + 5 * (threadIdx.x >> 5), acc);
+    __syncthreads();
     if (threadIdx.x == 0) {
-        const d3 psi = mk(acc.px, acc.py, acc.pz) + spsi;
-        const double th = acc.th + sth;
-        const d3 J = finalize_j(CLS, psi, th, nj, p.Si);
-        double *raw = A.raw4 + 4 * (long long)t;
-        raw[0] = psi.x; raw[1] = psi.y; raw[2] = psi.z; raw[3] = th;
-        double *Jo = A.J3 + 3 * (long long)t;
-        Jo[0] = J.x; Jo[1] = J.y; Jo[2] = J.z;
-        if (CLS == kFar) A.P[t] = kInv4Pi * acc.pot;
-        if (mode == kAdaptiveRelative) {
-            A.stop[t] = kept;
-            if (A.level_out) A.level_out[t] = kept;
+        acc5 tot = zero5();
+        for (int w = 0; w < kFixChunk / 32; ++w) {
+            const acc5 v = load5(red + 5 * w);
+            tot.px += v.px; tot.py += v.py; tot.pz += v.pz; tot.th += v.th; tot.pot += v.pot;
         }
+        store5(A.fix_part + 5 * ((long long)k * kFixSlots + slot), tot);
     }
     __syncthreads();
+}
+
+template <int CLS>
+__device__ __forceinline__ acc5 fix_level_total(const ClassArgs &A, int k, int L)
+{
+    acc5 tot = zero5();
+    for (int c = 0; c < fix_chunks(L); ++c) {
+        const acc5 v = load5(A.fix_part + 5 * ((long long)k * kFixSlots + fix_slot0(L) + c));
+        tot.px += v.px; tot.py += v.py; tot.pz += v.pz; tot.th += v.th; tot.pot += v.pot;
+    }
+    return tot;
+}
+
+// listed pair k: the deep levels' chunk sums in order, the decision, the outputs (one thread)
+template <int CLS>
+__device__ void fix_finish_item(const ClassArgs &A, int mode, int fixed_level, double tol, int kmax, int k)
+{
+    const int t = A.fix_deep[k];
+    d3 nj, spsi;
+    double sth;
+    const FixupPair<CLS> p = fixup_pair<CLS>(A, t, nj, spsi, sth);
+    acc5 acc;
+    int kept;
+    if (mode == kAdaptiveRelative) {
+        acc = load5(A.fix_base + 5 * (long long)k);
+        kept = kFixDirect;
+        for (int L = kFixDirect + 1; L <= kmax; ++L) {
+            const acc5 nxt = fix_level_total<CLS>(A, k, L);
+            const bool unconv = fixup_unconverged<CLS>(nxt, acc, p, nj, spsi, sth, tol);
+            acc = nxt;
+            kept = L;
+            if (!unconv) break;
+        }
+    } else {
+        kept = fixup_kept_level(A, mode, fixed_level, t);
+        acc = fix_level_total<CLS>(A, k, kept);
+    }
+    fixup_store<CLS>(A, t, acc, p, nj, spsi, sth, kept, mode);
+}
+
+template <int CLS>
+__global__ void __launch_bounds__(kFixChunk) k_fix_spread(ClassArgs A, QuadTables Q, int mode, int fixed_level, int kmax)
+{
+    __shared__ double red[5 * (kFixChunk / 32)];
+    const long long items = (long long)min(A.cnt[kCntFixDeep], A.fix_cap) * kFixSlots;
+    for (long long q = blockIdx.x; q < items; q += gridDim.x) fix_spread_item<CLS>(A, Q, mode, fixed_level, kmax, (int)(q / kFixSlots), (int)(q % kFixSlots), red);
+}
+
+template <int CLS>
+__global__ void __launch_bounds__(128) k_fix_finish(ClassArgs A, int mode, int fixed_level, double tol, int kmax)
+{
+    const int count = min(A.cnt[kCntFixDeep], A.fix_cap);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x)
+        fix_finish_item<CLS>(A, mode, fixed_level, tol, kmax, k);
 }
 
 template <int CLS>
@@ -687,9 +856,28 @@ void launch_fp64_fixup(int cls, const ClassArgs &A, const QuadTables &Q, const R
     if (!list) return;  // fixed mode without active lists: nothing to gather into
     if (cls == kFar) k_fixup_collect<kFar><<<persistent_blocks, 256, 0, s>>>(A, list, count);
     else k_fixup_collect<kEdge><<<persistent_blocks, 256, 0, s>>>(A, list, count);
-    if (cls == kEdge) k_fp64_fixup<kEdge><<<persistent_blocks, 256, 0, s>>>(A, Q, cfg.mode, cfg.level, cfg.tol, cfg.max_level, list, count);
-    else if (cls == kVertex) k_fp64_fixup<kVertex><<<persistent_blocks, 256, 0, s>>>(A, Q, cfg.mode, cfg.level, cfg.tol, cfg.max_level, list, count);
-    else if (cls == kFar) k_fp64_fixup<kFar><<<persistent_blocks, 256, 0, s>>>(A, Q, cfg.mode, cfg.level, cfg.tol, cfg.max_level, list, count);
+    const int m = cfg.mode, lv = cfg.level, km = cfg.max_level;
+    const double tol = cfg.tol;
+    const int spread_blocks = persistent_blocks * 4;
+    if (cls == kEdge) {
+        k_fp64_fixup<kEdge><<<persistent_blocks, 256, 0, s>>>(A, Q, m, lv, tol, km, list, count);
+        if (A.fix_deep) {
+            k_fix_spread<kEdge><<<spread_blocks, kFixChunk, 0, s>>>(A, Q, m, lv, km);
+            k_fix_finish<kEdge><<<8, 128, 0, s>>>(A, m, lv, tol, km);
+        }
+    } else if (cls == kVertex) {
+        k_fp64_fixup<kVertex><<<persistent_blocks, 256, 0, s>>>(A, Q, m, lv, tol, km, list, count);
+        if (A.fix_deep) {
+            k_fix_spread<kVertex><<<spread_blocks, kFixChunk, 0, s>>>(A, Q, m, lv, km);
+            k_fix_finish<kVertex><<<8, 128, 0, s>>>(A, m, lv, tol, km);
+        }
+    } else if (cls == kFar) {
+        k_fp64_fixup<kFar><<<persistent_blocks, 256, 0, s>>>(A, Q, m, lv, tol, km, list, count);
+        if (A.fix_deep) {
+            k_fix_spread<kFar><<<spread_blocks, kFixChunk, 0, s>>>(A, Q, m, lv, km);
+            k_fix_finish<kFar><<<8, 128, 0, s>>>(A, m, lv, tol, km);
+        }
+    }
 }
 
 // ------------------------------------------------------------------ launchers
@@ -910,6 +1098,42 @@ __global__ void __launch_bounds__(256) k_batch_fp64_fixup(const BatchSeg *__rest
     }
 }
 
+__global__ void __launch_bounds__(kFixChunk) k_batch_fix_spread(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q, int mode,
+                                                                 int fixed_level, int kmax)
+{
+    extern __shared__ long long prefix[];
+    __shared__ double red[5 * (kFixChunk / 32)];
+    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
+        return seg_fixup(S) && S.A.fix_deep ? (long long)min(S.A.cnt[kCntFixDeep], S.A.fix_cap) * kFixSlots : 0;
+    });
+    for (long long g = blockIdx.x; g < total; g += gridDim.x) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        const long long q = g - prefix[sg];
+        const int k = (int)(q / kFixSlots), slot = (int)(q % kFixSlots);
+        if (S.cls == kFar) fix_spread_item<kFar>(S.A, Q, mode, fixed_level, kmax, k, slot, red);
+        else if (S.cls == kEdge) fix_spread_item<kEdge>(S.A, Q, mode, fixed_level, kmax, k, slot, red);
+        else fix_spread_item<kVertex>(S.A, Q, mode, fixed_level, kmax, k, slot, red);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_batch_fix_finish(const BatchSeg *__restrict__ segs, int nseg, int mode, int fixed_level,
+                                                          double tol, int kmax)
+{
+    extern __shared__ long long prefix[];
+    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
+        return seg_fixup(S) && S.A.fix_deep ? min(S.A.cnt[kCntFixDeep], S.A.fix_cap) : 0;
+    });
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        const int k = (int)(g - prefix[sg]);
+        if (S.cls == kFar) fix_finish_item<kFar>(S.A, mode, fixed_level, tol, kmax, k);
+        else if (S.cls == kEdge) fix_finish_item<kEdge>(S.A, mode, fixed_level, tol, kmax, k);
+        else fix_finish_item<kVertex>(S.A, mode, fixed_level, tol, kmax, k);
+    }
+}
+
 static size_t seg_smem(int nseg) { return (size_t)(nseg + 1) * sizeof(long long); }
 
 void launch_batch_prelude(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTables &Q, const QuadTablesF &Qf,
@@ -950,6 +1174,8 @@ void launch_batch_fixup(const BatchSeg *segs, int nseg, const BatchTotals &tot, 
         const int nc = std::min(kBatchSegChunk, nseg - c0);
         k_batch_fixup_collect<<<blocks, 256, seg_smem(nc), s>>>(segs + c0, nc);
         k_batch_fp64_fixup<<<persistent_blocks, 256, seg_smem(nc), s>>>(segs + c0, nc, Q, cfg.mode, cfg.level, cfg.tol, cfg.max_level);
+        k_batch_fix_spread<<<persistent_blocks * 4, kFixChunk, seg_smem(nc), s>>>(segs + c0, nc, Q, cfg.mode, cfg.level, cfg.max_level);
+        k_batch_fix_finish<<<64, 128, seg_smem(nc), s>>>(segs + c0, nc, cfg.mode, cfg.level, cfg.tol, cfg.max_level);
     }
 }
 
