@@ -334,7 +334,7 @@ def run_batch(batch, flush, stream, steps, warmup):
 
 
 # kernels of one batched step, whatever the number of segments
-BATCH_LAUNCHES = 1 + 1 + 2 + (2 + 12) + 1 + 1 + 2
+BATCH_LAUNCHES = 1 + 2 + 2 + (2 + 12) + 1 + 1 + 4
 
 
 def uneven_batch_section(args):
@@ -593,11 +593,12 @@ def gpu_arm(args):
     n_cpu, dt_cpu, thr = cpu_run(V, C, lists, args.cpu_fraction, args.tol)
     # kernels per step: adjacent classes run singular + tiers 2 and 2b + adaptive potential (seed,
     # 12 depths, final); per-class chains add levels 0..5 + finalize per class, self pairs 1; the
-    # mixed chains add the needle fix-up (collect + FP64 pass) per non-self class.  The batched
-    # form runs each stage once for all segments: reset, singular, tiers 2 and 2b, seed, 12
-    # depths, final, self, the cooperative level kernel, collect, fix-up.
+    # mixed chains add tier 1 as its own kernel and the needle fix-up (collect, FP64 pass, spread,
+    # finish) per non-self class.  The batched form runs each stage once for all segments: reset,
+    # closed forms, tier 1, tiers 2 and 2b, seed, 12 depths, final, self, the cooperative level
+    # kernel, and the four fix-up kernels.
     pot_chain = 4 + 12
-    launches = {"fp64": 2 * (1 + pot_chain + 7) + 7 + 1, "mixed": 2 * (1 + pot_chain + 7) + 7 + 1 + 3 * 2, "batch": BATCH_LAUNCHES}
+    launches = {"fp64": 2 * (1 + pot_chain + 7) + 7 + 1, "mixed": 2 * (2 + pot_chain + 7) + 7 + 1 + 3 * 4, "batch": BATCH_LAUNCHES}
     names4 = ("vertex", "edge", "near", "self")
     form_desc = {"batch": "mixed precision, batched: 4 class segments, one persistent cooperative level kernel, CUDA graph replay",
                  "mixed": "mixed precision, per-class kernel chains", "fp64": "plain FP64, per-class kernel chains"}

@@ -440,7 +440,30 @@ __device__ __forceinline__ void singular_mixed_item(const ClassArgs &A, const Qu
         double *sg = A.sing + 4 * (long long)t;
         sg[0] = psi.x; sg[1] = psi.y; sg[2] = psi.z; sg[3] = th;
     }
-    // FP32: tier 1 of the potential (main and check Duffy rules)
+}
+
+// tier 1 of the potential in FP32 (main graded Duffy rule, and the check rule unless the pair
+// goes straight to the adaptive rule), by a group of 8 lanes per pair: the 128 points of the two
+// rules, 16 per lane, would be a long serial chain for one thread.  The lanes' Kahan partial sums
+// are added in FP64.
+constexpr int kTier1Lanes = 8;
+
+__device__ __forceinline__ double group_sum8(double x)
+{
+    const unsigned mask = 0xffu << (threadIdx.x & 24);
+    for (int off = 1; off < kTier1Lanes; off <<= 1) x += __shfl_xor_sync(mask, x, off, kTier1Lanes);
+    return x;
+}
+
+template <int CLS>
+__device__ __forceinline__ void tier1_mixed_item(const ClassArgs &A, const QuadTablesF &Qf, long long t, int g)
+{
+    const int2 pr = A.pairs[t];
+    const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
+    int si, sj;
+    if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
+    else shifts_vertex(ci, cj, si, sj);
+    const double Si = A.panels[pr.x].v[0].w;
     const PanelJf K = load_panel_f(A.panels_f, pr.y);
     const FarCtxF F{crossf(K.ta, K.n), crossf(K.tb, K.n), crossf(K.tc, K.n)};
     f3 m_in = f3{0, 0, 0};
@@ -448,19 +471,28 @@ __device__ __forceinline__ void singular_mixed_item(const ClassArgs &A, const Qu
     double sig = 0.0;
     const int p1v = (sj + 1) % 3;  // JB, start of the shared edge in K_j's orientation
     if (CLS == kEdge) edge_sigma_setup(A, pr, si, sj, K, Si, m_in, c, h, sig);
-    const float pm = duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, K, F, p1v, m_in, c, h, Qf.du_u, Qf.du_w, Qf.nu, Qf.dv_v, Qf.dv_w, Qf.nv);
-    const double pmd = (double)pm + sig;
-    A.padj[t] = kInv4Pi * pmd;
-    if (A.hard_list) {
-        const double c10 = 0.98480775301220806;
-        if (dot(ni, Kd.n) < 0.5 || A.panels[pr.x].v[2].w > c10 || A.panels[pr.y].v[2].w > c10) {
-            A.hard_list[atomicAdd(A.hard_cnt, 1)] = (int)t;
-        } else {
-            const float pl = duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, K, F, p1v, m_in, c, h, Qf.lo_u, Qf.lo_uw, Qf.lo_nu, Qf.lo_v,
-                                                Qf.lo_vw, Qf.lo_nv);
-            if (fabs(pmd - ((double)pl + sig)) > A.tier_tol * fabs(pmd)) A.tier2_list[atomicAdd(A.tier2_cnt, 1)] = (int)t;
-        }
+    const double pmd = group_sum8((double)duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, K, F, p1v, m_in, c, h, Qf.du_u, Qf.du_w, Qf.nu,
+                                                             Qf.dv_v, Qf.dv_w, Qf.nv, g, kTier1Lanes)) + sig;
+    if (g == 0) A.padj[t] = kInv4Pi * pmd;
+    if (!A.hard_list) return;
+    const double c10 = 0.98480775301220806;
+    const double4_32a ni4 = A.panels[pr.x].v[3], nj4 = A.panels[pr.y].v[3];
+    if (ni4.x * nj4.x + ni4.y * nj4.y + ni4.z * nj4.z < 0.5 || A.panels[pr.x].v[2].w > c10 || A.panels[pr.y].v[2].w > c10) {
+        if (g == 0) A.hard_list[atomicAdd(A.hard_cnt, 1)] = (int)t;
+        return;
     }
+    const double pl = group_sum8((double)duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, K, F, p1v, m_in, c, h, Qf.lo_u, Qf.lo_uw, Qf.lo_nu,
+                                                            Qf.lo_v, Qf.lo_vw, Qf.lo_nv, g, kTier1Lanes)) + sig;
+    if (g == 0 && fabs(pmd - pl) > A.tier_tol * fabs(pmd)) A.tier2_list[atomicAdd(A.tier2_cnt, 1)] = (int)t;
+}
+
+template <int CLS>
+__global__ void __launch_bounds__(128) k_tier1_mixed(ClassArgs A, QuadTablesF Qf)
+{
+    // every pair's group of 8 lanes is one aligned group of a warp, and the whole group is valid
+    // or invalid together
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid / kTier1Lanes < A.n) tier1_mixed_item<CLS>(A, Qf, gid / kTier1Lanes, (int)(gid % kTier1Lanes));
 }
 
 template <int CLS>
@@ -923,6 +955,7 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
         break;
     case kEdge:
         k_singular_mixed<kEdge><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
+        k_tier1_mixed<kEdge><<<blocks_for_m((long long)kTier1Lanes * A.n, tpb), tpb, 0, s>>>(A, Qf);
         if (A.hard_list) {
             k_pot_tier2_mixed<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Qf, Q);
             k_pot_tier2b<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Q, 0);
@@ -933,6 +966,7 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
         break;
     case kVertex:
         k_singular_mixed<kVertex><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
+        k_tier1_mixed<kVertex><<<blocks_for_m((long long)kTier1Lanes * A.n, tpb), tpb, 0, s>>>(A, Qf);
         if (A.hard_list) {
             k_pot_tier2_mixed<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Qf, Q);
             k_pot_tier2b<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Q, 0);
@@ -1030,6 +1064,23 @@ __global__ void __launch_bounds__(128) k_batch_singular(const BatchSeg *__restri
         const BatchSeg &S = segs[sg];
         if (S.cls == kEdge) singular_mixed_item<kEdge>(S.A, Qf, g - prefix[sg]);
         else singular_mixed_item<kVertex>(S.A, Qf, g - prefix[sg]);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_batch_tier1(const BatchSeg *__restrict__ segs, int nseg, QuadTablesF Qf)
+{
+    extern __shared__ long long prefix[];
+    // eight items per pair (as k_batch_self): every count is a multiple of 8, and so is the grid's
+    // thread count, so a pair's items land in one aligned group of eight lanes
+    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
+        return seg_adjacent(S) ? (long long)kTier1Lanes * S.A.n : 0;
+    });
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        const long long loc = g - prefix[sg];
+        if (S.cls == kEdge) tier1_mixed_item<kEdge>(S.A, Qf, loc / kTier1Lanes, (int)(loc % kTier1Lanes));
+        else tier1_mixed_item<kVertex>(S.A, Qf, loc / kTier1Lanes, (int)(loc % kTier1Lanes));
     }
 }
 
@@ -1149,6 +1200,11 @@ void launch_batch_prelude(const BatchSeg *segs, int nseg, const BatchTotals &tot
         for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
             const int nc = std::min(kBatchSegChunk, nseg - c0);
             k_batch_singular<<<blocks, tpb, seg_smem(nc), s>>>(segs + c0, nc, Qf);
+        }
+        const int blocks8 = std::max(1, std::min(blocks_for_m((long long)kTier1Lanes * tot.adjacent_pairs, tpb), 1 << 16));
+        for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
+            const int nc = std::min(kBatchSegChunk, nseg - c0);
+            k_batch_tier1<<<blocks8, tpb, seg_smem(nc), s>>>(segs + c0, nc, Qf);
         }
         if (tot.hard_lists) {
             for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
