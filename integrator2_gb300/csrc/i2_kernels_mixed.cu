@@ -502,11 +502,6 @@ __global__ void __launch_bounds__(128) k_singular_mixed(ClassArgs A, QuadTablesF
     if (t < A.n) singular_mixed_item<CLS>(A, Qf, t);
 }
 
-__device__ __forceinline__ float warp_sum_f(float x)
-{
-    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
-    return x;
-}
 
 // tier 2 in FP32, one warp per listed pair (the lanes share each rule's points); the pairs it
 // rejects are listed for tier 2b, which runs in FP64 because the FP32 rules can share a bias of
@@ -528,8 +523,9 @@ __device__ __forceinline__ void tier2_mixed_item(const ClassArgs &A, const QuadT
     double sig = 0.0;
     const int p1v = (sj + 1) % 3;
     if (CLS == kEdge) edge_sigma_setup(A, pr, si, sj, Kf, Si, m_in, c, hh, sig);
-    const double ph = (double)warp_sum_f(duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, Kf, Ff, p1v, m_in, c, hh, Qf.hi_u, Qf.hi_uw,
-                                                            Qf.hi_nu, Qf.hi_v, Qf.hi_vw, Qf.hi_nv, lane, 32)) + sig;
+    // the lanes' Kahan partial sums added in FP64 (an FP32 butterfly adds noise the tier bar sees)
+    const double ph = warp_sum((double)duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, Kf, Ff, p1v, m_in, c, hh, Qf.hi_u, Qf.hi_uw,
+                                                          Qf.hi_nu, Qf.hi_v, Qf.hi_vw, Qf.hi_nv, lane, 32)) + sig;
     const double pm = A.padj[t] * (4.0 * kPi);
     if (lane != 0) return;
     if (fabs(ph - pm) <= A.tier_tol * fabs(ph)) A.padj[t] = kInv4Pi * ph;
