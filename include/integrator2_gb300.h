@@ -180,9 +180,9 @@ i2_status i2_evaluator_result_count(const i2_evaluator_t *ev, i2_pair_class cls,
  * failed; out[2] pairs that reached tier 2b; out[3] pairs given the adaptive potential rule;
  * out[4] adaptive-rule cells kept because a depth's list was full; out[5] needle pairs
  * recomputed in FP64 (mixed form); out[6] the class's last refinement level; out[6 + L] pairs
- * still unconverged after level L (L = 1..7, adaptive modes).  Synchronises the evaluator's
- * stream. */
-#define I2_RUN_STATS 14
+ * still unconverged after level L (L = 1..7, adaptive modes); out[14] of the needle pairs, those
+ * whose levels 4-5 were spread over the GPU.  Synchronises the evaluator's stream. */
+#define I2_RUN_STATS 15
 i2_status i2_evaluator_run_stats(const i2_evaluator_t *ev, i2_pair_class cls, int64_t *out, int32_t n);
 /* full-precision copy of a result channel (replaces subclassing for d_*Results) */
 i2_status i2_evaluator_copy_results(const i2_evaluator_t *ev, i2_pair_class cls, i2_channel channel, double *out,

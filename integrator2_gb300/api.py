@@ -233,11 +233,11 @@ class EvaluatorJ3DK:
 
     def getRunStats(self, cls: int) -> dict:
         """counters of the last run of a class (i2_evaluator_run_stats)"""
-        out = np.zeros(14, np.int64)
+        out = np.zeros(15, np.int64)
         call("i2_evaluator_run_stats", self._h, cls, _p(out), len(out))
         return {"pairs": int(out[0]), "tier2": int(out[1]), "tier2b": int(out[2]), "adaptive_potential": int(out[3]),
                 "adaptive_overflow": int(out[4]), "fp64_fixup": int(out[5]), "max_level": int(out[6]),
-                "unconverged_after_level": [int(x) for x in out[7:14]]}
+                "unconverged_after_level": [int(x) for x in out[7:14]], "fp64_fixup_spread": int(out[14])}
 
     def synchronize(self) -> None:
         call("i2_evaluator_synchronize", self._h)

@@ -1222,6 +1222,7 @@ i2_status i2_evaluator_run_stats(const i2_evaluator_t *ev, i2_pair_class cls, in
         out[5] = c[i2::kCntFixup];
         out[6] = maxlev;
         for (int L = 1; L <= 7; ++L) out[6 + L] = R.cfg.mode == i2::kFixed ? 0 : c[L];
+        out[14] = std::min(c[i2::kCntFixDeep], i2::kFixDeepCap);
     });
 }
 

@@ -149,3 +149,43 @@ def test_run_stats_are_consistent(api):
                 assert 0 < st["tier2b"] <= st["tier2"] < st["pairs"] and st["adaptive_potential"] > 0
             if prec == api.PRECISION_FP64:
                 assert st["fp64_fixup"] == 0
+
+
+def test_fp64_fixup_of_needle_pairs_matches_fp64_form(api):
+    """pairs holding a needle cell (a corner below 3 degrees; for the disjoint class the cell K_j)
+    are recomputed by the mixed form in FP64 with the FP64 form's relative refinement, their
+    deepest levels spread over the GPU: J and P equal the FP64 form's to rounding and the kept
+    levels are the same"""
+    from integrator2_gb300 import meshes, pairs as P
+    V, C = meshes.jittered_icosphere(5, 0.15, 2026)  # two needles, corners of 0.6 and 1.5 degrees
+    pl = P.build_pairs(V, C)
+    e = np.linalg.norm(V[C[:, [1, 2, 0]]] - V[C], axis=2)
+    a, b, c = e[:, 0], e[:, 1], e[:, 2]
+    cos_max = np.max([(b * b + c * c - a * a) / (2 * b * c), (a * a + c * c - b * b) / (2 * a * c),
+                      (a * a + b * b - c * c) / (2 * a * b)], axis=0)
+    needle = np.where(cos_max > np.cos(np.radians(3.0)))[0]
+    assert len(needle) >= 2
+    m = api.Mesh3D()
+    m.setGeometry(V, C)
+    m.prepareMesh(3.0)
+    spread = 0
+    for cls in (0, 1, 2):
+        pr = pl.by_class(cls)
+        hit = np.isin(pr[:, 1], needle) if cls == 2 else (np.isin(pr[:, 0], needle) | np.isin(pr[:, 1], needle))
+        pr = np.ascontiguousarray(pr[hit])
+        out = {}
+        for prec in (api.PRECISION_FP64, api.PRECISION_MIXED):
+            it = api.NumericalIntegrator3D(m, api.qf3D13)
+            it.setErrorControl(api.RELATIVE_ERROR_CONTROL, 1e-6, 5)
+            it.setPrecision(prec)
+            ev = api.EvaluatorJ3DK(m, it)
+            ev.runClass(cls, pr)
+            out[prec] = (ev.getResults(cls), ev.getPotentials(cls), ev.getLevels(cls), ev.getRunStats(cls))
+        (J64, P64, L64, _), (J32, P32, L32, st) = out[api.PRECISION_FP64], out[api.PRECISION_MIXED]
+        assert st["fp64_fixup"] == len(pr), (cls, st)
+        spread += st["fp64_fixup_spread"]
+        assert np.array_equal(L32, L64), cls
+        assert rel_rows(J32, J64).max() < 1e-11, (cls, rel_rows(J32, J64).max())
+        if cls == 2:
+            assert (np.abs(P32 - P64) / np.abs(P64)).max() < 1e-11
+    assert spread > 0  # levels 4-5 of some pairs ran spread over the GPU
