@@ -720,16 +720,6 @@ __device__ inline void closed_vertex(TriT<R> Ti, TriT<R> Tj, V3<R> ni, V3<R> nj,
 }
 
 // ------------------------------------------------------------------ potential helpers
-// potential of K_j seen from x (no 1/4pi): sum_e t_e L_e - d Theta
-template <class R>
-__device__ __forceinline__ R potential_inner(V3<R> x, const PanelJT<R> &K, const FarCtxT<R> &F)
-{
-    V3<R> psi;
-    R th, pot;
-    far_integrand(x, K, F, psi, th, pot);
-    return pot;
-}
-
 // common-edge potential: subtracted s ln s term along the shared edge (sigma = -2 c s ln(s/h),
 // integral over K_i = (5/9) c S_i h)
 template <class R>
