@@ -172,3 +172,38 @@ def test_uneven_mesh_set_and_scale_invariance(api):
         else:
             assert rel_rows(Jb[same] / 5e-4 ** 2, Ja[same]).max() < 1e-9, cls
         assert (np.abs(Pb[same] / 5e-4 ** 3 - Pa[same]) / np.abs(Pa[same])).max() < 1e-9, cls
+
+
+def test_batch_more_segments_than_one_chunk(api):
+    """more segments than one stage launch walks (2,048): the stages run chunk by chunk and the
+    results match class-by-class runs, for segments on both sides of the chunk boundary"""
+    from integrator2_gb300 import meshes, pairs as P
+    V, C = meshes.jittered_icosphere(1, 0.1, 3)
+    m = api.Mesh3D()
+    m.setGeometry(V, C)
+    m.prepareMesh(3.0)
+    pl = P.build_pairs(V, C)
+    it = _integrator(api, m, "relative")
+    batch = api.BatchEvaluator(it)
+    rng = np.random.default_rng(4)
+    segs = []
+    for k in range(2100):
+        # mostly small disjoint and self segments; a few adjacent ones, all past the first chunk
+        cls = (0 if k % 2 else 1) if (k > 2048 and k % 13 == 0) else (2 if k % 2 else 3)
+        pr = pl.by_class(cls)
+        pr = np.ascontiguousarray(pr[np.sort(rng.choice(len(pr), min(len(pr), 6), replace=False))])
+        segs.append((cls, pr, batch.add(m, cls, pr)))
+    batch.run()
+    ev = api.EvaluatorJ3DK(m, it)
+    checked = 0
+    for cls, pr, s in segs[2030:2080] + segs[:5]:
+        ev.runClass(cls, pr)
+        J, J1 = batch.getResults(s), ev.getResults(cls)
+        if cls == 3:
+            assert np.array_equal(J, J1) and np.array_equal(batch.getPotentials(s), ev.getPotentials(cls))
+            continue
+        same = batch.getLevels(s) == ev.getLevels(cls)
+        assert rel_rows(J[same], J1[same]).max() < 1e-5, cls
+        assert np.array_equal(batch.getLevels(s), ev.getLevels(cls)) or same.mean() > 0.8
+        checked += cls in (0, 1)
+    assert checked >= 2
