@@ -175,6 +175,19 @@ __device__ __forceinline__ void kahan_add(kahan5 &k, int i, float v)
     k.s[i] = t;
 }
 
+// (s - c) += (s2 - c2) for two Kahan pairs: the rounding error of s + s2 from Knuth's TwoSum
+// moves into the compensation, so a sum across lanes keeps about 2^-48 of relative precision with
+// no FP64 work on every lane.  TwoSum's error is the exact rounding error, whichever lane forms
+// it, so the two lanes of an xor butterfly end with identical pairs.
+__device__ __forceinline__ void kahan_pair_add(float &s, float &c, float s2, float c2)
+{
+    const float t = s + s2;
+    const float z = t - s;
+    const float err = (s - (t - z)) + (s2 - z);  // (s + s2) - t, exactly
+    c = (c + c2) - err;
+    s = t;
+}
+
 struct QuadTablesF {
     float L1[kMaxGauss], L2[kMaxGauss], L3[kMaxGauss], w[kMaxGauss];
     int npts;

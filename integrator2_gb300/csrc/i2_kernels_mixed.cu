@@ -132,16 +132,6 @@ __device__ __forceinline__ TriF subcellf(TriF t, int level, int s)
     return t;
 }
 
-__device__ __forceinline__ acc5 shfl_xor5m(acc5 a, int off)
-{
-    acc5 r;
-    r.px = __shfl_xor_sync(0xffffffffu, a.px, off);
-    r.py = __shfl_xor_sync(0xffffffffu, a.py, off);
-    r.pz = __shfl_xor_sync(0xffffffffu, a.pz, off);
-    r.th = __shfl_xor_sync(0xffffffffu, a.th, off);
-    r.pot = __shfl_xor_sync(0xffffffffu, a.pot, off);
-    return r;
-}
 
 
 // one refinement level of the regular part, FP32 evaluation, FP64 bookkeeping (same contract
@@ -166,6 +156,8 @@ __device__ void level_items_mixed(const ClassArgs &A, const QuadTablesF &Qf, int
         const int lane_g = (int)(idx % G);
         const int t = valid ? (listed ? A.act_in[slot] : slot) : 0;
         acc5 acc = zero5();
+        kahan5 ks;  // this lane's sums (value s - c); zero for lanes past the last item
+        kahan_zero(ks);
         int2 pr = make_int2(0, 0);
         if (valid) {
             pr = A.pairs[t];
@@ -222,8 +214,6 @@ __device__ void level_items_mixed(const ClassArgs &A, const QuadTablesF &Qf, int
             df_offsets(A.panels_f, pr.x, pr.y, origin, T0.a, T0.b, T0.c);
             df_offsets(A.panels_f, pr.x, pr.y, (origin + 1) % 3, T1.a, T1.b, T1.c);
             df_offsets(A.panels_f, pr.x, pr.y, (origin + 2) % 3, T2.a, T2.b, T2.c);
-            kahan5 ks;
-            kahan_zero(ks);
             for (int s = lane_g * per_lane; s < (lane_g + 1) * per_lane; ++s) {
                 const TriF U0 = subcellf(T0, level, s), U1 = subcellf(T1, level, s), U2 = subcellf(T2, level, s);
                 float c0 = 0, c1 = 0, c2 = 0, c3 = 0, c4 = 0;
@@ -251,17 +241,21 @@ __device__ void level_items_mixed(const ClassArgs &A, const QuadTablesF &Qf, int
                 kahan_add(ks, 3, Ssub * c3);
                 kahan_add(ks, 4, Ssub * c4);
             }
-            acc.px = (double)ks.s[0] - (double)ks.c[0];
-            acc.py = (double)ks.s[1] - (double)ks.c[1];
-            acc.pz = (double)ks.s[2] - (double)ks.c[2];
-            acc.th = (double)ks.s[3] - (double)ks.c[3];
-            acc.pot = (double)ks.s[4] - (double)ks.c[4];
         }
+        // the lanes' Kahan pairs added across the group in FP32 (kahan_pair_add); lane 0 converts
         for (int off = 1; off < G; off <<= 1) {
-            const acc5 o = shfl_xor5m(acc, off);
-            acc.px += o.px; acc.py += o.py; acc.pz += o.pz; acc.th += o.th; acc.pot += o.pot;
+#pragma unroll
+            for (int i = 0; i < 5; ++i) {
+                const float s2 = __shfl_xor_sync(0xffffffffu, ks.s[i], off), c2 = __shfl_xor_sync(0xffffffffu, ks.c[i], off);
+                kahan_pair_add(ks.s[i], ks.c[i], s2, c2);
+            }
         }
         if (!valid || lane_g != 0) continue;
+        acc.px = (double)ks.s[0] - (double)ks.c[0];
+        acc.py = (double)ks.s[1] - (double)ks.c[1];
+        acc.pz = (double)ks.s[2] - (double)ks.c[2];
+        acc.th = (double)ks.s[3] - (double)ks.c[3];
+        acc.pot = (double)ks.s[4] - (double)ks.c[4];
         double *cur = A.cur + 5 * (long long)t;
         if (mode == kFixed || level == 0) {
             cur[0] = acc.px; cur[1] = acc.py; cur[2] = acc.pz; cur[3] = acc.th; cur[4] = acc.pot;
