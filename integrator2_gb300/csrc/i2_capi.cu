@@ -751,6 +751,7 @@ void batch_prepare(i2_batch *b)
         if (sp->n == 0) continue;
         if (sp->cls == I2_SELF) b->totals.self_pairs += sp->n;
         else {
+            b->totals.present[sp->cls] = true;
             if (sp->cls != I2_NOT_NEIGHBORS) {
                 b->totals.adjacent_pairs += sp->n;
                 b->totals.hard_lists = b->totals.hard_lists || sp->args.hard_list != nullptr;
@@ -777,10 +778,8 @@ void batch_enqueue(i2_batch *b, cudaStream_t s, int threads, int bps, int gcap, 
     i2::RunConfig cfg = b->cfg;
     cfg.hard_tol = adaptive_tolerance(cfg, true);  // the batched form is mixed precision
     i2::launch_batch_prelude(b->d_segs.ptr, nseg, b->totals, b->Q, b->Qf, cfg, persistent, s);
-    const int maxb = i2::batch_max_blocks_per_sm(threads, variant);
-    I2_REQUIRE(maxb > 0, I2_ERR_CUDA, "batch kernel cannot be resident with this block size");
-    const int blocks = std::max(1, b->sms) * std::max(1, std::min(bps > 0 ? bps : maxb, maxb));
-    I2_CHECK_CUDA(i2::launch_batch_levels(b->d_segs.ptr, nseg, b->Qf, b->cfg, blocks, threads, gcap, variant, s));
+    I2_REQUIRE(i2::batch_max_blocks_per_sm(threads, variant) > 0, I2_ERR_CUDA, "batch kernel cannot be resident with this block size");
+    I2_CHECK_CUDA(i2::launch_batch_levels(b->d_segs.ptr, nseg, b->totals.present, b->Qf, b->cfg, b->sms, bps, threads, gcap, variant, s));
     i2::launch_batch_fixup(b->d_segs.ptr, nseg, b->totals, b->Q, b->cfg, persistent, s);
     I2_CHECK_CUDA(cudaGetLastError());
 }

@@ -99,16 +99,20 @@ struct BatchSeg {
     ClassArgs A;
     int cls;
 };
-// variant 0: registers unconstrained; 1: capped at 128 per thread (two 256-thread blocks per SM)
+// variant 0: registers unconstrained; 1: capped at 128 per thread (two 256-thread blocks per SM);
+// the largest resident block count of the three class kernels
 int batch_max_blocks_per_sm(int threads, int variant);
-cudaError_t launch_batch_levels(const BatchSeg *segs, int nseg, const QuadTablesF &Qf, const RunConfig &cfg, int blocks,
-                                int threads, int G_cap, int variant, cudaStream_t s);
+// bps: blocks per SM, capped at each class kernel's own maximum (0: the maximum); present[cls]:
+// some segment holds pairs of class cls (0..2)
+cudaError_t launch_batch_levels(const BatchSeg *segs, int nseg, const bool present[3], const QuadTablesF &Qf, const RunConfig &cfg,
+                                int sms, int bps, int threads, int G_cap, int variant, cudaStream_t s);
 // sizes the host knows about a batch (launch shapes of the batched stages)
 struct BatchTotals {
     long long adjacent_pairs = 0;  // pairs of common-edge and common-vertex segments
     long long self_pairs = 0;
     long long fixup_pairs = 0;     // pairs the FP64 fix-up screens (segments with an active list)
     bool hard_lists = false;       // some adjacent segment has the potential's tier lists
+    bool present[3] = {false, false, false};  // some segment holds pairs of class 0, 1, 2
 };
 // every segment's counter reset, tier 1 with the singular parts, tiers 2 / 2b, the adaptive
 // potential and the self pairs: one launch per stage for the whole batch

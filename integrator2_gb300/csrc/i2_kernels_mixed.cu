@@ -138,15 +138,29 @@ __device__ __forceinline__ TriF subcellf(TriF t, int level, int s)
 // as k_level of the FP64 form).  Work items are (pair, lane of its lane group) over a grid-stride
 // loop starting at `first` with stride `stride` (multiples of 32), so the same body serves the
 // per-class kernels and the batched persistent kernel.
+// a level's active lists: the pairs to integrate (act_in, count *cnt_in; all pairs when
+// act_in is null) and the list the unconverged ones go to
+struct LevelLists {
+    const int *act_in, *cnt_in;
+    int *act_out, *cnt_out;
+};
+
+__device__ __forceinline__ LevelLists level_lists(const ClassArgs &A, int level, int mode)
+{
+    if (mode == kFixed || level == 0) return LevelLists{A.act_in, A.cnt_in, A.act_out, A.cnt_out};
+    return LevelLists{level == 1 ? nullptr : (level % 2 ? A.act_b : A.act_a), level == 1 ? nullptr : A.cnt + (level - 1),
+                      level % 2 ? A.act_a : A.act_b, A.cnt + level};
+}
+
 template <int CLS>
-__device__ void level_items_mixed(const ClassArgs &A, const QuadTablesF &Qf, int level, int mode, double tol, int kmax,
-                                  long long first, long long stride, int G_cap)
+__device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, const QuadTablesF &Qf, int level, int mode, double tol,
+                                  int kmax, long long first, long long stride, int G_cap)
 {
     const int nsub = 1 << (2 * level);
     const int G = nsub < G_cap ? nsub : G_cap;
     const int per_lane = nsub / G;
-    const bool listed = A.act_in != nullptr;
-    const int count = listed ? *A.cnt_in : A.n;
+    const bool listed = Lst.act_in != nullptr;
+    const int count = listed ? *Lst.cnt_in : A.n;
     const long long total = (long long)count * G;
     const long long total_r = (total + 31) & ~31LL;
     const float sub_scale = ldexpf(1.0f, -2 * level);
@@ -154,7 +168,7 @@ __device__ void level_items_mixed(const ClassArgs &A, const QuadTablesF &Qf, int
         const bool valid = idx < total;
         const int slot = (int)(idx / G);
         const int lane_g = (int)(idx % G);
-        const int t = valid ? (listed ? A.act_in[slot] : slot) : 0;
+        const int t = valid ? (listed ? Lst.act_in[slot] : slot) : 0;
         acc5 acc = zero5();
         kahan5 ks;  // this lane's sums (value s - c); zero for lanes past the last item
         kahan_zero(ks);
@@ -304,7 +318,7 @@ __device__ void level_items_mixed(const ClassArgs &A, const QuadTablesF &Qf, int
                 fb[0] = prev.px; fb[1] = prev.py; fb[2] = prev.pz; fb[3] = prev.th; fb[4] = prev.pot;
             }
         } else {
-            A.act_out[atomicAdd(A.cnt_out, 1)] = t;
+            Lst.act_out[atomicAdd(Lst.cnt_out, 1)] = t;
         }
     }
 }
@@ -312,8 +326,9 @@ __device__ void level_items_mixed(const ClassArgs &A, const QuadTablesF &Qf, int
 template <int CLS>
 __global__ void __launch_bounds__(256, 2) k_level_mixed(ClassArgs A, QuadTablesF Qf, int level, int mode, double tol, int kmax)
 {
-    level_items_mixed<CLS>(A, Qf, level, mode, tol, kmax, (long long)blockIdx.x * blockDim.x + threadIdx.x,
-                           (long long)gridDim.x * blockDim.x, 32);
+    // the host sets this level's lists in A (level_chain_mixed)
+    level_items_mixed<CLS>(A, LevelLists{A.act_in, A.cnt_in, A.act_out, A.cnt_out}, Qf, level, mode, tol, kmax,
+                           (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, 32);
 }
 
 // ------------------------------------------------------------------ adjacent pairs: singular parts + FP32 Duffy potential
@@ -981,7 +996,7 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
 // refinement is spread over the whole GPU at every level, across meshes and classes.
 // MINB = 1: registers unconstrained (fewer resident warps); MINB = 2: at most 128 registers per
 // thread so that two 256-thread blocks stay resident per SM (some spilling).  The autotuner picks.
-template <int MINB>
+template <int MINB, int CLS>
 __global__ void __launch_bounds__(256, MINB) k_batch_levels(const BatchSeg *__restrict__ segs, int nseg, QuadTablesF Qf, int mode,
                                                       int level_fixed, double tol, int kmax, int G_cap)
 {
@@ -992,45 +1007,62 @@ __global__ void __launch_bounds__(256, MINB) k_batch_levels(const BatchSeg *__re
     const int lo = mode == kFixed ? level_fixed : 0, hi = mode == kFixed ? level_fixed : kmax;
     for (int level = lo; level <= hi; ++level) {
         for (int sgi = 0; sgi < nseg; ++sgi) {
-            const int cls = segs[sgi].cls;
-            if (cls == kSelf) continue;
-            ClassArgs A = segs[sgi].A;
+            if (segs[sgi].cls != CLS) continue;
+            const ClassArgs &A = segs[sgi].A;  // read in place, no per-thread copy
             if (A.n <= 0) continue;
-            if (mode != kFixed && level >= 1) {
-                A.act_in = level == 1 ? nullptr : (level % 2 ? A.act_b : A.act_a);
-                A.cnt_in = level == 1 ? nullptr : A.cnt + (level - 1);
-                A.act_out = level % 2 ? A.act_a : A.act_b;
-                A.cnt_out = A.cnt + level;
-            }
-            if (cls == kFar) level_items_mixed<kFar>(A, Qf, level, mode, tol, kmax, first, stride, G_cap);
-            else if (cls == kEdge) level_items_mixed<kEdge>(A, Qf, level, mode, tol, kmax, first, stride, G_cap);
-            else level_items_mixed<kVertex>(A, Qf, level, mode, tol, kmax, first, stride, G_cap);
+            level_items_mixed<CLS>(A, level_lists(A, level, mode), Qf, level, mode, tol, kmax, first, stride, G_cap);
         }
         grid.sync();
     }
-    for (int sgi = 0; sgi < nseg; ++sgi) {
-        const int cls = segs[sgi].cls;
-        if (cls != kSelf) finalize_all(cls, segs[sgi].A, mode, first, stride);
-    }
+    for (int sgi = 0; sgi < nseg; ++sgi)
+        if (segs[sgi].cls == CLS) finalize_all(CLS, segs[sgi].A, mode, first, stride);
 }
+
+namespace {
+
+const void *batch_levels_fn(int variant, int cls)
+{
+    if (variant == 0) return cls == kFar ? (const void *)k_batch_levels<1, kFar> : cls == kEdge ? (const void *)k_batch_levels<1, kEdge>
+                                                                                                 : (const void *)k_batch_levels<1, kVertex>;
+    return cls == kFar ? (const void *)k_batch_levels<2, kFar> : cls == kEdge ? (const void *)k_batch_levels<2, kEdge>
+                                                                              : (const void *)k_batch_levels<2, kVertex>;
+}
+
+int batch_levels_occupancy(int threads, int variant, int cls)
+{
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_levels_fn(variant, cls), threads, 0) != cudaSuccess) return 0;
+    return nb;
+}
+
+} // namespace
 
 int batch_max_blocks_per_sm(int threads, int variant)
 {
     int nb = 0;
-    if (variant == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_levels<1>, threads, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_levels<2>, threads, 0);
+    for (int cls : {kVertex, kEdge, kFar}) nb = std::max(nb, batch_levels_occupancy(threads, variant, cls));
     return nb;
 }
 
-cudaError_t launch_batch_levels(const BatchSeg *segs, int nseg, const QuadTablesF &Qf, const RunConfig &cfg, int blocks,
-                                int threads, int G_cap, int variant, cudaStream_t s)
+// one cooperative launch per pair class present, each over every segment of that class: a kernel
+// holding one class's integrand keeps that class's register footprint (the far-field one fits
+// 128 registers without spills; a kernel with all three classes spilled there)
+cudaError_t launch_batch_levels(const BatchSeg *segs, int nseg, const bool present[3], const QuadTablesF &Qf, const RunConfig &cfg,
+                                int sms, int bps, int threads, int G_cap, int variant, cudaStream_t s)
 {
     int mode = cfg.mode, level = cfg.level, kmax = cfg.max_level;
     double tol = cfg.tol;
     QuadTablesF q = Qf;
     void *args[] = {(void *)&segs, (void *)&nseg, (void *)&q, (void *)&mode, (void *)&level, (void *)&tol, (void *)&kmax, (void *)&G_cap};
-    const void *fn = variant == 0 ? (const void *)k_batch_levels<1> : (const void *)k_batch_levels<2>;
-    return cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(threads), args, 0, s);
+    for (int cls : {kVertex, kEdge, kFar}) {
+        if (!present[cls]) continue;
+        const int maxb = batch_levels_occupancy(threads, variant, cls);
+        if (maxb <= 0) return cudaErrorInvalidConfiguration;
+        const int blocks = std::max(1, sms) * std::max(1, std::min(bps > 0 ? bps : maxb, maxb));
+        const cudaError_t e = cudaLaunchCooperativeKernel(batch_levels_fn(variant, cls), dim3(blocks), dim3(threads), args, 0, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 // ------------------------------------------------------------------ batched stages
