@@ -334,7 +334,7 @@ def run_batch(batch, flush, stream, steps, warmup):
 
 
 # kernels of one batched step, whatever the number of segments
-BATCH_LAUNCHES = 1 + 2 + 2 + (2 + 12) + 1 + 1 + 4
+BATCH_LAUNCHES = 1 + 2 + 2 + (2 + 12) + 1 + 3 + 4
 
 
 def uneven_batch_section(args):
@@ -595,8 +595,8 @@ def gpu_arm(args):
     # 12 depths, final); per-class chains add levels 0..5 + finalize per class, self pairs 1; the
     # mixed chains add tier 1 as its own kernel and the needle fix-up (collect, FP64 pass, spread,
     # finish) per non-self class.  The batched form runs each stage once for all segments: reset,
-    # closed forms, tier 1, tiers 2 and 2b, seed, 12 depths, final, self, the cooperative level
-    # kernel, and the four fix-up kernels.
+    # closed forms, tier 1, tiers 2 and 2b, seed, 12 depths, final, self, one cooperative level
+    # kernel per pair class, and the four fix-up kernels.
     pot_chain = 4 + 12
     launches = {"fp64": 2 * (1 + pot_chain + 7) + 7 + 1, "mixed": 2 * (2 + pot_chain + 7) + 7 + 1 + 3 * 4, "batch": BATCH_LAUNCHES}
     names4 = ("vertex", "edge", "near", "self")
