@@ -463,20 +463,30 @@ static void pot_adaptive_chain(const ClassArgs &A, const QuadTables &Q, double t
 // eight lanes per pair: lanes 0..5 take one (edge, piece) of the self-pair rule each, the group
 // sums them (an edge's pieces are integrated independently, so the pair's 6 x nself point
 // evaluations run in parallel)
-// item g (0..7) of self pair t; the eight items of a pair sit in eight consecutive lanes
-// (lanes 8k .. 8k+7) that call this together
-__device__ __forceinline__ void self_item(const ClassArgs &A, const QuadTables &Q, int self_sign, long long t, int g)
+// Self pairs, five to a warp: lanes 6k .. 6k+5 (k < 5) take the six (edge, piece) integrals of
+// one pair, the first of the six writes the pair's outputs, lanes 30 and 31 idle (groups of eight
+// lanes left two of every eight idle).
+constexpr int kSelfPairsPerWarp = 5;
+
+__device__ __forceinline__ double self_piece_of(const ClassArgs &A, const QuadTables &Q, long long t, int g)
 {
-    const int i = A.pairs[t].x;
-    const PanelJ K = load_panel(A.panels, i);
-    double part = 0.0;
-    if (g < 6) {
-        const d3 P[3] = {K.A, K.B, K.C};
-        part = self_potential_piece(P, g >> 1, g & 1, Q);
-    }
-    const unsigned group = 0xffu << (threadIdx.x & 24);
-    for (int off = 1; off < 8; off <<= 1) part += __shfl_xor_sync(group, part, off, 8);
-    if (g != 0) return;
+    const PanelJ K = load_panel(A.panels, A.pairs[t].x);
+    const d3 P[3] = {K.A, K.B, K.C};
+    return self_potential_piece(P, g >> 1, g & 1, Q);
+}
+
+// the parts of a lane's six-lane group, added in a fixed order (every lane of the warp calls it)
+__device__ __forceinline__ double self_gather6(double part)
+{
+    const int lane = threadIdx.x & 31, base = lane - lane % 6;
+    double sum = 0.0;
+    for (int k = 0; k < 6; ++k) sum += __shfl_sync(0xffffffffu, part, (base + k) & 31);
+    return sum;
+}
+
+__device__ __forceinline__ void self_store(const ClassArgs &A, int self_sign, long long t, double part)
+{
+    const PanelJ K = load_panel(A.panels, A.pairs[t].x);
     const double th = self_sign == 0 ? 0.0 : (self_sign > 0 ? kTwoPi : -kTwoPi) * K.S;
     const d3 J = kInv4Pi * (th * K.n);
     double *raw = A.raw4 + 4 * t;
@@ -488,8 +498,11 @@ __device__ __forceinline__ void self_item(const ClassArgs &A, const QuadTables &
 
 __global__ void __launch_bounds__(128) k_self(ClassArgs A, QuadTables Q, int self_sign)
 {
-    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if ((gid >> 3) < A.n) self_item(A, Q, self_sign, gid >> 3, threadIdx.x & 7);
+    const int lane = threadIdx.x & 31, k = lane / 6;
+    const long long t = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kSelfPairsPerWarp + k;
+    const bool valid = k < kSelfPairsPerWarp && t < A.n;
+    const double sum = self_gather6(valid ? self_piece_of(A, Q, t, lane % 6) : 0.0);
+    if (valid && lane % 6 == 0) self_store(A, self_sign, t, sum);
 }
 
 // ------------------------------------------------------------------ batched stages
@@ -551,15 +564,25 @@ __global__ void __launch_bounds__(128) k_batch_pot_final(const BatchSeg *__restr
 __global__ void __launch_bounds__(128) k_batch_self(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q, int self_sign)
 {
     extern __shared__ long long prefix[];
-    // eight items per pair; every segment's item count is a multiple of 8, and so is the grid's
-    // thread count, so a pair's items land in one aligned group of eight lanes
     const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
-        return S.cls == kSelf && S.A.n > 0 ? 8LL * S.A.n : 0;
+        return S.cls == kSelf && S.A.n > 0 ? S.A.n : 0;
     });
-    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
-        const int sg = seg_find(prefix, nseg, g);
-        const long long loc = g - prefix[sg];
-        self_item(segs[sg].A, Q, self_sign, loc >> 3, (int)(loc & 7));
+    // five pairs to a warp (as k_self); the loop is uniform over the warp
+    const int lane = threadIdx.x & 31, k = lane / 6;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * kSelfPairsPerWarp < total; w += nwarps) {
+        const long long g = w * kSelfPairsPerWarp + k;
+        const bool valid = k < kSelfPairsPerWarp && g < total;
+        int sg = 0;
+        long long t = 0;
+        double part = 0.0;
+        if (valid) {
+            sg = seg_find(prefix, nseg, g);
+            t = g - prefix[sg];
+            part = self_piece_of(segs[sg].A, Q, t, lane % 6);
+        }
+        const double sum = self_gather6(part);
+        if (valid && lane % 6 == 0) self_store(segs[sg].A, self_sign, t, sum);
     }
 }
 
@@ -615,7 +638,8 @@ void launch_finalize(int cls, const ClassArgs &A, int mode, cudaStream_t s)
 
 void launch_self(const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, cudaStream_t s)
 {
-    k_self<<<blocks_for(8LL * A.n, 128), 128, 0, s>>>(A, Q, cfg.self_sign);
+    const long long warps = (A.n + kSelfPairsPerWarp - 1) / kSelfPairsPerWarp;
+    k_self<<<blocks_for(32 * warps, 128), 128, 0, s>>>(A, Q, cfg.self_sign);
 }
 
 void launch_pot_hard(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s)
@@ -647,7 +671,8 @@ void launch_batch_pot_chain(const BatchSeg *segs, int nseg, const QuadTables &Q,
 void launch_batch_self(const BatchSeg *segs, int nseg, long long self_pairs, const QuadTables &Q, const RunConfig &cfg, cudaStream_t s)
 {
     if (self_pairs <= 0) return;
-    const int blocks = std::max(1, std::min(blocks_for(8 * self_pairs, 128), 1 << 16));
+    const long long warps = (self_pairs + kSelfPairsPerWarp - 1) / kSelfPairsPerWarp;
+    const int blocks = std::max(1, std::min(blocks_for(32 * warps, 128), 1 << 16));
     for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
         const int nc = std::min(kBatchSegChunk, nseg - c0);
         k_batch_self<<<blocks, 128, seg_smem(nc), s>>>(segs + c0, nc, Q, cfg.self_sign);
