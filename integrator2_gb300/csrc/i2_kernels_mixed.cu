@@ -426,16 +426,13 @@ __device__ __forceinline__ void singular_mixed_item(const ClassArgs &A, const Qu
     else shifts_vertex(ci, cj, si, sj);
     // FP64: closed-form singular part (a4 / a5) and, for the vertex class, the asymptote's constants
     {
-        const Tri Ti0 = load_tri(A.panels, pr.x);
-        const Tri T0[3] = {Ti0, Tri{Ti0.b, Ti0.c, Ti0.a}, Tri{Ti0.c, Ti0.a, Ti0.b}};
-        const Tri Tj0 = Tri{Kd.A, Kd.B, Kd.C};
-        const Tri J0[3] = {Tj0, Tri{Tj0.b, Tj0.c, Tj0.a}, Tri{Tj0.c, Tj0.a, Tj0.b}};
+        const Tri Ti = rotate(load_tri(A.panels, pr.x), si), Tj = rotate(Tri{Kd.A, Kd.B, Kd.C}, sj);
         d3 psi;
         double th;
-        if (CLS == kEdge) closed_edge(T0[si], J0[sj], ni, Kd.n, Si, psi, th);
+        if (CLS == kEdge) closed_edge(Ti, Tj, ni, Kd.n, Si, psi, th);
         else {
-            closed_vertex(T0[si], J0[sj], ni, Kd.n, Si, psi, th);
-            const d3 ta = unit(J0[sj].a - J0[sj].c), tb = unit(J0[sj].b - J0[sj].a);
+            closed_vertex(Ti, Tj, ni, Kd.n, Si, psi, th);
+            const d3 ta = unit(Tj.a - Tj.c), tb = unit(Tj.b - Tj.a);
             double dA, dB;
             const d3 e = vertex_direction(ni, Kd.n, ta, tb, dA, dB);
             const d3 w1 = cross(ta, e), p1 = e - ta, w2 = cross(tb, e), p2 = e + tb;
