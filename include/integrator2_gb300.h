@@ -140,8 +140,8 @@ i2_status i2_integrator_set_error_control(i2_integrator_t *it, i2_error_control 
 i2_status i2_integrator_get_error_control(const i2_integrator_t *it, i2_error_control *mode, int32_t *level);
 i2_status i2_integrator_set_precision(i2_integrator_t *it, i2_precision precision);
 /* potential rule of common-edge / common-vertex pairs (graded Duffy, n_radial x n_angular per
- * piece, radial grading exponent) and of self pairs (n_self points per edge piece; 0 = by
- * precision: 24 in FP64, 12 in the mixed form) */
+ * piece, radial grading exponent) and of self pairs (n_self points per edge piece of the graded
+ * edge rule; 0 = the closed form, exact, the default in both precisions) */
 i2_status i2_integrator_set_potential_rule(i2_integrator_t *it, int32_t n_radial, int32_t n_angular, int32_t grading,
                                            int32_t n_self);
 /* relative tolerance of the locally adaptive potential rule used for hard common-edge /

@@ -166,8 +166,8 @@ class NumericalIntegrator3D:
         call("i2_integrator_set_precision", self._h, int(precision))
 
     def setPotentialRule(self, n_radial=10, n_angular=8, grading=3, n_self=0) -> None:
-        """graded Duffy rule of adjacent pairs; n_self points per edge piece of the self-pair rule
-        (0: 24 in FP64, 12 in the mixed form)"""
+        """graded Duffy rule of adjacent pairs; n_self points per edge piece of the self-pair edge
+        rule (0: the closed form, exact, the default in both precisions)"""
         call("i2_integrator_set_potential_rule", self._h, n_radial, n_angular, grading, n_self)
 
     def setHardPairTolerance(self, rel_tol: float) -> None:

@@ -226,11 +226,11 @@ struct i2_integrator {
     i2::RunConfig cfg;
     int precision = I2_PRECISION_FP64;
     int pot_nu = 10, pot_nv = 8, pot_grade = 3;
-    // points per edge piece of the self-pair rule; 0: by precision, 24 in FP64 (1e-12 of a 96-point
-    // rule on the 20,480-triangle jittered sphere, needle cells included) and 12 in the mixed form
-    // (4e-8 there, against its 1e-6 target)
+    // points per edge piece of the self-pair rule; 0 (default): the closed form in both precisions
+    // (exact; the edge rule converges slowly on distorted cells: 8e-6 at 12 points on a sphere
+    // jittered by 0.3 h)
     int pot_nself = 0;
-    int self_points() const { return pot_nself > 0 ? pot_nself : (precision == I2_PRECISION_MIXED ? 12 : 24); }
+    int self_points() const { return pot_nself > 0 ? pot_nself : 0; }
     i2::QuadTables tables() const
     {
         i2::QuadTables Q;

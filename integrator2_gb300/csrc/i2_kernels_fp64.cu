@@ -468,10 +468,13 @@ static void pot_adaptive_chain(const ClassArgs &A, const QuadTables &Q, double t
 // lanes left two of every eight idle).
 constexpr int kSelfPairsPerWarp = 5;
 
+// lane g (0..5) of a pair's group: one (edge, piece) of the edge rule, or, for the closed form
+// (Q.nself == 0), the whole value on lane 0
 __device__ __forceinline__ double self_piece_of(const ClassArgs &A, const QuadTables &Q, long long t, int g)
 {
     const PanelJ K = load_panel(A.panels, A.pairs[t].x);
     const d3 P[3] = {K.A, K.B, K.C};
+    if (Q.nself == 0) return g == 0 ? self_potential_closed(P) : 0.0;
     return self_potential_piece(P, g >> 1, g & 1, Q);
 }
 

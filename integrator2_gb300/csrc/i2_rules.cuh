@@ -220,11 +220,37 @@ __device__ R self_potential_piece(const V3<R> P[3], int e, int piece, const Quad
     return (1.0 / (s * s * s)) * self_potential_piece_unit(Ps, e, piece, Q);
 }
 
-// int_K int_K 1/|x - y| (no 1/4pi) of the triangle (P0, P1, P2)
+// int_K int_K 1/|x - y| in closed form: (4 S^2 / 3) sum_s ln(p / (p - 2 s)) / s over the sides s,
+// p the perimeter.  Scaling K about the vertex opposite an edge e moves only e, so Euler's relation
+// for this integral (homogeneous of degree 3) gives F = (2 H_e / 3) int_e phi ds, H_e the height
+// over e and phi the potential of K (both integrals' domains move).  On e, phi is the sum over the
+// other two edges of t L (distance to the edge line times the edge log); along e these integrate
+// in closed form because d/du ln((r + u + c) / (r + u - c)) = -c / (u r) (u the distance from the
+// edge's end, r the distance to its far end, c its length), and the logs combine into the
+// symmetric form.  Only the longest side's p - 2s can cancel (a flat cell): the smallest of the
+// three is taken from Heron's 16 S^2 = p prod_s (p - 2 s), S from the cross product.  No absolute
+// threshold: exact at every scale.
+template <class R>
+__device__ R self_potential_closed(const V3<R> P[3])
+{
+    const R a = norm(P[2] - P[1]), b = norm(P[0] - P[2]), c = norm(P[1] - P[0]);
+    const V3<R> cr = cross(P[1] - P[0], P[2] - P[0]);
+    const R s4 = dot(cr, cr);  // (2S)^2
+    const R p = a + b + c;
+    R da = (b + c) - a, db = (c + a) - b, dc = (a + b) - c;
+    if (value_of(da) <= value_of(db) && value_of(da) <= value_of(dc)) da = 4.0 * s4 / (p * db * dc);
+    else if (value_of(db) <= value_of(dc)) db = 4.0 * s4 / (p * da * dc);
+    else dc = 4.0 * s4 / (p * da * db);
+    return (1.0 / 3.0) * s4 * (log(p / da) / a + log(p / db) / b + log(p / dc) / c);
+}
+
+// int_K int_K 1/|x - y| (no 1/4pi) of the triangle (P0, P1, P2): the closed form when the rule
+// has no points (Q.nself == 0, the default), else the edge rule above
 template <class R>
 __device__ R self_potential(V3<R> P0, V3<R> P1v, V3<R> P2v, const QuadTables &Q)
 {
     const V3<R> P[3] = {P0, P1v, P2v};
+    if (Q.nself == 0) return self_potential_closed(P);
     R total = 0.0;
 #pragma unroll 1
     for (int e = 0; e < 3; ++e) total += self_potential_piece(P, e, 0, Q) + self_potential_piece(P, e, 1, Q);

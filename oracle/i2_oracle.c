@@ -592,10 +592,32 @@ static inline double ray_side(double a, double alpha, double u1)
     return 0.5 * a * a * sa * sa * (F1 - F0);
 }
 
-/* Gauss-Legendre points per piece of the self-pair rule used by o_integrate_class (default 96;
- * the library's default is 24) */
+/* Gauss-Legendre points per piece of the self-pair rule used by o_integrate_class (default 96);
+ * 0 selects the closed form below (the library's default) */
 static int g_self_nquad = 96;
-void o_set_self_rule(int nquad) { g_self_nquad = nquad; }
+void o_set_self_rule(int nquad) { g_self_nquad = nquad < 0 ? 0 : nquad; }
+
+/* Self potential in closed form, the library's default self rule:
+ *   int_K int_K 1/|x-y| = (4 S^2 / 3) sum over the sides s of ln(p / (p - 2 s)) / s,
+ * p the perimeter.  Scaling K about the vertex opposite edge e moves only e, so Euler's relation
+ * (the integral is homogeneous of degree 3) gives (2 H_e / 3) int_e phi ds, phi the potential of K;
+ * on e, phi = sum of t L over the other two edges, and d/du ln((r + u + c) / (r + u - c)) =
+ * -c / (u r) makes those edge integrals elementary.  The smallest p - 2 s (the longest side, which
+ * cancels in a flat cell) is taken from Heron's 16 S^2 = p prod (p - 2 s).  Checked against the
+ * 96-point edge rule (o_self_potential) in the CPU tests. */
+double o_self_potential_closed(const double *Ap, const double *Bp, const double *Cp)
+{
+    v3 A = ld(Ap), B = ld(Bp), C = ld(Cp);
+    double a = len(sub(C, B)), b = len(sub(A, C)), c = len(sub(B, A));
+    v3 cr = crs(sub(B, A), sub(C, A));
+    double s4 = dot(cr, cr); /* (2S)^2 */
+    double p = a + b + c;
+    double da = (b + c) - a, db = (c + a) - b, dc = (a + b) - c;
+    if (da <= db && da <= dc) da = 4.0 * s4 / (p * db * dc);
+    else if (db <= dc) db = 4.0 * s4 / (p * da * dc);
+    else dc = 4.0 * s4 / (p * da * db);
+    return O_INV_4PI * (s4 / 3.0) * (log(p / da) / a + log(p / db) / b + log(p / dc) / c);
+}
 
 double o_self_potential(const double *Ap, const double *Bp, const double *Cp, int nquad)
 {
@@ -1066,7 +1088,7 @@ int o_integrate_class(int cls, int ntasks, const int *ti, const int *tj,
             v3 J = finalize_j(O_FAR, r, nj, S[i]);
             if (raw4) memcpy(raw4 + 4 * t, r.v, sizeof r.v);
             if (J3) { J3[3 * t] = J.x; J3[3 * t + 1] = J.y; J3[3 * t + 2] = J.z; }
-            if (P) P[t] = o_self_potential(&a.x, &b.x, &c.x, g_self_nquad);
+            if (P) P[t] = g_self_nquad > 0 ? o_self_potential(&a.x, &b.x, &c.x, g_self_nquad) : o_self_potential_closed(&a.x, &b.x, &c.x);
             if (levels) levels[t] = 0;
             continue;
         }

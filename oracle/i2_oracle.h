@@ -65,6 +65,7 @@ int o_pair_is_hard(int i, int j, const double *V, const int *C);
 
 /* potential of a self pair (1/4pi included) */
 double o_self_potential(const double *A, const double *B, const double *C, int nquad);
+double o_self_potential_closed(const double *A, const double *B, const double *C);
 
 /*
  * Integrate one class of tasks.

@@ -57,6 +57,8 @@ def lib():
             L.o_integrate_class.restype = i
             L.o_self_potential.argtypes = [vp, vp, vp, i]
             L.o_self_potential.restype = d
+            L.o_self_potential_closed.argtypes = [vp, vp, vp]
+            L.o_self_potential_closed.restype = d
             L.o_potential_inner.argtypes = [vp, vp, vp, vp]
             L.o_potential_inner.restype = d
             L.o_theta_psi.argtypes = [vp, vp, vp, vp, vp]

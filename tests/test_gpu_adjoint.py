@@ -75,7 +75,7 @@ def test_adjoint_matches_oracle_gradient(setup):
 
     def oracle_loss(Vx):
         tot = 0.0
-        with O.potential_rule(10, 8, 3, adaptive=0, self_n=24):
+        with O.potential_rule(10, 8, 3, adaptive=0, self_n=0):
             for cls, (pr, ck) in enumerate(zip(lists, c)):
                 _, J, P, _ = O.integrate(cls, pr, Vx, C, mode=O.FIXED, level=1)
                 tot += float(np.sum(ck * (P + J @ w)))

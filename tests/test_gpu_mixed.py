@@ -189,3 +189,33 @@ def test_fp64_fixup_of_needle_pairs_matches_fp64_form(api):
         if cls == 2:
             assert (np.abs(P32 - P64) / np.abs(P64)).max() < 1e-11
     assert spread > 0  # levels 4-5 of some pairs ran spread over the GPU
+
+
+def test_mixed_adaptive_potential_of_hard_pairs(api):
+    """hard adjacent pairs (folded, or a corner below 10 degrees) take the adaptive potential rule
+    in FP64 in both forms (the mixed form with a 2e-8 floor on its tolerance): the FP32 potential
+    integrand is ill-conditioned there (emulated: per-pair biases of 1e-7 to 4e-5 on folded pairs
+    and slivers).  On a strongly jittered sphere (sigma 0.3 h: over 2,000 slivers and folds) the
+    potential of every hard pair stays within 5e-7 of the oracle's high-order answer in the FP64
+    form and within 1e-6 (rms 5e-8) in the mixed form"""
+    from integrator2_gb300 import meshes, pairs as P
+    from oracle import oracle as O
+    V, C = meshes.jittered_icosphere(3, 0.3, 7)
+    pl = P.build_pairs(V, C)
+    report = {}
+    for cls in (0, 1):
+        pr = pl.by_class(cls)
+        pr = np.ascontiguousarray(pr[O.hard_pairs(pr, V, C)])
+        assert len(pr) >= 20, (cls, len(pr))
+        with O.potential_rule(40, 32, 3, adaptive=1e-10, depth=18, every_pair=True):
+            _, _, oP, _ = O.integrate(cls, pr, V, C, mode=O.FIXED, level=0)
+        err = {}
+        for prec in (api.PRECISION_FP64, api.PRECISION_MIXED):
+            _, Pm, _ = _run(api, V, C, cls, pr, prec)
+            err[prec] = np.abs(Pm - oP) / np.abs(oP)
+        report[cls] = (len(pr), float(err[api.PRECISION_FP64].max()), float(err[api.PRECISION_MIXED].max()),
+                       float(np.sqrt(np.mean(err[api.PRECISION_MIXED] ** 2))))
+        assert err[api.PRECISION_FP64].max() < 5e-7, (cls, report[cls])
+        assert err[api.PRECISION_MIXED].max() < 1e-6, (cls, report[cls])
+        assert np.sqrt(np.mean(err[api.PRECISION_MIXED] ** 2)) < 5e-8, (cls, report[cls])
+    print("hard pairs (count, FP64 max, mixed max, mixed rms):", report)

@@ -133,6 +133,37 @@ def test_self_class(api, sign):
     assert (np.abs(Pg - oP) / oP).max() < 1e-9
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_self_potential_closed_form(api, precision):
+    """the default self rule (n_self = 0) is the closed form in both precisions: equal to the
+    oracle's closed form to rounding and to its 96-point edge rule to 1e-12 on a well-shaped
+    mesh; on a sphere jittered by 0.3 h (where the edge rule itself is only good to ~1e-10) and at
+    scale 2^-12 (where the oracle's edge rule has no valid thresholds) it still matches the
+    oracle's closed form"""
+    from integrator2_gb300 import meshes
+    from oracle import oracle as O
+    for V, C, bar96 in ((*meshes.jittered_icosphere(3, 0.15, 4), 1e-12), (*meshes.jittered_icosphere(3, 0.3, 7), None)):
+        for scale in (1.0, 2.0 ** -12):
+            Vs = V * scale
+            pairs = np.stack([np.arange(len(C)), np.arange(len(C))], 1)
+            m = api.Mesh3D()
+            m.setGeometry(Vs, C)
+            m.prepareMesh(3.0)
+            it = api.NumericalIntegrator3D(m, api.qf3D13)
+            it.setFixedRefinementLevel(0)
+            if precision == "mixed":
+                it.setPrecision(api.PRECISION_MIXED)
+            ev = api.EvaluatorJ3DK(m, it)
+            ev.runClass(3, pairs)
+            Pg = ev.getPotentials(3)
+            with O.potential_rule(self_n=0):
+                _, _, oP, _ = O.integrate(3, pairs, Vs, C, mode=O.FIXED)
+            assert (np.abs(Pg - oP) / oP).max() < 1e-14, (scale, (np.abs(Pg - oP) / oP).max())
+            if bar96 is not None and scale == 1.0:
+                _, _, o96, _ = O.integrate(3, pairs, Vs, C, mode=O.FIXED)
+                assert (np.abs(Pg - o96) / o96).max() < bar96
+
+
 def test_relative_mode_matches_oracle(api):
     from integrator2_gb300 import meshes, pairs as P
     from oracle import oracle as O
