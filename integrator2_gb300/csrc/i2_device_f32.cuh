@@ -60,6 +60,28 @@ __device__ __forceinline__ f3 df_edge(const PanelF *__restrict__ P, int q, int k
     return df_sub(w[2 * k], w[2 * k + 1], w[2 * m], w[2 * m + 1]);
 }
 
+// a - b for a = ah + al, b = bh + bl as an unevaluated sum hi + lo: Knuth's TwoSum gives the
+// exact rounding error of ah - bh, the low parts are added to it, and Fast2Sum renormalises
+__device__ __forceinline__ void df_diff(float ah, float al, float bh, float bl, float &hi, float &lo)
+{
+    const float s = ah - bh;
+    const float bb = s - ah;
+    const float e = (ah - (s - bb)) + (-bh - bb);
+    const float t = e + (al - bl);
+    hi = s + t;
+    lo = t - (hi - s);
+}
+
+// vertex k minus vertex m of panel q in double-float
+__device__ __forceinline__ void df_edge_pair(const PanelF *__restrict__ P, int q, int k, int m, f3 &hi, f3 &lo)
+{
+    const float4 *w = P[q].v;
+    const float4 kh = w[2 * k], kl = w[2 * k + 1], mh = w[2 * m], ml = w[2 * m + 1];
+    df_diff(kh.x, kl.x, mh.x, ml.x, hi.x, lo.x);
+    df_diff(kh.y, kl.y, mh.y, ml.y, hi.y, lo.y);
+    df_diff(kh.z, kl.z, mh.z, ml.z, hi.z, lo.z);
+}
+
 __device__ __forceinline__ PanelJf load_panel_f(const PanelF *__restrict__ P, int c)
 {
     const float4 *w = P[c].v;

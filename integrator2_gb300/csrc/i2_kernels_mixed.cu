@@ -223,20 +223,43 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
                 }
             }
             // K_i's vertices as offsets from each vertex of K_j, in the (rotated) order the
-            // integrand expects: every point-to-vertex offset keeps full relative precision
+            // integrand expects: every point-to-vertex offset keeps full relative precision.
+            // The disjoint class keeps only the offsets from A and forms a point's offsets from B
+            // and C as (o_A - e_hi) - e_lo with K_j's edges B - A, C - A in double-float: o_A's
+            // rounding is then a shift of the point shared by all three offsets (harmless), the
+            // two subtractions add half an ulp each, and no rounded edge vector enters the logs
+            // (that would be a per-pair bias, amplified by the cancellation in Psi).  Two
+            // sub-cell walks and 18 live floats fewer.
             TriF T0, T1, T2;
+            f3 ABh, ABl, ACh, ACl;
             df_offsets(A.panels_f, pr.x, pr.y, origin, T0.a, T0.b, T0.c);
-            df_offsets(A.panels_f, pr.x, pr.y, (origin + 1) % 3, T1.a, T1.b, T1.c);
-            df_offsets(A.panels_f, pr.x, pr.y, (origin + 2) % 3, T2.a, T2.b, T2.c);
+            if (CLS == kFar) {
+                df_edge_pair(A.panels_f, pr.y, 1, 0, ABh, ABl);
+                df_edge_pair(A.panels_f, pr.y, 2, 0, ACh, ACl);
+            } else {
+                df_offsets(A.panels_f, pr.x, pr.y, (origin + 1) % 3, T1.a, T1.b, T1.c);
+                df_offsets(A.panels_f, pr.x, pr.y, (origin + 2) % 3, T2.a, T2.b, T2.c);
+            }
             for (int s = lane_g * per_lane; s < (lane_g + 1) * per_lane; ++s) {
-                const TriF U0 = subcellf(T0, level, s), U1 = subcellf(T1, level, s), U2 = subcellf(T2, level, s);
+                const TriF U0 = subcellf(T0, level, s);
+                TriF U1, U2;
+                if (CLS != kFar) {
+                    U1 = subcellf(T1, level, s);
+                    U2 = subcellf(T2, level, s);
+                }
                 float c0 = 0, c1 = 0, c2 = 0, c3 = 0, c4 = 0;
 #pragma unroll 1
                 for (int g = 0; g < Qf.npts; ++g) {
                     const float l1 = Qf.L1[g], l2 = Qf.L2[g], l3 = Qf.L3[g];
                     const f3 oA = l1 * U0.a + l2 * U0.b + l3 * U0.c;
-                    const f3 oB = l1 * U1.a + l2 * U1.b + l3 * U1.c;
-                    const f3 oC = l1 * U2.a + l2 * U2.b + l3 * U2.c;
+                    f3 oB, oC;
+                    if (CLS == kFar) {
+                        oB = (oA - ABh) - ABl;
+                        oC = (oA - ACh) - ACl;
+                    } else {
+                        oB = l1 * U1.a + l2 * U1.b + l3 * U1.c;
+                        oC = l1 * U2.a + l2 * U2.b + l3 * U2.c;
+                    }
                     f3 psi;
                     float th, pot = 0.0f;
                     if (CLS == kFar) far_field_integrand_f(oA, oB, oC, K, F, psi, th, pot);
