@@ -462,8 +462,9 @@ def adjoint_section(args):
 FAR_CHAIN_DRAM_BYTES = 147407616 + 91512576
 
 # FP32 operation counts of the far-field integrand (far_field_integrand_f with the point's
-# offsets): flops, sqrtf, divide, log1pf, atan2f
-POINT_OPS_F32 = {"far": (203, 3, 6, 3, 1)}
+# offsets: o_A interpolated from the sub-cell, 15 flops; o_B and o_C as o_A minus K_j's edges in
+# double-float, 12 flops): flops, sqrtf, divide, log1pf, atan2f
+POINT_OPS_F32 = {"far": (185, 3, 6, 3, 1)}
 
 
 def point_flops_f32(cal):
