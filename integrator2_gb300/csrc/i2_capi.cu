@@ -312,6 +312,7 @@ struct Workspace {
     DevBuf<int> stop, act_a, act_b, cnt, maxlev, hard_list, tier2_list, tier2b_list, pot_qcnt, fix_deep;
     DevBuf<i2::PotCellItem> pot_q_a, pot_q_b;
     DevBuf<long long> pot_fx;
+    DevBuf<double> pot_ctx, pot_tri_a, pot_tri_b;
     DevBuf<double> fix_base, fix_part;
     DevBuf<int2> pairs;
 };
@@ -543,6 +544,13 @@ double adaptive_tolerance(const i2::RunConfig &cfg, bool mixed)
 // at depth 1; deeper lists hold a few tens of thousands of cells on the meshes measured (C2: at
 // most 27,516).  Capped at 2^26 cells (1.5 GB per list).
 size_t pot_queue_capacity(int64_t n) { return (size_t)std::min<int64_t>(std::max<int64_t>(4 * n, 1 << 18), 1 << 26); }
+// caches of the adaptive potential, sized to the class (hard pairs are a small fraction; entries
+// past the caps are recomputed): hard-pair set-ups, and parent-cell triangles per depth list
+int pot_ctx_capacity(int64_t n)
+{
+    return (int)std::min<int64_t>(std::min<int64_t>(n, (int64_t)pot_queue_capacity(n) / 4), std::max<int64_t>(4096, n / 16));
+}
+int pot_tri_capacity(int64_t n) { return (int)std::min<int64_t>((int64_t)pot_queue_capacity(n) / 4, std::max<int64_t>(16384, n / 4)); }
 
 i2_pair_class checked_class(int cls)
 {
@@ -601,6 +609,9 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         W.pot_q_b.reserve(pot_queue_capacity(n));
         W.pot_qcnt.reserve(16);
         W.pot_fx.reserve(n);
+        W.pot_ctx.reserve((size_t)i2::kPotCtxDoubles * pot_ctx_capacity(n));
+        W.pot_tri_a.reserve(9 * (size_t)pot_tri_capacity(n));
+        W.pot_tri_b.reserve(9 * (size_t)pot_tri_capacity(n));
         if (ev->integrator->precision == I2_PRECISION_MIXED) W.ctx_e.reserve((size_t)i2::kVertexCtxFloats * n);
     }
     // the run's counters (layout: kCnt* in i2_engine.h)
@@ -640,6 +651,11 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         A.pot_qcap = (int)pot_queue_capacity(n);
         A.pot_qcnt = W.pot_qcnt.ptr;
         A.pot_fx = W.pot_fx.ptr;
+        A.pot_ctx = W.pot_ctx.ptr;
+        A.pot_ctx_cap = pot_ctx_capacity(n);
+        A.pot_tri_a = W.pot_tri_a.ptr;
+        A.pot_tri_b = W.pot_tri_b.ptr;
+        A.pot_tri_cap = pot_tri_capacity(n);
         A.tier2_cnt = W.cnt.ptr + i2::kCntTier2;
         A.tier_tol = tier_tol;
         A.top_tol = top_tol;
@@ -710,6 +726,7 @@ struct BatchSegment {
     DevBuf<double> fix_base, fix_part;
     DevBuf<i2::PotCellItem> pot_q_a, pot_q_b;
     DevBuf<long long> pot_fx;
+    DevBuf<double> pot_ctx, pot_tri_a, pot_tri_b;
     DevBuf<float> ctx_e;
     i2::ClassArgs args;
 };
@@ -1350,6 +1367,8 @@ i2_status i2_batch_add(i2_batch_t *batch, const i2_mesh_t *mesh, i2_pair_class c
         if (adj) {
             sp->sing.reserve(4 * m); sp->padj.reserve(m); sp->hard_list.reserve(m); sp->tier2_list.reserve(m); sp->tier2b_list.reserve(m); sp->ctx_e.reserve((size_t)i2::kVertexCtxFloats * m);
             sp->pot_q_a.reserve(pot_queue_capacity(m)); sp->pot_q_b.reserve(pot_queue_capacity(m)); sp->pot_qcnt.reserve(16); sp->pot_fx.reserve(m);
+            sp->pot_ctx.reserve((size_t)i2::kPotCtxDoubles * pot_ctx_capacity(m));
+            sp->pot_tri_a.reserve(9 * (size_t)pot_tri_capacity(m)); sp->pot_tri_b.reserve(9 * (size_t)pot_tri_capacity(m));
         }
         i2::ClassArgs &A = sp->args;
         A.n = (int)n;
@@ -1366,6 +1385,8 @@ i2_status i2_batch_add(i2_batch_t *batch, const i2_mesh_t *mesh, i2_pair_class c
             A.tier2_list = sp->tier2_list.ptr; A.tier2_cnt = sp->cnt.ptr + i2::kCntTier2; A.tier2b_list = sp->tier2b_list.ptr;
             A.pot_q_a = sp->pot_q_a.ptr; A.pot_q_b = sp->pot_q_b.ptr; A.pot_qcap = (int)pot_queue_capacity(m);
             A.pot_qcnt = sp->pot_qcnt.ptr; A.pot_fx = sp->pot_fx.ptr;
+            A.pot_ctx = sp->pot_ctx.ptr; A.pot_ctx_cap = pot_ctx_capacity(m);
+            A.pot_tri_a = sp->pot_tri_a.ptr; A.pot_tri_b = sp->pot_tri_b.ptr; A.pot_tri_cap = pot_tri_capacity(m);
             A.tier_tol = tier_tolerance(batch->cfg);
             A.top_tol = top_tolerance(batch->cfg, true);
         }

@@ -40,6 +40,9 @@ struct RunConfig {
     double hard_tol = 1e-8;  // relative tolerance of the adaptive potential of hard adjacent pairs (0: off)
 };
 
+// doubles of one hard pair's cached FP64 set-up (PotPairCtx in i2_kernels_fp64.cu)
+constexpr int kPotCtxDoubles = 54;
+
 // one cell of the breadth-first adaptive potential rule of hard adjacent pairs
 struct PotCellItem {
     unsigned long long path;  // base-4 digits of the sub-cell of K_i, first split most significant
@@ -81,6 +84,14 @@ struct ClassArgs {
     int pot_qcap = 0;                         // capacity of each list (>= 4 x hard pairs)
     int *pot_qcnt = nullptr;                  // cells per depth (kHardMaxDepth + 2 ints)
     long long *pot_fx = nullptr;              // per hard pair: accepted sums in 64-bit fixed point
+    // caches of the adaptive potential, bit-identical to recomputing (entries past a cap are
+    // recomputed): per hard pair its FP64 set-up (kPotCtxDoubles doubles, written by the seed),
+    // and per splitting cell its triangle (9 doubles at the children's slot / 4 in the next
+    // depth's list; two ping-pong arrays like the cell lists)
+    double *pot_ctx = nullptr;
+    int pot_ctx_cap = 0;
+    double *pot_tri_a = nullptr, *pot_tri_b = nullptr;
+    int pot_tri_cap = 0;
     double tier_tol = 1e-7;                   // main/check (and main/higher-order) rule agreement bar
     double top_tol = 1e-8;                    // 16 x 16 / 24 x 24 agreement bar (tier 2b)
     // outputs

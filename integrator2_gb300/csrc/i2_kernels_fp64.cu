@@ -292,6 +292,31 @@ __device__ __forceinline__ PotPairCtx pot_pair_ctx(const ClassArgs &A, int t, do
     return c;
 }
 
+static_assert(sizeof(PotPairCtx) == 8 * kPotCtxDoubles, "cached hard-pair set-up size");
+
+// the cached set-up of hard pair h (written by the seed), or the set-up recomputed past the cap
+template <int CLS>
+__device__ __forceinline__ PotPairCtx pot_ctx_of(const ClassArgs &A, int h, int t, double tol)
+{
+    if (h < A.pot_ctx_cap) return *reinterpret_cast<const PotPairCtx *>(A.pot_ctx + (long long)kPotCtxDoubles * h);
+    return pot_pair_ctx<CLS>(A, t, tol);
+}
+
+// cell triangles of the parents of depth d's cells (written while depth d - 1 split them)
+__device__ __forceinline__ double *pot_tri_list(const ClassArgs &A, int depth) { return depth % 2 ? A.pot_tri_a : A.pot_tri_b; }
+
+__device__ __forceinline__ void pot_tri_store(double *dst, const Tri &T)
+{
+    dst[0] = T.a.x; dst[1] = T.a.y; dst[2] = T.a.z;
+    dst[3] = T.b.x; dst[4] = T.b.y; dst[5] = T.b.z;
+    dst[6] = T.c.x; dst[7] = T.c.y; dst[8] = T.c.z;
+}
+
+__device__ __forceinline__ Tri pot_tri_load(const double *p)
+{
+    return Tri{mk(p[0], p[1], p[2]), mk(p[3], p[4], p[5]), mk(p[6], p[7], p[8])};
+}
+
 // the four children of cell T (corner slot of each in cc[]) integrated by one warp: the lanes
 // stride over the flattened (child, quadrature point) list -- the graded Duffy rule for a child
 // that holds the shared vertex, the 13-point rule otherwise -- and a butterfly leaves the four
@@ -375,7 +400,11 @@ __device__ __forceinline__ void pot_seed_item(const ClassArgs &A, const QuadTabl
     double v[4];
     pot_children_warp<CLS>(c.Ti, cc, c, Q, lane, v);
     if (lane < 4) A.pot_q_a[4 * (long long)h + lane] = PotCellItem{(unsigned long long)lane, v[lane], h, cc[lane]};
-    if (lane == 0) A.pot_fx[h] = 0;
+    if (lane == 0) {
+        A.pot_fx[h] = 0;
+        if (h < A.pot_ctx_cap) *reinterpret_cast<PotPairCtx *>(A.pot_ctx + (long long)kPotCtxDoubles * h) = c;
+        if (h < A.pot_tri_cap) pot_tri_store(pot_tri_list(A, 1) + 9LL * h, c.Ti);  // parent of depth 1's slots 4h..4h+3
+    }
 }
 
 template <int CLS>
@@ -397,8 +426,10 @@ __device__ __forceinline__ void pot_depth_item(const ClassArgs &A, const QuadTab
     const PotCellItem it = in[idx];
     if (it.h < 0) return;
     const int t = A.hard_list[it.h];
-    const PotPairCtx c = pot_pair_ctx<CLS>(A, t, tol);
-    const Tri T = subcell(c.Ti, depth, (int)it.path);
+    const PotPairCtx c = pot_ctx_of<CLS>(A, it.h, t, tol);
+    // siblings sit at 4 consecutive slots, so the parent's triangle is at slot idx / 4
+    const Tri T = (idx >> 2) < A.pot_tri_cap ? child(pot_tri_load(pot_tri_list(A, depth) + 9LL * (idx >> 2)), (int)(it.path & 3))
+                                             : subcell(c.Ti, depth, (int)it.path);
     int cc[4];
     for (int k = 0; k < 4; ++k) cc[k] = child_corner(it.corner, k);
     double v[4];
@@ -410,6 +441,7 @@ __device__ __forceinline__ void pot_depth_item(const ClassArgs &A, const QuadTab
         const int pos = atomicAdd(&A.pot_qcnt[depth + 1], 4);
         if (pos + 4 <= A.pot_qcap) {
             for (int k = 0; k < 4; ++k) out[pos + k] = PotCellItem{(it.path << 2) | (unsigned long long)k, v[k], it.h, cc[k]};
+            if ((pos >> 2) < A.pot_tri_cap) pot_tri_store(pot_tri_list(A, depth + 1) + 9LL * (pos >> 2), T);
         } else {
             // list full: keep this cell's sum (counted as an overflow) and blank the slots it
             // was given below the capacity, so the next depth skips them
@@ -425,7 +457,7 @@ __device__ __forceinline__ int pot_depth_count(const ClassArgs &A, int depth) { 
 
 // one depth: one warp per cell
 template <int CLS>
-__global__ void __launch_bounds__(128) k_pot_depth(ClassArgs A, QuadTables Q, double tol, int depth, const PotCellItem *__restrict__ in,
+__global__ void __launch_bounds__(128, 3) k_pot_depth(ClassArgs A, QuadTables Q, double tol, int depth, const PotCellItem *__restrict__ in,
                                                    PotCellItem *__restrict__ out)
 {
     const int count = pot_depth_count(A, depth);
@@ -439,7 +471,7 @@ template <int CLS>
 __device__ __forceinline__ void pot_final_item(const ClassArgs &A, double tol, int h)
 {
     const int t = A.hard_list[h];
-    const PotPairCtx c = pot_pair_ctx<CLS>(A, t, tol);
+    const PotPairCtx c = pot_ctx_of<CLS>(A, h, t, tol);
     A.padj[t] = kInv4Pi * ((double)A.pot_fx[h] / c.scale + c.sig_int);
 }
 
@@ -531,7 +563,7 @@ __global__ void __launch_bounds__(128) k_batch_pot_seed(const BatchSeg *__restri
     }
 }
 
-__global__ void __launch_bounds__(128) k_batch_pot_depth(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q, double tol, int depth)
+__global__ void __launch_bounds__(128, 3) k_batch_pot_depth(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q, double tol, int depth)
 {
     extern __shared__ long long prefix[];
     const long long total = seg_prefix(segs, nseg, prefix, [depth](const BatchSeg &S) -> long long {
