@@ -576,8 +576,8 @@ __global__ void __launch_bounds__(128) k_pot_tier2_mixed(ClassArgs A, QuadTables
 // there (measured: errors up to 1e-3 on the 20,480-triangle jittered sphere, whose two needles
 // have corners of 0.6 and 1.5 degrees).  After the mixed chain has finished, each such pair's
 // regular part is recomputed in FP64 by one whole block, the threads striding over the 4^L
-// sub-cells (a few pairs at level 5 would otherwise set the time), and J (and the disjoint
-// class's potential) is finalised again.  Other pairs cost two loads.
+// sub-cells x 13 points (a few pairs at level 5 would otherwise set the time), and J (and the
+// disjoint class's potential) is finalised again.  Other pairs cost two loads.
 template <int CLS>
 struct FixupPair {
     PanelJ K;
@@ -596,20 +596,20 @@ __device__ acc5 fixup_level_sum(const FixupPair<CLS> &p, const QuadTables &Q, in
     const int nsub = 1 << (2 * level);
     const double Ssub = p.Si * ldexp(1.0, -2 * level);
     acc5 acc = zero5();
-    for (int sc = threadIdx.x; sc < nsub; sc += blockDim.x) {
+    // the flattened (sub-cell, point) list over the block: level 0's 13 points already keep 13
+    // threads busy (one thread per sub-cell left levels 0-2 nearly idle), at the price of one
+    // sub-cell walk (at most kFixDirect midpoint splits) per point
+    const int total = nsub * Q.npts;
+    for (int j = threadIdx.x; j < total; j += blockDim.x) {
+        const int sc = j / Q.npts, g = j - sc * Q.npts;
         const Tri T = subcell(p.Ti, level, sc);
-        acc5 cell = zero5();
-        for (int g = 0; g < Q.npts; ++g) {
-            const d3 x = Q.L1[g] * T.a + Q.L2[g] * T.b + Q.L3[g] * T.c;
-            d3 psi;
-            double th, pot = 0.0;
-            if (CLS == kFar) far_integrand(x, p.K, p.F, psi, th, pot);
-            else if (CLS == kEdge) edge_integrand(x, p.K, p.E, psi, th);
-            else vertex_integrand(x, p.K, p.Vx, psi, th);
-            axpy5(cell, Q.w[g], psi, th, pot);
-        }
-        acc.px += Ssub * cell.px; acc.py += Ssub * cell.py; acc.pz += Ssub * cell.pz;
-        acc.th += Ssub * cell.th; acc.pot += Ssub * cell.pot;
+        const d3 x = Q.L1[g] * T.a + Q.L2[g] * T.b + Q.L3[g] * T.c;
+        d3 psi;
+        double th, pot = 0.0;
+        if (CLS == kFar) far_integrand(x, p.K, p.F, psi, th, pot);
+        else if (CLS == kEdge) edge_integrand(x, p.K, p.E, psi, th);
+        else vertex_integrand(x, p.K, p.Vx, psi, th);
+        axpy5(acc, Ssub * Q.w[g], psi, th, pot);
     }
     for (int off = 16; off > 0; off >>= 1) {
         acc.px += __shfl_xor_sync(0xffffffffu, acc.px, off);
