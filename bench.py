@@ -12,8 +12,9 @@ value  = pair-integrals/s with pair lists and outputs resident in HBM (CUDA even
          launching stream, L2 flushed between steps by a 512 MiB write).
 e2e    = the same through the C-ABI from pinned host lists: H2D of the lists and D2H of J and P
          inside the timed region.
-roofline: the pair kernels are bounded by the FP64 pipe; peaks are measured live by
-         i2_calibrate_pipes (MEASURED_PEAKS.json carries only HBM and bf16 figures).
+roofline: the pair kernels are bounded by the FP32 pipe (mixed bulk: `roofline`) or the FP64 pipe
+         (plain form: `roofline_fp64`); peaks are measured live by i2_calibrate_pipes
+         (MEASURED_PEAKS.json carries only HBM and bf16 figures).
 cpu_baseline: the oracle (a C restatement of the reference's formulas, OpenMP) on the host.
 """
 from __future__ import annotations
@@ -648,7 +649,8 @@ def gpu_arm(args):
     rk = "mixed" if "mixed" in roof else ("fp64" if "fp64" in roof else None)
     if rk:
         line["roofline"] = {"bound": "fp32" if rk == "mixed" else "fp64",
-                            "kernel": ("k_level_mixed" if rk == "mixed" else "k_level") + "<far> chain (levels 0..5), per-class form",
+                            "kernel": ("k_level_mixed" if rk == "mixed" else "k_level") + "<far> chain (levels 0..5), per-class form; "
+                                      "timed over the whole disjoint class (chain, finalisation, needle fix-up)",
                             "unit": "TFLOP/s", "traffic": FAR_CHAIN_DRAM_BYTES if rk == "mixed" else None,
                             "traffic_unit": "bytes per chain run (ncu)", **roof[rk]}
     if "fp64" in roof and rk != "fp64":
