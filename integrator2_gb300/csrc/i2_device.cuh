@@ -181,6 +181,10 @@ __device__ __forceinline__ V3<R> panel_vertex(const PanelJT<R> &P, int k)
     return k == 0 ? P.A : (k == 1 ? P.B : P.C);
 }
 
+// index of this thread's warp when items are dealt warp-major over the grid: item k goes to warp
+// k mod (warps in the grid), and consecutive items land in different blocks (hence SMs)
+__device__ __forceinline__ long long warp_item_index() { return (long long)(threadIdx.x >> 5) * gridDim.x + blockIdx.x; }
+
 // 1 -> 4 midpoint split in the reference's child order (NumericalIntegrator3d.cu:37-87):
 // child 0 = (m_ab, b, m_bc), 1 = (m_bc, c, m_ca), 2 = (m_ca, a, m_ab), 3 = (m_bc, m_ca, m_ab)
 template <class R>

@@ -141,6 +141,10 @@ void launch_adjoint(int cls, bool fp32, const int2 *pairs, int n, const int3 *ce
                     const QuadTables &Q, int persistent_blocks, cudaStream_t s);
 // mixed form: FP64 recomputation of the pairs with a needle cell (corner below 3 degrees)
 void launch_fp64_fixup(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s);
+// blocks of `kernel` that are resident at once on the current device (occupancy x SMs): the grid
+// of the FP64 warp-per-item passes, whose items go to the warps warp-major (warp_item_index), so
+// that every SM gets the same share and no partial second wave runs on a few SMs
+int resident_grid(const void *kernel, int threads, size_t smem);
 // sets the thread's message returned by i2_last_error()
 void set_last_error(const std::string &msg);
 // kernels shared by both forms

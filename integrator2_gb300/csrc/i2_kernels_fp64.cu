@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(128) k_pot_tier2(ClassArgs A, QuadTables Q)
     const int count = *A.tier2_cnt;
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < count; h += nwarps) {
+    for (int h = (int)warp_item_index(); h < count; h += nwarps) {
         const int t = A.tier2_list[h];
         const int2 pr = A.pairs[t];
         const int3 ci = A.cells[pr.x], cj = A.cells[pr.y];
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(128) k_pot_seed(ClassArgs A, QuadTables Q, dou
     if (blockIdx.x == 0 && threadIdx.x == 0) pot_seed_init(A);
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < count; h += nwarps) pot_seed_item<CLS>(A, Q, tol, h, lane);
+    for (int h = (int)warp_item_index(); h < count; h += nwarps) pot_seed_item<CLS>(A, Q, tol, h, lane);
 }
 
 // one cell of one depth, by one warp
@@ -463,7 +463,7 @@ __global__ void __launch_bounds__(128, 3) k_pot_depth(ClassArgs A, QuadTables Q,
     const int count = pot_depth_count(A, depth);
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < count; idx += nwarps)
+    for (int idx = (int)warp_item_index(); idx < count; idx += nwarps)
         pot_depth_item<CLS>(A, Q, tol, depth, in, out, idx, lane);
 }
 
@@ -485,9 +485,10 @@ __global__ void __launch_bounds__(128) k_pot_final(ClassArgs A, double tol)
 template <int CLS>
 static void pot_adaptive_chain(const ClassArgs &A, const QuadTables &Q, double tol, int persistent_blocks, cudaStream_t s)
 {
-    k_pot_seed<CLS><<<persistent_blocks, 128, 0, s>>>(A, Q, tol);
+    k_pot_seed<CLS><<<resident_grid((const void *)k_pot_seed<CLS>, 128, 0), 128, 0, s>>>(A, Q, tol);
+    const int grid = resident_grid((const void *)k_pot_depth<CLS>, 128, 0);
     for (int d = 1; d <= kHardMaxDepth; ++d)
-        k_pot_depth<CLS><<<persistent_blocks, 128, 0, s>>>(A, Q, tol, d, d % 2 ? A.pot_q_a : A.pot_q_b, d % 2 ? A.pot_q_b : A.pot_q_a);
+        k_pot_depth<CLS><<<grid, 128, 0, s>>>(A, Q, tol, d, d % 2 ? A.pot_q_a : A.pot_q_b, d % 2 ? A.pot_q_b : A.pot_q_a);
     k_pot_final<CLS><<<persistent_blocks, 128, 0, s>>>(A, tol);
 }
 // ------------------------------------------------------------------ self pairs
@@ -554,7 +555,7 @@ __global__ void __launch_bounds__(128) k_batch_pot_seed(const BatchSeg *__restri
     if (gid < nseg && seg_adjacent(segs[gid]) && segs[gid].A.hard_list) pot_seed_init(segs[gid].A);
     const int lane = threadIdx.x & 31;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long g = gid >> 5; g < total; g += nwarps) {
+    for (long long g = warp_item_index(); g < total; g += nwarps) {
         const int sg = seg_find(prefix, nseg, g);
         const BatchSeg &S = segs[sg];
         const int h = (int)(g - prefix[sg]);
@@ -571,7 +572,7 @@ __global__ void __launch_bounds__(128, 3) k_batch_pot_depth(const BatchSeg *__re
     });
     const int lane = threadIdx.x & 31;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < total; g += nwarps) {
+    for (long long g = warp_item_index(); g < total; g += nwarps) {
         const int sg = seg_find(prefix, nseg, g);
         const BatchSeg &S = segs[sg];
         const int idx = (int)(g - prefix[sg]);
@@ -635,6 +636,14 @@ __global__ void __launch_bounds__(128) k_finalize(ClassArgs A, int mode)
 // ------------------------------------------------------------------ host-side launchers
 static int blocks_for(long long n, int tpb) { return (int)((n + tpb - 1) / tpb); }
 
+int resident_grid(const void *kernel, int threads, size_t smem)
+{
+    int dev = 0, sms = 0, nb = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) sms = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, smem) != cudaSuccess || nb <= 0) nb = 1;
+    return std::max(1, sms) * nb;
+}
+
 void launch_prepare_panels(int nc, const double *V, const int *C, Panel *out, cudaStream_t s)
 {
     if (nc > 0) k_prepare_panels<<<blocks_for(nc, 128), 128, 0, s>>>(nc, V, C, out);
@@ -690,12 +699,13 @@ void launch_batch_pot_chain(const BatchSeg *segs, int nseg, const QuadTables &Q,
     for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
         const int nc = std::min(kBatchSegChunk, nseg - c0);
         // the seed initialises every segment of the chunk: at least one thread per segment
-        k_batch_pot_seed<<<std::max(persistent_blocks, blocks_for(nc, 128)), 128, seg_smem(nc), s>>>(segs + c0, nc, Q, tol);
+        k_batch_pot_seed<<<std::max(resident_grid((const void *)k_batch_pot_seed, 128, seg_smem(nc)), blocks_for(nc, 128)), 128, seg_smem(nc),
+                           s>>>(segs + c0, nc, Q, tol);
     }
     for (int d = 1; d <= kHardMaxDepth; ++d)
         for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
             const int nc = std::min(kBatchSegChunk, nseg - c0);
-            k_batch_pot_depth<<<persistent_blocks, 128, seg_smem(nc), s>>>(segs + c0, nc, Q, tol, d);
+            k_batch_pot_depth<<<resident_grid((const void *)k_batch_pot_depth, 128, seg_smem(nc)), 128, seg_smem(nc), s>>>(segs + c0, nc, Q, tol, d);
         }
     for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
         const int nc = std::min(kBatchSegChunk, nseg - c0);
@@ -725,8 +735,8 @@ void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const R
     case kEdge:
         k_singular<kEdge><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q);
         if (A.hard_list) {
-            k_pot_tier2<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Q);
-            k_pot_tier2b<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Q, 1);
+            k_pot_tier2<kEdge><<<resident_grid((const void *)k_pot_tier2<kEdge>, tpb, 0), tpb, 0, s>>>(A, Q);
+            k_pot_tier2b<kEdge><<<resident_grid((const void *)k_pot_tier2b<kEdge>, tpb, 0), tpb, 0, s>>>(A, Q, 1);
             pot_adaptive_chain<kEdge>(A, Q, cfg.hard_tol, persistent_blocks, s);
         }
         level_chain<kEdge>(A, Q, cfg, persistent_blocks, s);
@@ -734,8 +744,8 @@ void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const R
     case kVertex:
         k_singular<kVertex><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q);
         if (A.hard_list) {
-            k_pot_tier2<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Q);
-            k_pot_tier2b<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Q, 1);
+            k_pot_tier2<kVertex><<<resident_grid((const void *)k_pot_tier2<kVertex>, tpb, 0), tpb, 0, s>>>(A, Q);
+            k_pot_tier2b<kVertex><<<resident_grid((const void *)k_pot_tier2b<kVertex>, tpb, 0), tpb, 0, s>>>(A, Q, 1);
             pot_adaptive_chain<kVertex>(A, Q, cfg.hard_tol, persistent_blocks, s);
         }
         level_chain<kVertex>(A, Q, cfg, persistent_blocks, s);

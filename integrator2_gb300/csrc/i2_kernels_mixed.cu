@@ -567,7 +567,7 @@ __global__ void __launch_bounds__(128) k_pot_tier2_mixed(ClassArgs A, QuadTables
     const int count = *A.tier2_cnt;
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < count; h += nwarps) tier2_mixed_item<CLS>(A, Qf, Q, h, lane);
+    for (int h = (int)warp_item_index(); h < count; h += nwarps) tier2_mixed_item<CLS>(A, Qf, Q, h, lane);
 }
 
 // ------------------------------------------------------------------ FP64 fix-up of ill-conditioned pairs
@@ -982,8 +982,8 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
         k_singular_mixed<kEdge><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
         k_tier1_mixed<kEdge><<<blocks_for_m((long long)kTier1Lanes * A.n, tpb), tpb, 0, s>>>(A, Qf);
         if (A.hard_list) {
-            k_pot_tier2_mixed<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Qf, Q);
-            k_pot_tier2b<kEdge><<<persistent_blocks, tpb, 0, s>>>(A, Q, 0);
+            k_pot_tier2_mixed<kEdge><<<resident_grid((const void *)k_pot_tier2_mixed<kEdge>, tpb, 0), tpb, 0, s>>>(A, Qf, Q);
+            k_pot_tier2b<kEdge><<<resident_grid((const void *)k_pot_tier2b<kEdge>, tpb, 0), tpb, 0, s>>>(A, Q, 0);
             launch_pot_hard(kEdge, A, Q, cfg, persistent_blocks, s);
         }
         level_chain_mixed<kEdge>(A, Qf, cfg, persistent_blocks, s);
@@ -993,8 +993,8 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
         k_singular_mixed<kVertex><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
         k_tier1_mixed<kVertex><<<blocks_for_m((long long)kTier1Lanes * A.n, tpb), tpb, 0, s>>>(A, Qf);
         if (A.hard_list) {
-            k_pot_tier2_mixed<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Qf, Q);
-            k_pot_tier2b<kVertex><<<persistent_blocks, tpb, 0, s>>>(A, Q, 0);
+            k_pot_tier2_mixed<kVertex><<<resident_grid((const void *)k_pot_tier2_mixed<kVertex>, tpb, 0), tpb, 0, s>>>(A, Qf, Q);
+            k_pot_tier2b<kVertex><<<resident_grid((const void *)k_pot_tier2b<kVertex>, tpb, 0), tpb, 0, s>>>(A, Q, 0);
             launch_pot_hard(kVertex, A, Q, cfg, persistent_blocks, s);
         }
         level_chain_mixed<kVertex>(A, Qf, cfg, persistent_blocks, s);
@@ -1134,7 +1134,7 @@ __global__ void __launch_bounds__(128) k_batch_tier2(const BatchSeg *__restrict_
     });
     const int lane = threadIdx.x & 31;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < total; g += nwarps) {
+    for (long long g = warp_item_index(); g < total; g += nwarps) {
         const int sg = seg_find(prefix, nseg, g);
         const BatchSeg &S = segs[sg];
         if (S.cls == kEdge) tier2_mixed_item<kEdge>(S.A, Qf, Q, (int)(g - prefix[sg]), lane);
@@ -1151,7 +1151,7 @@ __global__ void __launch_bounds__(128, 3) k_batch_tier2b(const BatchSeg *__restr
     });
     const int lane = threadIdx.x & 31;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < total; g += nwarps) {
+    for (long long g = warp_item_index(); g < total; g += nwarps) {
         const int sg = seg_find(prefix, nseg, g);
         const BatchSeg &S = segs[sg];
         if (S.cls == kEdge) tier2b_item<kEdge>(S.A, Q, false, (int)(g - prefix[sg]), lane);
@@ -1251,11 +1251,11 @@ void launch_batch_prelude(const BatchSeg *segs, int nseg, const BatchTotals &tot
         if (tot.hard_lists) {
             for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
                 const int nc = std::min(kBatchSegChunk, nseg - c0);
-                k_batch_tier2<<<persistent_blocks, tpb, seg_smem(nc), s>>>(segs + c0, nc, Qf, Q);
+                k_batch_tier2<<<resident_grid((const void *)k_batch_tier2, tpb, seg_smem(nc)), tpb, seg_smem(nc), s>>>(segs + c0, nc, Qf, Q);
             }
             for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
                 const int nc = std::min(kBatchSegChunk, nseg - c0);
-                k_batch_tier2b<<<persistent_blocks, tpb, seg_smem(nc), s>>>(segs + c0, nc, Q);
+                k_batch_tier2b<<<resident_grid((const void *)k_batch_tier2b, tpb, seg_smem(nc)), tpb, seg_smem(nc), s>>>(segs + c0, nc, Q);
             }
             launch_batch_pot_chain(segs, nseg, Q, cfg.hard_tol, persistent_blocks, s);
         }

@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(128, 3) k_pot_tier2b(ClassArgs A, QuadTables Q
     const int count = A.cnt[kCntTier2b];
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; h < count; h += nwarps) tier2b_item<CLS>(A, Q, hi_known != 0, h, lane);
+    for (long long h = warp_item_index(); h < count; h += nwarps) tier2b_item<CLS>(A, Q, hi_known != 0, (int)h, lane);
 }
 
 } // namespace i2
