@@ -157,12 +157,18 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
                                   int kmax, long long first, long long stride, int G_cap)
 {
     const int nsub = 1 << (2 * level);
-    const int G = nsub < G_cap ? nsub : G_cap;
+    // lanes per pair: up to a warp (G_cap), or the whole block once a pair has at least a block's
+    // worth of sub-cells (levels 4 and 5, where only a few pairs remain and one warp per pair left
+    // each lane hundreds of points in series).  first and stride are thread-linear and the item
+    // count is then a multiple of the block, so every block runs the loop uniformly and the
+    // __syncthreads of the block-wide reduction below is reached by all its threads.
+    const bool block_group = blockDim.x > 32 && nsub >= (int)blockDim.x;
+    const int G = block_group ? (int)blockDim.x : (nsub < G_cap ? nsub : G_cap);
     const int per_lane = nsub / G;
     const bool listed = Lst.act_in != nullptr;
     const int count = listed ? *Lst.cnt_in : A.n;
     const long long total = (long long)count * G;
-    const long long total_r = (total + 31) & ~31LL;
+    const long long total_r = block_group ? total : (total + 31) & ~31LL;
     const float sub_scale = ldexpf(1.0f, -2 * level);
     for (long long idx = first; idx < total_r; idx += stride) {
         const bool valid = idx < total;
@@ -280,12 +286,31 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
             }
         }
         // the lanes' Kahan pairs added across the group in FP32 (kahan_pair_add); lane 0 converts
-        for (int off = 1; off < G; off <<= 1) {
+        for (int off = 1; off < (G < 32 ? G : 32); off <<= 1) {
 #pragma unroll
             for (int i = 0; i < 5; ++i) {
                 const float s2 = __shfl_xor_sync(0xffffffffu, ks.s[i], off), c2 = __shfl_xor_sync(0xffffffffu, ks.c[i], off);
                 kahan_pair_add(ks.s[i], ks.c[i], s2, c2);
             }
+        }
+        if (block_group) {
+            // the warps' pairs through shared memory, added in warp order by thread 0 (at most
+            // 256 threads, 8 warps)
+            __shared__ float grp[8][10];
+            const int w = threadIdx.x >> 5;
+            if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+                for (int i = 0; i < 5; ++i) {
+                    grp[w][i] = ks.s[i];
+                    grp[w][5 + i] = ks.c[i];
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0)
+                for (int k = 1; k < (int)(blockDim.x >> 5); ++k)
+#pragma unroll
+                    for (int i = 0; i < 5; ++i) kahan_pair_add(ks.s[i], ks.c[i], grp[k][i], grp[k][5 + i]);
+            __syncthreads();
         }
         if (!valid || lane_g != 0) continue;
         acc.px = (double)ks.s[0] - (double)ks.c[0];
