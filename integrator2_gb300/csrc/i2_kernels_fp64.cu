@@ -67,12 +67,17 @@ template <int CLS>
 __global__ void __launch_bounds__(128) k_level(ClassArgs A, QuadTables Q, int level, int mode, double tol, int kmax)
 {
     const int nsub = 1 << (2 * level);
-    const int G = nsub < 32 ? nsub : 32;          // lanes per pair
+    // lanes per pair: up to a warp, or the whole block once a pair has at least a block's worth
+    // of sub-cells (levels 4 and 5: only a few pairs remain, and one warp per pair left each lane
+    // hundreds of points in series).  The item count is then a multiple of the block, so every
+    // block runs the loop uniformly and reaches the __syncthreads of the reduction below.
+    const bool block_group = blockDim.x > 32 && nsub >= (int)blockDim.x;
+    const int G = block_group ? (int)blockDim.x : (nsub < 32 ? nsub : 32);  // lanes per pair
     const int per_lane = nsub / G;                // sub-cells per lane
     const bool listed = A.act_in != nullptr;
     const int count = listed ? *A.cnt_in : A.n;
     const long long total = (long long)count * G;
-    const long long total_r = (total + 31) & ~31LL;
+    const long long total_r = block_group ? total : (total + 31) & ~31LL;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const double sub_scale = ldexp(1.0, -2 * level);  // measure of a sub-cell / measure of K_i
     for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total_r; idx += stride) {
@@ -124,9 +129,23 @@ __global__ void __launch_bounds__(128) k_level(ClassArgs A, QuadTables Q, int le
             }
         }
         // segmented butterfly over the G lanes of this pair (groups never straddle a warp)
-        for (int off = 1; off < G; off <<= 1) {
+        for (int off = 1; off < (G < 32 ? G : 32); off <<= 1) {
             const acc5 o = shfl_xor5(acc, off);
             acc.px += o.px; acc.py += o.py; acc.pz += o.pz; acc.th += o.th; acc.pot += o.pot;
+        }
+        if (block_group) {
+            // the warps' sums through shared memory, added in warp order by thread 0 (the
+            // kernel's blocks have at most 128 threads, 4 warps)
+            __shared__ double grp[4][5];
+            const int w = threadIdx.x >> 5;
+            if ((threadIdx.x & 31) == 0) store5(grp[w], acc);
+            __syncthreads();
+            if (threadIdx.x == 0)
+                for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+                    const acc5 o = load5(grp[k]);
+                    acc.px += o.px; acc.py += o.py; acc.pz += o.pz; acc.th += o.th; acc.pot += o.pot;
+                }
+            __syncthreads();
         }
         if (!valid || lane_g != 0) continue;
         double *cur = A.cur + 5 * (long long)t;
