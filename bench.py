@@ -15,7 +15,9 @@ e2e    = the same through the C-ABI from pinned host lists: H2D of the lists and
 roofline: the pair kernels are bounded by the FP32 pipe (mixed bulk: `roofline`) or the FP64 pipe
          (plain form: `roofline_fp64`); peaks are measured live by i2_calibrate_pipes
          (MEASURED_PEAKS.json carries only HBM and bf16 figures).
-cpu_baseline: the oracle (a C restatement of the reference's formulas, OpenMP) on the host.
+cpu_baseline: the oracle (a C restatement of the reference's formulas, OpenMP) on the host, over
+         every pair of the workload.  --impl reference times the same over every pair in each of
+         its timed steps.
 """
 from __future__ import annotations
 
@@ -124,8 +126,8 @@ class ClockSampler:
 
 # ------------------------------------------------------------------ CPU leg
 def cpu_run(V, C, lists, frac, tol, nthreads=0):
-    """the oracle on a seeded sample (fraction frac of every class) with the product's rules;
-    returns (pairs, seconds, threads)"""
+    """the oracle with the product's rules on every pair of every class (frac >= 1) or on a
+    seeded sample (fraction frac of every class); returns (pairs, seconds, threads)"""
     from oracle import oracle as O
     rng = np.random.default_rng(1)
     n = 0
@@ -133,40 +135,55 @@ def cpu_run(V, C, lists, frac, tol, nthreads=0):
         t0 = time.perf_counter()
         for cls in CLASSES:
             pr = lists[cls]
-            k = max(1, int(len(pr) * frac))
-            sub = pr[np.sort(rng.choice(len(pr), k, replace=False))]
-            O.integrate(cls, sub, V, C, mode=O.ADAPTIVE_RELATIVE, tol=tol, nthreads=nthreads)
-            n += k
+            if frac < 1.0:
+                pr = pr[np.sort(rng.choice(len(pr), max(1, int(len(pr) * frac)), replace=False))]
+            O.integrate(cls, pr, V, C, mode=O.ADAPTIVE_RELATIVE, tol=tol, nthreads=nthreads)
+            n += len(pr)
         dt = time.perf_counter() - t0
     return n, dt, (nthreads or O.lib().o_max_threads())
 
 
+def workload_config(total, tol):
+    """the config dict both arms print (the same workload, rules and error control)"""
+    return {"workload": "jittered icosphere s5 (20480 triangles, sigma 0.15h, seed 2026): common-vertex, "
+                        "common-edge, self and near-field (< 3h) ordered pairs",
+            "pairs": int(total), "error_control": f"relative tol {tol}, levels 0..5",
+            "rule": "qf3D13; adjacent potential: tiered graded Duffy 10x8 / 8x6 check / 16x16 / adaptive"}
+
+
 def reference_arm(args):
+    """the reference's formulas on the host cores: the oracle (a C restatement of the reference's
+    path, OpenMP over pairs, the product's rules) over EVERY pair of the workload in each timed
+    step; warm-up steps run a 1 % sample"""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     V, C, lists = workload()
     total = sum(len(v) for v in lists.values())
-    frac = args.cpu_fraction
     for _ in range(args.warmup):
-        cpu_run(V, C, lists, frac * 0.1, args.tol)
-    rates, n, threads = [], 0, 1
+        cpu_run(V, C, lists, 0.01, args.tol)
+    times, threads = [], 1
     for _ in range(args.steps):
-        n, dt, threads = cpu_run(V, C, lists, frac, args.tol)
-        rates.append(n / dt)
-    v = float(np.median(rates))
+        n, dt, threads = cpu_run(V, C, lists, 1.0, args.tol)
+        assert n == total
+        times.append(dt)
+    ms = 1e3 * float(np.sum(times)) / args.steps
+    v = total / (ms * 1e-3)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "pair-integrals/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / v, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "jittered icosphere s5 (20480 triangles), 4 pair classes, near < 3h", "pairs": total,
-                       "tol": args.tol, "rule": "qf3D13 + graded Duffy 10x8", "parallelism": "host cores"},
+            "config": workload_config(total, args.tol),
+            "form": "the reference's formulas (oracle C restatement, FP64) on the host cores, OpenMP over pairs",
             "cpu_baseline": {"value": v, "unit": "pair-integrals/s", "cores": threads, "kind": "port",
-                             "sample": f"{frac:.3f} of every class per step ({n} pairs), oracle C restatement, OpenMP"},
+                             "sample": f"every pair of the workload ({total} pairs) in each of {args.steps} timed steps"},
             "e2e": {"value": v, "unit": "pair-integrals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
-METRIC = "pair-integrals/s at <=1e-6 rel err"
+# "<= 1e-6" holds per pair at the 99.9th percentile and normwise; about 0.06 % of the pairs (FP32
+# rounding of the edge logs amplified by the cancellation in Psi) lie above it, up to ~5e-6: the
+# line's accuracy_statement gives the measured figures over every pair
+METRIC = "pair-integrals/s at <=1e-6 rel err (per pair at p99.9 and normwise; tail share in accuracy_statement)"
 
 
 # ------------------------------------------------------------------ GPU arm
@@ -201,6 +218,44 @@ def accuracy(V, C, lists, J, P, levels, nsample=400):
         idx = np.sort(rng.choice(len(pr), min(nsample, len(pr)), replace=False))
         out[CLASS_NAMES[cls]] = class_accuracy(V, C, cls, pr[idx], J[cls][idx], P[cls][idx])
     return out
+
+
+def full_population(lists, form, fp64):
+    """the form against the FP64 form on EVERY pair of the workload, per class and channel: the
+    count and share of pairs above 1e-6 relative, the largest error, p99.9 and the pairs where the
+    two forms kept different refinement levels"""
+    out = {}
+    for cls in CLASSES:
+        j, j64 = form["J"][cls], fp64["J"][cls]
+        p, p64 = form["P"][cls], fp64["P"][cls]
+        if cls == 3:
+            eJ = np.abs(j - j64).max(axis=1) / max(np.abs(j64).max(), 1e-300)
+        else:
+            eJ = np.linalg.norm(j - j64, axis=1) / np.maximum(np.linalg.norm(j64, axis=1), 1e-300)
+        eP = np.abs(p - p64) / np.maximum(np.abs(p64), 1e-300)
+        d = {"pairs": int(len(j))}
+        for ch, e in (("J", eJ), ("P", eP)):
+            d[ch] = {"above_1e-6": int(np.sum(e > 1e-6)), "share_above_1e-6": float(np.mean(e > 1e-6)),
+                     "max": float(e.max()), "p99.9": float(np.percentile(e, 99.9)), "p99": float(np.percentile(e, 99))}
+        if cls != 3:
+            d["levels_differ"] = int(np.sum(form["levels"][cls] != fp64["levels"][cls]))
+        out[CLASS_NAMES[cls]] = d
+    return out
+
+
+def accuracy_statement(pop, sampled):
+    """one sentence with the measured per-pair figures behind the metric's "<= 1e-6" """
+    if not pop:
+        return None
+    cls = [c for c in ("vertex", "edge", "near") if c in pop]
+    n = sum(pop[c]["pairs"] for c in cls)
+    above = {ch: sum(pop[c][ch]["above_1e-6"] for c in cls) for ch in ("J", "P")}
+    p999 = {ch: max(pop[c][ch]["p99.9"] for c in cls) for ch in ("J", "P")}
+    mx = {ch: max(pop[c][ch]["max"] for c in cls) for ch in ("J", "P")}
+    nw = max(sampled[c]["J_normwise"] for c in cls) if sampled else None
+    return (f"against the FP64 form over all {n} non-self pairs: per-pair p99.9 {p999['J']:.2e} (J) / {p999['P']:.2e} (P); "
+            f"{above['J']} (J) and {above['P']} (P) pairs above 1e-6 ({100 * above['J'] / n:.3f} % / {100 * above['P'] / n:.3f} %), "
+            f"max {mx['J']:.2e} / {mx['P']:.2e}; self pairs exact; normwise vs the high-order oracle {nw:.1e} (J, sampled)")
 
 
 class DeviceRows:
@@ -592,6 +647,8 @@ def gpu_arm(args):
     if "fp64" in forms:
         roof["fp64"] = far_roofline(forms["fp64"], point_flops("far", w), float(cal[0]), "FP64 FMA peak measured live")
     acc = {name: accuracy(V, C, lists, f["J"], f["P"], f["levels"]) for name, f in forms.items()}
+    population = {name: full_population(lists, f, forms["fp64"]) for name, f in forms.items()
+                  if name != "fp64" and "fp64" in forms}
     n_cpu, dt_cpu, thr = cpu_run(V, C, lists, args.cpu_fraction, args.tol)
     # kernels per step: adjacent classes run singular + tiers 2 and 2b + adaptive potential (seed,
     # 12 depths, final); per-class chains add levels 0..5 + finalize per class, self pairs 1; the
@@ -610,25 +667,24 @@ def gpu_arm(args):
         "warmup": args.warmup, "ms_per_step": head["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if hname == "fp64" else "f32 bulk / f64 singular, estimator and hard pairs",
         "data": "synthetic",
-        "config": {"workload": "jittered icosphere s5 (20480 triangles, sigma 0.15h, seed 2026): common-vertex, "
-                               "common-edge, self and near-field (< 3h) ordered pairs",
-                   "pairs": total, "form": form_desc[hname],
-                   "error_control": f"relative tol {args.tol}, levels 0..5",
-                   "rule": "qf3D13; adjacent potential: tiered graded Duffy 10x8 / 8x6 check / 16x16 / adaptive",
-                   "l2": "flushed (512 MiB write) between steps", "parallelism": f"replicas x{world}"},
+        "config": workload_config(total, args.tol),
+        "form": form_desc[hname], "l2": "flushed (512 MiB write) between steps", "parallelism": f"replicas x{world}",
         "e2e": {"value": e2e_value, "unit": "pair-integrals/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "path": "EvaluatorJ3DK device entry point per class (mixed precision), pinned host lists in, J and P out"},
         "forms": {n: {"value": f["value"], "ms_per_step": f["ms"] / args.steps,
                       "class_ms": dict(zip(names4, map(float, f["cls_ms"]))) if n != "batch" else None,
                       "accuracy": acc[n], "gpu_launches_per_step": launches[n]} for n, f in forms.items()},
         "accuracy": acc[hname],
+        "accuracy_all_pairs_vs_fp64": population.get(hname),
+        "accuracy_statement": accuracy_statement(population.get(hname), acc[hname]),
         "levels": {n: np.bincount(head["levels"][c][head["levels"][c] >= 0], minlength=6).tolist() for n, c in
                    zip(("vertex", "edge", "near"), (0, 1, 2))},
         "calibration": {"fp64_tflops": float(cal[0]), "fp32_tflops": float(cal[1]),
                         "fp64_fma_units": dict(zip(("sqrt", "div", "log", "atan2", "sincos", "acos"), map(float, cal[2:8]))),
                         "fp32_fma_units": dict(zip(("sqrtf", "div", "log1pf", "atan2f", "logf"), map(float, cal[8:13])))},
         "cpu_baseline": {"value": n_cpu / dt_cpu, "unit": "pair-integrals/s", "cores": thr, "kind": "port",
-                         "sample": f"{args.cpu_fraction:.3f} of every class ({n_cpu} pairs), oracle C restatement, OpenMP, same rules"},
+                         "sample": (f"every pair ({n_cpu})" if args.cpu_fraction >= 1 else
+                                    f"{args.cpu_fraction:.3f} of every class ({n_cpu} pairs)") + ", oracle C restatement, OpenMP, same rules"},
         "clocks": head["clocks"],
         "gpu_launches": launches[hname] * args.steps,
     }
@@ -665,7 +721,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--tol", type=float, default=1e-6)
-    ap.add_argument("--cpu-fraction", type=float, default=0.02)
+    ap.add_argument("--cpu-fraction", type=float, default=1.0,
+                    help="cpu_baseline leg of the GPU arm: share of every class (1 = every pair, about 2.5 s on 16 cores)")
     ap.add_argument("--fd-coords", type=int, default=10, help="adjoint section: coordinates checked by finite differences")
     ap.add_argument("--forms", default="fp64,mixed,batch",
                     help="forms to run: fp64, mixed (per-class chains), batch (headline when present)")

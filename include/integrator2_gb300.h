@@ -239,8 +239,9 @@ i2_status i2_batch_copy_results(const i2_batch_t *batch, int32_t segment, i2_cha
  * aligned, indices valid: they are read on the device only), J (3 n doubles) and P (n
  * doubles).  Limits: nc <= I2_NOALLOC_MAX_CELLS, n <= I2_NOALLOC_MAX_PAIRS; larger inputs are
  * rejected with I2_ERR_INVALID_ARGUMENT before any launch.  Asynchronous on `stream`.  The
- * first call on a device looks up the array's device address (make it before any stream
- * capture).  Every call shares the array: calls that overlap on the GPU race. */
+ * first call in each CUDA context (normally one per device) looks up the array's device
+ * address in that context (make it before any stream capture).  Every call shares the array:
+ * calls that overlap on the GPU race. */
 #define I2_NOALLOC_MAX_CELLS 8192
 #define I2_NOALLOC_MAX_PAIRS 16384
 i2_status i2_not_neighbors_noalloc(const double *d_vertices, int32_t nv, const int32_t *d_cells, int32_t nc,

@@ -40,38 +40,82 @@ constexpr size_t kActBOff = kActAOff + sizeof(int) * (size_t)kMaxPairs;
 constexpr size_t kCntOff = kActBOff + sizeof(int) * (size_t)kMaxPairs;
 constexpr size_t kCntInts = 64;  // cnt[0..15] active counts per level, cnt[16] deepest level
 constexpr size_t kScratchBytes = kCntOff + sizeof(int) * kCntInts;
-static_assert(kCurOff % 256 == 0 && kFinAOff % 256 == 0 && kRawOff % 256 == 0 && kStopOff % 256 == 0 &&
-                  kActBOff % 256 == 0 && kCntOff % 256 == 0,
+static_assert(kCurOff % 256 == 0 && kFinAOff % 256 == 0 && kFinBOff % 256 == 0 && kRawOff % 256 == 0 && kStopOff % 256 == 0 &&
+                  kActAOff % 256 == 0 && kActBOff % 256 == 0 && kCntOff % 256 == 0,
               "scratch regions are 256-byte aligned");
 
 // the scratch array; in host code this name is only a handle for cudaGetSymbolAddress
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
+// The array's device address belongs to a CUDA context, not to a device ordinal: a host
+// application may run its own driver-API context on a device, and a cudaDeviceReset makes a new
+// primary context.  The set-up below therefore runs once per context (normally once per device,
+// for its primary context), with that context current, and is cached under the context's ID
+// (cuCtxGetId: unique for the life of the process, unlike a handle, which can be reused after
+// its context is destroyed).
+struct Setup {
+    unsigned long long id;
+    void *ptr;
+    int sms;
+};
+constexpr int kMaxSetups = 4 * kMaxDevices;
 std::mutex g_setup_mutex;
-void *g_scratch_ptr[kMaxDevices] = {};
-int g_sms[kMaxDevices] = {};
+Setup g_setup[kMaxSetups] = {};
+int g_nsetup = 0, g_next = 0;
 
-// once per device, with that device current: the device address of the array and the SM count
+// cuCtxGetCurrent / cuCtxGetId through the runtime's driver entry points (no libcuda link)
+using CtxGetCurrentFn = int (*)(void **);
+using CtxGetIdFn = int (*)(void *, unsigned long long *);
+void *driver_fn(const char *name)
+{
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &f, 12000, cudaEnableDefault, &q) != cudaSuccess || q != cudaDriverEntryPointSuccess)
+        return nullptr;
+    return f;
+}
+
+// the ID of the context current on this thread; false when there is none (or no driver support)
+bool current_context_id(unsigned long long &id)
+{
+    static const CtxGetCurrentFn get = reinterpret_cast<CtxGetCurrentFn>(driver_fn("cuCtxGetCurrent"));
+    static const CtxGetIdFn get_id = reinterpret_cast<CtxGetIdFn>(driver_fn("cuCtxGetId"));
+    void *ctx = nullptr;
+    if (!get || !get_id || get(&ctx) != 0 || !ctx) return false;
+    return get_id(ctx, &id) == 0;
+}
+
+// with device dev current: the device address of the array in the current context and the SM count
 i2_status device_setup(int dev, void **ptr, int *sms, std::string &err)
 {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[dev]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-        if (e != cudaSuccess || !p) {
-            err = std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e);
-            return I2_ERR_CUDA;
-        }
-        int n = 0;
-        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
-            err = "cannot read the SM count";
-            return I2_ERR_CUDA;
-        }
-        g_sms[dev] = n;
-        g_scratch_ptr[dev] = p;
+    unsigned long long id = 0;
+    bool have_id = current_context_id(id);
+    if (have_id)
+        for (int k = 0; k < g_nsetup; ++k)
+            if (g_setup[k].id == id) {
+                *ptr = g_setup[k].ptr;
+                *sms = g_setup[k].sms;
+                return I2_OK;
+            }
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);  // makes the device's primary context current if none was
+    if (e != cudaSuccess || !p) {
+        err = std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e);
+        return I2_ERR_CUDA;
     }
-    *ptr = g_scratch_ptr[dev];
-    *sms = g_sms[dev];
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+        err = "cannot read the SM count";
+        return I2_ERR_CUDA;
+    }
+    if (!have_id) have_id = current_context_id(id);
+    if (have_id) {  // without an ID (no driver entry point) the lookup simply repeats on every call
+        const int k = g_nsetup < kMaxSetups ? g_nsetup++ : (g_next++ % kMaxSetups);
+        g_setup[k] = Setup{id, p, n};
+    }
+    *ptr = p;
+    *sms = n;
     return I2_OK;
 }
 

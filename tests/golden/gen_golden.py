@@ -4,6 +4,7 @@ Run here (where the reference checkout exists), not on the GPU machine:
 
     python tests/golden/gen_golden.py            # reference at /root/reference
     I2_REFERENCE=/path/to/integrator2 python tests/golden/gen_golden.py
+    python tests/golden/gen_golden.py --only-all # only the all-disjoint fixture (ico1_all.npz)
 
 It builds oracle/_ref/libi2ref.so (oracle/ref_build.sh: the reference's src/ compiled for the
 host through oracle/ref_shim.h, plus oracle/ref_driver.cu, which mirrors the reference's kernel
@@ -72,6 +73,20 @@ def run_mesh(name, V, C, pl: P.PairLists, far_sample=None, seed=0, modes=(0, 1, 
     print(f"{name}: " + ", ".join(f"{k}={v.shape}" for k, v in out.items() if k.startswith("pairs")))
 
 
+def all_disjoint(name, V, C):
+    """every disjoint pair, the rows runAllPairs integrates (evaluator3d.cu:120-204: the full
+    not-neighbours list plus its reversed rows, kAddReversedPairs at :22-31), as ordered pairs
+    sorted i-major (the reference's list order comes from atomics, so tests match rows by
+    (i, j)); the reference's J at fixed levels 0 and 1"""
+    pl = P.build_pairs(V, C, near_factor=None)
+    rows = pl.far.astype(np.int32)
+    out = {"V": V, "C": C.astype(np.int32), "pairs": rows}
+    for lev in (0, 1):
+        out[f"J_L{lev}"] = O.ref_integrate(O.FAR, rows, V, C, level=lev)[1]
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    print(f"{name}: {len(rows)} ordered disjoint pairs")
+
+
 def point_samples(n=400, seed=11):
     """theta/psi of the reference at seeded points around a seeded triangle, including points
     close to the triangle's plane, edges and vertices."""
@@ -101,6 +116,12 @@ def main():
                    env=dict(os.environ, I2_REFERENCE=REF))
     if O.ref_lib() is None:
         raise SystemExit("reference host library not built")
+    # full not-neighbours semantics (prepareMesh without a near-field cutoff + runAllPairs) on a
+    # jittered 80-cell sphere
+    V, C = M.jittered_icosphere(1, 0.15, 5)
+    all_disjoint("ico1_all", V, C)
+    if "--only-all" in sys.argv:
+        return
     # C1 workload: icosphere subdivided twice, radius 1
     V, C = M.icosphere(2)
     run_mesh("ico2", V, C, P.build_pairs(V, C), far_sample=2500, seed=1, modes=(0, 1))

@@ -97,7 +97,8 @@ def test_batch_accuracy_against_high_order(api):
             _, oJ, oP, _ = O.integrate(cls, pr, V, C, mode=O.FIXED, level=4)
         eJ = rel_rows(batch.getResults(s), oJ)
         eP = np.abs(batch.getPotentials(s) - oP) / np.abs(oP)
-        assert eJ.max() < 1e-5 and eP.max() < 1e-5, (cls, eJ.max(), eP.max())
+        assert np.percentile(eJ, 99) <= 1e-6 and np.percentile(eP, 99) <= 1e-6, (cls, eJ.max(), eP.max())
+        assert eJ.max() < 5e-6 and eP.max() < 5e-6, (cls, eJ.max(), eP.max())
 
 
 def test_batch_rejects_bad_input(api):

@@ -56,6 +56,27 @@ def test_mixed_matches_fp64_at_fixed_level(api):
     print("mixed vs fp64 (J max, P max, J rms, kappa and pair of the worst):", worst)
 
 
+@pytest.mark.parametrize("level,npairs", [(4, 200), (5, 24)])
+def test_mixed_deep_levels_match_oracle(api, level, npairs):
+    """fixed levels 4 and 5 run the FP32 level kernel's block-per-pair path (the warps' Kahan
+    pairs combined in warp order through shared memory): against the oracle at the same level,
+    with the FP32 bar of the level-1 test above (a lost or doubled warp would be off by 1/8)"""
+    from integrator2_gb300 import meshes, pairs as P
+    from oracle import oracle as O
+    V, C = meshes.jittered_icosphere(2, 0.15, 9)
+    pl = P.build_pairs(V, C)
+    for cls in (0, 1, 2):
+        pr = pl.by_class(cls)[:npairs]
+        J, Pm, _ = _run(api, V, C, cls, pr, api.PRECISION_MIXED, "fixed", level)
+        with O.potential_rule(10, 8, 3, adaptive=0):
+            _, oJ, oP, _ = O.integrate(cls, pr, V, C, mode=O.FIXED, level=level)
+        eJ = rel_rows(J, oJ)
+        bar = np.maximum(1e-5, 1e-7 * O.conditioning(cls, pr, V, C, level))
+        assert np.all(eJ <= bar), (cls, level, float(eJ.max()))
+        if cls == 2:
+            assert (np.abs(Pm - oP) / np.abs(oP)).max() < 1e-5, (cls, level)
+
+
 def test_mixed_accuracy_against_high_order(api):
     from integrator2_gb300 import meshes, pairs as P
     from oracle import oracle as O
@@ -72,8 +93,45 @@ def test_mixed_accuracy_against_high_order(api):
         eJ = rel_rows(J, oJ)
         eP = np.abs(Pm - oP) / np.abs(oP)
         report[cls] = (float(eJ.max()), float(eP.max()))
-        assert eJ.max() < 1e-5 and eP.max() < 1e-5, (cls, report[cls])
+        # the accuracy statement of the mixed form: per pair <= 1e-6 at the 99th percentile of a
+        # sample (99.9th over a whole workload, test below), no pair above 5e-6
+        assert np.percentile(eJ, 99) <= 1e-6 and np.percentile(eP, 99) <= 1e-6, (cls, report[cls])
+        assert eJ.max() < 5e-6 and eP.max() < 5e-6, (cls, report[cls])
     print("mixed vs high-order oracle (J max, P max):", report)
+
+
+def test_mixed_full_population_against_fp64(api):
+    """the accuracy statement on every pair of the 20,480-triangle jittered sphere (1.42 M ordered
+    pairs, relative control 1e-6): mixed against the FP64 form, per class and channel, the 99.9th
+    percentile of the per-pair relative error is <= 1e-6, at most 0.1 % of pairs exceed 1e-6 and
+    none exceeds 6e-6 (the remaining tail is FP32 rounding of the edge logs, amplified by the
+    cancellation in Psi = sum_e lambda_e e_e: about u_fp32 times the ratio sum_e |L_e| / |J|)"""
+    from integrator2_gb300 import meshes, pairs as P
+    V, C = meshes.jittered_icosphere(5, 0.15, 2026)
+    pl = P.build_pairs(V, C, 3.0)
+    res = {}
+    for prec in (api.PRECISION_FP64, api.PRECISION_MIXED):
+        m = api.Mesh3D()
+        m.setGeometry(V, C)
+        m.prepareMesh(3.0)
+        it = api.NumericalIntegrator3D(m, api.qf3D13)
+        it.setErrorControl(api.RELATIVE_ERROR_CONTROL, 1e-6, 5)
+        it.setPrecision(prec)
+        ev = api.EvaluatorJ3DK(m, it)
+        out = {}
+        for cls in (0, 1, 2, 3):
+            ev.runClass(cls, pl.by_class(cls))
+            out[cls] = (ev.getResults(cls), ev.getPotentials(cls))
+        res[prec] = out
+    report = {}
+    for cls in (0, 1, 2, 3):
+        (J, Pm), (J64, P64) = res[api.PRECISION_MIXED][cls], res[api.PRECISION_FP64][cls]
+        eJ = rel_rows(J, J64) if cls != 3 else np.abs(J - J64).max(axis=1) / np.abs(J64).max()
+        eP = np.abs(Pm - P64) / np.abs(P64)
+        report[cls] = {ch: (float(np.percentile(e, 99.9)), float(np.mean(e > 1e-6)), float(e.max())) for ch, e in (("J", eJ), ("P", eP))}
+        for ch, e in (("J", eJ), ("P", eP)):
+            assert np.percentile(e, 99.9) <= 1e-6 and np.mean(e > 1e-6) <= 1e-3 and e.max() < 6e-6, (cls, ch, report[cls])
+    print("mixed vs FP64 over every pair (p99.9, share above 1e-6, max):", report)
 
 
 def _two_cells(V, C, i, j):

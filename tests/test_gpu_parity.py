@@ -82,15 +82,17 @@ def test_two_triangle_fixtures(api):
             assert_parity(J[ok], g[tag][ok], k, f"{nm} {tag}")
 
 
-@pytest.mark.parametrize("level", [0, 2, 3])
-def test_potential_and_deep_levels_match_oracle(api, level):
+@pytest.mark.parametrize("level,npairs", [(0, 600), (2, 600), (3, 600), (4, 200), (5, 24)])
+def test_potential_and_deep_levels_match_oracle(api, level, npairs):
+    """fixed levels 0..5 against the oracle; levels 4 and 5 run the level kernel's block-per-pair
+    path (every thread of a block on one pair, the warps' sums combined through shared memory)"""
     from integrator2_gb300 import meshes, pairs as P
     from oracle import oracle as O
     V, C = meshes.jittered_icosphere(2, 0.15, 9)
     pl = P.build_pairs(V, C)
     with O.potential_rule(10, 8, 3, adaptive=0):
         for cls in (0, 1, 2):
-            pr = pl.by_class(cls)[:600]
+            pr = pl.by_class(cls)[:npairs]
             raw, J, Pg, _ = run(api, V, C, cls, pr, "fixed", level, hard_tol=0)
             oraw, oJ, oP, _ = O.integrate(cls, pr, V, C, mode=O.FIXED, level=level)
             assert_parity(J, oJ, kappa(cls, pr, V, C, level), f"class {cls} level {level}")
@@ -180,9 +182,21 @@ def test_relative_mode_matches_oracle(api):
             assert (np.abs(Pg[same] - oP[same]) / np.abs(oP[same])).max() < TOL
 
 
+def _antisymmetry(J):
+    """delta = |J_ij + J_ji|_1 / max(|J_ij|_1, |J_ji|_1) for rows i and n + i (the reference's
+    kCalculateIntegrationError, evaluator3d.cu:45-57)"""
+    n = len(J) // 2
+    a, b = J[:n], J[n:]
+    d = np.abs(a + b).sum(1) / np.maximum(np.abs(a).sum(1), np.abs(b).sum(1))
+    return np.concatenate([d, d])
+
+
 def test_run_all_pairs_and_antisymmetry(api):
     """runAllPairs(check=True): rows n..2n-1 are the reversed pairs; delta = |J_ij + J_ji| / max
-    is the reference's built-in correctness check (evaluator3d.cu:45-57)."""
+    is the reference's built-in correctness check (evaluator3d.cu:45-57).  The library's delta
+    equals the delta of the oracle's results for the same rows to 1e-9 absolute (delta is a
+    property of the rule at this level, not of the arithmetic), so a sign or branch error in
+    either orientation of a pair shows up as a changed delta."""
     from integrator2_gb300 import meshes
     from oracle import oracle as O
     V, C = meshes.icosphere(2)
@@ -198,11 +212,72 @@ def test_run_all_pairs_and_antisymmetry(api):
         n = len(lst)
         assert len(J) == 2 * n
         err = ev.getErrors(cls)
-        assert err.max() < 0.05, cls
         allp = np.concatenate([lst[:, :2], lst[:, 1::-1]])
         _, oJ, _, _ = O.integrate(cls, allp, V, C, mode=O.FIXED, level=1)
         assert_parity(J, oJ, kappa(cls, allp, V, C, 1), f"runAllPairs class {cls}")
+        assert np.abs(err - _antisymmetry(oJ)).max() < 1e-9, cls
+        assert np.abs(err - _antisymmetry(J)).max() < 1e-15, cls
     assert ev.resultCount(3) == len(C)
+
+
+@pytest.mark.parametrize("level", [0, 1])
+def test_run_all_pairs_every_disjoint_pair(api, level):
+    """prepareMesh without a near-field cutoff keeps every disjoint pair (the reference's
+    not-neighbours list, Mesh3d.cu:93-142) and runAllPairs integrates them with their reversed
+    rows (evaluator3d.cu:120-204); J against the reference's results on a jittered 80-cell sphere
+    (golden vectors, matched by (i, j))"""
+    g = np.load(os.path.join(GOLD, "ico1_all.npz"))
+    V, C = g["V"], g["C"]
+    m = api.Mesh3D()
+    m.setGeometry(V, C)
+    m.prepareMesh(None)
+    it = api.NumericalIntegrator3D(m, api.qf3D13)
+    it.setFixedRefinementLevel(level)
+    ev = api.EvaluatorJ3DK(m, it)
+    ev.runAllPairs(True)
+    lst = m.getNotNeighbors()[:, :2]
+    rows = np.concatenate([lst, lst[:, ::-1]]).astype(np.int64)
+    gp = g["pairs"].astype(np.int64)
+    assert len(rows) == len(gp)
+    nc = len(C)
+    order = np.argsort(gp[:, 0] * nc + gp[:, 1])
+    pos = order[np.searchsorted((gp[:, 0] * nc + gp[:, 1])[order], rows[:, 0] * nc + rows[:, 1])]
+    assert np.array_equal(gp[pos], rows)
+    J = ev.getResults(2)
+    ref = g[f"J_L{level}"][pos]
+    assert_parity(J, ref, kappa(2, rows, V, C, level), f"all disjoint pairs, level {level}")
+    assert np.abs(ev.getErrors(2) - _antisymmetry(ref)).max() < 1e-9
+
+
+def test_run_pairs_matches_run_class(api):
+    """runPairs (evaluator3d.cu:213-288): user lists of (i, j, k) rows for the three reference
+    classes in one call give the results runClass gives for the same rows"""
+    from integrator2_gb300 import meshes, pairs as P
+    V, C = meshes.jittered_icosphere(2, 0.15, 21)
+    pl = P.build_pairs(V, C)
+    rng = np.random.default_rng(4)
+    lists = []
+    for cls in (0, 1, 2):
+        pr = pl.by_class(cls)
+        pr = pr[rng.choice(len(pr), min(500, len(pr)), replace=False)]
+        lists.append(np.ascontiguousarray(np.column_stack([pr, np.arange(len(pr))]).astype(np.int32)))
+    m = api.Mesh3D()
+    m.setGeometry(V, C)
+    m.prepareMesh(3.0)
+    it = api.NumericalIntegrator3D(m, api.qf3D13)
+    it.setErrorControl(api.RELATIVE_ERROR_CONTROL, 1e-7, 5)
+    ev = api.EvaluatorJ3DK(m, it)
+    ev.runPairs(*lists)
+    got = [(ev.getResults(c), ev.getPotentials(c), ev.getLevels(c)) for c in (0, 1, 2)]
+    for cls in (0, 1, 2):
+        ev.runClass(cls, lists[cls][:, :2])
+        assert np.array_equal(got[cls][0], ev.getResults(cls)), cls
+        assert np.array_equal(got[cls][1], ev.getPotentials(cls)), cls
+        assert np.array_equal(got[cls][2], ev.getLevels(cls)), cls
+    # one empty list leaves the other classes' work intact
+    ev.runPairs(lists[0], np.zeros((0, 3), np.int32), lists[2][:7])
+    assert ev.resultCount(0) == len(lists[0]) and ev.resultCount(2) == 7
+    assert np.array_equal(ev.getResults(2), got[2][0][:7])
 
 
 def test_device_entry_point_and_edge_cases(api):

@@ -56,6 +56,14 @@ def test_two_triangle_fixtures():
             assert _close(J[ok], g[tag][ok]) < TOL, (nm, tag)
 
 
+def test_every_disjoint_pair_matches_reference():
+    """the full not-neighbours list (no near-field cutoff) at fixed levels 0 and 1"""
+    g = np.load(os.path.join(GOLD, "ico1_all.npz"))
+    for lev in (0, 1):
+        _, J, _, _ = O.integrate(O.FAR, g["pairs"], g["V"], g["C"], mode=O.FIXED, level=lev)
+        assert _close(J, g[f"J_L{lev}"]) < TOL, lev
+
+
 def test_theta_psi_points():
     rows = np.load(os.path.join(GOLD, "theta_psi_points.npz"))["rows"]
     L = O.lib()
