@@ -151,6 +151,38 @@ def workload_config(total, tol):
             "rule": "qf3D13; adjacent potential: tiered graded Duffy 10x8 / 8x6 check / 16x16 / adaptive"}
 
 
+def level0_workloads():
+    """C1 (icosphere s2, 320 triangles) and the C2 workload: the pair lists of the reference's
+    three classes, for the J-only fixed-level-0 comparison with the reference's CUDA build"""
+    from integrator2_gb300 import meshes, pairs
+    V1, C1 = meshes.icosphere(2)
+    pl = pairs.build_pairs(V1, C1, NEAR)
+    V2, C2, l2 = workload()
+    return {"C1": (V1, C1, {c: pl.by_class(c) for c in (0, 1, 2)}), "C2": (V2, C2, {c: l2[c] for c in (0, 1, 2)})}
+
+
+def reference_cuda_section():
+    """the reference's own CUDA build (its src/ compiled unmodified for sm_103a, a cubin built
+    where the reference checkout exists) on this GPU: integrateOver<class> timed per class as the
+    reference's GpuTimer brackets it (regular part, gather, singular part, finalisation), fixed
+    refinement level 0, qf3D13, J only (the reference computes no potential)"""
+    try:
+        from oracle import ref_cuda
+        if not ref_cuda.available():
+            return {"unavailable": "oracle/_ref/ref_kernels.cubin was not built (the reference checkout is needed where it is built)"}
+        ref = ref_cuda.RefCuda()
+    except Exception as e:  # no GPU or no driver
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+    out = {}
+    for name, (V, C, lists) in level0_workloads().items():
+        ms = {CLASS_NAMES[c]: ref.time_class(c, V, C, lists[c], 0) for c in (0, 1, 2)}
+        n = sum(len(lists[c]) for c in (0, 1, 2))
+        out[name] = {"pairs": int(n), "class_ms": ms, "ms_per_step": float(sum(ms.values())),
+                     "value": n / (sum(ms.values()) * 1e-3), "unit": "pair-integrals/s (J only, fixed level 0)"}
+    ref.close()
+    return out
+
+
 def reference_arm(args):
     """the reference's formulas on the host cores: the oracle (a C restatement of the reference's
     path, OpenMP over pairs, the product's rules) over EVERY pair of the workload in each timed
@@ -177,6 +209,8 @@ def reference_arm(args):
             "cpu_baseline": {"value": v, "unit": "pair-integrals/s", "cores": threads, "kind": "port",
                              "sample": f"every pair of the workload ({total} pairs) in each of {args.steps} timed steps"},
             "e2e": {"value": v, "unit": "pair-integrals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if "level0" in args.sections:
+        line["reference_cuda"] = reference_cuda_section()
     print(json.dumps(line))
 
 
@@ -217,6 +251,43 @@ def accuracy(V, C, lists, J, P, levels, nsample=400):
         pr = lists[cls]
         idx = np.sort(rng.choice(len(pr), min(nsample, len(pr)), replace=False))
         out[CLASS_NAMES[cls]] = class_accuracy(V, C, cls, pr[idx], J[cls][idx], P[cls][idx])
+    return out
+
+
+def fp64_level0_j_only(stream):
+    """the library's plain FP64 form on the reference's own workload: J only (potential off),
+    fixed refinement level 0, qf3D13, the reference's three classes on C1 and C2, per class
+    through the device entry point (lists resident), CUDA events, mean of 5 runs after 2"""
+    import torch
+    from integrator2_gb300 import api
+    out = {}
+    for name, (V, C, lists) in level0_workloads().items():
+        m = api.Mesh3D()
+        m.setGeometry(V, C)
+        m.prepareMesh(NEAR)
+        it = api.NumericalIntegrator3D(m, api.qf3D13)
+        it.setFixedRefinementLevel(0)
+        it.setPotential(False)
+        ev = api.EvaluatorJ3DK(m, it)
+        ev.setStream(stream.cuda_stream)
+        ms = {}
+        with torch.cuda.stream(stream):
+            for c in (0, 1, 2):
+                d = torch.from_numpy(np.ascontiguousarray(lists[c])).cuda()
+                J = torch.empty(len(d), 3, dtype=torch.float64, device="cuda")
+                P = torch.empty(len(d), dtype=torch.float64, device="cuda")
+                for _ in range(2):
+                    ev.runClassDevice(c, d.data_ptr(), len(d), 0, J.data_ptr(), P.data_ptr())
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(5):
+                    ev.runClassDevice(c, d.data_ptr(), len(d), 0, J.data_ptr(), P.data_ptr())
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms[CLASS_NAMES[c]] = e0.elapsed_time(e1) / 5
+        n = sum(len(lists[c]) for c in (0, 1, 2))
+        out[name] = {"pairs": int(n), "class_ms": ms, "ms_per_step": float(sum(ms.values())),
+                     "value": n / (sum(ms.values()) * 1e-3), "unit": "pair-integrals/s (J only, fixed level 0)"}
     return out
 
 
@@ -334,12 +405,82 @@ def c5_section(args):
         idx = torch.as_tensor(np.sort(rng.choice(len(rows[c]), 200, replace=False)), device="cuda")
         pr = rows[c][idx].cpu().numpy()
         acc[CLASS_NAMES[c]] = class_accuracy(V * s, C, c, pr, J[c][idx].cpu().numpy() * s ** 2, P[c][idx].cpu().numpy() * s ** 3)
+    backward = c5_backward(V, C, rows, ev, stream)
     return {"workload": "C5: torus R=1, r=0.1, 2000 x 500 grid, x 5e-4, normal jitter 0.05 h, near < 3h, relative 1e-6, mixed",
-            "triangles": int(len(C)), "pairs": int(total), "pairs_by_class": counts,
+            "triangles": int(len(C)), "pairs": int(total), "pairs_by_class": counts, "backward": backward,
             "edge_length": [float(e.min()), float(e.max())], "aspect_ratio": {"mean": float(aspect.mean()), "max": float(aspect.max())},
             "pair_builder_s": {"gpu": t_dev, "host": t_host, "same_lists": True},
             "value": total / (ms * 1e-3), "unit": "pair-integrals/s", "ms_per_step": ms, "steps": steps, "warmup": 1,
             "clocks": clk.summary(), "accuracy": acc}
+
+
+def c5_backward(V, C, rows, ev, stream, ncoords=3):
+    """adjoint of L = sum_p (gJ_p . J_p + gP_p P_p) (seeded gJ, gP ~ N(0, 1)) after the mixed C5
+    forward pass: the FP32 adjoint over all 194 M pairs, refined sub-cells recomputed at the levels
+    the forward kept (one timed pass, CUDA events); spot check on a few coordinates against central
+    differences of the FP64 forward with every pair held at its kept level (h = 1e-6 x the local
+    edge length), each over the pairs that touch the coordinate's vertex, run on the sub-mesh of
+    the cells those pairs use (a pair's integrals depend on its two cells only)"""
+    import torch
+    from integrator2_gb300 import api
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    gJ = {c: torch.randn(len(rows[c]), 3, dtype=torch.float64, device="cuda", generator=gen) for c in CLASSES}
+    gP = {c: torch.randn(len(rows[c]), dtype=torch.float64, device="cuda", generator=gen) for c in CLASSES}
+    gradV = torch.zeros(len(V), 3, dtype=torch.float64, device="cuda")
+    with torch.cuda.stream(stream):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for c in CLASSES:
+            ev.backwardClass(c, rows[c].data_ptr(), len(rows[c]), gJ[c].data_ptr(), gP[c].data_ptr(), gradV.data_ptr())
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    g = gradV.cpu().numpy().reshape(-1)
+    levels = {c: torch.as_tensor(ev.getLevels(c), device="cuda") if c != 3 else torch.zeros(len(rows[c]), dtype=torch.int32, device="cuda")
+              for c in CLASSES}
+    rng = np.random.default_rng(9)
+    Ct = torch.as_tensor(np.asarray(C, np.int32), device="cuda")
+    checks = []
+    for k in rng.choice(V.size, ncoords, replace=False):
+        v = int(k) // 3
+        cells = torch.nonzero((Ct == v).any(dim=1)).flatten()
+        edge = float(np.linalg.norm(V[C[int(cells[0])]][1] - V[C[int(cells[0])]][0]))
+        h = 1e-6 * edge
+        sub = {}
+        for c in CLASSES:
+            m = torch.isin(rows[c][:, 0], cells) | torch.isin(rows[c][:, 1], cells)
+            sub[c] = (rows[c][m].cpu().numpy(), levels[c][m].cpu().numpy(), gJ[c][m].cpu().numpy(), gP[c][m].cpu().numpy())
+        used = np.unique(np.concatenate([sub[c][0].reshape(-1) for c in CLASSES]))
+        Cs = np.asarray(C)[used]
+        vused, Cl = np.unique(Cs.reshape(-1), return_inverse=True)
+        Cl = Cl.reshape(-1, 3).astype(np.int32)
+        remap = {int(x): i for i, x in enumerate(used)}
+        vals = []
+        for sgn in (1.0, -1.0):
+            Vp = np.array(V, np.float64)
+            Vp.reshape(-1)[k] += sgn * h
+            m = api.Mesh3D()
+            m.setGeometry(np.ascontiguousarray(Vp[vused]), Cl)
+            m.prepareMesh(NEAR)
+            tot = 0.0
+            for c in CLASSES:
+                pr, lev, gj, gp = sub[c]
+                if not len(pr):
+                    continue
+                prl = np.vectorize(remap.get)(pr).astype(np.int32).reshape(-1, 2)
+                for L in np.unique(lev):
+                    sel = lev == L
+                    it = api.NumericalIntegrator3D(m, api.qf3D13)
+                    it.setFixedRefinementLevel(int(max(L, 0)))
+                    e = api.EvaluatorJ3DK(m, it)
+                    e.runClass(c, prl[sel])
+                    tot += float(np.sum(gj[sel] * e.getResults(c)) + np.sum(gp[sel] * e.getPotentials(c)))
+            vals.append(tot)
+        fd = (vals[0] - vals[1]) / (2 * h)
+        checks.append({"coordinate": int(k), "adjoint": float(g[k]), "fd": fd, "abs_err_over_max_grad": abs(fd - g[k]) / np.abs(g).max()})
+    return {"ms": ms, "variant": "FP32 adjoint (after the mixed forward), sub-cells recomputed at the kept levels",
+            "fd_spot_check": {"coordinates": checks, "of": "FP64 forward at the kept levels", "h": "1e-6 x local edge length",
+                              "max_abs_err_over_max_grad": max(x["abs_err_over_max_grad"] for x in checks)}}
 
 
 def run_form(ev, lists, d_pairs, d_J, d_P, stream, flush, steps, warmup):
@@ -457,11 +598,38 @@ def uneven_batch_section(args):
             "per_class": {"value": total / (ms_per_class * 1e-3), "ms_per_step": ms_per_class, "launches": "4 class chains x 48 meshes"}}
 
 
+def local_fd(V, C, lists, c, w, k, h, loss, groups=None, **settings):
+    """central difference of the loss with respect to coordinate k over the pairs that touch its
+    vertex's cells (no other pair depends on that coordinate, so this equals the difference of the
+    whole loss); groups: per class, the refinement level each pair is held at (a frozen
+    refinement), None to run the settings as given"""
+    import torch
+    cells = np.where((np.asarray(C) == k // 3).any(axis=1))[0]
+    sel = [np.isin(l[:, 0], cells) | np.isin(l[:, 1], cells) for l in lists]
+    runs = []
+    if groups is None:
+        runs.append(([l[m] for l, m in zip(lists, sel)], [ck[m] for ck, m in zip(c, sel)], settings))
+    else:
+        for L in sorted({int(x) for g, m in zip(groups, sel) for x in np.asarray(g)[m]}):
+            ms = [m & (np.asarray(g) == L) for g, m in zip(groups, sel)]
+            runs.append(([l[m] for l, m in zip(lists, ms)], [ck[m] for ck, m in zip(c, ms)], dict(settings, mode="fixed", level=max(L, 0))))
+    vals = []
+    for sgn in (1.0, -1.0):
+        Vp = np.array(V, np.float64).reshape(-1)
+        Vp[k] += sgn * h
+        Vq = torch.tensor(Vp.reshape(-1, 3), dtype=torch.float64, device="cuda")
+        with torch.no_grad():
+            vals.append(sum(float(loss(Vq, sub, cs, **kw)) for sub, cs, kw in runs))
+    return (vals[0] - vals[1]) / (2 * h)
+
+
 def adjoint_section(args):
     """C4 workload: 5,120-triangle sphere displaced radially by spherical harmonics of degree <= 6
     (coefficients ~ N(0, 0.05^2), seed 4), all four pair classes (near < 3h).  Times forward +
     backward of L = sum_p c_p (P_p + w . J_p) through the torch front-end (FP64 and FP32 adjoint)
-    and checks the FP64 gradient against central differences (h = 1e-6) on a few coordinates."""
+    and checks both gradients against central differences (h = 1e-6) of the FP64 forward on
+    --fd-coords seeded coordinates (each difference over the pairs that touch the coordinate's
+    vertex, which equals the difference of the whole loss)."""
     import torch
     from integrator2_gb300 import api, meshes, pairs
     from integrator2_gb300.autograd import pair_integrals
@@ -469,16 +637,18 @@ def adjoint_section(args):
     pl = pairs.build_pairs(V, C, NEAR)
     lists = [pl.vertex, pl.edge, pl.far, pl.self_]
     rng = np.random.default_rng(11)
-    c = [torch.as_tensor(rng.standard_normal(len(l)), device="cuda") for l in lists]
-    w = torch.as_tensor(rng.standard_normal(3), device="cuda")
+    c = [rng.standard_normal(len(l)) for l in lists]
+    w = rng.standard_normal(3)
+    wt = torch.as_tensor(w, device="cuda")
     settings = dict(mode="fixed", level=1, hard_tol=0.0)
 
-    def loss(Vt, **kw):
-        outs = pair_integrals(Vt, C, lists, **kw)
-        return sum((ck * (P + J @ w)).sum() for (J, P), ck in zip(outs, c))
+    def loss(Vt, lst, cs, **kw):
+        outs = pair_integrals(Vt, C, lst, **kw)
+        return sum((torch.as_tensor(ck, device="cuda") * (P + J @ wt)).sum() for (J, P), ck in zip(outs, cs))
 
     out = {"workload": "C4: sphere s4 (5120 triangles) with SH displacement l<=6, 4 classes, fixed level 1",
            "pairs": int(sum(len(l) for l in lists))}
+    grads = {}
     for name, prec in (("fp64", api.PRECISION_FP64), ("fp32", api.PRECISION_MIXED)):
         kw = dict(settings, precision=prec)
         times = []
@@ -486,7 +656,7 @@ def adjoint_section(args):
             Vt = torch.tensor(V, dtype=torch.float64, device="cuda", requires_grad=True)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            L = loss(Vt, **kw)
+            L = loss(Vt, lists, c, **kw)
             t1 = time.perf_counter()
             L.backward()
             torch.cuda.synchronize()
@@ -494,21 +664,15 @@ def adjoint_section(args):
             times.append((t1 - t0, t2 - t1))
         fwd, bwd = np.median([t[0] for t in times]), np.median([t[1] for t in times])
         out[name] = {"forward_ms": 1e3 * fwd, "backward_ms": 1e3 * bwd}
-        if name == "fp64":
-            g64 = Vt.grad.detach().cpu().numpy().reshape(-1)
-        else:
-            g32 = Vt.grad.detach().cpu().numpy().reshape(-1)
-    h, err = 1e-6, 0.0
-    for k in rng.choice(V.size, max(1, args.fd_coords), replace=False):
-        Vp, Vm = V.reshape(-1).copy(), V.reshape(-1).copy()
-        Vp[k] += h
-        Vm[k] -= h
-        with torch.no_grad():
-            fd = (float(loss(torch.tensor(Vp.reshape(-1, 3), device="cuda"), **settings)) -
-                  float(loss(torch.tensor(Vm.reshape(-1, 3), device="cuda"), **settings))) / (2 * h)
-        err = max(err, abs(fd - g64[k]) / np.abs(g64).max())
-    out["fd_check"] = {"coordinates": int(args.fd_coords), "h": h, "max_abs_err_over_max_grad": float(err)}
-    out["fp32_vs_fp64_max_rel"] = float(np.abs(g32 - g64).max() / np.abs(g64).max())
+        grads[name] = Vt.grad.detach().cpu().numpy().reshape(-1)
+    h = 1e-6
+    coords = rng.choice(V.size, max(1, args.fd_coords), replace=False)
+    fd = np.array([local_fd(V, C, lists, c, w, int(k), h, loss, **settings) for k in coords])
+    for name, g in grads.items():
+        out[name]["fd_max_abs_err_over_max_grad"] = float(np.max(np.abs(fd - g[coords])) / np.abs(g).max())
+    out["fd_check"] = {"coordinates": int(len(coords)), "h": h, "of": "FP64 forward",
+                       "max_abs_err_over_max_grad": {n: out[n]["fd_max_abs_err_over_max_grad"] for n in grads}}
+    out["fp32_vs_fp64_max_rel"] = float(np.abs(grads["fp32"] - grads["fp64"]).max() / np.abs(grads["fp64"]).max())
     return out
 
 
@@ -695,6 +859,8 @@ def gpu_arm(args):
         line["uneven_batch"] = uneven_batch_section(args)
     if "c5" in sections:
         line["c5"] = c5_section(args)
+    if "level0" in sections:
+        line["fp64_level0_j_only"] = fp64_level0_j_only(stream)
     if "adjoint" in sections:
         line["adjoint"] = adjoint_section(args)
     if "batch" in forms:
@@ -723,12 +889,13 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--cpu-fraction", type=float, default=1.0,
                     help="cpu_baseline leg of the GPU arm: share of every class (1 = every pair, about 2.5 s on 16 cores)")
-    ap.add_argument("--fd-coords", type=int, default=10, help="adjoint section: coordinates checked by finite differences")
+    ap.add_argument("--fd-coords", type=int, default=200, help="adjoint section: coordinates checked by finite differences")
     ap.add_argument("--forms", default="fp64,mixed,batch",
                     help="forms to run: fp64, mixed (per-class chains), batch (headline when present)")
-    ap.add_argument("--sections", default="uneven,c5,adjoint",
+    ap.add_argument("--sections", default="uneven,c5,adjoint,level0",
                     help="side sections after the C2 line: uneven (48 meshes, batched vs per class), c5 (2 M triangles), "
-                         "adjoint (C4); empty for the C2 line alone")
+                         "adjoint (C4), level0 (plain FP64, J only, fixed level 0 on C1/C2: the reference's own "
+                         "workload; --impl reference times the reference's CUDA build on it); empty for the C2 line alone")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)

@@ -148,6 +148,11 @@ i2_status i2_integrator_set_potential_rule(i2_integrator_t *it, int32_t n_radial
  * common-vertex pairs (folded: normals more than 60 degrees apart, or a cell with an angle
  * below 10 degrees); 0 keeps the plain Duffy rule for them too.  Default 1e-8. */
 i2_status i2_integrator_set_hard_pair_tolerance(i2_integrator_t *it, double rel_tol);
+/* No counterpart in the reference, which computes J only: enabled = 0 computes J only here too.
+ * The potential rule of the adjacent classes (graded Duffy tiers, adaptive rule) is skipped and
+ * their P reads NaN; the disjoint and self classes keep P (it costs them almost nothing).
+ * Default 1.  The batched form and the adjoint need the potential (I2_ERR_UNSUPPORTED). */
+i2_status i2_integrator_set_potential(i2_integrator_t *it, int32_t enabled);
 /* self-class normal convention: 0 principal value (J = 0), +1 / -1 one-sided limit */
 i2_status i2_integrator_set_self_convention(i2_integrator_t *it, int32_t sign);
 

@@ -45,6 +45,7 @@ SIGNATURES = {
     "i2_integrator_set_precision": (ctypes.c_int, [_vp, ctypes.c_int]),
     "i2_integrator_set_potential_rule": (ctypes.c_int, [_vp, _i32, _i32, _i32, _i32]),
     "i2_integrator_set_self_convention": (ctypes.c_int, [_vp, _i32]),
+    "i2_integrator_set_potential": (ctypes.c_int, [_vp, _i32]),
     "i2_integrator_set_hard_pair_tolerance": (ctypes.c_int, [_vp, _d]),
     "i2_evaluator_create": (ctypes.c_int, [_vp, _vp, _pp]),
     "i2_evaluator_destroy": (None, [_vp]),

@@ -174,6 +174,11 @@ class NumericalIntegrator3D:
         """adaptive potential of folded / sliver adjacent pairs (0 disables)"""
         call("i2_integrator_set_hard_pair_tolerance", self._h, float(rel_tol))
 
+    def setPotential(self, enabled: bool) -> None:
+        """False: J only, as the reference computes it (the adjacent classes' potential rule is
+        skipped and their P reads NaN)"""
+        call("i2_integrator_set_potential", self._h, 1 if enabled else 0)
+
     def setSelfConvention(self, sign: int) -> None:
         call("i2_integrator_set_self_convention", self._h, int(sign))
 

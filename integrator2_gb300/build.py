@@ -74,8 +74,10 @@ CLI_OUT = os.path.join(HERE, "integrator2test3D")
 def build_cli() -> str:
     """the command-line driver (host C++ over the C-ABI), linked to libi2gb300.so next to it"""
     cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
-    r = subprocess.run([cxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), CLI_SRC, "-o", CLI_OUT, "-L", HERE,
-                        "-li2gb300", "-Wl,-rpath,$ORIGIN"], capture_output=True, text=True)
+    cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+    r = subprocess.run([cxx, "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(cuda, "include"), CLI_SRC,
+                        "-o", CLI_OUT, "-L", HERE, "-li2gb300", "-Wl,-rpath,$ORIGIN", "-L", os.path.join(cuda, "lib64"), "-lcudart"],
+                       capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"CLI build failed:\n{r.stderr}")
     return CLI_OUT

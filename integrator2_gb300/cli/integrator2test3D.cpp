@@ -1,7 +1,7 @@
 // integrator2test3D -- command-line driver with the options of the reference's test program
 // (tests/integrator3D/main.cu: -f/--meshfile, -s/--scale, -r/--refine, -c/--checkresults,
-// --exporttoobj, --exporttovtk, --exporttocsv, --exportresults), written over the C++ layer of
-// this library (include/integrator2_gb300.hpp).  Additions: --near=<factor> (disjoint pairs with
+// --exporttoobj, --exporttovtk, --exporttocsv, --exportresults), written over the C++ drop-in
+// headers of this library (include/integrator2/).  Additions: --near=<factor> (disjoint pairs with
 // centroid distance < factor x mean edge length only; default: every disjoint pair, as the
 // reference), --relative=<tol> (scale-invariant error control), --mixed (mixed precision),
 // --fullprecision (CSV with 17 significant digits).
@@ -9,17 +9,19 @@
 // Output files have the reference's names: SimpleNeighbors / AttachedNeighbors / NotNeighbors
 // .dat (plain text) or .csv, OriginalMesh.obj / RefinedMesh.obj, OriginalMesh.vtp / RefinedMesh.vtp.
 // The VTK export of an adaptive run carries, per cell and per pair class, the refinement level
-// the cell's pairs (the cell as K_i) needed: the largest kept level over those pairs.
-#include "integrator2_gb300.hpp"
+// the cell's pairs (the cell as K_i) needed: the largest kept level over those pairs.  The
+// refined mesh of a fixed-level run is the reference's (every cell split at its own edge
+// midpoints, NumericalIntegrator3D::getRefinedVertices / getRefinedCells).
+#include "integrator2/Mesh3d.cuh"
+#include "integrator2/NumericalIntegrator3d.cuh"
+#include "integrator2/evaluators/evaluatorJ3DK.cuh"
 
+#include <array>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <fstream>
-#include <map>
 #include <string>
-#include <utility>
 #include <vector>
 
 namespace {
@@ -50,72 +52,27 @@ bool numeric(const char *s)
     return end != s && *end == 0;
 }
 
-void write_obj(const std::string &name, const std::vector<double> &V, const std::vector<Int3> &C)
-{
-    std::ofstream f(name);
-    for (size_t k = 0; k < V.size() / 3; ++k) f << "v " << V[3 * k] << " " << V[3 * k + 1] << " " << V[3 * k + 2] << "\n";
-    for (const Int3 &c : C) f << "f " << c.x + 1 << " " << c.y + 1 << " " << c.z + 1 << "\n";
-    std::printf("Mesh saved to %s\n", name.c_str());
-}
-
-void write_vtp(const std::string &name, const std::vector<double> &V, const std::vector<Int3> &C,
-               const std::vector<std::vector<int>> &refinements)
-{
-    std::ofstream f(name);
-    f << "<?xml version=\"1.0\" ?>\n<VTKFile type=\"PolyData\" version=\"0.1\" byte_order=\"LittleEndian\">\n  <PolyData>\n";
-    f << "    <Piece NumberOfPoints=\"" << V.size() / 3 << "\" NumberOfPolys=\"" << C.size() << "\">\n";
-    f << "      <Points>\n        <DataArray type=\"Float32\" NumberOfComponents=\"3\" Format=\"ascii\">\n        ";
-    for (double x : V) f << x << " ";
-    f << "\n        </DataArray>\n      </Points>\n      <Polys>\n";
-    f << "        <DataArray type=\"Int32\" Name=\"connectivity\" Format=\"ascii\">\n          ";
-    for (const Int3 &c : C) f << c.x << " " << c.y << " " << c.z << " ";
-    f << "\n        </DataArray>\n        <DataArray type=\"Int32\" Name=\"offsets\" Format=\"ascii\">\n          ";
-    for (size_t k = 0; k < C.size(); ++k) f << 3 * (k + 1) << " ";
-    f << "\n        </DataArray>\n      </Polys>\n";
-    bool any = false;
-    for (const auto &r : refinements) any = any || !r.empty();
-    if (any) {
-        f << "      <CellData>\n";
-        const neighbour_type_enum types[3] = {neighbour_type_enum::simple_neighbors, neighbour_type_enum::attached_neighbors,
-                                              neighbour_type_enum::not_neighbors};
-        for (int k = 0; k < 3; ++k) {
-            if (refinements[k].empty()) continue;
-            f << "        <DataArray type=\"Int32\" Name=\"" << neighborTypeString(types[k]) << "Refinements\" Format=\"ascii\">\n          ";
-            for (int v : refinements[k]) f << v << " ";
-            f << "\n        </DataArray>\n";
-        }
-        f << "      </CellData>\n";
+// the evaluator with the largest (i,j)/(j,i) difference per class after runAllPairs(true)
+class Evaluator : public EvaluatorJ3DK {
+public:
+    Evaluator(const Mesh3D &m, NumericalIntegrator3D &it) : EvaluatorJ3DK(m, it) {}
+    double largestError(neighbour_type_enum t) const
+    {
+        const deviceVector<double> &e = t == neighbour_type_enum::simple_neighbors ? simpleNeighborsErrors
+                                      : t == neighbour_type_enum::attached_neighbors ? attachedNeighborsErrors : notNeighborsErrors;
+        std::vector<double> h(e.size);
+        if (e.size) copy_d2h(e.data, h.data(), h.size());
+        double mx = 0.0;
+        for (double x : h) mx = x > mx ? x : mx;
+        return mx;
     }
-    f << "    </Piece>\n  </PolyData>\n</VTKFile>\n";
-    std::printf("Mesh saved to %s\n", name.c_str());
-}
+};
 
-// every cell split `level` times by midpoints in the reference's child order; vertices at edge
-// midpoints are shared between the cells on both sides
-void refine(std::vector<double> &V, std::vector<Int3> &C, int level)
+template <class T> std::vector<T> host_copy(const deviceVector<T> &d)
 {
-    for (int l = 0; l < level; ++l) {
-        std::map<std::pair<int, int>, int> mid;
-        auto midpoint = [&](int a, int b) {
-            const std::pair<int, int> key(std::min(a, b), std::max(a, b));
-            auto it = mid.find(key);
-            if (it != mid.end()) return it->second;
-            const int id = (int)(V.size() / 3);
-            for (int k = 0; k < 3; ++k) V.push_back(0.5 * (V[3 * a + k] + V[3 * b + k]));
-            mid[key] = id;
-            return id;
-        };
-        std::vector<Int3> out;
-        out.reserve(4 * C.size());
-        for (const Int3 &c : C) {
-            const int mab = midpoint(c.x, c.y), mbc = midpoint(c.y, c.z), mca = midpoint(c.z, c.x);
-            out.push_back({mab, c.y, mbc});
-            out.push_back({mbc, c.z, mca});
-            out.push_back({mca, c.x, mab});
-            out.push_back({mbc, mca, mab});
-        }
-        C.swap(out);
-    }
+    std::vector<T> h(d.size);
+    if (d.size) copy_d2h(d.data, h.data(), h.size());
+    return h;
 }
 
 } // namespace
@@ -175,10 +132,7 @@ int main(int argc, char **argv)
     }
     try {
         Mesh3D mesh;
-        if (!mesh.loadMeshFromFile(meshfile, scale)) {
-            std::fprintf(stderr, "%s\n", i2_last_error());
-            return EXIT_FAILURE;
-        }
+        if (!mesh.loadMeshFromFile(meshfile, scale)) return EXIT_FAILURE;
         mesh.prepareMesh(near);
         NumericalIntegrator3D integrator(mesh, qf3D13);
         if (refineLevel >= 0) {
@@ -192,29 +146,26 @@ int main(int argc, char **argv)
             std::printf("Using adaptive error control procedure\n");
         }
         if (mixed) integrator.setPrecision(I2_PRECISION_MIXED);
-        const std::vector<double> V = mesh.getVertices();
-        const std::vector<Int3> C = mesh.getCells();
-        if (obj) write_obj("OriginalMesh.obj", V, C);
-        if (vtk && refineLevel >= 0) write_vtp("OriginalMesh.vtp", V, C, {{}, {}, {}});
+        const std::vector<Point3> V = host_copy(mesh.getVertices());
+        const std::vector<int3> C = host_copy(mesh.getCells());
+        const std::array<std::vector<unsigned char>, 3> none;
+        if (obj) exportMeshToObj("OriginalMesh.obj", V, C);
+        if (vtk && refineLevel >= 0) exportMeshToVtk("OriginalMesh.vtp", V, C, none);
 
-        EvaluatorJ3DK evaluator(mesh, integrator);
+        Evaluator evaluator(mesh, integrator);
         const auto t0 = std::chrono::steady_clock::now();
         evaluator.runAllPairs(check);
         const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         const neighbour_type_enum types[3] = {neighbour_type_enum::simple_neighbors, neighbour_type_enum::attached_neighbors,
                                               neighbour_type_enum::not_neighbors};
-        const size_t counts[3] = {mesh.getSimpleNeighbors().size(), mesh.getAttachedNeighbors().size(), mesh.getNotNeighbors().size()};
+        const size_t counts[3] = {(size_t)mesh.getSimpleNeighbors().size, (size_t)mesh.getAttachedNeighbors().size,
+                                  (size_t)mesh.getNotNeighbors().size};
         std::printf("Integration of %zu ordered pairs (simple %zu, attached %zu, not neighbours %zu): %.3f ms\n",
                     2 * (counts[0] + counts[1] + counts[2]), 2 * counts[0], 2 * counts[1], 2 * counts[2], ms);
-        if (check) {
-            for (int k = 0; k < 3; ++k) {
-                if (!counts[k]) continue;
-                const std::vector<double> e = evaluator.getErrors(types[k]);
-                double mx = 0.0;
-                for (double x : e) mx = x > mx ? x : mx;
-                std::printf("%s: largest (i,j)/(j,i) difference %.3e\n", neighborTypeString(types[k]).c_str(), mx);
-            }
-        }
+        if (check)
+            for (int k = 0; k < 3; ++k)
+                if (counts[k])
+                    std::printf("%s: largest (i,j)/(j,i) difference %.3e\n", neighborTypeString(types[k]).c_str(), evaluator.largestError(types[k]));
         if (plain || csv) {
             const output_format_enum fmt = plain && !csv ? output_format_enum::plainText
                                                          : (full ? output_format_enum::csvFullPrecision : output_format_enum::csv);
@@ -222,29 +173,18 @@ int main(int argc, char **argv)
                 if (counts[k]) evaluator.outputResultsToFile(types[k], fmt);
         }
         if ((obj || vtk) && refineLevel > 0) {
-            std::vector<double> Vr = V;
-            std::vector<Int3> Cr = C;
-            refine(Vr, Cr, refineLevel);
-            if (obj) write_obj("RefinedMesh.obj", Vr, Cr);
-            if (vtk) write_vtp("RefinedMesh.vtp", Vr, Cr, {{}, {}, {}});
+            const std::vector<Point3> Vr = host_copy(integrator.getRefinedVertices());
+            const std::vector<int3> Cr = host_copy(integrator.getRefinedCells());
+            if (obj) exportMeshToObj("RefinedMesh.obj", Vr, Cr);
+            if (vtk) exportMeshToVtk("RefinedMesh.vtp", Vr, Cr, none);
         }
         if (vtk && refineLevel < 0) {
-            std::vector<std::vector<int>> ref(3);
-            const std::vector<std::vector<Int3>> lists = {mesh.getSimpleNeighbors(), mesh.getAttachedNeighbors(), mesh.getNotNeighbors()};
-            for (int k = 0; k < 3; ++k) {
-                if (lists[k].empty()) continue;
-                ref[k].assign(C.size(), 0);
-                const std::vector<double> lev = evaluator.getLevels(types[k]);
-                const size_t n = lists[k].size();
-                for (size_t p = 0; p < lev.size(); ++p) {
-                    const Int3 &pr = lists[k][p % n];
-                    const int i = p < n ? pr.x : pr.y;  // rows n..2n-1 are the reversed pairs
-                    ref[k][i] = std::max(ref[k][i], (int)lev[p]);
-                }
-            }
-            write_vtp("OriginalMesh.vtp", V, C, ref);
+            std::array<std::vector<unsigned char>, 3> ref;
+            for (int k = 0; k < 3; ++k)
+                if (counts[k]) ref[k] = host_copy(*integrator.getRefinementsRequired(types[k]));
+            exportMeshToVtk("OriginalMesh.vtp", V, C, ref);
         }
-    } catch (const i2::Error &e) {
+    } catch (const i2dropin::Error &e) {
         std::fprintf(stderr, "%s\n", e.what());
         return EXIT_FAILURE;
     }

@@ -647,7 +647,8 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         A.fix_part = W.fix_part.ptr;
         A.fix_cap = i2::kFixDeepCap;
     }
-    if ((cls == I2_SIMPLE_NEIGHBORS || cls == I2_ATTACHED_NEIGHBORS) && cfg.hard_tol > 0) {
+    A.pot_off = cfg.potential ? 0 : 1;
+    if ((cls == I2_SIMPLE_NEIGHBORS || cls == I2_ATTACHED_NEIGHBORS) && cfg.hard_tol > 0 && cfg.potential) {
         A.hard_list = W.hard_list.ptr;
         A.hard_cnt = W.cnt.ptr + i2::kCntHard;
         A.hard_overflow = W.cnt.ptr + i2::kCntOverflow;
@@ -1079,6 +1080,14 @@ i2_status i2_integrator_set_hard_pair_tolerance(i2_integrator_t *it, double rel_
     });
 }
 
+i2_status i2_integrator_set_potential(i2_integrator_t *it, int32_t enabled)
+{
+    return guarded([&] {
+        I2_REQUIRE(it, I2_ERR_INVALID_ARGUMENT, "null integrator");
+        it->cfg.potential = enabled != 0;
+    });
+}
+
 i2_status i2_integrator_set_self_convention(i2_integrator_t *it, int32_t sign)
 {
     return guarded([&] {
@@ -1195,6 +1204,7 @@ i2_status i2_evaluator_backward_class(i2_evaluator_t *ev, i2_pair_class cls, con
         I2_REQUIRE(m.on_device, I2_ERR_STATE, "mesh not on the device");
         // the settings and tier bars of the forward pass (run_class_device)
         i2::RunConfig cfg = R.cfg;
+        I2_REQUIRE(cfg.potential, I2_ERR_UNSUPPORTED, "the adjoint needs the forward run with the potential (i2_integrator_set_potential)");
         const double tier_tol = R.tier_tol, top_tol = R.top_tol;
         if (ev->persistent_blocks == 0) {
             int dev = 0, sms = 0;
@@ -1314,6 +1324,7 @@ i2_status i2_batch_create(const i2_integrator_t *settings, i2_batch_t **out)
 {
     return guarded([&] {
         I2_REQUIRE(settings && out, I2_ERR_INVALID_ARGUMENT, "null argument");
+        I2_REQUIRE(settings->cfg.potential, I2_ERR_UNSUPPORTED, "the batched form computes the potential (i2_integrator_set_potential)");
         auto b = std::make_unique<i2_batch>();
         b->cfg = settings->cfg;
         b->Q = settings->tables(true);  // the batched form is mixed precision

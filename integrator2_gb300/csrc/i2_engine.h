@@ -38,6 +38,7 @@ struct RunConfig {
     double tol = 1e-6;    // relative tolerance of the adaptive relative mode
     int self_sign = 0;    // self-class normal convention
     double hard_tol = 1e-8;  // relative tolerance of the adaptive potential of hard adjacent pairs (0: off)
+    bool potential = true;   // false: J only, as the reference computes (adjacent pairs' P is not computed)
 };
 
 // doubles of one hard pair's cached FP64 set-up (PotPairCtx in i2_kernels_fp64.cu)
@@ -93,6 +94,7 @@ struct ClassArgs {
     double *pot_tri_a = nullptr, *pot_tri_b = nullptr;
     int pot_tri_cap = 0;
     double tier_tol = 1e-7;                   // main/check (and main/higher-order) rule agreement bar
+    int pot_off = 0;                          // 1: J only; adjacent pairs' potential is not computed (P reads NaN)
     double top_tol = 1e-8;                    // 16 x 16 / 24 x 24 agreement bar (tier 2b)
     // outputs
     double *raw4 = nullptr, *J3 = nullptr, *P = nullptr;

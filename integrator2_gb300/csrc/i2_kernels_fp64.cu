@@ -211,6 +211,7 @@ __global__ void __launch_bounds__(128) k_singular(ClassArgs A, QuadTables Q)
     else closed_vertex(Ti, Tj, ni, K.n, Si, psi, th);
     double *sg = A.sing + 4 * (long long)t;
     sg[0] = psi.x; sg[1] = psi.y; sg[2] = psi.z; sg[3] = th;
+    if (A.pot_off) return;  // J only (P was filled with NaN before the launch)
 
     // potential: tier 1 of the tiered rule (graded Duffy, main and lower-order check)
     const FarCtx F = make_far_ctx(K);
@@ -752,6 +753,7 @@ void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const R
         launch_self(A, Q, cfg, s);
         break;
     case kEdge:
+        if (A.pot_off) cudaMemsetAsync(A.padj, 0xff, sizeof(double) * (size_t)A.n, s);  // all-ones bytes: NaN
         k_singular<kEdge><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q);
         if (A.hard_list) {
             k_pot_tier2<kEdge><<<resident_grid((const void *)k_pot_tier2<kEdge>, tpb, 0), tpb, 0, s>>>(A, Q);
@@ -761,6 +763,7 @@ void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const R
         level_chain<kEdge>(A, Q, cfg, persistent_blocks, s);
         break;
     case kVertex:
+        if (A.pot_off) cudaMemsetAsync(A.padj, 0xff, sizeof(double) * (size_t)A.n, s);
         k_singular<kVertex><<<blocks_for(A.n, tpb), tpb, 0, s>>>(A, Q);
         if (A.hard_list) {
             k_pot_tier2<kVertex><<<resident_grid((const void *)k_pot_tier2<kVertex>, tpb, 0), tpb, 0, s>>>(A, Q);

@@ -1005,7 +1005,8 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
         break;
     case kEdge:
         k_singular_mixed<kEdge><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
-        k_tier1_mixed<kEdge><<<blocks_for_m((long long)kTier1Lanes * A.n, tpb), tpb, 0, s>>>(A, Qf);
+        if (A.pot_off) cudaMemsetAsync(A.padj, 0xff, sizeof(double) * (size_t)A.n, s);  // J only: P reads NaN
+        else k_tier1_mixed<kEdge><<<blocks_for_m((long long)kTier1Lanes * A.n, tpb), tpb, 0, s>>>(A, Qf);
         if (A.hard_list) {
             k_pot_tier2_mixed<kEdge><<<resident_grid((const void *)k_pot_tier2_mixed<kEdge>, tpb, 0), tpb, 0, s>>>(A, Qf, Q);
             k_pot_tier2b<kEdge><<<resident_grid((const void *)k_pot_tier2b<kEdge>, tpb, 0), tpb, 0, s>>>(A, Q, 0);
@@ -1016,7 +1017,8 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
         break;
     case kVertex:
         k_singular_mixed<kVertex><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
-        k_tier1_mixed<kVertex><<<blocks_for_m((long long)kTier1Lanes * A.n, tpb), tpb, 0, s>>>(A, Qf);
+        if (A.pot_off) cudaMemsetAsync(A.padj, 0xff, sizeof(double) * (size_t)A.n, s);  // J only: P reads NaN
+        else k_tier1_mixed<kVertex><<<blocks_for_m((long long)kTier1Lanes * A.n, tpb), tpb, 0, s>>>(A, Qf);
         if (A.hard_list) {
             k_pot_tier2_mixed<kVertex><<<resident_grid((const void *)k_pot_tier2_mixed<kVertex>, tpb, 0), tpb, 0, s>>>(A, Qf, Q);
             k_pot_tier2b<kVertex><<<resident_grid((const void *)k_pot_tier2b<kVertex>, tpb, 0), tpb, 0, s>>>(A, Q, 0);

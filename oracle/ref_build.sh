@@ -12,6 +12,8 @@ if [ ! -d "$ref/src" ]; then
     exit 0
 fi
 mkdir -p "$out"
+# where the checkout was found, for tests that compile the reference's own test program
+(cd "$ref" && pwd) > "$out/reference_path"
 flags=(-x cu -std=c++17 -O2 -rdc=true -Xcompiler -fPIC -Xcompiler -ffp-contract=off
        -Xcompiler -Wno-deprecated-declarations -diag-suppress 1444,20091,20092
        -include "$here/ref_shim.h" -I"$ref/src"

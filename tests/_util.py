@@ -41,3 +41,13 @@ def assert_parity(J, Jref, kappa, what=""):
     bad = r > bar
     assert not bad.any(), f"{what}: {bad.sum()} pairs above the bar, worst {r.max():.3e} (bar {bar[r.argmax()]:.1e})"
     return float(r.max())
+
+
+def reference_checkout():
+    """the reference checkout where oracle/ref_build.sh found it (it records the path in
+    oracle/_ref/reference_path), or None where it was not built from one"""
+    f = os.path.join(ROOT, "oracle", "_ref", "reference_path")
+    if not os.path.exists(f):
+        return None
+    path = open(f).read().strip()
+    return path if os.path.isdir(os.path.join(path, "src")) else None

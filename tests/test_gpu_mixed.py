@@ -126,7 +126,7 @@ def test_mixed_full_population_against_fp64(api):
     report = {}
     for cls in (0, 1, 2, 3):
         (J, Pm), (J64, P64) = res[api.PRECISION_MIXED][cls], res[api.PRECISION_FP64][cls]
-        eJ = rel_rows(J, J64) if cls != 3 else np.abs(J - J64).max(axis=1) / np.abs(J64).max()
+        eJ = rel_rows(J, J64) if cls != 3 else np.abs(J - J64).max(axis=1) / max(np.abs(J64).max(), 1e-300)
         eP = np.abs(Pm - P64) / np.abs(P64)
         report[cls] = {ch: (float(np.percentile(e, 99.9)), float(np.mean(e > 1e-6)), float(e.max())) for ch, e in (("J", eJ), ("P", eP))}
         for ch, e in (("J", eJ), ("P", eP)):
