@@ -254,10 +254,10 @@ def accuracy(V, C, lists, J, P, levels, nsample=400):
     return out
 
 
-def fp64_level0_j_only(stream):
-    """the library's plain FP64 form on the reference's own workload: J only (potential off),
-    fixed refinement level 0, qf3D13, the reference's three classes on C1 and C2, per class
-    through the device entry point (lists resident), CUDA events, mean of 5 runs after 2"""
+def level0_j_only(stream, precision):
+    """the library on the reference's own workload: J only (potential off), fixed refinement
+    level 0, qf3D13, the reference's three classes on C1 and C2, per class through the device
+    entry point (lists resident), CUDA events, mean of 5 runs after 2"""
     import torch
     from integrator2_gb300 import api
     out = {}
@@ -268,6 +268,7 @@ def fp64_level0_j_only(stream):
         it = api.NumericalIntegrator3D(m, api.qf3D13)
         it.setFixedRefinementLevel(0)
         it.setPotential(False)
+        it.setPrecision(precision)
         ev = api.EvaluatorJ3DK(m, it)
         ev.setStream(stream.cuda_stream)
         ms = {}
@@ -381,6 +382,7 @@ def c5_section(args):
     ev.setStream(stream.cuda_stream)
     J = {c: torch.empty(len(rows[c]), 3, dtype=torch.float64, device="cuda") for c in CLASSES}
     P = {c: torch.empty(len(rows[c]), dtype=torch.float64, device="cuda") for c in CLASSES}
+    torch.cuda.synchronize()  # the rows were made on torch's default stream; the evaluator runs on `stream`
 
     def step():
         for c in CLASSES:
@@ -405,7 +407,7 @@ def c5_section(args):
         idx = torch.as_tensor(np.sort(rng.choice(len(rows[c]), 200, replace=False)), device="cuda")
         pr = rows[c][idx].cpu().numpy()
         acc[CLASS_NAMES[c]] = class_accuracy(V * s, C, c, pr, J[c][idx].cpu().numpy() * s ** 2, P[c][idx].cpu().numpy() * s ** 3)
-    backward = c5_backward(V, C, rows, ev, stream)
+    backward = c5_backward(V, C, rows, ev, stream, args.c5_backward_fraction)
     return {"workload": "C5: torus R=1, r=0.1, 2000 x 500 grid, x 5e-4, normal jitter 0.05 h, near < 3h, relative 1e-6, mixed",
             "triangles": int(len(C)), "pairs": int(total), "pairs_by_class": counts, "backward": backward,
             "edge_length": [float(e.min()), float(e.max())], "aspect_ratio": {"mean": float(aspect.mean()), "max": float(aspect.max())},
@@ -414,27 +416,50 @@ def c5_section(args):
             "clocks": clk.summary(), "accuracy": acc}
 
 
-def c5_backward(V, C, rows, ev, stream, ncoords=3):
+def c5_backward(V, C, all_rows, ev, stream, fraction, ncoords=3):
     """adjoint of L = sum_p (gJ_p . J_p + gP_p P_p) (seeded gJ, gP ~ N(0, 1)) after the mixed C5
-    forward pass: the FP32 adjoint over all 194 M pairs, refined sub-cells recomputed at the levels
-    the forward kept (one timed pass, CUDA events); spot check on a few coordinates against central
-    differences of the FP64 forward with every pair held at its kept level (h = 1e-6 x the local
-    edge length), each over the pairs that touch the coordinate's vertex, run on the sub-mesh of
-    the cells those pairs use (a pair's integrals depend on its two cells only)"""
+    forward pass, on a seeded share `fraction` of every class's pairs (1: all 194 M pairs; the
+    adjacent classes' adjoint recomputes their rules in FP64 dual numbers, which makes a full pass
+    take minutes): the forward pass over the sample, then the FP32 adjoint with the refined
+    sub-cells recomputed at the levels the forward kept (one timed pass, CUDA events); spot check
+    on a few coordinates against central differences of the FP64 forward with every sampled pair
+    held at its kept level (h = 1e-6 x the local edge length), each over the sampled pairs that
+    touch the coordinate's vertex, run on the sub-mesh of the cells those pairs use (a pair's
+    integrals depend on its two cells only)"""
     import torch
     from integrator2_gb300 import api
     gen = torch.Generator(device="cuda").manual_seed(3)
-    gJ = {c: torch.randn(len(rows[c]), 3, dtype=torch.float64, device="cuda", generator=gen) for c in CLASSES}
-    gP = {c: torch.randn(len(rows[c]), dtype=torch.float64, device="cuda", generator=gen) for c in CLASSES}
-    gradV = torch.zeros(len(V), 3, dtype=torch.float64, device="cuda")
+    rows = {}
+    # everything the evaluator reads is made on the evaluator's stream and finished before its
+    # launches (the evaluator runs on `stream`, not on torch's default stream)
     with torch.cuda.stream(stream):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
         for c in CLASSES:
-            ev.backwardClass(c, rows[c].data_ptr(), len(rows[c]), gJ[c].data_ptr(), gP[c].data_ptr(), gradV.data_ptr())
-        e1.record(stream)
+            n = len(all_rows[c])
+            k = n if fraction >= 1 else max(1, int(n * fraction))
+            sel = torch.randperm(n, device="cuda", generator=gen)[:k].sort().values if k < n else None
+            rows[c] = all_rows[c] if sel is None else all_rows[c][sel].contiguous()
+        gJ = {c: torch.randn(len(rows[c]), 3, dtype=torch.float64, device="cuda", generator=gen) for c in CLASSES}
+        gP = {c: torch.randn(len(rows[c]), dtype=torch.float64, device="cuda", generator=gen) for c in CLASSES}
+        gradV = torch.zeros(len(V), 3, dtype=torch.float64, device="cuda")
         torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+        for c in CLASSES:
+            if len(rows[c]) < len(all_rows[c]):  # the forward pass over the sample (backward needs it just before)
+                k = len(rows[c])
+                J = torch.empty(k, 3, dtype=torch.float64, device="cuda")
+                P = torch.empty(k, dtype=torch.float64, device="cuda")
+                ev.runClassDevice(c, rows[c].data_ptr(), k, 0, J.data_ptr(), P.data_ptr())
+        torch.cuda.synchronize()
+    cls_ms = {}
+    with torch.cuda.stream(stream):
+        torch.cuda.synchronize()
+        for c in CLASSES:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ev.backwardClass(c, rows[c].data_ptr(), len(rows[c]), gJ[c].data_ptr(), gP[c].data_ptr(), gradV.data_ptr())
+            e1.record(stream)
+            torch.cuda.synchronize()
+            cls_ms[CLASS_NAMES[c]] = e0.elapsed_time(e1)
+    ms = sum(cls_ms.values())
     g = gradV.cpu().numpy().reshape(-1)
     levels = {c: torch.as_tensor(ev.getLevels(c), device="cuda") if c != 3 else torch.zeros(len(rows[c]), dtype=torch.int32, device="cuda")
               for c in CLASSES}
@@ -478,7 +503,10 @@ def c5_backward(V, C, rows, ev, stream, ncoords=3):
             vals.append(tot)
         fd = (vals[0] - vals[1]) / (2 * h)
         checks.append({"coordinate": int(k), "adjoint": float(g[k]), "fd": fd, "abs_err_over_max_grad": abs(fd - g[k]) / np.abs(g).max()})
-    return {"ms": ms, "variant": "FP32 adjoint (after the mixed forward), sub-cells recomputed at the kept levels",
+    npairs = int(sum(len(rows[c]) for c in CLASSES))
+    return {"ms": ms, "class_ms": cls_ms, "pairs": npairs, "pairs_per_s": npairs / (ms * 1e-3),
+            "sample": "every pair" if fraction >= 1 else f"seeded {fraction:.0%} of every class ({npairs} pairs)",
+            "variant": "FP32 adjoint (after the mixed forward), sub-cells recomputed at the kept levels",
             "fd_spot_check": {"coordinates": checks, "of": "FP64 forward at the kept levels", "h": "1e-6 x local edge length",
                               "max_abs_err_over_max_grad": max(x["abs_err_over_max_grad"] for x in checks)}}
 
@@ -545,7 +573,7 @@ def uneven_batch_section(args):
     from integrator2_gb300 import api, meshes
     mset = meshes.uneven_mesh_set(2026, 48, 500, 60000)
     stream = torch.cuda.Stream()
-    evs, segs_dev, total = [], [], 0
+    evs, segs_dev, total, seg_of = [], [], 0, []
     batch = None
     for V, C, kind, scale in mset:
         m = api.Mesh3D()
@@ -564,9 +592,9 @@ def uneven_batch_section(args):
         if batch is None:
             batch = api.BatchEvaluator(it)
             batch.setStream(stream.cuda_stream)
-        for c, l in zip(CLASSES, lists):
-            batch.add(m, c, l)
+        segs = [batch.add(m, c, l) for c, l in zip(CLASSES, lists)]
         evs.append((m, it, ev, dev))
+        seg_of.append((V, C, scale, lists, segs))
         total += sum(len(l) for l in lists)
 
     def per_class_step():
@@ -588,11 +616,37 @@ def uneven_batch_section(args):
             torch.cuda.synchronize()
         return e0.elapsed_time(e1) / 3
 
+    torch.cuda.synchronize()  # the lists were copied on torch's default stream; the runs use `stream`
     ms_per_class = timed(per_class_step)
     shape = batch.autotune()
     ms_batch = timed(batch.run)
-    return {"workload": "C3: 48 meshes (ellipsoids, tori, jittered spheres), 500-60000 triangles, scales 5e-4..1e2, near < 3h, relative 1e-6",
-            "triangles": int(sum(len(c) for _, c, _, _ in mset)), "pairs": int(total),
+    # accuracy of the batched results: 50 seeded pairs per class of six meshes (two of each
+    # kind) against the oracle's high-order answer, on the geometry rescaled by a power of two
+    # to unit size (J scales as s^2, P as s^3 exactly; the oracle's absolute thresholds then apply)
+    rng = np.random.default_rng(13)
+    acc = {}
+    for mi in range(6):
+        V, C, scale, lists, segs = seg_of[mi]
+        s2 = 2.0 ** -round(np.log2(np.abs(V).max()))
+        for c, l, sg in zip(CLASSES, lists, segs):
+            if not len(l):
+                continue
+            idx = np.sort(rng.choice(len(l), min(50, len(l)), replace=False))
+            a = class_accuracy(V * s2, C, c, l[idx], batch.getResults(sg)[idx] * s2 ** 2, batch.getPotentials(sg)[idx] * s2 ** 3)
+            key = CLASS_NAMES[c]
+            prev = acc.get(key)
+            if prev is None:
+                acc[key] = a
+            else:
+                for k2 in a:
+                    if k2 != "sample" and k2 in prev:
+                        prev[k2] = max(prev[k2], a[k2])
+                prev["sample"] += a["sample"]
+    sizes = [len(c) for _, c, _, _ in mset]
+    return {"workload": "C3: 48 meshes (ellipsoids, tori, jittered geodesic spheres), 500-60000 triangles, scales 5e-4..1e2, near < 3h, relative 1e-6",
+            "triangles": int(sum(sizes)), "triangles_per_mesh": [int(min(sizes)), int(max(sizes))], "pairs": int(total),
+            "accuracy": {"vs": "oracle high-order answer (fixed level 4, adaptive potential 1e-10), 50 pairs per class of 6 meshes, "
+                               "largest of the per-mesh figures", **acc},
             "batched": {"value": total / (ms_batch * 1e-3), "ms_per_step": ms_batch, "cuda_graph": batch.usesGraph(),
                         "shape": [int(x) for x in shape], "launches": f"{BATCH_LAUNCHES} for all {4 * len(mset)} segments"},
             "per_class": {"value": total / (ms_per_class * 1e-3), "ms_per_step": ms_per_class, "launches": "4 class chains x 48 meshes"}}
@@ -719,6 +773,7 @@ def gpu_arm(args):
     d_J = {c: torch.empty(len(lists[c]), 3, dtype=torch.float64, device="cuda") for c in CLASSES}
     d_P = {c: torch.empty(len(lists[c]), dtype=torch.float64, device="cuda") for c in CLASSES}
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()  # inputs made on torch's default stream, evaluators run on `stream`
 
     forms = {}
     wanted = [f.strip() for f in args.forms.split(",") if f.strip()]
@@ -860,7 +915,9 @@ def gpu_arm(args):
     if "c5" in sections:
         line["c5"] = c5_section(args)
     if "level0" in sections:
-        line["fp64_level0_j_only"] = fp64_level0_j_only(stream)
+        line["level0_j_only"] = {"fp64": level0_j_only(stream, api.PRECISION_FP64), "mixed": level0_j_only(stream, api.PRECISION_MIXED),
+                                 "note": "the reference's own workload (J only, fixed level 0, qf3D13, its three classes); "
+                                         "--impl reference times the reference's CUDA build on it (reference_cuda)"}
     if "adjoint" in sections:
         line["adjoint"] = adjoint_section(args)
     if "batch" in forms:
@@ -890,6 +947,8 @@ def main():
     ap.add_argument("--cpu-fraction", type=float, default=1.0,
                     help="cpu_baseline leg of the GPU arm: share of every class (1 = every pair, about 2.5 s on 16 cores)")
     ap.add_argument("--fd-coords", type=int, default=200, help="adjoint section: coordinates checked by finite differences")
+    ap.add_argument("--c5-backward-fraction", type=float, default=0.05,
+                    help="c5 section: share of every class's pairs the timed backward pass covers (1 = all 194 M pairs, minutes)")
     ap.add_argument("--forms", default="fp64,mixed,batch",
                     help="forms to run: fp64, mixed (per-class chains), batch (headline when present)")
     ap.add_argument("--sections", default="uneven,c5,adjoint,level0",

@@ -157,16 +157,23 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
                                   int kmax, long long first, long long stride, int G_cap)
 {
     const int nsub = 1 << (2 * level);
-    // lanes per pair: up to a warp (G_cap), or the whole block once a pair has at least a block's
-    // worth of sub-cells (levels 4 and 5, where only a few pairs remain and one warp per pair left
-    // each lane hundreds of points in series).  first and stride are thread-linear and the item
-    // count is then a multiple of the block, so every block runs the loop uniformly and the
-    // __syncthreads of the block-wide reduction below is reached by all its threads.
-    const bool block_group = blockDim.x > 32 && nsub >= (int)blockDim.x;
-    const int G = block_group ? (int)blockDim.x : (nsub < G_cap ? nsub : G_cap);
-    const int per_lane = nsub / G;
     const bool listed = Lst.act_in != nullptr;
     const int count = listed ? *Lst.cnt_in : A.n;
+    // lanes per pair: the fewest (a power of two, at most a warp: G_cap) that still give the grid
+    // about two work items per thread -- at levels 1-2 the active pairs alone outnumber the
+    // threads, and each extra lane repeats the pair's set-up (some twenty panel loads) and a
+    // butterfly step for its 13 points; or the whole block once a pair has at least a block's
+    // worth of sub-cells (levels 4 and 5, where only a few pairs remain and one warp per pair left
+    // each lane hundreds of points in series).  count is the same for every thread, so G is
+    // uniform.  first and stride are thread-linear and the item count is then a multiple of the
+    // block, so every block runs the loop uniformly and the __syncthreads of the block-wide
+    // reduction below is reached by all its threads.
+    const bool block_group = blockDim.x > 32 && nsub >= (int)blockDim.x;
+    int G = 1;
+    if (block_group) G = (int)blockDim.x;
+    else
+        while (G < G_cap && G < nsub && (long long)count * G < 2 * stride) G <<= 1;
+    const int per_lane = nsub / G;
     const long long total = (long long)count * G;
     const long long total_r = block_group ? total : (total + 31) & ~31LL;
     const float sub_scale = ldexpf(1.0f, -2 * level);

@@ -57,6 +57,49 @@ def icosphere(subdivisions: int, radius: float = 1.0) -> Mesh:
     return radius * v, f
 
 
+def geodesic_sphere(freq: int, radius: float = 1.0) -> Mesh:
+    """Class-I geodesic sphere: every icosahedron face split into freq^2 triangles on a
+    barycentric grid, projected to the sphere; 20 freq^2 cells, 10 freq^2 + 2 vertices, any
+    freq >= 1 (the 1->4 icospheres are freq = 2^s).  A grid point a + i (b - a) / n + j (c - a) / n
+    is keyed by its integer barycentric weights on the icosahedron's vertices, so points on an edge
+    or corner shared by two faces are one vertex."""
+    v0, f0 = icosahedron()
+    n = int(freq)
+    if n < 1:
+        raise ValueError("freq must be >= 1")
+    index, verts, cells = {}, [], []
+
+    def vid(face, i, j):
+        w = {face[0]: n - i - j, face[1]: i, face[2]: j}
+        key = tuple(sorted((int(k), int(c)) for k, c in w.items() if c))
+        if key not in index:
+            p = sum(c * v0[k] for k, c in key) / n
+            index[key] = len(verts)
+            verts.append(p / np.linalg.norm(p))
+        return index[key]
+
+    for face in f0:
+        for i in range(n):
+            for j in range(n - i):
+                cells.append((vid(face, i, j), vid(face, i + 1, j), vid(face, i, j + 1)))
+                if i + j < n - 1:
+                    cells.append((vid(face, i + 1, j), vid(face, i + 1, j + 1), vid(face, i, j + 1)))
+    return radius * np.asarray(verts), np.asarray(cells, np.int32)
+
+
+def tangential_jitter(v: np.ndarray, f: np.ndarray, sigma_rel: float, seed: int) -> np.ndarray:
+    """vertices of a sphere mesh moved by a seeded Gaussian tangential jitter of sigma_rel x the
+    mean edge length and reprojected to the sphere's radius"""
+    r = np.linalg.norm(v, axis=1, keepdims=True)
+    u = v / r
+    h = mean_edge_length(u, f)
+    rng = np.random.default_rng(seed)
+    d = rng.normal(0.0, sigma_rel * h, size=v.shape)
+    d -= np.sum(d * u, axis=1, keepdims=True) * u
+    w = u + d
+    return r * (w / np.linalg.norm(w, axis=1, keepdims=True))
+
+
 def edge_lengths(v: np.ndarray, f: np.ndarray) -> np.ndarray:
     e = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]])
     e = np.unique(np.sort(e, axis=1), axis=0)
@@ -156,30 +199,36 @@ def ellipsoid(n_theta: int, n_phi: int, axes=(1.0, 1.0, 1.0), scale: float = 1.0
 
 def uneven_mesh_set(seed: int, count: int = 48, tri_min: int = 500, tri_max: int = 60000):
     """A seeded set of independent closed meshes of uneven size and scale (a many-mesh batch
-    workload): ellipsoids with semi-axes uniform in [0.3, 3] (stretched icospheres), tori with R/r
-    uniform in [2, 6] and jittered icospheres, in turn; triangle counts log-uniform in
-    [tri_min, tri_max] (the nearest grid or subdivision level); scales uniform in [5e-4, 1e2].
+    workload): ellipsoids with semi-axes uniform in [0.3, 3] (stretched geodesic spheres), tori
+    with R/r uniform in [2, 6] and jittered geodesic spheres (sigma 0.15 h), in turn; triangle
+    counts log-uniform in [tri_min, tri_max] (the nearest grid size inside that range: 20 n^2 for
+    the spheres, 2 n_major n_minor for the tori); scales uniform in [5e-4, 1e2].
     Returns [(V, C, kind, scale)]."""
     rng = np.random.default_rng(seed)
     out = []
+    f_lo, f_hi = math.ceil(math.sqrt(tri_min / 20.0)), math.floor(math.sqrt(tri_max / 20.0))
     for k in range(count):
         target = float(np.exp(rng.uniform(np.log(tri_min), np.log(tri_max))))
         scale = float(rng.uniform(5e-4, 1e2))
         kind = ("ellipsoid", "torus", "icosphere")[k % 3]
+        freq = int(np.clip(round(math.sqrt(target / 20.0)), f_lo, f_hi))
         if kind == "ellipsoid":
-            # an icosphere stretched along its axes (a latitude-longitude grid would add pole fans
-            # of needle triangles)
+            # a stretched geodesic sphere (a latitude-longitude grid would add pole fans of needles)
             axes = rng.uniform(0.3, 3.0, size=3)
-            sub = int(np.clip(round(np.log(target / 20.0) / np.log(4.0)), 1, 6))
-            V, C = icosphere(sub, 1.0)
+            V, C = geodesic_sphere(freq, 1.0)
             V = scale * V * axes
         elif kind == "torus":
             ratio = rng.uniform(2.0, 6.0)
-            n_minor = max(4, int(round(np.sqrt(target / (2.0 * ratio)))))
+            n_minor = max(4, int(round(math.sqrt(target / (2.0 * ratio)))))
+            cells = lambda m: 2 * int(round(ratio * m)) * m
+            while cells(n_minor) > tri_max:
+                n_minor -= 1
+            while cells(n_minor) < tri_min:
+                n_minor += 1
             V, C = torus(int(round(ratio * n_minor)), n_minor, 1.0, 1.0 / ratio, scale)
         else:
-            sub = int(np.clip(round(np.log(target / 20.0) / np.log(4.0)), 1, 6))
-            V, C = jittered_icosphere(sub, 0.15, int(rng.integers(1 << 30)), scale)
+            V, C = geodesic_sphere(freq, 1.0)
+            V = scale * tangential_jitter(V, C, 0.15, int(rng.integers(1 << 30)))
         out.append((V, C.astype(np.int32), kind, scale))
     return out
 

@@ -164,6 +164,12 @@ def test_uneven_mesh_set_and_scale_invariance(api):
             ev.runClass(cls, pl.by_class(cls))
             out[cls] = (ev.getResults(cls), ev.getPotentials(cls), ev.getLevels(cls))
         res.append(out)
+    # 5e-4 is not a power of two, so the closed forms' power-of-two normalisation rounds the two
+    # copies differently: the per-pair bar is 1e-9, or 1e-12 x kappa for ill-conditioned pairs
+    # (kappa = the pair's relative sensitivity at unit scale; one common-vertex pair of this mesh
+    # has 3.6e4)
+    from oracle import oracle as O
+    Vu, Cu = mset[-2][0], mset[-2][1]
     for cls in (0, 1, 2, 3):
         (Ja, Pa, La), (Jb, Pb, Lb) = res[0][cls], res[1][cls]
         same = La == Lb
@@ -171,7 +177,9 @@ def test_uneven_mesh_set_and_scale_invariance(api):
         if cls == 3:
             assert np.abs(Jb / 5e-4 ** 2 - Ja).max() <= 1e-12 * max(1.0, np.abs(Ja).max())
         else:
-            assert rel_rows(Jb[same] / 5e-4 ** 2, Ja[same]).max() < 1e-9, cls
+            kap = O.conditioning(cls, P.build_pairs(Vu, Cu).by_class(cls)[same], Vu, Cu)
+            bar = np.maximum(1e-9, 1e-12 * kap)
+            assert np.all(rel_rows(Jb[same] / 5e-4 ** 2, Ja[same]) < bar), cls
         assert (np.abs(Pb[same] / 5e-4 ** 3 - Pa[same]) / np.abs(Pa[same])).max() < 1e-9, cls
 
 
