@@ -64,7 +64,10 @@ typedef enum i2_pair_class {
 typedef enum i2_error_control {
     I2_FIXED_REFINEMENT_LEVEL = 0,
     I2_AUTOMATIC_ERROR_CONTROL = 1,  /* the reference's Runge loop, including its buffer parity */
-    I2_RELATIVE_ERROR_CONTROL = 2    /* scale-invariant: |J_L - J_{L-1}| <= tol |J_L| */
+    I2_RELATIVE_ERROR_CONTROL = 2    /* scale-invariant: level L is kept once |J_L - J_{L-1}| <= 4 tol |J_L|
+                                        (and |P_L - P_{L-1}| <= 4 tol |P_L| for disjoint pairs): the
+                                        difference divided by 4, a Runge estimate of J_L's error
+                                        (the 13-point rule's errors fall about 256-fold a level) */
 } i2_error_control;
 
 typedef enum i2_precision { I2_PRECISION_FP64 = 0, I2_PRECISION_MIXED = 1 } i2_precision;

@@ -13,7 +13,10 @@
 #include "i2_batch.cuh"
 #include "i2_engine.h"
 #include "i2_finalize.cuh"
+#include "i2_self.cuh"
 #include "i2_tiers.cuh"
+
+#include <cooperative_groups.h>
 
 namespace i2 {
 
@@ -171,8 +174,9 @@ __global__ void __launch_bounds__(128) k_level(ClassArgs A, QuadTables Q, int le
             }
             const d3 Jc = finalize_j(CLS, mk(acc.px, acc.py, acc.pz) + spsi, acc.th + sth, nj, Si);
             const d3 dJ = kInv4Pi * ((acc.th - prev.th) * nj + cross(mk(acc.px - prev.px, acc.py - prev.py, acc.pz - prev.pz), nj));
-            unconv = norm(dJ) > tol * norm(Jc);
-            if (CLS == kFar) unconv = unconv || fabs(acc.pot - prev.pot) > tol * fabs(acc.pot);
+            const double bound = kRelativeRunge * tol;
+            unconv = norm(dJ) > bound * norm(Jc);
+            if (CLS == kFar) unconv = unconv || fabs(acc.pot - prev.pot) > bound * fabs(acc.pot);
         }
         atomicMax(A.maxlev, level);
         if (!unconv || level >= kmax) {
@@ -511,47 +515,7 @@ static void pot_adaptive_chain(const ClassArgs &A, const QuadTables &Q, double t
         k_pot_depth<CLS><<<grid, 128, 0, s>>>(A, Q, tol, d, d % 2 ? A.pot_q_a : A.pot_q_b, d % 2 ? A.pot_q_b : A.pot_q_a);
     k_pot_final<CLS><<<persistent_blocks, 128, 0, s>>>(A, tol);
 }
-// ------------------------------------------------------------------ self pairs
-// J(K_i, K_i) by the chosen convention, potential by self_potential (i2_rules.cuh)
-// eight lanes per pair: lanes 0..5 take one (edge, piece) of the self-pair rule each, the group
-// sums them (an edge's pieces are integrated independently, so the pair's 6 x nself point
-// evaluations run in parallel)
-// Self pairs, five to a warp: lanes 6k .. 6k+5 (k < 5) take the six (edge, piece) integrals of
-// one pair, the first of the six writes the pair's outputs, lanes 30 and 31 idle (groups of eight
-// lanes left two of every eight idle).
-constexpr int kSelfPairsPerWarp = 5;
-
-// lane g (0..5) of a pair's group: one (edge, piece) of the edge rule, or, for the closed form
-// (Q.nself == 0), the whole value on lane 0
-__device__ __forceinline__ double self_piece_of(const ClassArgs &A, const QuadTables &Q, long long t, int g)
-{
-    const PanelJ K = load_panel(A.panels, A.pairs[t].x);
-    const d3 P[3] = {K.A, K.B, K.C};
-    if (Q.nself == 0) return g == 0 ? self_potential_closed(P) : 0.0;
-    return self_potential_piece(P, g >> 1, g & 1, Q);
-}
-
-// the parts of a lane's six-lane group, added in a fixed order (every lane of the warp calls it)
-__device__ __forceinline__ double self_gather6(double part)
-{
-    const int lane = threadIdx.x & 31, base = lane - lane % 6;
-    double sum = 0.0;
-    for (int k = 0; k < 6; ++k) sum += __shfl_sync(0xffffffffu, part, (base + k) & 31);
-    return sum;
-}
-
-__device__ __forceinline__ void self_store(const ClassArgs &A, int self_sign, long long t, double part)
-{
-    const PanelJ K = load_panel(A.panels, A.pairs[t].x);
-    const double th = self_sign == 0 ? 0.0 : (self_sign > 0 ? kTwoPi : -kTwoPi) * K.S;
-    const d3 J = kInv4Pi * (th * K.n);
-    double *raw = A.raw4 + 4 * t;
-    raw[0] = 0.0; raw[1] = 0.0; raw[2] = 0.0; raw[3] = th;
-    double *Jo = A.J3 + 3 * t;
-    Jo[0] = J.x; Jo[1] = J.y; Jo[2] = J.z;
-    A.P[t] = kInv4Pi * part;
-}
-
+// ------------------------------------------------------------------ self pairs (helpers: i2_self.cuh)
 __global__ void __launch_bounds__(128) k_self(ClassArgs A, QuadTables Q, int self_sign)
 {
     const int lane = threadIdx.x & 31, k = lane / 6;
@@ -617,29 +581,90 @@ __global__ void __launch_bounds__(128) k_batch_pot_final(const BatchSeg *__restr
     }
 }
 
-__global__ void __launch_bounds__(128) k_batch_self(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q, int self_sign)
+// ------------------------------------------------------------------ batched hard-pair potential, one launch
+// Tier 2b of the adjacent pairs' potential, the adaptive rule's seed, its twelve depths and the
+// final sums of every segment in ONE cooperative launch: the stages run in turn over the whole
+// grid with a grid-wide barrier between them (each stage's item counts are device counters the
+// stage before wrote), in place of fifteen launches.  The grid is exactly the resident blocks.
+__device__ __forceinline__ void batch_tier2b_stage(const BatchSeg *__restrict__ segs, int nseg, const QuadTables &Q, long long *prefix)
 {
-    extern __shared__ long long prefix[];
     const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
-        return S.cls == kSelf && S.A.n > 0 ? S.A.n : 0;
+        return seg_adjacent(S) && S.A.hard_list ? S.A.cnt[kCntTier2b] : 0;
     });
-    // five pairs to a warp (as k_self); the loop is uniform over the warp
-    const int lane = threadIdx.x & 31, k = lane / 6;
+    const int lane = threadIdx.x & 31;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * kSelfPairsPerWarp < total; w += nwarps) {
-        const long long g = w * kSelfPairsPerWarp + k;
-        const bool valid = k < kSelfPairsPerWarp && g < total;
-        int sg = 0;
-        long long t = 0;
-        double part = 0.0;
-        if (valid) {
-            sg = seg_find(prefix, nseg, g);
-            t = g - prefix[sg];
-            part = self_piece_of(segs[sg].A, Q, t, lane % 6);
-        }
-        const double sum = self_gather6(part);
-        if (valid && lane % 6 == 0) self_store(segs[sg].A, self_sign, t, sum);
+    for (long long g = warp_item_index(); g < total; g += nwarps) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        if (S.cls == kEdge) tier2b_item<kEdge>(S.A, Q, false, (int)(g - prefix[sg]), lane);
+        else tier2b_item<kVertex>(S.A, Q, false, (int)(g - prefix[sg]), lane);
     }
+}
+
+__device__ __forceinline__ void batch_pot_seed_stage(const BatchSeg *__restrict__ segs, int nseg, const QuadTables &Q, double tol, long long *prefix)
+{
+    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
+        return seg_adjacent(S) && S.A.hard_list ? pot_seeded(S.A) : 0;
+    });
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid < nseg && seg_adjacent(segs[gid]) && segs[gid].A.hard_list) pot_seed_init(segs[gid].A);
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long g = warp_item_index(); g < total; g += nwarps) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        const int h = (int)(g - prefix[sg]);
+        if (S.cls == kEdge) pot_seed_item<kEdge>(S.A, Q, tol, h, lane);
+        else pot_seed_item<kVertex>(S.A, Q, tol, h, lane);
+    }
+}
+
+__device__ __forceinline__ void batch_pot_depth_stage(const BatchSeg *__restrict__ segs, int nseg, const QuadTables &Q, double tol, int depth,
+                                                      long long *prefix)
+{
+    const long long total = seg_prefix(segs, nseg, prefix, [depth](const BatchSeg &S) -> long long {
+        return seg_adjacent(S) && S.A.hard_list ? pot_depth_count(S.A, depth) : 0;
+    });
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long g = warp_item_index(); g < total; g += nwarps) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        const int idx = (int)(g - prefix[sg]);
+        const PotCellItem *in = depth % 2 ? S.A.pot_q_a : S.A.pot_q_b;
+        PotCellItem *out = depth % 2 ? S.A.pot_q_b : S.A.pot_q_a;
+        if (S.cls == kEdge) pot_depth_item<kEdge>(S.A, Q, tol, depth, in, out, idx, lane);
+        else pot_depth_item<kVertex>(S.A, Q, tol, depth, in, out, idx, lane);
+    }
+}
+
+__device__ __forceinline__ void batch_pot_final_stage(const BatchSeg *__restrict__ segs, int nseg, double tol, long long *prefix)
+{
+    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
+        return seg_adjacent(S) && S.A.hard_list ? pot_seeded(S.A) : 0;
+    });
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        if (S.cls == kEdge) pot_final_item<kEdge>(S.A, tol, (int)(g - prefix[sg]));
+        else pot_final_item<kVertex>(S.A, tol, (int)(g - prefix[sg]));
+    }
+}
+
+__global__ void __launch_bounds__(128, 3) k_batch_hard_chain(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q, double tol)
+{
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    extern __shared__ long long prefix[];
+    batch_tier2b_stage(segs, nseg, Q, prefix);
+    grid.sync();
+    batch_pot_seed_stage(segs, nseg, Q, tol, prefix);
+    grid.sync();
+    for (int d = 1; d <= kHardMaxDepth; ++d) {
+        batch_pot_depth_stage(segs, nseg, Q, tol, d, prefix);
+        grid.sync();
+    }
+    batch_pot_final_stage(segs, nseg, tol, prefix);
 }
 
 // ------------------------------------------------------------------ finalisation
@@ -733,15 +758,20 @@ void launch_batch_pot_chain(const BatchSeg *segs, int nseg, const QuadTables &Q,
     }
 }
 
-void launch_batch_self(const BatchSeg *segs, int nseg, long long self_pairs, const QuadTables &Q, const RunConfig &cfg, cudaStream_t s)
+// tier 2b and the adaptive potential of every segment as one cooperative launch (one chunk of
+// segments); false when the launch is not possible (the caller then runs the stages one by one)
+bool launch_batch_hard_chain(const BatchSeg *segs, int nseg, const QuadTables &Q, double tol, cudaStream_t s)
 {
-    if (self_pairs <= 0) return;
-    const long long warps = (self_pairs + kSelfPairsPerWarp - 1) / kSelfPairsPerWarp;
-    const int blocks = std::max(1, std::min(blocks_for(32 * warps, 128), 1 << 16));
-    for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
-        const int nc = std::min(kBatchSegChunk, nseg - c0);
-        k_batch_self<<<blocks, 128, seg_smem(nc), s>>>(segs + c0, nc, Q, cfg.self_sign);
-    }
+    if (nseg > kBatchSegChunk) return false;
+    const size_t smem = (size_t)(nseg + 1) * sizeof(long long);
+    int dev = 0, sms = 0, nb = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)k_batch_hard_chain, 128, smem) != cudaSuccess || nb <= 0)
+        return false;
+    QuadTables q = Q;
+    double t = tol;
+    void *args[] = {(void *)&segs, (void *)&nseg, (void *)&q, (void *)&t};
+    return cudaLaunchCooperativeKernel((const void *)k_batch_hard_chain, dim3(sms * nb), dim3(128), args, smem, s) == cudaSuccess;
 }
 
 void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s)

@@ -12,6 +12,7 @@
 #include "i2_batch.cuh"
 #include "i2_engine.h"
 #include "i2_finalize.cuh"
+#include "i2_self.cuh"
 #include "i2_tiers.cuh"
 
 #include <cooperative_groups.h>
@@ -355,7 +356,7 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
         const f3 Jf = (float)th_tot * nf + crossf(psif, nf);
         const f3 dpsif = f3{(float)(acc.px - prev.px), (float)(acc.py - prev.py), (float)(acc.pz - prev.pz)};
         const f3 dJf = (float)(acc.th - prev.th) * nf + crossf(dpsif, nf);
-        const float tolf = (float)tol;
+        const float tolf = (float)(kRelativeRunge * tol);
         bool unconv;
         if (mode == kAdaptiveCompat) {
             unconv = runge_unconverged(acc, prev, Qf.pow2p);
@@ -724,8 +725,9 @@ __device__ __forceinline__ bool fixup_unconverged(const acc5 &nxt, const acc5 &p
 {
     const d3 Jc = finalize_j(CLS, mk(nxt.px, nxt.py, nxt.pz) + spsi, nxt.th + sth, nj, p.Si);
     const d3 dJ = kInv4Pi * ((nxt.th - prev.th) * nj + cross(mk(nxt.px - prev.px, nxt.py - prev.py, nxt.pz - prev.pz), nj));
-    bool unconv = norm(dJ) > tol * norm(Jc);
-    if (CLS == kFar) unconv = unconv || fabs(nxt.pot - prev.pot) > tol * fabs(nxt.pot);
+    const double bound = kRelativeRunge * tol;
+    bool unconv = norm(dJ) > bound * norm(Jc);
+    if (CLS == kFar) unconv = unconv || fabs(nxt.pot - prev.pot) > bound * fabs(nxt.pot);
     return unconv;
 }
 
@@ -759,14 +761,14 @@ __device__ __forceinline__ int fixup_kept_level(const ClassArgs &A, int mode, in
 // Levels deeper than kFixDirect are spread over the GPU: the block that owns a pair stops after
 // level kFixDirect, lists the pair (up to ClassArgs::fix_cap pairs; later ones stay in the block)
 // with its last sums, and k_fix_spread integrates levels kFixDirect+1..5 in chunks of kFixChunk
-// sub-cells, one block per chunk; k_fix_finish adds the chunks in order and decides.  A needle pair
-// refined to level 5 is 17.7 MFLOP of FP64, about 2 ms on one SM, which otherwise sets the length
-// of the whole pass.
+// sub-cells, one block per chunk (one sub-cell a thread: 1,024 threads over a level-5 pair);
+// k_fix_finish adds the chunks in order and decides.  A needle pair refined to level 5 is
+// 17.7 MFLOP of FP64, about 2 ms on one SM, which otherwise sets the length of the whole pass.
 constexpr int kFixDirect = 3;
-constexpr int kFixChunk = 64;
-constexpr int kFixSlots = kFixDeepSlots;  // chunks of levels 4 and 5: 4 + 16
-static_assert(kFixSlots == 4 + 16 && kFixChunk * 4 == 256, "chunk layout of levels 4 and 5");
-__device__ __forceinline__ int fix_slot0(int L) { return L == 4 ? 0 : 4; }
+constexpr int kFixChunk = 256;
+constexpr int kFixSlots = kFixDeepSlots;  // chunks of levels 4 and 5: 1 + 4
+static_assert(kFixSlots == 1 + 4 && kFixChunk == 256, "chunk layout of levels 4 and 5");
+__device__ __forceinline__ int fix_slot0(int L) { return L == 4 ? 0 : 1; }
 __device__ __forceinline__ int fix_chunks(int L) { return (1 << (2 * L)) / kFixChunk; }
 
 // pair t, by the whole block (red: 5 doubles per warp of shared memory)
@@ -1123,17 +1125,16 @@ cudaError_t launch_batch_levels(const BatchSeg *segs, int nseg, const bool prese
 // The stages that precede and follow the level sweep, each as one launch over every segment of
 // the batch (flattened walks of i2_batch.cuh): counter reset, tier 1 with the singular parts,
 // tiers 2 / 2b, the adaptive potential (i2_kernels_fp64.cu), self pairs, and the FP64 fix-up.
-__global__ void k_batch_reset(const BatchSeg *__restrict__ segs, int nseg)
-{
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nseg || segs[s].A.n <= 0) return;
-    for (int k = 0; k < 16; ++k) segs[s].A.cnt[k] = 0;
-    *segs[s].A.maxlev = 0;
-}
-
+// the closed forms of every adjacent pair; before them, thread s clears segment s's counters (the
+// stages that count into them run in later launches; the grid has at least one thread a segment)
 __global__ void __launch_bounds__(128) k_batch_singular(const BatchSeg *__restrict__ segs, int nseg, QuadTablesF Qf)
 {
     extern __shared__ long long prefix[];
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid < nseg && segs[gid].A.n > 0) {
+        for (int k = 0; k < 16; ++k) segs[gid].A.cnt[k] = 0;
+        *segs[gid].A.maxlev = 0;
+    }
     const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long { return seg_adjacent(S) ? S.A.n : 0; });
     for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
         const int sg = seg_find(prefix, nseg, g);
@@ -1143,20 +1144,48 @@ __global__ void __launch_bounds__(128) k_batch_singular(const BatchSeg *__restri
     }
 }
 
-__global__ void __launch_bounds__(128) k_batch_tier1(const BatchSeg *__restrict__ segs, int nseg, QuadTablesF Qf)
+// tier 1 of the adjacent pairs' potential (eight lanes a pair) and the self pairs (five to a warp,
+// six lanes each) in one launch: global warps [0, w1) take the tier-1 items, warps [w1, w1 + w2)
+// the self pairs, so every branch below is uniform over a warp.  prefix holds two prefix-sum
+// arrays (tier-1 items, self pairs) of nseg + 1 entries each.
+__global__ void __launch_bounds__(128) k_batch_tier1_self(const BatchSeg *__restrict__ segs, int nseg, QuadTablesF Qf, QuadTables Q,
+                                                          int self_sign)
 {
     extern __shared__ long long prefix[];
-    // eight items per pair (as k_batch_self): every count is a multiple of 8, and so is the grid's
-    // thread count, so a pair's items land in one aligned group of eight lanes
-    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
+    long long *p1 = prefix, *ps = prefix + nseg + 1;
+    const long long t1 = seg_prefix(segs, nseg, p1, [](const BatchSeg &S) -> long long {
         return seg_adjacent(S) ? (long long)kTier1Lanes * S.A.n : 0;
     });
-    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
-        const int sg = seg_find(prefix, nseg, g);
-        const BatchSeg &S = segs[sg];
-        const long long loc = g - prefix[sg];
-        if (S.cls == kEdge) tier1_mixed_item<kEdge>(S.A, Qf, loc / kTier1Lanes, (int)(loc % kTier1Lanes));
-        else tier1_mixed_item<kVertex>(S.A, Qf, loc / kTier1Lanes, (int)(loc % kTier1Lanes));
+    const long long ts = seg_prefix(segs, nseg, ps, [](const BatchSeg &S) -> long long { return S.cls == kSelf && S.A.n > 0 ? S.A.n : 0; });
+    const long long w1 = (t1 + 31) >> 5, w2 = (ts + kSelfPairsPerWarp - 1) / kSelfPairsPerWarp;
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < w1 + w2; w += nwarps) {
+        if (w < w1) {
+            // a pair's eight items are one aligned group of eight lanes (every count is a multiple of 8)
+            const long long g = w * 32 + lane;
+            if (g < t1) {
+                const int sg = seg_find(p1, nseg, g);
+                const BatchSeg &S = segs[sg];
+                const long long loc = g - p1[sg];
+                if (S.cls == kEdge) tier1_mixed_item<kEdge>(S.A, Qf, loc / kTier1Lanes, (int)(loc % kTier1Lanes));
+                else tier1_mixed_item<kVertex>(S.A, Qf, loc / kTier1Lanes, (int)(loc % kTier1Lanes));
+            }
+        } else {
+            const int k = lane / 6;
+            const long long g = (w - w1) * kSelfPairsPerWarp + k;
+            const bool valid = k < kSelfPairsPerWarp && g < ts;
+            int sg = 0;
+            long long t = 0;
+            double part = 0.0;
+            if (valid) {
+                sg = seg_find(ps, nseg, g);
+                t = g - ps[sg];
+                part = self_piece_of(segs[sg].A, Q, t, lane % 6);
+            }
+            const double sum = self_gather6(part);
+            if (valid && lane % 6 == 0) self_store(segs[sg].A, self_sign, t, sum);
+        }
     }
 }
 
@@ -1261,32 +1290,108 @@ __global__ void __launch_bounds__(128) k_batch_fix_finish(const BatchSeg *__rest
     }
 }
 
+// The four fix-up stages of every segment in ONE cooperative launch (256 threads a block, the
+// grid exactly the resident blocks): gather the needle pairs; recompute them in FP64, a block per
+// pair, up to level kFixDirect; their levels 4-5 in chunks of kFixChunk sub-cells, a block per
+// chunk; add the chunks in order and decide -- with a grid-wide barrier between the stages.
+__global__ void __launch_bounds__(256) k_batch_fixup_chain(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q, int mode,
+                                                           int fixed_level, double tol, int kmax)
+{
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    extern __shared__ long long prefix[];
+    __shared__ double red[5 * 8];
+    long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long { return seg_fixup(S) ? S.A.n : 0; });
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+        const int sg = seg_find(prefix, nseg, g);
+        const ClassArgs &A = segs[sg].A;
+        if (segs[sg].cls == kFar) fixup_collect_item<kFar>(A, A.act_a, A.cnt + kCntFixup, g - prefix[sg]);
+        else fixup_collect_item<kEdge>(A, A.act_a, A.cnt + kCntFixup, g - prefix[sg]);
+    }
+    grid.sync();
+    total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long { return seg_fixup(S) ? S.A.cnt[kCntFixup] : 0; });
+    for (long long g = blockIdx.x; g < total; g += gridDim.x) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        const int t = S.A.act_a[g - prefix[sg]];
+        if (S.cls == kFar) fp64_fixup_item<kFar>(S.A, Q, mode, fixed_level, tol, kmax, t, red);
+        else if (S.cls == kEdge) fp64_fixup_item<kEdge>(S.A, Q, mode, fixed_level, tol, kmax, t, red);
+        else fp64_fixup_item<kVertex>(S.A, Q, mode, fixed_level, tol, kmax, t, red);
+    }
+    grid.sync();
+    total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
+        return seg_fixup(S) && S.A.fix_deep ? (long long)min(S.A.cnt[kCntFixDeep], S.A.fix_cap) * kFixSlots : 0;
+    });
+    for (long long g = blockIdx.x; g < total; g += gridDim.x) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        const long long q = g - prefix[sg];
+        const int k = (int)(q / kFixSlots), slot = (int)(q % kFixSlots);
+        if (S.cls == kFar) fix_spread_item<kFar>(S.A, Q, mode, fixed_level, kmax, k, slot, red);
+        else if (S.cls == kEdge) fix_spread_item<kEdge>(S.A, Q, mode, fixed_level, kmax, k, slot, red);
+        else fix_spread_item<kVertex>(S.A, Q, mode, fixed_level, kmax, k, slot, red);
+    }
+    grid.sync();
+    total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
+        return seg_fixup(S) && S.A.fix_deep ? min(S.A.cnt[kCntFixDeep], S.A.fix_cap) : 0;
+    });
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+        const int sg = seg_find(prefix, nseg, g);
+        const BatchSeg &S = segs[sg];
+        const int k = (int)(g - prefix[sg]);
+        if (S.cls == kFar) fix_finish_item<kFar>(S.A, mode, fixed_level, tol, kmax, k);
+        else if (S.cls == kEdge) fix_finish_item<kEdge>(S.A, mode, fixed_level, tol, kmax, k);
+        else fix_finish_item<kVertex>(S.A, mode, fixed_level, tol, kmax, k);
+    }
+}
+
 static size_t seg_smem(int nseg) { return (size_t)(nseg + 1) * sizeof(long long); }
+
+// k_batch_fixup_chain for one chunk of segments; false when the batch has more chunks or the
+// cooperative launch was refused
+static bool launch_batch_fixup_chain(const BatchSeg *segs, int nseg, const QuadTables &Q, const RunConfig &cfg, cudaStream_t s)
+{
+    if (nseg > kBatchSegChunk) return false;
+    const size_t smem = seg_smem(nseg);
+    int dev = 0, sms = 0, nb = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)k_batch_fixup_chain, 256, smem) != cudaSuccess || nb <= 0)
+        return false;
+    QuadTables q = Q;
+    int mode = cfg.mode, level = cfg.level, kmax = cfg.max_level;
+    double tol = cfg.tol;
+    void *args[] = {(void *)&segs, (void *)&nseg, (void *)&q, (void *)&mode, (void *)&level, (void *)&tol, (void *)&kmax};
+    return cudaLaunchCooperativeKernel((const void *)k_batch_fixup_chain, dim3(sms * nb), dim3(256), args, smem, s) == cudaSuccess;
+}
 
 void launch_batch_prelude(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTables &Q, const QuadTablesF &Qf,
                           const RunConfig &cfg, int persistent_blocks, cudaStream_t s)
 {
     const int tpb = 128;
+    // closed forms, with the counter reset in front (always launched: the reset is needed by
+    // every segment), then tier 1 with the self pairs
     for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
         const int nc = std::min(kBatchSegChunk, nseg - c0);
-        k_batch_reset<<<blocks_for_m(nc, 128), 128, 0, s>>>(segs + c0, nc);
+        const int blocks = std::max(blocks_for_m(nc, tpb), std::min(blocks_for_m(tot.adjacent_pairs, tpb), 1 << 16));
+        k_batch_singular<<<std::max(1, blocks), tpb, seg_smem(nc), s>>>(segs + c0, nc, Qf);
     }
-    if (tot.adjacent_pairs > 0) {
-        const int blocks = std::max(1, std::min(blocks_for_m(tot.adjacent_pairs, tpb), 1 << 16));
+    const long long warps = (kTier1Lanes * tot.adjacent_pairs + 31) / 32 + (tot.self_pairs + kSelfPairsPerWarp - 1) / kSelfPairsPerWarp;
+    if (warps > 0) {
+        const int blocks = (int)std::max(1LL, std::min((warps * 32 + tpb - 1) / tpb, 1LL << 16));
         for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
             const int nc = std::min(kBatchSegChunk, nseg - c0);
-            k_batch_singular<<<blocks, tpb, seg_smem(nc), s>>>(segs + c0, nc, Qf);
+            k_batch_tier1_self<<<blocks, tpb, 2 * seg_smem(nc), s>>>(segs + c0, nc, Qf, Q, cfg.self_sign);
         }
-        const int blocks8 = std::max(1, std::min(blocks_for_m((long long)kTier1Lanes * tot.adjacent_pairs, tpb), 1 << 16));
+    }
+    if (tot.adjacent_pairs > 0 && tot.hard_lists) {
         for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
             const int nc = std::min(kBatchSegChunk, nseg - c0);
-            k_batch_tier1<<<blocks8, tpb, seg_smem(nc), s>>>(segs + c0, nc, Qf);
+            k_batch_tier2<<<resident_grid((const void *)k_batch_tier2, tpb, seg_smem(nc)), tpb, seg_smem(nc), s>>>(segs + c0, nc, Qf, Q);
         }
-        if (tot.hard_lists) {
-            for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
-                const int nc = std::min(kBatchSegChunk, nseg - c0);
-                k_batch_tier2<<<resident_grid((const void *)k_batch_tier2, tpb, seg_smem(nc)), tpb, seg_smem(nc), s>>>(segs + c0, nc, Qf, Q);
-            }
+        // tier 2b and the adaptive potential: one cooperative launch for a single chunk of
+        // segments, else stage by stage
+        if (!launch_batch_hard_chain(segs, nseg, Q, cfg.hard_tol, s)) {
+            cudaGetLastError();  // a refused cooperative launch leaves no work queued
             for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
                 const int nc = std::min(kBatchSegChunk, nseg - c0);
                 k_batch_tier2b<<<resident_grid((const void *)k_batch_tier2b, tpb, seg_smem(nc)), tpb, seg_smem(nc), s>>>(segs + c0, nc, Q);
@@ -1294,13 +1399,14 @@ void launch_batch_prelude(const BatchSeg *segs, int nseg, const BatchTotals &tot
             launch_batch_pot_chain(segs, nseg, Q, cfg.hard_tol, persistent_blocks, s);
         }
     }
-    launch_batch_self(segs, nseg, tot.self_pairs, Q, cfg, s);
 }
 
 void launch_batch_fixup(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTables &Q, const RunConfig &cfg,
                         int persistent_blocks, cudaStream_t s)
 {
     if (tot.fixup_pairs <= 0) return;
+    if (launch_batch_fixup_chain(segs, nseg, Q, cfg, s)) return;
+    cudaGetLastError();  // a refused cooperative launch leaves no work queued: run the stages one by one
     const int blocks = std::max(1, std::min(blocks_for_m(tot.fixup_pairs, 256), 1 << 16));
     for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
         const int nc = std::min(kBatchSegChunk, nseg - c0);
