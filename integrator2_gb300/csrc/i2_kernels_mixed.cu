@@ -770,6 +770,7 @@ constexpr int kFixSlots = kFixDeepSlots;  // chunks of levels 4 and 5: 1 + 4
 static_assert(kFixSlots == 1 + 4 && kFixChunk == 256, "chunk layout of levels 4 and 5");
 __device__ __forceinline__ int fix_slot0(int L) { return L == 4 ? 0 : 1; }
 __device__ __forceinline__ int fix_chunks(int L) { return (1 << (2 * L)) / kFixChunk; }
+static_assert((1 << 8) / kFixChunk == 1 && (1 << 10) / kFixChunk == 4, "level 4 is slot 0, level 5 slots 1..4");
 
 // pair t, by the whole block (red: 5 doubles per warp of shared memory)
 template <int CLS>
@@ -833,7 +834,7 @@ __device__ void fp64_fixup_item(const ClassArgs &A, const QuadTables &Q, int mod
 template <int CLS>
 __device__ void fix_spread_item(const ClassArgs &A, const QuadTables &Q, int mode, int fixed_level, int kmax, int k, int slot, double *red)
 {
-    const int L = slot < 4 ? 4 : 5;
+    const int L = slot < fix_slot0(5) ? 4 : 5;  // slots [fix_slot0(4), fix_slot0(5)) are level 4's chunks
     const int t = A.fix_deep[k];
     const bool wanted = L <= kmax && (mode == kAdaptiveRelative || fixup_kept_level(A, mode, fixed_level, t) == L);
     if (!wanted) return;  // uniform over the block
