@@ -4,7 +4,7 @@ Workload (one "step"): every ordered pair of the four pair classes of a 20,480-t
 icosphere (5 subdivisions) whose vertices carry a seeded tangential Gaussian jitter of 0.15 x
 mean edge length, reprojected to the unit sphere: common-vertex, common-edge, self, and
 disjoint pairs with centroid distance < 3 x mean edge length (1,418,734 ordered pairs), each
-producing J (3-vector) and P.  Refinement: relative error control (|J_L - J_{L-1}| <= 4 tol |J_L|,
+producing J (3-vector) and P.  Refinement: relative error control (|J_L - J_{L-1}| <= tol |J_L|,
 levels 0..5) with the 13-point degree-7 rule; the potential of adjacent pairs uses the graded
 Duffy rule.  Data are synthetic (no data set exists for this path).
 
@@ -147,7 +147,7 @@ def workload_config(total, tol):
     """the config dict both arms print (the same workload, rules and error control)"""
     return {"workload": "jittered icosphere s5 (20480 triangles, sigma 0.15h, seed 2026): common-vertex, "
                         "common-edge, self and near-field (< 3h) ordered pairs",
-            "pairs": int(total), "error_control": f"relative tol {tol} (level kept once its change is <= 4 tol), levels 0..5",
+            "pairs": int(total), "error_control": f"relative tol {tol}, levels 0..5",
             "rule": "qf3D13; adjacent potential: tiered graded Duffy 10x8 / 8x6 check / 16x16 / adaptive"}
 
 
@@ -559,10 +559,10 @@ def run_batch(batch, flush, stream, steps, warmup):
 
 
 # kernels of one batched step, whatever the number of segments (up to 2,048): closed forms with the
-# counter reset, tier 1 with the self pairs, tier 2, the cooperative chain of tier 2b and the
-# adaptive potential (seed, 12 depths, final sums), one cooperative level kernel per pair class, and
-# the cooperative fix-up chain (collect, FP64 pass, spread, finish)
-BATCH_LAUNCHES = 1 + 1 + 1 + 1 + 3 + 1
+# counter reset, tier 1 with the self pairs, tier 2, tier 2b, the adaptive potential (seed, 12
+# depths, final sums), one cooperative level kernel per pair class, and the fix-up (collect, FP64
+# pass, spread, finish)
+BATCH_LAUNCHES = 1 + 1 + 1 + 1 + (1 + 12 + 1) + 3 + 4
 
 
 def uneven_batch_section(args):
@@ -924,7 +924,7 @@ def gpu_arm(args):
     if "batch" in forms:
         line["batch"] = {"shape": {"threads": forms["batch"]["shape"][0], "blocks_per_sm": forms["batch"]["shape"][1],
                                    "lanes_per_pair": forms["batch"]["shape"][2],
-                                   "registers": "capped at 128" if forms["batch"]["shape"][3] else "unconstrained"},
+                                   "registers": {0: "unconstrained", 1: "capped at 128", 2: "capped at 85"}[int(forms["batch"]["shape"][3])]},
                          "cuda_graph": forms["batch"]["graph"]}
     rk = "mixed" if "mixed" in roof else ("fp64" if "fp64" in roof else None)
     if rk:

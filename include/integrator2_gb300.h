@@ -64,10 +64,7 @@ typedef enum i2_pair_class {
 typedef enum i2_error_control {
     I2_FIXED_REFINEMENT_LEVEL = 0,
     I2_AUTOMATIC_ERROR_CONTROL = 1,  /* the reference's Runge loop, including its buffer parity */
-    I2_RELATIVE_ERROR_CONTROL = 2    /* scale-invariant: level L is kept once |J_L - J_{L-1}| <= 4 tol |J_L|
-                                        (and |P_L - P_{L-1}| <= 4 tol |P_L| for disjoint pairs): the
-                                        difference divided by 4, a Runge estimate of J_L's error
-                                        (the 13-point rule's errors fall about 256-fold a level) */
+    I2_RELATIVE_ERROR_CONTROL = 2    /* scale-invariant: |J_L - J_{L-1}| <= tol |J_L| */
 } i2_error_control;
 
 typedef enum i2_precision { I2_PRECISION_FP64 = 0, I2_PRECISION_MIXED = 1 } i2_precision;
@@ -213,7 +210,8 @@ i2_status i2_evaluator_backward_class(i2_evaluator_t *ev, i2_pair_class cls, con
 
 /* ------------------------------------------------------------------ batched form */
 /* Many (mesh, pair class) segments integrated together (no reference counterpart): the
- * refinement levels of all segments run in ONE persistent cooperative kernel, the whole run is
+ * refinement levels of all segments of one pair class run in ONE persistent cooperative kernel
+ * (three in all), a fixed number of launches whatever the number of segments; the whole run is
  * captured into a CUDA graph on the first i2_batch_run and replayed afterwards.  Settings
  * (rule, error control, potential rule) come from the integrator given at creation; the
  * batched form computes in mixed precision (FP32 bulk, FP64 singular parts, estimator and hard
@@ -226,7 +224,7 @@ i2_status i2_batch_set_stream(i2_batch_t *batch, void *stream);
 i2_status i2_batch_add(i2_batch_t *batch, const i2_mesh_t *mesh, i2_pair_class cls, const int32_t *rows, int64_t n,
                        int32_t row_stride, int32_t *segment);
 /* times the candidate launch shapes (threads per block, resident blocks per SM, lanes per pair,
- * register variant: 0 unconstrained, 1 capped at 128 per thread) on the batch and keeps the
+ * register variant: 0 unconstrained, 1 capped at 128 per thread, 2 capped at 85) on the batch and keeps the
  * fastest; the chosen shape is returned in shape[4] (may be NULL) */
 i2_status i2_batch_autotune(i2_batch_t *batch, int32_t *shape);
 /* enqueues the batch on its stream (graph replay after the first call); asynchronous */

@@ -1429,7 +1429,7 @@ i2_status i2_batch_autotune(i2_batch_t *batch, int32_t *shape)
         I2_CHECK_CUDA(cudaEventCreate(&e1));
         float best = 1e30f;
         int bt = batch->threads, bb = batch->blocks_per_sm, bg = batch->g_cap, bv = batch->variant;
-        for (int variant : {0, 1}) {
+        for (int variant : {0, 1, 2}) {
             for (int threads : {128, 256}) {
                 const int maxb = i2::batch_max_blocks_per_sm(threads, variant);
                 if (maxb <= 0) continue;

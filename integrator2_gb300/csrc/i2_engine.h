@@ -27,7 +27,7 @@ constexpr int kCntFixDeep = 13;   // FP64 fix-up pairs whose deeper levels were 
 // FP64 fix-up pairs per class run whose levels 4..5 can be spread over the GPU (820 KB of chunk
 // sums); further deep pairs stay with their own block
 constexpr int kFixDeepCap = 1024;
-constexpr int kFixDeepSlots = 5;  // chunks of 256 sub-cells in levels 4 and 5
+constexpr int kFixDeepSlots = 20;  // chunks of 64 sub-cells in levels 4 and 5
 // refinement / error-control modes
 enum { kFixed = 0, kAdaptiveCompat = 1, kAdaptiveRelative = 2 };
 
@@ -40,15 +40,6 @@ struct RunConfig {
     double hard_tol = 1e-8;  // relative tolerance of the adaptive potential of hard adjacent pairs (0: off)
     bool potential = true;   // false: J only, as the reference computes (adjacent pairs' P is not computed)
 };
-
-// Relative error control accepts level L of a pair when |J_L - J_{L-1}| <= kRelativeRunge tol
-// |J_L| (and the same for P in the disjoint class).  The difference of two levels overestimates
-// the finer level's own error by the ratio of successive levels' errors minus one -- 255 for the
-// 13-point degree-7 rule in its asymptotic range; the reference's Runge criterion divides by
-// 2^7 - 1 (evaluator3d.cu:76-99) -- so accepting a difference of 4 tol keeps J_L's error well
-// inside tol: on the 20,480-triangle sphere the accepted sums stay within 1e-7 (p99.9) of the
-// level-4 answer at tol 1e-6, with a quarter to a third fewer points than a bound of 1 x tol.
-constexpr double kRelativeRunge = 4.0;
 
 // doubles of one hard pair's cached FP64 set-up (PotPairCtx in i2_kernels_fp64.cu)
 constexpr int kPotCtxDoubles = 54;
@@ -142,9 +133,6 @@ void launch_batch_prelude(const BatchSeg *segs, int nseg, const BatchTotals &tot
                           const RunConfig &cfg, int persistent_blocks, cudaStream_t s);
 // the adaptive potential of every segment's hard pairs (seed, depths, final sums)
 void launch_batch_pot_chain(const BatchSeg *segs, int nseg, const QuadTables &Q, double tol, int persistent_blocks, cudaStream_t s);
-// tier 2b and the adaptive potential of every segment as one cooperative launch; false when the
-// batch has more than one chunk of segments or the launch was refused (run the stages then)
-bool launch_batch_hard_chain(const BatchSeg *segs, int nseg, const QuadTables &Q, double tol, cudaStream_t s);
 // the FP64 fix-up of needle pairs after the level sweep, for every segment
 void launch_batch_fixup(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTables &Q, const RunConfig &cfg,
                         int persistent_blocks, cudaStream_t s);

@@ -16,7 +16,6 @@
 #include "i2_self.cuh"
 #include "i2_tiers.cuh"
 
-#include <cooperative_groups.h>
 
 namespace i2 {
 
@@ -174,9 +173,8 @@ __global__ void __launch_bounds__(128) k_level(ClassArgs A, QuadTables Q, int le
             }
             const d3 Jc = finalize_j(CLS, mk(acc.px, acc.py, acc.pz) + spsi, acc.th + sth, nj, Si);
             const d3 dJ = kInv4Pi * ((acc.th - prev.th) * nj + cross(mk(acc.px - prev.px, acc.py - prev.py, acc.pz - prev.pz), nj));
-            const double bound = kRelativeRunge * tol;
-            unconv = norm(dJ) > bound * norm(Jc);
-            if (CLS == kFar) unconv = unconv || fabs(acc.pot - prev.pot) > bound * fabs(acc.pot);
+            unconv = norm(dJ) > tol * norm(Jc);
+            if (CLS == kFar) unconv = unconv || fabs(acc.pot - prev.pot) > tol * fabs(acc.pot);
         }
         atomicMax(A.maxlev, level);
         if (!unconv || level >= kmax) {
@@ -581,92 +579,6 @@ __global__ void __launch_bounds__(128) k_batch_pot_final(const BatchSeg *__restr
     }
 }
 
-// ------------------------------------------------------------------ batched hard-pair potential, one launch
-// Tier 2b of the adjacent pairs' potential, the adaptive rule's seed, its twelve depths and the
-// final sums of every segment in ONE cooperative launch: the stages run in turn over the whole
-// grid with a grid-wide barrier between them (each stage's item counts are device counters the
-// stage before wrote), in place of fifteen launches.  The grid is exactly the resident blocks.
-__device__ __forceinline__ void batch_tier2b_stage(const BatchSeg *__restrict__ segs, int nseg, const QuadTables &Q, long long *prefix)
-{
-    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
-        return seg_adjacent(S) && S.A.hard_list ? S.A.cnt[kCntTier2b] : 0;
-    });
-    const int lane = threadIdx.x & 31;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long g = warp_item_index(); g < total; g += nwarps) {
-        const int sg = seg_find(prefix, nseg, g);
-        const BatchSeg &S = segs[sg];
-        if (S.cls == kEdge) tier2b_item<kEdge>(S.A, Q, false, (int)(g - prefix[sg]), lane);
-        else tier2b_item<kVertex>(S.A, Q, false, (int)(g - prefix[sg]), lane);
-    }
-}
-
-__device__ __forceinline__ void batch_pot_seed_stage(const BatchSeg *__restrict__ segs, int nseg, const QuadTables &Q, double tol, long long *prefix)
-{
-    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
-        return seg_adjacent(S) && S.A.hard_list ? pot_seeded(S.A) : 0;
-    });
-    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid < nseg && seg_adjacent(segs[gid]) && segs[gid].A.hard_list) pot_seed_init(segs[gid].A);
-    const int lane = threadIdx.x & 31;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long g = warp_item_index(); g < total; g += nwarps) {
-        const int sg = seg_find(prefix, nseg, g);
-        const BatchSeg &S = segs[sg];
-        const int h = (int)(g - prefix[sg]);
-        if (S.cls == kEdge) pot_seed_item<kEdge>(S.A, Q, tol, h, lane);
-        else pot_seed_item<kVertex>(S.A, Q, tol, h, lane);
-    }
-}
-
-__device__ __forceinline__ void batch_pot_depth_stage(const BatchSeg *__restrict__ segs, int nseg, const QuadTables &Q, double tol, int depth,
-                                                      long long *prefix)
-{
-    const long long total = seg_prefix(segs, nseg, prefix, [depth](const BatchSeg &S) -> long long {
-        return seg_adjacent(S) && S.A.hard_list ? pot_depth_count(S.A, depth) : 0;
-    });
-    const int lane = threadIdx.x & 31;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long g = warp_item_index(); g < total; g += nwarps) {
-        const int sg = seg_find(prefix, nseg, g);
-        const BatchSeg &S = segs[sg];
-        const int idx = (int)(g - prefix[sg]);
-        const PotCellItem *in = depth % 2 ? S.A.pot_q_a : S.A.pot_q_b;
-        PotCellItem *out = depth % 2 ? S.A.pot_q_b : S.A.pot_q_a;
-        if (S.cls == kEdge) pot_depth_item<kEdge>(S.A, Q, tol, depth, in, out, idx, lane);
-        else pot_depth_item<kVertex>(S.A, Q, tol, depth, in, out, idx, lane);
-    }
-}
-
-__device__ __forceinline__ void batch_pot_final_stage(const BatchSeg *__restrict__ segs, int nseg, double tol, long long *prefix)
-{
-    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
-        return seg_adjacent(S) && S.A.hard_list ? pot_seeded(S.A) : 0;
-    });
-    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
-        const int sg = seg_find(prefix, nseg, g);
-        const BatchSeg &S = segs[sg];
-        if (S.cls == kEdge) pot_final_item<kEdge>(S.A, tol, (int)(g - prefix[sg]));
-        else pot_final_item<kVertex>(S.A, tol, (int)(g - prefix[sg]));
-    }
-}
-
-__global__ void __launch_bounds__(128, 3) k_batch_hard_chain(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q, double tol)
-{
-    namespace cg = cooperative_groups;
-    cg::grid_group grid = cg::this_grid();
-    extern __shared__ long long prefix[];
-    batch_tier2b_stage(segs, nseg, Q, prefix);
-    grid.sync();
-    batch_pot_seed_stage(segs, nseg, Q, tol, prefix);
-    grid.sync();
-    for (int d = 1; d <= kHardMaxDepth; ++d) {
-        batch_pot_depth_stage(segs, nseg, Q, tol, d, prefix);
-        grid.sync();
-    }
-    batch_pot_final_stage(segs, nseg, tol, prefix);
-}
-
 // ------------------------------------------------------------------ finalisation
 
 template <int CLS>
@@ -756,22 +668,6 @@ void launch_batch_pot_chain(const BatchSeg *segs, int nseg, const QuadTables &Q,
         const int nc = std::min(kBatchSegChunk, nseg - c0);
         k_batch_pot_final<<<persistent_blocks, 128, seg_smem(nc), s>>>(segs + c0, nc, tol);
     }
-}
-
-// tier 2b and the adaptive potential of every segment as one cooperative launch (one chunk of
-// segments); false when the launch is not possible (the caller then runs the stages one by one)
-bool launch_batch_hard_chain(const BatchSeg *segs, int nseg, const QuadTables &Q, double tol, cudaStream_t s)
-{
-    if (nseg > kBatchSegChunk) return false;
-    const size_t smem = (size_t)(nseg + 1) * sizeof(long long);
-    int dev = 0, sms = 0, nb = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)k_batch_hard_chain, 128, smem) != cudaSuccess || nb <= 0)
-        return false;
-    QuadTables q = Q;
-    double t = tol;
-    void *args[] = {(void *)&segs, (void *)&nseg, (void *)&q, (void *)&t};
-    return cudaLaunchCooperativeKernel((const void *)k_batch_hard_chain, dim3(sms * nb), dim3(128), args, smem, s) == cudaSuccess;
 }
 
 void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s)

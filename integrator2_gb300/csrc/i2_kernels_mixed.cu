@@ -356,7 +356,7 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
         const f3 Jf = (float)th_tot * nf + crossf(psif, nf);
         const f3 dpsif = f3{(float)(acc.px - prev.px), (float)(acc.py - prev.py), (float)(acc.pz - prev.pz)};
         const f3 dJf = (float)(acc.th - prev.th) * nf + crossf(dpsif, nf);
-        const float tolf = (float)(kRelativeRunge * tol);
+        const float tolf = (float)tol;
         bool unconv;
         if (mode == kAdaptiveCompat) {
             unconv = runge_unconverged(acc, prev, Qf.pow2p);
@@ -725,9 +725,8 @@ __device__ __forceinline__ bool fixup_unconverged(const acc5 &nxt, const acc5 &p
 {
     const d3 Jc = finalize_j(CLS, mk(nxt.px, nxt.py, nxt.pz) + spsi, nxt.th + sth, nj, p.Si);
     const d3 dJ = kInv4Pi * ((nxt.th - prev.th) * nj + cross(mk(nxt.px - prev.px, nxt.py - prev.py, nxt.pz - prev.pz), nj));
-    const double bound = kRelativeRunge * tol;
-    bool unconv = norm(dJ) > bound * norm(Jc);
-    if (CLS == kFar) unconv = unconv || fabs(nxt.pot - prev.pot) > bound * fabs(nxt.pot);
+    bool unconv = norm(dJ) > tol * norm(Jc);
+    if (CLS == kFar) unconv = unconv || fabs(nxt.pot - prev.pot) > tol * fabs(nxt.pot);
     return unconv;
 }
 
@@ -764,13 +763,14 @@ __device__ __forceinline__ int fixup_kept_level(const ClassArgs &A, int mode, in
 // sub-cells, one block per chunk (one sub-cell a thread: 1,024 threads over a level-5 pair);
 // k_fix_finish adds the chunks in order and decides.  A needle pair refined to level 5 is
 // 17.7 MFLOP of FP64, about 2 ms on one SM, which otherwise sets the length of the whole pass.
+// Small blocks keep several resident per SM (chunks of 256 sub-cells measured 0.16 ms slower on
+// the 20,480-triangle sphere's batched step).
 constexpr int kFixDirect = 3;
-constexpr int kFixChunk = 256;
-constexpr int kFixSlots = kFixDeepSlots;  // chunks of levels 4 and 5: 1 + 4
-static_assert(kFixSlots == 1 + 4 && kFixChunk == 256, "chunk layout of levels 4 and 5");
-__device__ __forceinline__ int fix_slot0(int L) { return L == 4 ? 0 : 1; }
+constexpr int kFixChunk = 64;
+constexpr int kFixSlots = kFixDeepSlots;  // chunks of levels 4 and 5: 4 + 16
+static_assert(kFixSlots == 4 + 16 && kFixChunk * 4 == 256, "chunk layout of levels 4 and 5");
+__device__ __forceinline__ int fix_slot0(int L) { return L == 4 ? 0 : 4; }
 __device__ __forceinline__ int fix_chunks(int L) { return (1 << (2 * L)) / kFixChunk; }
-static_assert((1 << 8) / kFixChunk == 1 && (1 << 10) / kFixChunk == 4, "level 4 is slot 0, level 5 slots 1..4");
 
 // pair t, by the whole block (red: 5 doubles per warp of shared memory)
 template <int CLS>
@@ -1052,7 +1052,9 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
 // every pair.  Converged pairs drop out of the lists, so the uneven work left by adaptive
 // refinement is spread over the whole GPU at every level, across meshes and classes.
 // MINB = 1: registers unconstrained (fewer resident warps); MINB = 2: at most 128 registers per
-// thread so that two 256-thread blocks stay resident per SM (some spilling).  The autotuner picks.
+// thread so that two 256-thread blocks stay resident per SM (some spilling); MINB = 3: at most 85
+// registers, three blocks a SM (more spilling; the level kernels are latency-bound at 8-16 warps
+// a SM).  The autotuner picks.
 template <int MINB, int CLS>
 __global__ void __launch_bounds__(256, MINB) k_batch_levels(const BatchSeg *__restrict__ segs, int nseg, QuadTablesF Qf, int mode,
                                                       int level_fixed, double tol, int kmax, int G_cap)
@@ -1081,8 +1083,10 @@ const void *batch_levels_fn(int variant, int cls)
 {
     if (variant == 0) return cls == kFar ? (const void *)k_batch_levels<1, kFar> : cls == kEdge ? (const void *)k_batch_levels<1, kEdge>
                                                                                                  : (const void *)k_batch_levels<1, kVertex>;
-    return cls == kFar ? (const void *)k_batch_levels<2, kFar> : cls == kEdge ? (const void *)k_batch_levels<2, kEdge>
-                                                                              : (const void *)k_batch_levels<2, kVertex>;
+    if (variant == 1) return cls == kFar ? (const void *)k_batch_levels<2, kFar> : cls == kEdge ? (const void *)k_batch_levels<2, kEdge>
+                                                                                                 : (const void *)k_batch_levels<2, kVertex>;
+    return cls == kFar ? (const void *)k_batch_levels<3, kFar> : cls == kEdge ? (const void *)k_batch_levels<3, kEdge>
+                                                                              : (const void *)k_batch_levels<3, kVertex>;
 }
 
 int batch_levels_occupancy(int threads, int variant, int cls)
@@ -1291,79 +1295,7 @@ __global__ void __launch_bounds__(128) k_batch_fix_finish(const BatchSeg *__rest
     }
 }
 
-// The four fix-up stages of every segment in ONE cooperative launch (256 threads a block, the
-// grid exactly the resident blocks): gather the needle pairs; recompute them in FP64, a block per
-// pair, up to level kFixDirect; their levels 4-5 in chunks of kFixChunk sub-cells, a block per
-// chunk; add the chunks in order and decide -- with a grid-wide barrier between the stages.
-__global__ void __launch_bounds__(256) k_batch_fixup_chain(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q, int mode,
-                                                           int fixed_level, double tol, int kmax)
-{
-    namespace cg = cooperative_groups;
-    cg::grid_group grid = cg::this_grid();
-    extern __shared__ long long prefix[];
-    __shared__ double red[5 * 8];
-    long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long { return seg_fixup(S) ? S.A.n : 0; });
-    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
-        const int sg = seg_find(prefix, nseg, g);
-        const ClassArgs &A = segs[sg].A;
-        if (segs[sg].cls == kFar) fixup_collect_item<kFar>(A, A.act_a, A.cnt + kCntFixup, g - prefix[sg]);
-        else fixup_collect_item<kEdge>(A, A.act_a, A.cnt + kCntFixup, g - prefix[sg]);
-    }
-    grid.sync();
-    total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long { return seg_fixup(S) ? S.A.cnt[kCntFixup] : 0; });
-    for (long long g = blockIdx.x; g < total; g += gridDim.x) {
-        const int sg = seg_find(prefix, nseg, g);
-        const BatchSeg &S = segs[sg];
-        const int t = S.A.act_a[g - prefix[sg]];
-        if (S.cls == kFar) fp64_fixup_item<kFar>(S.A, Q, mode, fixed_level, tol, kmax, t, red);
-        else if (S.cls == kEdge) fp64_fixup_item<kEdge>(S.A, Q, mode, fixed_level, tol, kmax, t, red);
-        else fp64_fixup_item<kVertex>(S.A, Q, mode, fixed_level, tol, kmax, t, red);
-    }
-    grid.sync();
-    total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
-        return seg_fixup(S) && S.A.fix_deep ? (long long)min(S.A.cnt[kCntFixDeep], S.A.fix_cap) * kFixSlots : 0;
-    });
-    for (long long g = blockIdx.x; g < total; g += gridDim.x) {
-        const int sg = seg_find(prefix, nseg, g);
-        const BatchSeg &S = segs[sg];
-        const long long q = g - prefix[sg];
-        const int k = (int)(q / kFixSlots), slot = (int)(q % kFixSlots);
-        if (S.cls == kFar) fix_spread_item<kFar>(S.A, Q, mode, fixed_level, kmax, k, slot, red);
-        else if (S.cls == kEdge) fix_spread_item<kEdge>(S.A, Q, mode, fixed_level, kmax, k, slot, red);
-        else fix_spread_item<kVertex>(S.A, Q, mode, fixed_level, kmax, k, slot, red);
-    }
-    grid.sync();
-    total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
-        return seg_fixup(S) && S.A.fix_deep ? min(S.A.cnt[kCntFixDeep], S.A.fix_cap) : 0;
-    });
-    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
-        const int sg = seg_find(prefix, nseg, g);
-        const BatchSeg &S = segs[sg];
-        const int k = (int)(g - prefix[sg]);
-        if (S.cls == kFar) fix_finish_item<kFar>(S.A, mode, fixed_level, tol, kmax, k);
-        else if (S.cls == kEdge) fix_finish_item<kEdge>(S.A, mode, fixed_level, tol, kmax, k);
-        else fix_finish_item<kVertex>(S.A, mode, fixed_level, tol, kmax, k);
-    }
-}
-
 static size_t seg_smem(int nseg) { return (size_t)(nseg + 1) * sizeof(long long); }
-
-// k_batch_fixup_chain for one chunk of segments; false when the batch has more chunks or the
-// cooperative launch was refused
-static bool launch_batch_fixup_chain(const BatchSeg *segs, int nseg, const QuadTables &Q, const RunConfig &cfg, cudaStream_t s)
-{
-    if (nseg > kBatchSegChunk) return false;
-    const size_t smem = seg_smem(nseg);
-    int dev = 0, sms = 0, nb = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)k_batch_fixup_chain, 256, smem) != cudaSuccess || nb <= 0)
-        return false;
-    QuadTables q = Q;
-    int mode = cfg.mode, level = cfg.level, kmax = cfg.max_level;
-    double tol = cfg.tol;
-    void *args[] = {(void *)&segs, (void *)&nseg, (void *)&q, (void *)&mode, (void *)&level, (void *)&tol, (void *)&kmax};
-    return cudaLaunchCooperativeKernel((const void *)k_batch_fixup_chain, dim3(sms * nb), dim3(256), args, smem, s) == cudaSuccess;
-}
 
 void launch_batch_prelude(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTables &Q, const QuadTablesF &Qf,
                           const RunConfig &cfg, int persistent_blocks, cudaStream_t s)
@@ -1389,16 +1321,11 @@ void launch_batch_prelude(const BatchSeg *segs, int nseg, const BatchTotals &tot
             const int nc = std::min(kBatchSegChunk, nseg - c0);
             k_batch_tier2<<<resident_grid((const void *)k_batch_tier2, tpb, seg_smem(nc)), tpb, seg_smem(nc), s>>>(segs + c0, nc, Qf, Q);
         }
-        // tier 2b and the adaptive potential: one cooperative launch for a single chunk of
-        // segments, else stage by stage
-        if (!launch_batch_hard_chain(segs, nseg, Q, cfg.hard_tol, s)) {
-            cudaGetLastError();  // a refused cooperative launch leaves no work queued
-            for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
-                const int nc = std::min(kBatchSegChunk, nseg - c0);
-                k_batch_tier2b<<<resident_grid((const void *)k_batch_tier2b, tpb, seg_smem(nc)), tpb, seg_smem(nc), s>>>(segs + c0, nc, Q);
-            }
-            launch_batch_pot_chain(segs, nseg, Q, cfg.hard_tol, persistent_blocks, s);
+        for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
+            const int nc = std::min(kBatchSegChunk, nseg - c0);
+            k_batch_tier2b<<<resident_grid((const void *)k_batch_tier2b, tpb, seg_smem(nc)), tpb, seg_smem(nc), s>>>(segs + c0, nc, Q);
         }
+        launch_batch_pot_chain(segs, nseg, Q, cfg.hard_tol, persistent_blocks, s);
     }
 }
 
@@ -1406,8 +1333,6 @@ void launch_batch_fixup(const BatchSeg *segs, int nseg, const BatchTotals &tot, 
                         int persistent_blocks, cudaStream_t s)
 {
     if (tot.fixup_pairs <= 0) return;
-    if (launch_batch_fixup_chain(segs, nseg, Q, cfg, s)) return;
-    cudaGetLastError();  // a refused cooperative launch leaves no work queued: run the stages one by one
     const int blocks = std::max(1, std::min(blocks_for_m(tot.fixup_pairs, 256), 1 << 16));
     for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
         const int nc = std::min(kBatchSegChunk, nseg - c0);

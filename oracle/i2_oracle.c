@@ -986,12 +986,6 @@ static v3 finalize_j(int cls, q4 r, v3 nj, double si)
 /* scale-invariant change between two refinement levels: max of |dJ|_2/|J|_2 and |dP|/|P|,
  * both measured on the complete values (regular part + closed-form singular part) */
 static v3 finalize_j(int cls, q4 r, v3 nj, double si);
-/* The library's relative error control (not the reference's): level L is accepted when the
- * relative change from level L-1 is at most O_RELATIVE_RUNGE x tol.  The change overestimates
- * level L's own error by the ratio of successive levels' errors minus one (as the reference's
- * Runge criterion divides by 2^order - 1, evaluator3d.cu:76-99). */
-#define O_RELATIVE_RUNGE 4.0
-
 static double rel_change(int cls, q4 cur, q4 prev, q4 sing, double pc, double pp, v3 nj, double si)
 {
     v3 jc = finalize_j(cls, q4add(cur, sing), nj, si), jp = finalize_j(cls, q4add(prev, sing), nj, si);
@@ -1121,8 +1115,8 @@ int o_integrate_class(int cls, int ntasks, const int *ti, const int *tj,
                 h[k] = level_integral(&ctx, root, S[i], k);
                 int unconv;
                 if (mode == O_ADAPTIVE_COMPAT) unconv = runge_unconverged(h[k].r, h[k - 1].r, pow2p);
-                else if (cls == O_FAR) unconv = rel_change(cls, h[k].r, h[k - 1].r, sing, h[k].p, h[k - 1].p, nj, S[i]) > O_RELATIVE_RUNGE * tol;
-                else unconv = rel_change(cls, h[k].r, h[k - 1].r, sing, 1.0, 1.0, nj, S[i]) > O_RELATIVE_RUNGE * tol;
+                else if (cls == O_FAR) unconv = rel_change(cls, h[k].r, h[k - 1].r, sing, h[k].p, h[k - 1].p, nj, S[i]) > tol;
+                else unconv = rel_change(cls, h[k].r, h[k - 1].r, sing, 1.0, 1.0, nj, S[i]) > tol;
                 if (!unconv) break;
             }
             if (k > O_MAX_LEVEL) k = O_MAX_LEVEL;
