@@ -17,7 +17,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libi2gb300.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["i2_capi.cu", "i2_kernels_fp64.cu", "i2_kernels_mixed.cu", "i2_calibrate.cu", "i2_noalloc.cu", "i2_adjoint.cu",
+SOURCES = ["i2_capi.cu", "i2_kernels_fp64.cu", "i2_kernels_mixed.cu", "i2_kernels_df.cu", "i2_calibrate.cu", "i2_noalloc.cu", "i2_adjoint.cu",
            "i2_pairs.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code is compiled without floating-point contraction (GCC fuses a*b+c on Arm by default),

@@ -41,8 +41,9 @@ struct RunConfig {
     bool potential = true;   // false: J only, as the reference computes (adjacent pairs' P is not computed)
 };
 
-// doubles of one hard pair's cached FP64 set-up (PotPairCtx in i2_kernels_fp64.cu)
-constexpr int kPotCtxDoubles = 54;
+// doubles of one hard pair's cached set-up (PotPairCtx in i2_kernels_fp64.cu, 54 doubles;
+// PotPairCtxD in i2_kernels_df.cu, 55)
+constexpr int kPotCtxDoubles = 56;
 
 // one cell of the breadth-first adaptive potential rule of hard adjacent pairs
 struct PotCellItem {
@@ -131,8 +132,11 @@ struct BatchTotals {
 // potential and the self pairs: one launch per stage for the whole batch
 void launch_batch_prelude(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTables &Q, const QuadTablesF &Qf,
                           const RunConfig &cfg, int persistent_blocks, cudaStream_t s);
-// the adaptive potential of every segment's hard pairs (seed, depths, final sums)
-void launch_batch_pot_chain(const BatchSeg *segs, int nseg, const QuadTables &Q, double tol, int persistent_blocks, cudaStream_t s);
+// tier 2b and the adaptive potential of every segment's hard pairs (seed, depths, final sums),
+// in double-float (i2_kernels_df.cu)
+void launch_batch_pot_df(const BatchSeg *segs, int nseg, const QuadTables &Q, double tol, int persistent_blocks, cudaStream_t s);
+// mixed form, one class: tier 2b and the adaptive potential in double-float
+void launch_pot_tiers_hard_df(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s);
 // the FP64 fix-up of needle pairs after the level sweep, for every segment
 void launch_batch_fixup(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTables &Q, const RunConfig &cfg,
                         int persistent_blocks, cudaStream_t s);

@@ -10,9 +10,9 @@
 //                              it also runs the convergence test and appends unconverged pairs
 //                              to the next level's active list (device-side counter)
 //   k_finalize<CLS>            kept level, singular part, J = (Theta n_j + Psi x n_j)/4pi
-#include "i2_batch.cuh"
 #include "i2_engine.h"
 #include "i2_finalize.cuh"
+#include "i2_pot.cuh"
 #include "i2_self.cuh"
 #include "i2_tiers.cuh"
 
@@ -314,7 +314,7 @@ __device__ __forceinline__ PotPairCtx pot_pair_ctx(const ClassArgs &A, int t, do
     return c;
 }
 
-static_assert(sizeof(PotPairCtx) == 8 * kPotCtxDoubles, "cached hard-pair set-up size");
+static_assert(sizeof(PotPairCtx) <= 8 * kPotCtxDoubles, "cached hard-pair set-up size");
 
 // the cached set-up of hard pair h (written by the seed), or the set-up recomputed past the cap
 template <int CLS>
@@ -323,9 +323,6 @@ __device__ __forceinline__ PotPairCtx pot_ctx_of(const ClassArgs &A, int h, int 
     if (h < A.pot_ctx_cap) return *reinterpret_cast<const PotPairCtx *>(A.pot_ctx + (long long)kPotCtxDoubles * h);
     return pot_pair_ctx<CLS>(A, t, tol);
 }
-
-// cell triangles of the parents of depth d's cells (written while depth d - 1 split them)
-__device__ __forceinline__ double *pot_tri_list(const ClassArgs &A, int depth) { return depth % 2 ? A.pot_tri_a : A.pot_tri_b; }
 
 __device__ __forceinline__ void pot_tri_store(double *dst, const Tri &T)
 {
@@ -390,21 +387,6 @@ __device__ void pot_children_warp(const Tri &T, const int cc[4], const PotPairCt
         for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
         v[k] = x;
     }
-}
-
-// seed: the root of every hard pair is split once (one warp per pair); its four children form
-// depth 1.  Pairs beyond a quarter of the list capacity keep their Duffy value and are counted
-// as overflows.
-__device__ __forceinline__ int pot_seeded(const ClassArgs &A) { return min(*A.hard_cnt, A.pot_qcap / 4); }
-
-// the seed's bookkeeping, once per segment before any depth kernel runs: depth 1 holds the
-// roots' children, the deeper lists start empty
-__device__ __forceinline__ void pot_seed_init(const ClassArgs &A)
-{
-    const int count = pot_seeded(A);
-    A.pot_qcnt[1] = 4 * count;
-    for (int d = 2; d <= kHardMaxDepth + 1; ++d) A.pot_qcnt[d] = 0;
-    if (*A.hard_cnt > count) atomicAdd(A.hard_overflow, *A.hard_cnt - count);
 }
 
 template <int CLS>
@@ -475,8 +457,6 @@ __device__ __forceinline__ void pot_depth_item(const ClassArgs &A, const QuadTab
     if (accept) atomicAdd(reinterpret_cast<unsigned long long *>(&A.pot_fx[it.h]), (unsigned long long)llrint(sum * c.scale));
 }
 
-__device__ __forceinline__ int pot_depth_count(const ClassArgs &A, int depth) { return min(A.pot_qcnt[depth], A.pot_qcap); }
-
 // one depth: one warp per cell
 template <int CLS>
 __global__ void __launch_bounds__(128, 3) k_pot_depth(ClassArgs A, QuadTables Q, double tol, int depth, const PotCellItem *__restrict__ in,
@@ -521,62 +501,6 @@ __global__ void __launch_bounds__(128) k_self(ClassArgs A, QuadTables Q, int sel
     const bool valid = k < kSelfPairsPerWarp && t < A.n;
     const double sum = self_gather6(valid ? self_piece_of(A, Q, t, lane % 6) : 0.0);
     if (valid && lane % 6 == 0) self_store(A, self_sign, t, sum);
-}
-
-// ------------------------------------------------------------------ batched stages
-// The stages above, each as one launch over every segment of a batch (i2_batch.cuh): the
-// adaptive potential's seed, depths and final sums, and the self pairs.  Segments are walked in
-// chunks of kBatchSegChunk; a chunk's prefix sums live in dynamic shared memory.
-__global__ void __launch_bounds__(128) k_batch_pot_seed(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q, double tol)
-{
-    extern __shared__ long long prefix[];
-    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
-        return seg_adjacent(S) && S.A.hard_list ? pot_seeded(S.A) : 0;
-    });
-    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid < nseg && seg_adjacent(segs[gid]) && segs[gid].A.hard_list) pot_seed_init(segs[gid].A);
-    const int lane = threadIdx.x & 31;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long g = warp_item_index(); g < total; g += nwarps) {
-        const int sg = seg_find(prefix, nseg, g);
-        const BatchSeg &S = segs[sg];
-        const int h = (int)(g - prefix[sg]);
-        if (S.cls == kEdge) pot_seed_item<kEdge>(S.A, Q, tol, h, lane);
-        else pot_seed_item<kVertex>(S.A, Q, tol, h, lane);
-    }
-}
-
-__global__ void __launch_bounds__(128, 3) k_batch_pot_depth(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q, double tol, int depth)
-{
-    extern __shared__ long long prefix[];
-    const long long total = seg_prefix(segs, nseg, prefix, [depth](const BatchSeg &S) -> long long {
-        return seg_adjacent(S) && S.A.hard_list ? pot_depth_count(S.A, depth) : 0;
-    });
-    const int lane = threadIdx.x & 31;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long g = warp_item_index(); g < total; g += nwarps) {
-        const int sg = seg_find(prefix, nseg, g);
-        const BatchSeg &S = segs[sg];
-        const int idx = (int)(g - prefix[sg]);
-        const PotCellItem *in = depth % 2 ? S.A.pot_q_a : S.A.pot_q_b;
-        PotCellItem *out = depth % 2 ? S.A.pot_q_b : S.A.pot_q_a;
-        if (S.cls == kEdge) pot_depth_item<kEdge>(S.A, Q, tol, depth, in, out, idx, lane);
-        else pot_depth_item<kVertex>(S.A, Q, tol, depth, in, out, idx, lane);
-    }
-}
-
-__global__ void __launch_bounds__(128) k_batch_pot_final(const BatchSeg *__restrict__ segs, int nseg, double tol)
-{
-    extern __shared__ long long prefix[];
-    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
-        return seg_adjacent(S) && S.A.hard_list ? pot_seeded(S.A) : 0;
-    });
-    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
-        const int sg = seg_find(prefix, nseg, g);
-        const BatchSeg &S = segs[sg];
-        if (S.cls == kEdge) pot_final_item<kEdge>(S.A, tol, (int)(g - prefix[sg]));
-        else pot_final_item<kVertex>(S.A, tol, (int)(g - prefix[sg]));
-    }
 }
 
 // ------------------------------------------------------------------ finalisation
@@ -647,27 +571,6 @@ void launch_pot_hard(int cls, const ClassArgs &A, const QuadTables &Q, const Run
 {
     if (cls == kEdge) pot_adaptive_chain<kEdge>(A, Q, cfg.hard_tol, persistent_blocks, s);
     else pot_adaptive_chain<kVertex>(A, Q, cfg.hard_tol, persistent_blocks, s);
-}
-
-static size_t seg_smem(int nseg) { return (size_t)(nseg + 1) * sizeof(long long); }
-
-void launch_batch_pot_chain(const BatchSeg *segs, int nseg, const QuadTables &Q, double tol, int persistent_blocks, cudaStream_t s)
-{
-    for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
-        const int nc = std::min(kBatchSegChunk, nseg - c0);
-        // the seed initialises every segment of the chunk: at least one thread per segment
-        k_batch_pot_seed<<<std::max(resident_grid((const void *)k_batch_pot_seed, 128, seg_smem(nc)), blocks_for(nc, 128)), 128, seg_smem(nc),
-                           s>>>(segs + c0, nc, Q, tol);
-    }
-    for (int d = 1; d <= kHardMaxDepth; ++d)
-        for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
-            const int nc = std::min(kBatchSegChunk, nseg - c0);
-            k_batch_pot_depth<<<resident_grid((const void *)k_batch_pot_depth, 128, seg_smem(nc)), 128, seg_smem(nc), s>>>(segs + c0, nc, Q, tol, d);
-        }
-    for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
-        const int nc = std::min(kBatchSegChunk, nseg - c0);
-        k_batch_pot_final<<<persistent_blocks, 128, seg_smem(nc), s>>>(segs + c0, nc, tol);
-    }
 }
 
 void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s)

@@ -1019,8 +1019,7 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
         else k_tier1_mixed<kEdge><<<blocks_for_m((long long)kTier1Lanes * A.n, tpb), tpb, 0, s>>>(A, Qf);
         if (A.hard_list) {
             k_pot_tier2_mixed<kEdge><<<resident_grid((const void *)k_pot_tier2_mixed<kEdge>, tpb, 0), tpb, 0, s>>>(A, Qf, Q);
-            k_pot_tier2b<kEdge><<<resident_grid((const void *)k_pot_tier2b<kEdge>, tpb, 0), tpb, 0, s>>>(A, Q, 0);
-            launch_pot_hard(kEdge, A, Q, cfg, persistent_blocks, s);
+            launch_pot_tiers_hard_df(kEdge, A, Q, cfg, persistent_blocks, s);
         }
         level_chain_mixed<kEdge>(A, Qf, cfg, persistent_blocks, s);
         launch_fp64_fixup(kEdge, A, Q, cfg, persistent_blocks, s);
@@ -1031,8 +1030,7 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
         else k_tier1_mixed<kVertex><<<blocks_for_m((long long)kTier1Lanes * A.n, tpb), tpb, 0, s>>>(A, Qf);
         if (A.hard_list) {
             k_pot_tier2_mixed<kVertex><<<resident_grid((const void *)k_pot_tier2_mixed<kVertex>, tpb, 0), tpb, 0, s>>>(A, Qf, Q);
-            k_pot_tier2b<kVertex><<<resident_grid((const void *)k_pot_tier2b<kVertex>, tpb, 0), tpb, 0, s>>>(A, Q, 0);
-            launch_pot_hard(kVertex, A, Q, cfg, persistent_blocks, s);
+            launch_pot_tiers_hard_df(kVertex, A, Q, cfg, persistent_blocks, s);
         }
         level_chain_mixed<kVertex>(A, Qf, cfg, persistent_blocks, s);
         launch_fp64_fixup(kVertex, A, Q, cfg, persistent_blocks, s);
@@ -1210,23 +1208,6 @@ __global__ void __launch_bounds__(128) k_batch_tier2(const BatchSeg *__restrict_
     }
 }
 
-// three blocks per SM, as k_pot_tier2b
-__global__ void __launch_bounds__(128, 3) k_batch_tier2b(const BatchSeg *__restrict__ segs, int nseg, QuadTables Q)
-{
-    extern __shared__ long long prefix[];
-    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
-        return seg_adjacent(S) && S.A.hard_list ? S.A.cnt[kCntTier2b] : 0;
-    });
-    const int lane = threadIdx.x & 31;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long g = warp_item_index(); g < total; g += nwarps) {
-        const int sg = seg_find(prefix, nseg, g);
-        const BatchSeg &S = segs[sg];
-        if (S.cls == kEdge) tier2b_item<kEdge>(S.A, Q, false, (int)(g - prefix[sg]), lane);
-        else tier2b_item<kVertex>(S.A, Q, false, (int)(g - prefix[sg]), lane);
-    }
-}
-
 // segments whose pairs the fix-up gathers (into act_a, counted in cnt[kCntFixup])
 __device__ __forceinline__ bool seg_fixup(const BatchSeg &S) { return S.A.n > 0 && S.cls != kSelf && S.A.act_a; }
 
@@ -1321,11 +1302,7 @@ void launch_batch_prelude(const BatchSeg *segs, int nseg, const BatchTotals &tot
             const int nc = std::min(kBatchSegChunk, nseg - c0);
             k_batch_tier2<<<resident_grid((const void *)k_batch_tier2, tpb, seg_smem(nc)), tpb, seg_smem(nc), s>>>(segs + c0, nc, Qf, Q);
         }
-        for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
-            const int nc = std::min(kBatchSegChunk, nseg - c0);
-            k_batch_tier2b<<<resident_grid((const void *)k_batch_tier2b, tpb, seg_smem(nc)), tpb, seg_smem(nc), s>>>(segs + c0, nc, Q);
-        }
-        launch_batch_pot_chain(segs, nseg, Q, cfg.hard_tol, persistent_blocks, s);
+        launch_batch_pot_df(segs, nseg, Q, cfg.hard_tol, persistent_blocks, s);
     }
 }
 
