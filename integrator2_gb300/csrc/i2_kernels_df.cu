@@ -114,6 +114,10 @@ __device__ __forceinline__ TriD tri_load_df(const double *src)
     return TriD{df3{v[0], v[1], v[2]}, df3{v[3], v[4], v[5]}, df3{v[6], v[7], v[8]}};
 }
 
+// resident 128-thread blocks per SM the double-float kernels are compiled for (at most 170
+// registers a thread); each warp's pair set-up lives in shared memory, not in registers
+constexpr int kDfBlocks = 3;
+
 // ------------------------------------------------------------------ rule tables
 struct QuadTablesD {
     dfl L1[kMaxGauss], L2[kMaxGauss], L3[kMaxGauss], w[kMaxGauss];
@@ -214,16 +218,52 @@ __device__ PotLocal pot_local(const ClassArgs &A, int t)
     return L;
 }
 
-// the integrand of the adjacent pairs' potential at a point with offsets oa, ob, oc from K_j's
-// vertices (local frame: oa is the point itself), less the shared-edge term for the edge class
-template <int CLS>
-__device__ __forceinline__ dfl pot_point_df(df3 oa, df3 ob, df3 oc, const PanelJD &K, const FarCtxD &F, const PotEdgeD &pe)
+// loads from a warp's shared-memory slot, one field at a time where it is used: the slot's pair
+// geometry (some 60 floats) is not held in registers across the point loop
+__device__ __forceinline__ dfl ldv(const volatile dfl &x) { return dfl(x.hi, x.lo); }
+__device__ __forceinline__ df3 ldv(const volatile df3 &v) { return df3{ldv(v.x), ldv(v.y), ldv(v.z)}; }
+
+// ln((l_from + q_from) / (l_to + q_to)) with the reference's collinear fallback (edge_log_fp64)
+__device__ __forceinline__ dfl edge_log_df(dfl l_from, dfl q_from, dfl l_to, dfl q_to)
 {
-    df3 psi;
-    dfl th, g;
-    far_integrand_o(oa, ob, oc, K, F, psi, th, g);
-    if (CLS == kEdge) g = g - pot_edge_sigma(oa, pe);
-    return g;
+    const dfl s_to = q_to + l_to;
+    if (fabs(s_to) < (0.5 * kEpsPsi2) * l_to) return log(l_to / l_from);
+    return log((l_from + q_from) / s_to);
+}
+
+// the integrand of the adjacent pairs' potential, sum_e t_e L_e - d Theta (far_integrand_o's
+// potential), at a point with offsets oa, ob, oc from K_j's vertices (local frame: oa is the
+// point itself), less the shared-edge term for the edge class; evaluated edge by edge so that
+// only one edge's quantities are live at a time
+template <int CLS>
+__device__ __forceinline__ dfl pot_point_df(df3 oa, df3 ob, df3 oc, const volatile PanelJD &K, const volatile FarCtxD &F,
+                                            const volatile PotEdgeD &pe)
+{
+    const dfl la = norm(oa), lb = norm(ob), lc = norm(oc);
+    dfl pot = dfl(0.0f, 0.0f);
+    {
+        const df3 tc = ldv(K.tc);
+        const dfl t_e = -dot(ldv(F.mc), oa);  // t_e L_e -> 0 on the edge's line even where L_e overflows
+        if (!(t_e == 0.0)) pot = t_e * edge_log_df(la, dot(oa, tc), lb, dot(ob, tc));  // A -> B
+    }
+    {
+        const df3 ta = ldv(K.ta);
+        const dfl t_e = -dot(ldv(F.ma), ob);
+        if (!(t_e == 0.0)) pot += t_e * edge_log_df(lb, dot(ob, ta), lc, dot(oc, ta));  // B -> C
+    }
+    {
+        const df3 tb = ldv(K.tb);
+        const dfl t_e = -dot(ldv(F.mb), oc);
+        if (!(t_e == 0.0)) pot += t_e * edge_log_df(lc, dot(oc, tb), la, dot(oa, tb));  // C -> A
+    }
+    const dfl d = dot(ldv(K.n), oa);
+    const dfl den = la * lb * lc + dot(oa, ob) * lc + dot(ob, oc) * la + dot(oc, oa) * lb;
+    pot -= d * (2.0f * atan2((2.0f * ldv(K.S)) * d, den));
+    if (CLS == kEdge) {
+        const dfl s = dot(oa - ldv(pe.P1), ldv(pe.m_in));
+        if (s > 0.0) pot += ((2.0f * ldv(pe.c)) * s) * log(s / ldv(pe.h));
+    }
+    return pot;
 }
 
 // ------------------------------------------------------------------ tier 2b
@@ -231,8 +271,8 @@ __device__ __forceinline__ dfl pot_point_df(df3 oa, df3 ob, df3 oc, const PanelJ
 // shared edge) over points p = first, first + step, ... of its flattened (piece, radial, angular)
 // list; a piece's geometry is formed once per lane and piece
 template <int CLS>
-__device__ dfl duffy_partial_df(const TriD &Ti, const PanelJD &K, const FarCtxD &F, const PotEdgeD &pe, const dfl *uu, const dfl *uw,
-                                int nu, const dfl *vv, const dfl *vw, int nv, int first, int step)
+__device__ dfl duffy_partial_df(const TriD &Ti, const volatile PanelJD &K, const volatile FarCtxD &F, const volatile PotEdgeD &pe,
+                                const dfl *uu, const dfl *uw, int nu, const dfl *vv, const dfl *vw, int nv, int first, int step)
 {
     const int npieces = CLS == kEdge ? 2 : 1;
     const int per = nu * nv;
@@ -264,8 +304,8 @@ __device__ dfl duffy_partial_df(const TriD &Ti, const PanelJD &K, const FarCtxD 
             }
             eB = B - Vx;
             eC = Cc - Vx;
-            dB = Vx - K.B;
-            dC = Vx - K.C;
+            dB = Vx - ldv(K.B);
+            dC = Vx - ldv(K.C);
             area2 = norm(cross(eB, eC));
         }
         const dfl u = uu[a], v = vv[b];
@@ -278,18 +318,23 @@ __device__ dfl duffy_partial_df(const TriD &Ti, const PanelJD &K, const FarCtxD 
 
 // listed pair h by one warp: the 16 x 16 and 20 x 20 rules; the pair is settled when they agree
 // to A.top_tol, else it goes to the adaptive rule with the 16 x 16 value as its tolerance base
+// the pair's local set-up is formed by lane 0 into the warp's shared-memory slot `L` (read by all
+// lanes from there rather than held in registers); the caller's next item waits for lane 0
 template <int CLS>
-__device__ void tier2b_item_df(const ClassArgs &A, const QuadTablesD &Q, int h, int lane)
+__device__ __noinline__ void tier2b_item_df(const ClassArgs &A, const QuadTablesD &Q, int h, int lane, PotLocal &L)
 {
     const int t = A.tier2b_list[h];
     const int2 pr = A.pairs[t];
-    const PotLocal L = pot_local<CLS>(A, t);
+    __syncwarp();
+    if (lane == 0) L = pot_local<CLS>(A, t);
+    __syncwarp();
     int si, sj;
     if (CLS == kEdge) shifts_edge(A.cells[pr.x], A.cells[pr.y], si, sj);
     else shifts_vertex(A.cells[pr.x], A.cells[pr.y], si, sj);
     const TriD Ti = rotate(L.Ti, si);
-    const dfl ph = warp_sum_df(duffy_partial_df<CLS>(Ti, L.K, L.F, L.pe, Q.hi_u, Q.hi_uw, Q.hi_nu, Q.hi_v, Q.hi_vw, Q.hi_nv, lane, 32));
-    const dfl pt = warp_sum_df(duffy_partial_df<CLS>(Ti, L.K, L.F, L.pe, Q.top_u, Q.top_uw, Q.top_nu, Q.top_v, Q.top_vw, Q.top_nv, lane, 32));
+    const volatile PotLocal &Lv = L;
+    const dfl ph = warp_sum_df(duffy_partial_df<CLS>(Ti, Lv.K, Lv.F, Lv.pe, Q.hi_u, Q.hi_uw, Q.hi_nu, Q.hi_v, Q.hi_vw, Q.hi_nv, lane, 32));
+    const dfl pt = warp_sum_df(duffy_partial_df<CLS>(Ti, Lv.K, Lv.F, Lv.pe, Q.top_u, Q.top_uw, Q.top_nu, Q.top_v, Q.top_vw, Q.top_nv, lane, 32));
     if (lane != 0) return;
     const double inv = 1.0 / L.s3;
     const double ph_t = (double)ph * inv + L.sig, pt_t = (double)pt * inv + L.sig;
@@ -302,12 +347,13 @@ __device__ void tier2b_item_df(const ClassArgs &A, const QuadTablesD &Q, int h, 
 }
 
 template <int CLS>
-__global__ void __launch_bounds__(128) k_pot_tier2b_df(ClassArgs A, QuadTablesD Q)
+__global__ void __launch_bounds__(128, kDfBlocks) k_pot_tier2b_df(ClassArgs A, QuadTablesD Q)
 {
+    __shared__ PotLocal slot[4];
     const int count = A.cnt[kCntTier2b];
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (long long h = warp_item_index(); h < count; h += nwarps) tier2b_item_df<CLS>(A, Q, (int)h, lane);
+    for (long long h = warp_item_index(); h < count; h += nwarps) tier2b_item_df<CLS>(A, Q, (int)h, lane, slot[threadIdx.x >> 5]);
 }
 
 // ------------------------------------------------------------------ adaptive rule of hard pairs
@@ -344,18 +390,27 @@ __device__ PotPairCtxD pot_pair_ctx_df(const ClassArgs &A, int t, double tol)
     return c;
 }
 
+// hard pair h's set-up into the warp's shared-memory slot: copied from the cache by the whole
+// warp, or recomputed by lane 0 past the cache's capacity
 template <int CLS>
-__device__ __forceinline__ PotPairCtxD pot_ctx_of_df(const ClassArgs &A, int h, int t, double tol)
+__device__ __forceinline__ void pot_ctx_to_slot(const ClassArgs &A, int h, int t, double tol, int lane, PotPairCtxD &slot)
 {
-    if (h < A.pot_ctx_cap) return *reinterpret_cast<const PotPairCtxD *>(A.pot_ctx + (long long)kPotCtxDoubles * h);
-    return pot_pair_ctx_df<CLS>(A, t, tol);
+    __syncwarp();  // the slot's previous item is done
+    if (h < A.pot_ctx_cap) {
+        const double *src = A.pot_ctx + (long long)kPotCtxDoubles * h;
+        double *dst = reinterpret_cast<double *>(&slot);
+        for (int i = lane; i < (int)(sizeof(PotPairCtxD) / 8); i += 32) dst[i] = src[i];
+    } else if (lane == 0) {
+        slot = pot_pair_ctx_df<CLS>(A, t, tol);
+    }
+    __syncwarp();
 }
 
 // the four children of cell T (corner slot of each in cc[]) by one warp: the flattened (child,
 // point) list is cut into 32 contiguous runs, one per lane, so a lane forms a child's geometry
 // once for all its points of that child; a butterfly leaves the four sums in every lane
 template <int CLS>
-__device__ void pot_children_warp_df(const TriD &T, const int cc[4], const PotPairCtxD &c, const QuadTablesD &Q, int lane, dfl v[4])
+__device__ void pot_children_warp_df(const TriD &T, const int cc[4], const volatile PotPairCtxD &c, const QuadTablesD &Q, int lane, dfl v[4])
 {
     const int nduffy = Q.nu * Q.nv;
     int start[5];
@@ -383,8 +438,8 @@ __device__ void pot_children_warp_df(const TriD &T, const int cc[4], const PotPa
                 Tc.a = Vx;  // the apex, kept for the points
                 eB = B - Vx;
                 eC = Cc - Vx;
-                dB = Vx - c.K.B;
-                dC = Vx - c.K.C;
+                dB = Vx - ldv(c.K.B);
+                dC = Vx - ldv(c.K.C);
                 area = norm(cross(eB, eC));
             } else {
                 area = df_half(norm(cross(Tc.b - Tc.a, Tc.c - Tc.a)));
@@ -399,7 +454,7 @@ __device__ void pot_children_warp_df(const TriD &T, const int cc[4], const PotPa
             g = ((Q.du_w[a] * u) * Q.dv_w[b]) * area * g;
         } else {
             const df3 x = Q.L1[p] * Tc.a + Q.L2[p] * Tc.b + Q.L3[p] * Tc.c;
-            g = pot_point_df<CLS>(x, x - c.K.B, x - c.K.C, c.K, c.F, c.pe);
+            g = pot_point_df<CLS>(x, x - ldv(c.K.B), x - ldv(c.K.C), c.K, c.F, c.pe);
             g = Q.w[p] * area * g;
         }
         if (k == 0) acc0 += g;
@@ -414,10 +469,12 @@ __device__ void pot_children_warp_df(const TriD &T, const int cc[4], const PotPa
 }
 
 template <int CLS>
-__device__ void pot_seed_item_df(const ClassArgs &A, const QuadTablesD &Q, double tol, int h, int lane)
+__device__ __noinline__ void pot_seed_item_df(const ClassArgs &A, const QuadTablesD &Q, double tol, int h, int lane, PotPairCtxD &c)
 {
     const int t = A.hard_list[h];
-    const PotPairCtxD c = pot_pair_ctx_df<CLS>(A, t, tol);
+    __syncwarp();
+    if (lane == 0) c = pot_pair_ctx_df<CLS>(A, t, tol);
+    __syncwarp();
     const int3 ci = A.cells[A.pairs[t].x], cj = A.cells[A.pairs[t].y];
     const int ia[3] = {ci.x, ci.y, ci.z};
     bool shared[3];
@@ -439,13 +496,13 @@ __device__ void pot_seed_item_df(const ClassArgs &A, const QuadTablesD &Q, doubl
 }
 
 template <int CLS>
-__device__ void pot_depth_item_df(const ClassArgs &A, const QuadTablesD &Q, double tol, int depth, const PotCellItem *__restrict__ in,
-                                  PotCellItem *__restrict__ out, int idx, int lane)
+__device__ __noinline__ void pot_depth_item_df(const ClassArgs &A, const QuadTablesD &Q, double tol, int depth, const PotCellItem *__restrict__ in,
+                                  PotCellItem *__restrict__ out, int idx, int lane, PotPairCtxD &c)
 {
     const PotCellItem it = in[idx];
     if (it.h < 0) return;
     const int t = A.hard_list[it.h];
-    const PotPairCtxD c = pot_ctx_of_df<CLS>(A, it.h, t, tol);
+    pot_ctx_to_slot<CLS>(A, it.h, t, tol, lane, c);
     // siblings sit at 4 consecutive slots, so the parent's triangle is at slot idx / 4
     const TriD T = (idx >> 2) < A.pot_tri_cap ? child_df(tri_load_df(pot_tri_list(A, depth) + 9LL * (idx >> 2)), (int)(it.path & 3))
                                               : subcell_df(c.Ti, depth, it.path);
@@ -496,24 +553,27 @@ __device__ __forceinline__ void pot_final_item_df(const ClassArgs &A, double tol
 }
 
 template <int CLS>
-__global__ void __launch_bounds__(128) k_pot_seed_df(ClassArgs A, QuadTablesD Q, double tol)
+__global__ void __launch_bounds__(128, kDfBlocks) k_pot_seed_df(ClassArgs A, QuadTablesD Q, double tol)
 {
+    __shared__ PotPairCtxD slot[4];
     const int count = pot_seeded(A);
     // the depth kernels run after this one on the same stream
     if (blockIdx.x == 0 && threadIdx.x == 0) pot_seed_init(A);
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int h = (int)warp_item_index(); h < count; h += nwarps) pot_seed_item_df<CLS>(A, Q, tol, h, lane);
+    for (int h = (int)warp_item_index(); h < count; h += nwarps) pot_seed_item_df<CLS>(A, Q, tol, h, lane, slot[threadIdx.x >> 5]);
 }
 
 template <int CLS>
-__global__ void __launch_bounds__(128) k_pot_depth_df(ClassArgs A, QuadTablesD Q, double tol, int depth, const PotCellItem *__restrict__ in,
-                                                     PotCellItem *__restrict__ out)
+__global__ void __launch_bounds__(128, kDfBlocks) k_pot_depth_df(ClassArgs A, QuadTablesD Q, double tol, int depth, const PotCellItem *__restrict__ in,
+                                                                PotCellItem *__restrict__ out)
 {
+    __shared__ PotPairCtxD slot[4];
     const int count = pot_depth_count(A, depth);
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int idx = (int)warp_item_index(); idx < count; idx += nwarps) pot_depth_item_df<CLS>(A, Q, tol, depth, in, out, idx, lane);
+    for (int idx = (int)warp_item_index(); idx < count; idx += nwarps)
+        pot_depth_item_df<CLS>(A, Q, tol, depth, in, out, idx, lane, slot[threadIdx.x >> 5]);
 }
 
 template <int CLS>
@@ -524,9 +584,10 @@ __global__ void __launch_bounds__(128) k_pot_final_df(ClassArgs A, double tol)
 }
 
 // ------------------------------------------------------------------ batched stages
-__global__ void __launch_bounds__(128) k_batch_tier2b(const BatchSeg *__restrict__ segs, int nseg, QuadTablesD Q)
+__global__ void __launch_bounds__(128, kDfBlocks) k_batch_tier2b(const BatchSeg *__restrict__ segs, int nseg, QuadTablesD Q)
 {
     extern __shared__ long long prefix[];
+    __shared__ PotLocal slot[4];
     const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
         return seg_adjacent(S) && S.A.hard_list ? S.A.cnt[kCntTier2b] : 0;
     });
@@ -535,14 +596,15 @@ __global__ void __launch_bounds__(128) k_batch_tier2b(const BatchSeg *__restrict
     for (long long g = warp_item_index(); g < total; g += nwarps) {
         const int sg = seg_find(prefix, nseg, g);
         const BatchSeg &S = segs[sg];
-        if (S.cls == kEdge) tier2b_item_df<kEdge>(S.A, Q, (int)(g - prefix[sg]), lane);
-        else tier2b_item_df<kVertex>(S.A, Q, (int)(g - prefix[sg]), lane);
+        if (S.cls == kEdge) tier2b_item_df<kEdge>(S.A, Q, (int)(g - prefix[sg]), lane, slot[threadIdx.x >> 5]);
+        else tier2b_item_df<kVertex>(S.A, Q, (int)(g - prefix[sg]), lane, slot[threadIdx.x >> 5]);
     }
 }
 
-__global__ void __launch_bounds__(128) k_batch_pot_seed(const BatchSeg *__restrict__ segs, int nseg, QuadTablesD Q, double tol)
+__global__ void __launch_bounds__(128, kDfBlocks) k_batch_pot_seed(const BatchSeg *__restrict__ segs, int nseg, QuadTablesD Q, double tol)
 {
     extern __shared__ long long prefix[];
+    __shared__ PotPairCtxD slot[4];
     const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long {
         return seg_adjacent(S) && S.A.hard_list ? pot_seeded(S.A) : 0;
     });
@@ -554,14 +616,15 @@ __global__ void __launch_bounds__(128) k_batch_pot_seed(const BatchSeg *__restri
         const int sg = seg_find(prefix, nseg, g);
         const BatchSeg &S = segs[sg];
         const int h = (int)(g - prefix[sg]);
-        if (S.cls == kEdge) pot_seed_item_df<kEdge>(S.A, Q, tol, h, lane);
-        else pot_seed_item_df<kVertex>(S.A, Q, tol, h, lane);
+        if (S.cls == kEdge) pot_seed_item_df<kEdge>(S.A, Q, tol, h, lane, slot[threadIdx.x >> 5]);
+        else pot_seed_item_df<kVertex>(S.A, Q, tol, h, lane, slot[threadIdx.x >> 5]);
     }
 }
 
-__global__ void __launch_bounds__(128) k_batch_pot_depth(const BatchSeg *__restrict__ segs, int nseg, QuadTablesD Q, double tol, int depth)
+__global__ void __launch_bounds__(128, kDfBlocks) k_batch_pot_depth(const BatchSeg *__restrict__ segs, int nseg, QuadTablesD Q, double tol, int depth)
 {
     extern __shared__ long long prefix[];
+    __shared__ PotPairCtxD slot[4];
     const long long total = seg_prefix(segs, nseg, prefix, [depth](const BatchSeg &S) -> long long {
         return seg_adjacent(S) && S.A.hard_list ? pot_depth_count(S.A, depth) : 0;
     });
@@ -573,8 +636,8 @@ __global__ void __launch_bounds__(128) k_batch_pot_depth(const BatchSeg *__restr
         const int idx = (int)(g - prefix[sg]);
         const PotCellItem *in = depth % 2 ? S.A.pot_q_a : S.A.pot_q_b;
         PotCellItem *out = depth % 2 ? S.A.pot_q_b : S.A.pot_q_a;
-        if (S.cls == kEdge) pot_depth_item_df<kEdge>(S.A, Q, tol, depth, in, out, idx, lane);
-        else pot_depth_item_df<kVertex>(S.A, Q, tol, depth, in, out, idx, lane);
+        if (S.cls == kEdge) pot_depth_item_df<kEdge>(S.A, Q, tol, depth, in, out, idx, lane, slot[threadIdx.x >> 5]);
+        else pot_depth_item_df<kVertex>(S.A, Q, tol, depth, in, out, idx, lane, slot[threadIdx.x >> 5]);
     }
 }
 
