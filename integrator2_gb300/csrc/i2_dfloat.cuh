@@ -44,10 +44,15 @@
 namespace i2 {
 
 // the C library's overloads stay visible beside the double-float ones declared below
+using ::acos;
 using ::atan2;
+using ::cos;
 using ::fabs;
 using ::log;
+using ::sin;
+using ::sincos;
 using ::sqrt;
+using ::tan;
 
 struct dfl {
     float hi, lo;
@@ -66,6 +71,9 @@ struct alignas(16) dfl_log_entry {
 struct alignas(8) dfl_pair {
     float hi, lo;
 };
+struct alignas(16) dfl_sincos_entry {
+    float s_hi, s_lo, c_hi, c_lo;
+};
 
 #if defined(__CUDACC__)
 static __device__ const dfl_log_entry kDfLogTableDev[385] = I2_DF_LOG_TABLE;
@@ -73,6 +81,20 @@ static __device__ const dfl_pair kDfAtanTableDev[513] = I2_DF_ATAN_TABLE;
 #endif
 static const dfl_log_entry kDfLogTableHost[385] = I2_DF_LOG_TABLE;
 static const dfl_pair kDfAtanTableHost[513] = I2_DF_ATAN_TABLE;
+#if defined(__CUDACC__)
+static __device__ const dfl_sincos_entry kDfSinCosTableDev[404] = I2_DF_SINCOS_TABLE;
+#endif
+static const dfl_sincos_entry kDfSinCosTableHost[404] = I2_DF_SINCOS_TABLE;
+
+I2_DF_HD dfl_sincos_entry df_sincos_entry(int j)
+{
+#if defined(__CUDA_ARCH__)
+    const float4 e = __ldg(reinterpret_cast<const float4 *>(kDfSinCosTableDev) + j);
+    return dfl_sincos_entry{e.x, e.y, e.z, e.w};
+#else
+    return kDfSinCosTableHost[j];
+#endif
+}
 
 I2_DF_HD dfl_log_entry df_log_entry(int j)
 {
@@ -316,6 +338,67 @@ I2_DF_HD dfl atan2(dfl y, dfl x)
     }
     if (nx) r = dfl(I2_PI_HI, I2_PI_LO) - r;
     return ny ? -r : r;
+}
+
+// sine and cosine: x - n pi/2 with pi/2 in three parts (n the nearest integer to x 2/pi), the
+// breakpoint c = j/512 nearest the remainder r (sin c, cos c tabulated), and the Taylor series
+// of s = r - c, |s| <= 2^-10: sin s = s - s^3/6 + s^5/120, cos s = 1 - s^2/2 + s^4/24 - s^6/720;
+// then the addition formulas and the quadrant of n.  For the moderate arguments of the closed
+// forms (angles and their sums, |x| < 2^10).
+I2_DF_HD void sincos(dfl x, dfl *ps, dfl *pc)
+{
+    const float n = rintf(x.hi * 0.636619772f);
+    dfl r = x;
+    if (n != 0.0f) {
+        r = r - df_two_prod(n, I2_PIO2_1);
+        r = r - df_two_prod(n, I2_PIO2_2);
+        r = r - n * I2_PIO2_3;
+    }
+    const float jf = rintf(r.hi * 512.0f);
+    const float c0 = jf * (1.0f / 512.0f);
+    const dfl sx = df_two_sum(r.hi - c0, r.lo);  // r.hi - c0 exact (Sterbenz)
+    const float sh = sx.hi, s2 = sh * sh;
+    const dfl sin_s = sx + fmaf(-0.5f * s2, sx.lo, sh * s2 * fmaf(s2, 0.00833333377f, -0.166666672f));
+    const dfl sq = df_two_prod(sh, sh);
+    const dfl half_sq = df_fast_two_sum(0.5f * sq.hi, 0.5f * fmaf(2.0f * sh, sx.lo, sq.lo));
+    const dfl cos_s = (dfl(1.0f) - half_sq) + s2 * s2 * fmaf(s2, -0.00138888892f, 0.0416666679f);
+    const dfl_sincos_entry e = df_sincos_entry(df_clamp((int)fabsf(jf), 403));
+    const dfl S = jf < 0.0f ? dfl(-e.s_hi, -e.s_lo) : dfl(e.s_hi, e.s_lo), C(e.c_hi, e.c_lo);
+    const dfl sr = S * cos_s + C * sin_s, cr = C * cos_s - S * sin_s;
+    switch (((int)n) & 3) {
+    case 0: *ps = sr; *pc = cr; break;
+    case 1: *ps = cr; *pc = -sr; break;
+    case 2: *ps = -sr; *pc = -cr; break;
+    default: *ps = -cr; *pc = sr; break;
+    }
+}
+
+I2_DF_HD dfl sin(dfl x)
+{
+    dfl s, c;
+    sincos(x, &s, &c);
+    return s;
+}
+
+I2_DF_HD dfl cos(dfl x)
+{
+    dfl s, c;
+    sincos(x, &s, &c);
+    return c;
+}
+
+I2_DF_HD dfl tan(dfl x)
+{
+    dfl s, c;
+    sincos(x, &s, &c);
+    return s / c;
+}
+
+// arccosine on [-1, 1] as atan2(sqrt((1 - c)(1 + c)), c)
+I2_DF_HD dfl acos(dfl c)
+{
+    const dfl one(1.0f);
+    return atan2(sqrt((one - c) * (one + c)), c);
 }
 
 } // namespace i2

@@ -9,6 +9,7 @@
 // The kernel chain per class mirrors the FP64 form (i2_kernels_fp64.cu) and shares its
 // finalisation, self and adaptive-potential kernels.
 #include "i2_device_f32.cuh"
+#include "i2_dfvec.cuh"
 #include "i2_batch.cuh"
 #include "i2_engine.h"
 #include "i2_finalize.cuh"
@@ -480,8 +481,14 @@ __device__ __forceinline__ void singular_mixed_item(const ClassArgs &A, const Qu
     int si, sj;
     if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
     else shifts_vertex(ci, cj, si, sj);
-    // FP64: closed-form singular part (a4 / a5) and, for the vertex class, the asymptote's constants
-    {
+    // closed-form singular part (a4 / a5) and, for the vertex class, the asymptote's constants.
+    // A pair that holds a needle cell is recomputed in FP64 after the level sweep, its J a small
+    // difference of large parts: its closed form is FP64 too (the path below), so that the fix-up
+    // reproduces the FP64 form.  Every other pair computes it in double-float, the pair translated
+    // to K_j's vertex A in FP64 (the closed forms depend on vertex differences only) and
+    // converted; the closed forms scale it by a power of two.
+    const double c3 = 0.99862953475457387;  // cos 3 degrees, as fixup_collect_item
+    if (A.panels[pr.x].v[2].w > c3 || A.panels[pr.y].v[2].w > c3) {
         const Tri Ti = rotate(load_tri(A.panels, pr.x), si), Tj = rotate(Tri{Kd.A, Kd.B, Kd.C}, sj);
         d3 psi;
         double th;
@@ -501,6 +508,30 @@ __device__ __forceinline__ void singular_mixed_item(const ClassArgs &A, const Qu
         }
         double *sg = A.sing + 4 * (long long)t;
         sg[0] = psi.x; sg[1] = psi.y; sg[2] = psi.z; sg[3] = th;
+    } else {
+        const Tri Ti0 = load_tri(A.panels, pr.x);
+        const d3 o = Kd.A;
+        const TriD Ti = to_df(rotate(Tri{Ti0.a - o, Ti0.b - o, Ti0.c - o}, si));
+        const TriD Tj = to_df(rotate(Tri{mk(0.0, 0.0, 0.0), Kd.B - o, Kd.C - o}, sj));
+        const df3 nid = to_df(ni), njd = to_df(Kd.n);
+        df3 psi;
+        dfl th;
+        if (CLS == kEdge) closed_edge(Ti, Tj, nid, njd, dfl(Si), psi, th);
+        else {
+            closed_vertex(Ti, Tj, nid, njd, dfl(Si), psi, th);
+            const df3 ta = unit(Tj.a - Tj.c), tb = unit(Tj.b - Tj.a);
+            dfl dA, dB;
+            const df3 e = vertex_direction(nid, njd, ta, tb, dA, dB);
+            const df3 w1 = cross(ta, e), p1 = e - ta, w2 = cross(tb, e), p2 = e + tb;
+            float4 *ce = reinterpret_cast<float4 *>(A.ctx_e + kVertexCtxFloats * (long long)t);
+            // w1, p1, w2, p2 (12 floats), then e
+            ce[0] = make_float4(w1.x.hi, w1.y.hi, w1.z.hi, p1.x.hi);
+            ce[1] = make_float4(p1.y.hi, p1.z.hi, w2.x.hi, w2.y.hi);
+            ce[2] = make_float4(w2.z.hi, p2.x.hi, p2.y.hi, p2.z.hi);
+            ce[3] = make_float4(e.x.hi, e.y.hi, e.z.hi, 0.0f);
+        }
+        double *sg = A.sing + 4 * (long long)t;
+        sg[0] = (double)psi.x; sg[1] = (double)psi.y; sg[2] = (double)psi.z; sg[3] = (double)th;
     }
 }
 

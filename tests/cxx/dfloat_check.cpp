@@ -51,6 +51,29 @@ int main()
         const dfl s = rnd(-40, -1);
         e_atan_small = fmaxl(e_atan_small, rel(val(i2::atan2(s, i2::fabs(b))), atan2l(val(s), fabsl(B))));
     }
+    // trigonometric functions on the closed forms' ranges
+    long double e_sin = 0, e_cos = 0, e_tan = 0, e_acos = 0, e_sin_abs = 0;
+    std::uniform_real_distribution<double> A(-7.0, 7.0), C1(-1.0, 1.0);
+    for (int i = 0; i < N; ++i) {
+        const dfl x = to_dfl((long double)A(rng) + (long double)U(rng) * 1e-9L);
+        const long double X = val(x);
+        // absolute error near the zeros, relative elsewhere
+        const long double s = sinl(X), c = cosl(X);
+        e_sin_abs = fmaxl(e_sin_abs, fabsl(val(i2::sin(x)) - s));
+        if (fabsl(s) > 1e-3L) e_sin = fmaxl(e_sin, rel(val(i2::sin(x)), s));
+        if (fabsl(c) > 1e-3L) e_cos = fmaxl(e_cos, rel(val(i2::cos(x)), c));
+        if (fabsl(c) > 1e-2L) e_tan = fmaxl(e_tan, rel(val(i2::tan(x)), tanl(X)));
+        const dfl y = to_dfl((long double)C1(rng) * (1.0L - 1e-7L));
+        e_acos = fmaxl(e_acos, rel(val(i2::acos(y)), acosl(val(y))));
+    }
+    // small arguments of sin (relative), as the closed forms' half-angles near 0
+    long double e_sin_small = 0;
+    for (int i = 0; i < N; ++i) {
+        const dfl x = rnd(-40, -3);
+        e_sin_small = fmaxl(e_sin_small, rel(val(i2::sin(x)), sinl(val(x))));
+    }
+    printf("sin %d %.3Le\ncos %d %.3Le\ntan %d %.3Le\nacos %d %.3Le\nsin_abs %d %.3Le\nsin_small %d %.3Le\n", N, e_sin, N, e_cos, N, e_tan,
+           N, e_acos, N, e_sin_abs, N, e_sin_small);
     // signed zeros and axes, as atan2
     const bool zeros = i2::atan2(dfl(0.0f), dfl(1.0f)).hi == 0.0f && !std::signbit(i2::atan2(dfl(0.0f), dfl(1.0f)).hi) &&
                        std::signbit(i2::atan2(dfl(-0.0f), dfl(1.0f)).hi) &&

@@ -1,8 +1,9 @@
 """Accuracy of the double-float arithmetic the mixed form's potential stages compute in
 (integrator2_gb300/csrc/i2_dfloat.cuh): the header compiled for the host by g++ runs seeded random
-operands through +, -, *, /, sqrt, log and atan2 and compares them with long double.  Bars: a few
-u^2 (u = 2^-24) for the arithmetic and the square root, 2^-43 for log and atan2; atan2 keeps the
-C library's signed-zero and quadrant conventions.  Also checks the generated tables are current."""
+operands through +, -, *, /, sqrt, log, atan2, sin, cos, tan and acos and compares them with long
+double.  Bars: a few u^2 (u = 2^-24) for the arithmetic and the square root, 2^-43 relative for
+the transcendental functions (sin and cos away from their zeros, 2^-46 absolute everywhere);
+atan2 keeps the C library's signed-zero and quadrant conventions.  Also checks the generated tables are current."""
 import os
 import subprocess
 
@@ -26,7 +27,8 @@ def results(tmp_path_factory):
 
 @pytest.mark.parametrize("op,bar", [("add", 3 * U2), ("sub", 3 * U2), ("mul", 5 * U2), ("div", 10 * U2), ("sqrt", 10 * U2),
                                     ("log", 2.0 ** -43), ("log_near_1", 2.0 ** -43), ("atan2", 2.0 ** -43),
-                                    ("atan2_small", 2.0 ** -43)])
+                                    ("atan2_small", 2.0 ** -43), ("sin", 2.0 ** -43), ("cos", 2.0 ** -43), ("tan", 2.0 ** -43),
+                                    ("acos", 2.0 ** -43), ("sin_small", 2.0 ** -43), ("sin_abs", 2.0 ** -46)])
 def test_dfloat_accuracy(results, op, bar):
     n, err = results[op]
     assert n >= 100000 and err <= bar, (op, err, bar)
