@@ -37,8 +37,13 @@
 
 #if defined(__CUDACC__)
 #define I2_DF_HD __host__ __device__ __forceinline__
+// the transcendental functions are called, not inlined: a kernel evaluating several of them per
+// point would otherwise outgrow the instruction cache (measured: instruction-fetch stalls were
+// the largest stall reason of the inlined version)
+#define I2_DF_CALL static __host__ __device__ __noinline__
 #else
 #define I2_DF_HD inline
+#define I2_DF_CALL static inline
 #endif
 
 namespace i2 {
@@ -276,7 +281,7 @@ I2_DF_HD dfl sqrt(dfl x)
 }
 
 // natural logarithm (Tang's table-driven method); -inf for 0, NaN below, +inf for +inf
-I2_DF_HD dfl log(dfl x)
+I2_DF_CALL dfl log(dfl x)
 {
     const float h = x.hi;
     if (!(h > 0.0f) || !(h < INFINITY)) return dfl(logf(h), 0.0f);
@@ -315,7 +320,7 @@ I2_DF_HD dfl log(dfl x)
 }
 
 // atan2 with the quadrant and signed-zero conventions of the C library's atan2
-I2_DF_HD dfl atan2(dfl y, dfl x)
+I2_DF_CALL dfl atan2(dfl y, dfl x)
 {
     const bool ny = signbit(y.hi), nx = signbit(x.hi);
     const dfl ay = ny ? -y : y, ax = nx ? -x : x;
@@ -345,7 +350,7 @@ I2_DF_HD dfl atan2(dfl y, dfl x)
 // of s = r - c, |s| <= 2^-10: sin s = s - s^3/6 + s^5/120, cos s = 1 - s^2/2 + s^4/24 - s^6/720;
 // then the addition formulas and the quadrant of n.  For the moderate arguments of the closed
 // forms (angles and their sums, |x| < 2^10).
-I2_DF_HD void sincos(dfl x, dfl *ps, dfl *pc)
+I2_DF_CALL void sincos(dfl x, dfl *ps, dfl *pc)
 {
     const float n = rintf(x.hi * 0.636619772f);
     dfl r = x;

@@ -145,7 +145,7 @@ __device__ __forceinline__ dfl edge_log_df(dfl l_from, dfl q_from, dfl l_to, dfl
 // point itself), less the shared-edge term for the edge class; evaluated edge by edge so that
 // only one edge's quantities are live at a time
 template <int CLS>
-__device__ __forceinline__ dfl pot_point_df(df3 oa, df3 ob, df3 oc, const volatile PanelJD &K, const volatile FarCtxD &F,
+__device__ __noinline__ dfl pot_point_df(df3 oa, df3 ob, df3 oc, const volatile PanelJD &K, const volatile FarCtxD &F,
                                             const volatile PotEdgeD &pe)
 {
     const dfl la = norm(oa), lb = norm(ob), lc = norm(oc);
