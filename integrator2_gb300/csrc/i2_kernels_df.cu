@@ -133,11 +133,12 @@ __device__ __forceinline__ dfl ldv(const volatile dfl &x) { return dfl(x.hi, x.l
 __device__ __forceinline__ df3 ldv(const volatile df3 &v) { return df3{ldv(v.x), ldv(v.y), ldv(v.z)}; }
 
 // ln((l_from + q_from) / (l_to + q_to)) with the reference's collinear fallback (edge_log_fp64)
+// (one division and one logarithm whichever form applies: the lanes of a warp share the call)
 __device__ __forceinline__ dfl edge_log_df(dfl l_from, dfl q_from, dfl l_to, dfl q_to)
 {
     const dfl s_to = q_to + l_to;
-    if (fabs(s_to) < (0.5 * kEpsPsi2) * l_to) return log(l_to / l_from);
-    return log((l_from + q_from) / s_to);
+    const bool collinear = fabs(s_to) < (0.5 * kEpsPsi2) * l_to;
+    return log((collinear ? l_to : l_from + q_from) / (collinear ? l_from : s_to));
 }
 
 // the integrand of the adjacent pairs' potential, sum_e t_e L_e - d Theta (far_integrand_o's
@@ -354,18 +355,25 @@ __device__ void pot_children_warp_df(const TriD &T, const int cc[4], const volat
                 area = df_half(norm(cross(Tc.b - Tc.a, Tc.c - Tc.a)));
             }
         }
-        dfl g;
+        // the point (offsets from K_j's vertices) and its weight by the child's rule; then one
+        // integrand call for the whole warp, whichever rules its lanes are on
+        df3 oa, ob, oc;
+        dfl wgt;
         if (cc[k] >= 0) {
             const int a = p / Q.nv, b = p - a * Q.nv;
             const dfl u = Q.du_u[a], vv = Q.dv_v[b];
             const df3 w = u * ((1.0f - vv) * eB + vv * eC);
-            g = pot_point_df<CLS>(Tc.a + w, dB + w, dC + w, c.K, c.F, c.pe);
-            g = ((Q.du_w[a] * u) * Q.dv_w[b]) * area * g;
+            oa = Tc.a + w;
+            ob = dB + w;
+            oc = dC + w;
+            wgt = ((Q.du_w[a] * u) * Q.dv_w[b]) * area;
         } else {
-            const df3 x = Q.L1[p] * Tc.a + Q.L2[p] * Tc.b + Q.L3[p] * Tc.c;
-            g = pot_point_df<CLS>(x, x - ldv(c.K.B), x - ldv(c.K.C), c.K, c.F, c.pe);
-            g = Q.w[p] * area * g;
+            oa = Q.L1[p] * Tc.a + Q.L2[p] * Tc.b + Q.L3[p] * Tc.c;
+            ob = oa - ldv(c.K.B);
+            oc = oa - ldv(c.K.C);
+            wgt = Q.w[p] * area;
         }
+        const dfl g = wgt * pot_point_df<CLS>(oa, ob, oc, c.K, c.F, c.pe);
         if (k == 0) acc0 += g;
         else if (k == 1) acc1 += g;
         else if (k == 2) acc2 += g;
