@@ -924,7 +924,9 @@ def gpu_arm(args):
     if "batch" in forms:
         line["batch"] = {"shape": {"threads": forms["batch"]["shape"][0], "blocks_per_sm": forms["batch"]["shape"][1],
                                    "lanes_per_pair": forms["batch"]["shape"][2],
-                                   "registers": {0: "unconstrained", 1: "capped at 128", 2: "capped at 85"}[int(forms["batch"]["shape"][3])]},
+                                   "registers": {name: {0: "unconstrained", 1: "capped at 128", 2: "capped at 85"}[
+                                       (int(forms["batch"]["shape"][3]) // place) % 3]
+                                                 for name, place in (("vertex", 1), ("edge", 3), ("near", 9))}},
                          "cuda_graph": forms["batch"]["graph"]}
     rk = "mixed" if "mixed" in roof else ("fp64" if "fp64" in roof else None)
     if rk:

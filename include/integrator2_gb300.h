@@ -224,8 +224,9 @@ i2_status i2_batch_set_stream(i2_batch_t *batch, void *stream);
 i2_status i2_batch_add(i2_batch_t *batch, const i2_mesh_t *mesh, i2_pair_class cls, const int32_t *rows, int64_t n,
                        int32_t row_stride, int32_t *segment);
 /* times the candidate launch shapes (threads per block, resident blocks per SM, lanes per pair,
- * register variant: 0 unconstrained, 1 capped at 128 per thread, 2 capped at 85) on the batch and keeps the
- * fastest; the chosen shape is returned in shape[4] (may be NULL) */
+ * register variant of each pair class's level kernel: 0 unconstrained, 1 capped at 128 per thread,
+ * 2 capped at 85) on the batch and keeps the fastest; the chosen shape is returned in shape[4] (may
+ * be NULL), the variants as one code v_vertex + 3 v_edge + 9 v_disjoint in shape[3] */
 i2_status i2_batch_autotune(i2_batch_t *batch, int32_t *shape);
 /* enqueues the batch on its stream (graph replay after the first call); asynchronous */
 i2_status i2_batch_run(i2_batch_t *batch);

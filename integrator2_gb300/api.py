@@ -315,7 +315,7 @@ class BatchEvaluator:
 
     def autotune(self):
         """times the candidate launch shapes; returns (threads, blocks per SM, lanes per pair,
-        register variant)"""
+        register variants as v_vertex + 3 v_edge + 9 v_disjoint)"""
         shape = np.zeros(4, np.int32)
         call("i2_batch_autotune", self._h, _p(shape))
         return tuple(int(x) for x in shape)

@@ -1429,22 +1429,36 @@ i2_status i2_batch_autotune(i2_batch_t *batch, int32_t *shape)
         I2_CHECK_CUDA(cudaEventCreate(&e1));
         float best = 1e30f;
         int bt = batch->threads, bb = batch->blocks_per_sm, bg = batch->g_cap, bv = batch->variant;
-        for (int variant : {0, 1, 2}) {
+        auto time_shape = [&](int threads, int bps, int gcap, int variant) {
+            batch_enqueue(batch, batch->stream, threads, bps, gcap, variant);  // warm-up
+            I2_CHECK_CUDA(cudaEventRecord(e0, batch->stream));
+            batch_enqueue(batch, batch->stream, threads, bps, gcap, variant);
+            I2_CHECK_CUDA(cudaEventRecord(e1, batch->stream));
+            I2_CHECK_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            I2_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) { best = ms; bt = threads; bb = bps; bg = gcap; bv = variant; }
+        };
+        // the shared shape with one register variant for every class ...
+        for (int u : {0, 1, 2}) {
+            const int variant = 13 * u;  // digit u for each of the three classes
             for (int threads : {128, 256}) {
                 const int maxb = i2::batch_max_blocks_per_sm(threads, variant);
                 if (maxb <= 0) continue;
-                for (int bps : {maxb, std::max(1, maxb / 2)}) {
-                    for (int gcap : {8, 16, 32}) {
-                        batch_enqueue(batch, batch->stream, threads, bps, gcap, variant);  // warm-up
-                        I2_CHECK_CUDA(cudaEventRecord(e0, batch->stream));
-                        batch_enqueue(batch, batch->stream, threads, bps, gcap, variant);
-                        I2_CHECK_CUDA(cudaEventRecord(e1, batch->stream));
-                        I2_CHECK_CUDA(cudaEventSynchronize(e1));
-                        float ms = 0;
-                        I2_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                        if (ms < best) { best = ms; bt = threads; bb = bps; bg = gcap; bv = variant; }
-                    }
-                }
+                for (int bps : {maxb, std::max(1, maxb / 2)})
+                    for (int gcap : {8, 16, 32}) time_shape(threads, bps, gcap, variant);
+            }
+        }
+        // ... then each class's variant in turn, the others held (a class's level kernel has its
+        // own register footprint: the disjoint class's fits 80 registers, the vertex class's
+        // spills there); blocks per SM at the new variants' limit
+        for (int place : {1, 3, 9}) {
+            const int base = bv;
+            for (int u : {0, 1, 2}) {
+                const int variant = base - ((base / place) % 3) * place + u * place;
+                if (variant == base) continue;
+                const int maxb = i2::batch_max_blocks_per_sm(bt, variant);
+                if (maxb > 0) time_shape(bt, bb == i2::batch_max_blocks_per_sm(bt, base) ? maxb : std::min(bb, maxb), bg, variant);
             }
         }
         cudaEventDestroy(e0);

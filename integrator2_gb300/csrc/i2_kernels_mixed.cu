@@ -449,9 +449,10 @@ __device__ float duffy_total_f(const PanelF *__restrict__ P, int pi, int pj, int
     return total;
 }
 
-// s ln s term along the shared edge of a common-edge pair, set up in FP64 once per pair
-__device__ __forceinline__ void edge_sigma_setup(const ClassArgs &A, int2 pr, int si, int sj, const PanelJf &Kf, double Si, f3 &m_in,
-                                                 float &c, float &h, double &sig)
+// s ln s term along the shared edge of a common-edge pair, set up in FP64 (pairs holding a
+// needle cell; the others form it in double-float in singular_mixed_item)
+__device__ __forceinline__ void edge_sigma_setup(const ClassArgs &A, int2 pr, int si, int sj, double Si, f3 &m_in, float &c, float &h,
+                                                 double &sig)
 {
     const PanelJ K = load_panel(A.panels, pr.y);
     const Tri Ti0 = load_tri(A.panels, pr.x);
@@ -466,7 +467,26 @@ __device__ __forceinline__ void edge_sigma_setup(const ClassArgs &A, int2 pr, in
     c = (float)cd;
     h = (float)hd;
     sig = (5.0 / 9.0) * cd * Si * hd;
-    (void)Kf;
+}
+
+// the shared-edge term's constants of a common-edge pair in ctx_e (written once per pair by the
+// closed-form kernel, read by the potential's FP32 tiers): m_in, c, h, then the integral over K_i
+// as a double's two halves
+__device__ __forceinline__ void store_edge_sigma(const ClassArgs &A, long long t, f3 m_in, float c, float h, double sig)
+{
+    float4 *ce = reinterpret_cast<float4 *>(A.ctx_e + kVertexCtxFloats * t);
+    ce[0] = make_float4(m_in.x, m_in.y, m_in.z, c);
+    ce[1] = make_float4(h, __int_as_float(__double2hiint(sig)), __int_as_float(__double2loint(sig)), 0.0f);
+}
+
+__device__ __forceinline__ void load_edge_sigma(const ClassArgs &A, long long t, f3 &m_in, float &c, float &h, double &sig)
+{
+    const float4 *ce = reinterpret_cast<const float4 *>(A.ctx_e + kVertexCtxFloats * t);
+    const float4 a = ce[0], b = ce[1];
+    m_in = f3{a.x, a.y, a.z};
+    c = a.w;
+    h = b.x;
+    sig = __hiloint2double(__float_as_int(b.y), __float_as_int(b.z));
 }
 
 template <int CLS>
@@ -492,8 +512,14 @@ __device__ __forceinline__ void singular_mixed_item(const ClassArgs &A, const Qu
         const Tri Ti = rotate(load_tri(A.panels, pr.x), si), Tj = rotate(Tri{Kd.A, Kd.B, Kd.C}, sj);
         d3 psi;
         double th;
-        if (CLS == kEdge) closed_edge(Ti, Tj, ni, Kd.n, Si, psi, th);
-        else {
+        if (CLS == kEdge) {
+            closed_edge(Ti, Tj, ni, Kd.n, Si, psi, th);
+            f3 m_in;
+            float c, h;
+            double sig;
+            edge_sigma_setup(A, pr, si, sj, Si, m_in, c, h, sig);
+            store_edge_sigma(A, t, m_in, c, h, sig);
+        } else {
             closed_vertex(Ti, Tj, ni, Kd.n, Si, psi, th);
             const d3 ta = unit(Tj.a - Tj.c), tb = unit(Tj.b - Tj.a);
             double dA, dB;
@@ -516,8 +542,16 @@ __device__ __forceinline__ void singular_mixed_item(const ClassArgs &A, const Qu
         const df3 nid = to_df(ni), njd = to_df(Kd.n);
         df3 psi;
         dfl th;
-        if (CLS == kEdge) closed_edge(Ti, Tj, nid, njd, dfl(Si), psi, th);
-        else {
+        if (CLS == kEdge) {
+            closed_edge(Ti, Tj, nid, njd, dfl(Si), psi, th);
+            // the shared edge JB -> JC (Tj rotated: JA off the edge), as edge_sigma_setup
+            const df3 tau = unit(Tj.c - Tj.b), m = cross(tau, njd), w = Ti.a - Tj.b;
+            const df3 perp = w - dot(w, tau) * tau;
+            const dfl hd = norm(perp);
+            const df3 mi = (1.0f / hd) * perp;
+            const dfl cd = -dot(m, mi);
+            store_edge_sigma(A, t, f3{mi.x.hi, mi.y.hi, mi.z.hi}, cd.hi, hd.hi, (double)(((5.0 / 9.0) * cd) * (dfl(Si) * hd)));
+        } else {
             closed_vertex(Ti, Tj, nid, njd, dfl(Si), psi, th);
             const df3 ta = unit(Tj.a - Tj.c), tb = unit(Tj.b - Tj.a);
             dfl dA, dB;
@@ -556,14 +590,13 @@ __device__ __forceinline__ void tier1_mixed_item(const ClassArgs &A, const QuadT
     int si, sj;
     if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
     else shifts_vertex(ci, cj, si, sj);
-    const double Si = A.panels[pr.x].v[0].w;
     const PanelJf K = load_panel_f(A.panels_f, pr.y);
     const FarCtxF F{crossf(K.ta, K.n), crossf(K.tb, K.n), crossf(K.tc, K.n)};
     f3 m_in = f3{0, 0, 0};
     float c = 0.0f, h = 1.0f;
     double sig = 0.0;
     const int p1v = (sj + 1) % 3;  // JB, start of the shared edge in K_j's orientation
-    if (CLS == kEdge) edge_sigma_setup(A, pr, si, sj, K, Si, m_in, c, h, sig);
+    if (CLS == kEdge) load_edge_sigma(A, t, m_in, c, h, sig);
     const double pmd = group_sum8((double)duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, K, F, p1v, m_in, c, h, Qf.du_u, Qf.du_w, Qf.nu,
                                                              Qf.dv_v, Qf.dv_w, Qf.nv, g, kTier1Lanes)) + sig;
     if (g == 0) A.padj[t] = kInv4Pi * pmd;
@@ -610,12 +643,11 @@ __device__ __forceinline__ void tier2_mixed_item(const ClassArgs &A, const QuadT
     else shifts_vertex(ci, cj, si, sj);
     const PanelJf Kf = load_panel_f(A.panels_f, pr.y);
     const FarCtxF Ff{crossf(Kf.ta, Kf.n), crossf(Kf.tb, Kf.n), crossf(Kf.tc, Kf.n)};
-    const double Si = A.panels[pr.x].v[0].w;
     f3 m_in = f3{0, 0, 0};
     float c = 0.0f, hh = 1.0f;
     double sig = 0.0;
     const int p1v = (sj + 1) % 3;
-    if (CLS == kEdge) edge_sigma_setup(A, pr, si, sj, Kf, Si, m_in, c, hh, sig);
+    if (CLS == kEdge) load_edge_sigma(A, t, m_in, c, hh, sig);
     // the lanes' Kahan partial sums added in FP64 (an FP32 butterfly adds noise the tier bar sees)
     const double ph = warp_sum((double)duffy_total_f<CLS>(A.panels_f, pr.x, pr.y, si, Kf, Ff, p1v, m_in, c, hh, Qf.hi_u, Qf.hi_uw,
                                                           Qf.hi_nu, Qf.hi_v, Qf.hi_vw, Qf.hi_nv, lane, 32)) + sig;
@@ -1127,10 +1159,13 @@ int batch_levels_occupancy(int threads, int variant, int cls)
 
 } // namespace
 
+// the register variant of class cls in a batch's variant code (one base-3 digit per class)
+static int class_variant(int code, int cls) { return (code / (cls == kVertex ? 1 : (cls == kEdge ? 3 : 9))) % 3; }
+
 int batch_max_blocks_per_sm(int threads, int variant)
 {
     int nb = 0;
-    for (int cls : {kVertex, kEdge, kFar}) nb = std::max(nb, batch_levels_occupancy(threads, variant, cls));
+    for (int cls : {kVertex, kEdge, kFar}) nb = std::max(nb, batch_levels_occupancy(threads, class_variant(variant, cls), cls));
     return nb;
 }
 
@@ -1146,10 +1181,11 @@ cudaError_t launch_batch_levels(const BatchSeg *segs, int nseg, const bool prese
     void *args[] = {(void *)&segs, (void *)&nseg, (void *)&q, (void *)&mode, (void *)&level, (void *)&tol, (void *)&kmax, (void *)&G_cap};
     for (int cls : {kVertex, kEdge, kFar}) {
         if (!present[cls]) continue;
-        const int maxb = batch_levels_occupancy(threads, variant, cls);
+        const int v = class_variant(variant, cls);
+        const int maxb = batch_levels_occupancy(threads, v, cls);
         if (maxb <= 0) return cudaErrorInvalidConfiguration;
         const int blocks = std::max(1, sms) * std::max(1, std::min(bps > 0 ? bps : maxb, maxb));
-        const cudaError_t e = cudaLaunchCooperativeKernel(batch_levels_fn(variant, cls), dim3(blocks), dim3(threads), args, 0, s);
+        const cudaError_t e = cudaLaunchCooperativeKernel(batch_levels_fn(v, cls), dim3(blocks), dim3(threads), args, 0, s);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
@@ -1182,7 +1218,8 @@ __global__ void __launch_bounds__(128) k_batch_singular(const BatchSeg *__restri
 // six lanes each) in one launch: global warps [0, w1) take the tier-1 items, warps [w1, w1 + w2)
 // the self pairs, so every branch below is uniform over a warp.  prefix holds two prefix-sum
 // arrays (tier-1 items, self pairs) of nseg + 1 entries each.
-__global__ void __launch_bounds__(128) k_batch_tier1_self(const BatchSeg *__restrict__ segs, int nseg, QuadTablesF Qf, QuadTables Q,
+// (at most 128 registers: four blocks per SM, without spills)
+__global__ void __launch_bounds__(128, 4) k_batch_tier1_self(const BatchSeg *__restrict__ segs, int nseg, QuadTablesF Qf, QuadTables Q,
                                                           int self_sign)
 {
     extern __shared__ long long prefix[];
