@@ -239,18 +239,21 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
             }
             // K_i's vertices as offsets from each vertex of K_j, in the (rotated) order the
             // integrand expects: every point-to-vertex offset keeps full relative precision.
-            // The disjoint class keeps only the offsets from A and forms a point's offsets from B
-            // and C as (o_A - e_hi) - e_lo with K_j's edges B - A, C - A in double-float: o_A's
-            // rounding is then a shift of the point shared by all three offsets (harmless), the
-            // two subtractions add half an ulp each, and no rounded edge vector enters the logs
-            // (that would be a per-pair bias, amplified by the cancellation in Psi).  Two
-            // sub-cell walks and 18 live floats fewer.
+            // The disjoint and common-vertex classes keep only the offsets from one vertex (A; the
+            // shared vertex for the common-vertex class) and form a point's offsets from the
+            // other two as (o_A - e_hi) - e_lo with K_j's edges in double-float: o_A's rounding is
+            // then a shift of the point shared by all three offsets (harmless), the two
+            // subtractions add half an ulp each, and no rounded edge vector enters the logs (that
+            // would be a per-pair bias, amplified by the cancellation in Psi).  Two sub-cell walks
+            // and 18 live floats fewer.  The common-edge class keeps three offset triangles: its
+            // points come close to two of K_j's vertices (the shared edge's ends), where an offset
+            // formed by subtraction would lose its relative precision.
             TriF T0, T1, T2;
             f3 ABh, ABl, ACh, ACl;
             df_offsets(A.panels_f, pr.x, pr.y, origin, T0.a, T0.b, T0.c);
-            if (CLS == kFar) {
-                df_edge_pair(A.panels_f, pr.y, 1, 0, ABh, ABl);
-                df_edge_pair(A.panels_f, pr.y, 2, 0, ACh, ACl);
+            if (CLS != kEdge) {
+                df_edge_pair(A.panels_f, pr.y, (origin + 1) % 3, origin, ABh, ABl);
+                df_edge_pair(A.panels_f, pr.y, (origin + 2) % 3, origin, ACh, ACl);
             } else {
                 df_offsets(A.panels_f, pr.x, pr.y, (origin + 1) % 3, T1.a, T1.b, T1.c);
                 df_offsets(A.panels_f, pr.x, pr.y, (origin + 2) % 3, T2.a, T2.b, T2.c);
@@ -258,7 +261,7 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
             for (int s = lane_g * per_lane; s < (lane_g + 1) * per_lane; ++s) {
                 const TriF U0 = subcellf(T0, level, s);
                 TriF U1, U2;
-                if (CLS != kFar) {
+                if (CLS == kEdge) {
                     U1 = subcellf(T1, level, s);
                     U2 = subcellf(T2, level, s);
                 }
@@ -268,7 +271,7 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
                     const float l1 = Qf.L1[g], l2 = Qf.L2[g], l3 = Qf.L3[g];
                     const f3 oA = l1 * U0.a + l2 * U0.b + l3 * U0.c;
                     f3 oB, oC;
-                    if (CLS == kFar) {
+                    if (CLS != kEdge) {
                         oB = (oA - ABh) - ABl;
                         oC = (oA - ACh) - ACl;
                     } else {
