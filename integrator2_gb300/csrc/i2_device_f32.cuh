@@ -36,6 +36,7 @@ static_assert(sizeof(PanelF) == 160, "FP32 panel record is 160 bytes");
 struct PanelJf {
     f3 AB, AC, n, ta, tb, tc;
     float S, lenA, lenB, lenC;
+    float rA, rB, rC;  // 1 / lenA, 1 / lenB, 1 / lenC, rounded from FP64
 };
 
 __device__ __forceinline__ f3 df_sub(float4 ahi, float4 alo, float4 bhi, float4 blo)
@@ -96,7 +97,22 @@ __device__ __forceinline__ PanelJf load_panel_f(const PanelF *__restrict__ P, in
     r.ta = xyzf(w[7]);
     r.tb = xyzf(w[8]);
     r.tc = xyzf(w[9]);
+    r.rA = w[7].w;
+    r.rB = w[8].w;
+    r.rC = w[9].w;
     return r;
+}
+
+// n / d from an approximate reciprocal and one correction of the quotient (Markstein's method,
+// IBM J. Res. Dev. 34(1), 1990): q0 = n r, e = n - q0 d exactly (one FMA), q = q0 + e r.  Within an
+// ulp of the correctly rounded quotient for the normal operands here (|d| < 2^126), at about a
+// third of the cost of an IEEE division; an infinite first quotient (d = 0) is returned as it is.
+__device__ __forceinline__ float div_q(float n, float d)
+{
+    const float r = __fdividef(1.0f, d);
+    const float q0 = n * r;
+    const float q = fmaf(fmaf(-q0, d, n), r, q0);
+    return isfinite(q0) ? q : q0;
 }
 
 // ln((l_P + q_P) / (l_Q + q_Q)) for the edge P -> Q of length L, q = (x - P).tau, from sums
@@ -131,7 +147,35 @@ __device__ __forceinline__ float edge_log_f32(float lP, float qP, f3 oP, float l
         n = (lP + qP) * L * (s - qP - qQ);
         d = s * h2;
     }
-    return log1pf(fminf(n / d, 3.0e38f));
+    return log1pf(fminf(div_q(n, d), 3.0e38f));
+}
+
+// lambda = ln((l_P + q_P) / (l_Q + q_Q)) / L for the edge P -> Q with rho = 1 / L rounded once
+// from FP64: edge_log_f32's cases with the factor L of their numerators moved into the
+// denominators as rho, and the result multiplied by rho.  As with L in both places before, the
+// rounding of rho enters x = n / d and the final factor alike and cancels to first order (for
+// small x, lambda ~ n / (d / rho) rho); it saves the division by L.
+__device__ __forceinline__ float edge_lambda_f32(float lP, float qP, f3 oP, float lQ, float qQ, f3 oQ, f3 tau, float rho)
+{
+    const float s = lP + lQ;
+    const f3 r = crossf(lP < lQ ? oP : oQ, tau);
+    const float h2 = dotf(r, r);
+    const float num = (lP + qP) * (lQ - qQ);
+    float n, d;
+    if (qQ >= 0.0f) {
+        n = s + qP + qQ;
+        d = rho * s * (lQ + qQ);
+    } else if (qP <= 0.0f) {
+        n = s - qP - qQ;
+        d = rho * s * (lP - qP);
+    } else if (num > 2.0f * h2) {
+        n = num - h2;
+        d = h2;
+    } else {
+        n = (lP + qP) * (s - qP - qQ);
+        d = rho * s * h2;
+    }
+    return log1pf(fminf(div_q(n, d), 3.0e38f)) * rho;
 }
 
 struct FarCtxF {
@@ -156,8 +200,9 @@ __device__ __forceinline__ void far_integrand_f(f3 oa, f3 ob, f3 oc, const Panel
 }
 
 // The same three quantities for a point away from K_j (the disjoint class), in a form whose FP32
-// errors do not add up into a bias.  With lambda_e = L_e / |e| (divided by the same rounded |e|
-// that scales L_e's argument, so that rounding cancels to first order) and e_a + e_b + e_c = 0:
+// errors do not add up into a bias.  With lambda_e = L_e / |e| (edge_lambda_f32: the same rounded
+// 1/|e| scales L_e's argument and multiplies the log, so that rounding cancels to first order)
+// and e_a + e_b + e_c = 0:
 //   Psi = sum_e lambda_e e_e = (lambda_a - lambda_c) e_a + (lambda_b - lambda_c) e_b,
 // where the rounding of the edge vectors only multiplies differences of lambda (sum_e tau_e L_e
 // with rounded unit tangents cancels down to Psi and keeps their rounding at full size), and
@@ -170,9 +215,9 @@ __device__ __forceinline__ void far_field_integrand_f(f3 oa, f3 ob, f3 oc, const
                                                       float &pot)
 {
     const float la = normf(oa), lb = normf(ob), lc = normf(oc);
-    const float lam_c = edge_log_f32(la, dotf(oa, K.tc), oa, lb, dotf(ob, K.tc), ob, K.tc, K.lenC) / K.lenC;  // A -> B
-    const float lam_a = edge_log_f32(lb, dotf(ob, K.ta), ob, lc, dotf(oc, K.ta), oc, K.ta, K.lenA) / K.lenA;  // B -> C
-    const float lam_b = edge_log_f32(lc, dotf(oc, K.tb), oc, la, dotf(oa, K.tb), oa, K.tb, K.lenB) / K.lenB;  // C -> A
+    const float lam_c = edge_lambda_f32(la, dotf(oa, K.tc), oa, lb, dotf(ob, K.tc), ob, K.tc, K.rC);  // A -> B
+    const float lam_a = edge_lambda_f32(lb, dotf(ob, K.ta), ob, lc, dotf(oc, K.ta), oc, K.ta, K.rA);  // B -> C
+    const float lam_b = edge_lambda_f32(lc, dotf(oc, K.tb), oc, la, dotf(oa, K.tb), oa, K.tb, K.rB);  // C -> A
     psi = (lam_a - lam_c) * F.ea + (lam_b - lam_c) * F.eb;
     const float d = dotf(K.n, oa);
     const float den = la * lb * lc + dotf(oa, ob) * lc + dotf(ob, oc) * la + dotf(oc, oa) * lb;

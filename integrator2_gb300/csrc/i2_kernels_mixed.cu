@@ -109,7 +109,7 @@ __device__ __forceinline__ void vertex_integrand_f(f3 oA, f3 oB, f3 oC, const Pa
     const float oe = dotf(oA, Vx.e);
     f3 r = oA - oe * Vx.e;
     r = r - dotf(r, Vx.e) * Vx.e;
-    const float q = oe > 0.0f ? dotf(r, r) / (lA + oe) : lA - oe;
+    const float q = oe > 0.0f ? div_q(dotf(r, r), lA + oe) : lA - oe;
     const float s1 = atan2f(dotf(r, Vx.w1), q * Vx.c1 - dotf(r, Vx.p1));
     const float s2 = atan2f(dotf(r, Vx.w2), q * Vx.c2 - dotf(r, Vx.p2));
     th = 2.0f * atan2f(2.0f * K.S * dotf(K.n, oA), den) - 2.0f * (s1 + s2);
