@@ -741,7 +741,10 @@ FAR_CHAIN_DRAM_BYTES = 147407616 + 91512576
 # FP32 operation counts of the far-field integrand (far_field_integrand_f with the point's
 # offsets: o_A interpolated from the sub-cell, 15 flops; o_B and o_C as o_A minus K_j's edges in
 # double-float, 12 flops): flops, sqrtf, divide, log1pf, atan2f
-POINT_OPS_F32 = {"far": (185, 3, 6, 3, 1)}
+# the FP32 far-field integrand (far_field_integrand_f): its three divisions by |e| are
+# multiplications by 1/|e| (counted in the flops), its three quotients are counted at the measured
+# cost of an IEEE division
+POINT_OPS_F32 = {"far": (188, 3, 3, 3, 1)}
 
 
 def point_flops_f32(cal):
