@@ -738,18 +738,25 @@ def adjoint_section(args):
 # summed over the chain's six launches); the chain is compute-bound, this is mostly per-pair state
 FAR_CHAIN_DRAM_BYTES = 147407616 + 91512576
 
-# FP32 operation counts of the far-field integrand (far_field_integrand_f with the point's
-# offsets: o_A interpolated from the sub-cell, 15 flops; o_B and o_C as o_A minus K_j's edges in
-# double-float, 12 flops): flops, sqrtf, divide, log1pf, atan2f
-# the FP32 far-field integrand (far_field_integrand_f): its three divisions by |e| are
-# multiplications by 1/|e| (counted in the flops), its three quotients are counted at the measured
-# cost of an IEEE division
+# The algorithmic work of one far-field point, frozen from the reference's formula (thetaPsi,
+# evaluatorJ3DK.cu:266-313; the hand count the roofline is defined on): about 150 flops, 3 sqrt,
+# 12 divisions, 3 logs and 1 atan2; the transcendentals and divisions are weighted by their
+# measured cost in the form's precision.  flops, sqrt, divide, log, atan2:
+FROZEN_FAR = (150, 3, 12, 3, 1)
+# the operations the kernels execute for the same point (the formulations avoid most divisions):
+# FP32 far_field_integrand_f with the point's offsets (o_A interpolated, 15 flops; o_B and o_C from
+# double-float edges, 12 flops), its divisions by |e| as multiplications, 3 quotients
 POINT_OPS_F32 = {"far": (188, 3, 3, 3, 1)}
 
 
-def point_flops_f32(cal):
-    a, sq, dv, lg, at = POINT_OPS_F32["far"]
+def point_flops_f32(cal, ops=None):
+    a, sq, dv, lg, at = ops or POINT_OPS_F32["far"]
     return a + 2.0 * (sq * cal[8] + dv * cal[9] + lg * cal[10] + at * cal[11])
+
+
+def point_flops_frozen(w):
+    a, sq, dv, lg, at = FROZEN_FAR
+    return a + sq * w["sqrt"] + dv * w["div"] + lg * w["log"] + at * w["atan2"]
 
 
 def gpu_arm(args):
@@ -875,19 +882,26 @@ def gpu_arm(args):
     if rank != 0:
         return
 
-    def far_roofline(form, per_point, peak, unit_note):
+    def far_roofline(form, per_point, per_point_exec, peak, unit_note):
         lev = form["levels"][2]
         evals = int(sum(np.sum(lev >= L) * 4 ** L for L in range(6)))
-        flops = evals * 13 * per_point
-        achieved = flops / (form["cls_ms"][2] * 1e-3) / 1e12
+        seconds = form["cls_ms"][2] * 1e-3
+        achieved = evals * 13 * per_point / seconds / 1e12
+        executed = evals * 13 * per_point_exec / seconds / 1e12
         return {"achieved": achieved, "peak": peak, "frac": achieved / peak, "flops_per_point": per_point,
-                "point_evaluations": evals * 13, "note": unit_note}
+                "point_evaluations": evals * 13, "note": unit_note,
+                "executed_ops": {"flops_per_point": per_point_exec, "achieved": executed, "frac": executed / peak,
+                                 "note": "the operations the kernel performs per point (fewer divisions than the frozen formula)"}}
 
     roof = {}
+    frozen_note = "frozen per-point work of the reference's far-field formula: 150 flops, 3 sqrt, 12 div, 3 log, 1 atan2"
     if "mixed" in forms:
-        roof["mixed"] = far_roofline(forms["mixed"], point_flops_f32(cal), float(cal[1]), "FP32 FMA peak measured live (i2_calibrate_pipes)")
+        w32 = {"sqrt": 2.0 * cal[8], "div": 2.0 * cal[9], "log": 2.0 * cal[10], "atan2": 2.0 * cal[11]}
+        roof["mixed"] = far_roofline(forms["mixed"], point_flops_frozen(w32), point_flops_f32(cal), float(cal[1]),
+                                     "FP32 FMA peak measured live (i2_calibrate_pipes); " + frozen_note)
     if "fp64" in forms:
-        roof["fp64"] = far_roofline(forms["fp64"], point_flops("far", w), float(cal[0]), "FP64 FMA peak measured live")
+        roof["fp64"] = far_roofline(forms["fp64"], point_flops_frozen(w), point_flops("far", w), float(cal[0]),
+                                    "FP64 FMA peak measured live; " + frozen_note)
     acc = {name: accuracy(V, C, lists, f["J"], f["P"], f["levels"]) for name, f in forms.items()}
     population = {name: full_population(lists, f, forms["fp64"]) for name, f in forms.items()
                   if name != "fp64" and "fp64" in forms}
