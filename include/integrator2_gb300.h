@@ -67,6 +67,10 @@ typedef enum i2_error_control {
     I2_RELATIVE_ERROR_CONTROL = 2    /* scale-invariant: |J_L - J_{L-1}| <= tol |J_L| */
 } i2_error_control;
 
+/* FP64: every stage in FP64 (matches the reference's CUDA build to 1e-12).  MIXED: the regular-part
+ * quadrature in FP32 with compensated sums; the closed forms, the potential's tier 2b and adaptive
+ * rule in double-float arithmetic on the FP32 pipe (about 2^-44 relative); the estimator's level
+ * differences, pairs holding a needle cell and self pairs in FP64 */
 typedef enum i2_precision { I2_PRECISION_FP64 = 0, I2_PRECISION_MIXED = 1 } i2_precision;
 
 typedef enum i2_channel {
@@ -214,8 +218,9 @@ i2_status i2_evaluator_backward_class(i2_evaluator_t *ev, i2_pair_class cls, con
  * (three in all), a fixed number of launches whatever the number of segments; the whole run is
  * captured into a CUDA graph on the first i2_batch_run and replayed afterwards.  Settings
  * (rule, error control, potential rule) come from the integrator given at creation; the
- * batched form computes in mixed precision (FP32 bulk, FP64 singular parts, estimator and hard
- * pairs) whatever the integrator's precision. */
+ * batched form computes in mixed precision (FP32 bulk; double-float closed forms, tier 2b and
+ * adaptive potential; FP64 estimator differences and needle pairs) whatever the integrator's
+ * precision. */
 typedef struct i2_batch i2_batch_t;
 i2_status i2_batch_create(const i2_integrator_t *settings, i2_batch_t **out);
 void i2_batch_destroy(i2_batch_t *batch);
