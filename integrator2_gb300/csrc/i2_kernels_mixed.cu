@@ -154,6 +154,11 @@ __device__ __forceinline__ LevelLists level_lists(const ClassArgs &A, int level,
                       level % 2 ? A.act_a : A.act_b, A.cnt + level};
 }
 
+// relative error control: level 0's pass also integrates level 1 (see level_items_mixed), and
+// the level-1 pass is skipped
+__device__ __forceinline__ bool fuse_levels01(int level, int mode, int kmax) { return level == 0 && mode == kAdaptiveRelative && kmax >= 1; }
+__host__ __device__ __forceinline__ bool level_pass_needed(int level, int mode) { return !(level == 1 && mode == kAdaptiveRelative); }
+
 template <int CLS>
 __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, const QuadTablesF &Qf, int level, int mode, double tol,
                                   int kmax, long long first, long long stride, int G_cap)
@@ -179,6 +184,13 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
     const long long total = (long long)count * G;
     const long long total_r = block_group ? total : (total + 31) & ~31LL;
     const float sub_scale = ldexpf(1.0f, -2 * level);
+    // Relative error control always computes levels 0 and 1 of every pair (the criterion compares
+    // two levels), so level 0 does both: one lane per pair (G is 1 at level 0) integrates the
+    // pair's 13 level-0 points and its 4 x 13 level-1 points with one set-up, and decides at level 1
+    // with level 0's sums still in registers -- no level-0 round trip through `cur`, no second
+    // set-up; the level-1 pass is then skipped (level_pass_needed).  The sums are the same
+    // operations as in two passes.
+    const bool fused01 = fuse_levels01(level, mode, kmax);
     for (long long idx = first; idx < total_r; idx += stride) {
         const bool valid = idx < total;
         const int slot = (int)(idx / G);
@@ -187,6 +199,8 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
         acc5 acc = zero5();
         kahan5 ks;  // this lane's sums (value s - c); zero for lanes past the last item
         kahan_zero(ks);
+        kahan5 ks0;  // level 0's sums when levels 0 and 1 are fused (ks then holds level 1's)
+        kahan_zero(ks0);
         int2 pr = make_int2(0, 0);
         if (valid) {
             pr = A.pairs[t];
@@ -258,12 +272,13 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
                 df_offsets(A.panels_f, pr.x, pr.y, (origin + 1) % 3, T1.a, T1.b, T1.c);
                 df_offsets(A.panels_f, pr.x, pr.y, (origin + 2) % 3, T2.a, T2.b, T2.c);
             }
-            for (int s = lane_g * per_lane; s < (lane_g + 1) * per_lane; ++s) {
-                const TriF U0 = subcellf(T0, level, s);
+            // sub-cell sc of level lev into the Kahan sums k (sub-cell area Ss)
+            auto add_subcell = [&](kahan5 &k, int lev, int sc, float Ss) {
+                const TriF U0 = subcellf(T0, lev, sc);
                 TriF U1, U2;
                 if (CLS == kEdge) {
-                    U1 = subcellf(T1, level, s);
-                    U2 = subcellf(T2, level, s);
+                    U1 = subcellf(T1, lev, sc);
+                    U2 = subcellf(T2, lev, sc);
                 }
                 float c0 = 0, c1 = 0, c2 = 0, c3 = 0, c4 = 0;
 #pragma unroll 1
@@ -290,11 +305,22 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
                     c3 = fmaf(w, th, c3);
                     c4 = fmaf(w, pot, c4);
                 }
-                kahan_add(ks, 0, Ssub * c0);
-                kahan_add(ks, 1, Ssub * c1);
-                kahan_add(ks, 2, Ssub * c2);
-                kahan_add(ks, 3, Ssub * c3);
-                kahan_add(ks, 4, Ssub * c4);
+                kahan_add(k, 0, Ss * c0);
+                kahan_add(k, 1, Ss * c1);
+                kahan_add(k, 2, Ss * c2);
+                kahan_add(k, 3, Ss * c3);
+                kahan_add(k, 4, Ss * c4);
+            };
+            // one copy of the loop for both passes: fused, step 0 is level 0's cell (its sums move
+            // to ks0) and steps 1-4 level 1's sub-cells
+            const int steps = fused01 ? 5 : per_lane;
+            for (int j = 0; j < steps; ++j) {
+                if (fused01) add_subcell(ks, j == 0 ? 0 : 1, j == 0 ? 0 : j - 1, j == 0 ? Ssub : Ssub * 0.25f);
+                else add_subcell(ks, level, lane_g * per_lane + j, Ssub);
+                if (fused01 && j == 0) {
+                    ks0 = ks;
+                    kahan_zero(ks);
+                }
             }
         }
         // the lanes' Kahan pairs added across the group in FP32 (kahan_pair_add); lane 0 converts
@@ -331,11 +357,21 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
         acc.th = (double)ks.s[3] - (double)ks.c[3];
         acc.pot = (double)ks.s[4] - (double)ks.c[4];
         double *cur = A.cur + 5 * (long long)t;
-        if (mode == kFixed || level == 0) {
-            cur[0] = acc.px; cur[1] = acc.py; cur[2] = acc.pz; cur[3] = acc.th; cur[4] = acc.pot;
-            continue;
+        int lev = level;  // the level decided on below
+        LevelLists out = Lst;
+        acc5 prev;
+        if (fused01) {
+            prev = acc5{(double)ks0.s[0] - (double)ks0.c[0], (double)ks0.s[1] - (double)ks0.c[1], (double)ks0.s[2] - (double)ks0.c[2],
+                        (double)ks0.s[3] - (double)ks0.c[3], (double)ks0.s[4] - (double)ks0.c[4]};
+            lev = 1;
+            out = level_lists(A, 1, mode);
+        } else {
+            if (mode == kFixed || level == 0) {
+                cur[0] = acc.px; cur[1] = acc.py; cur[2] = acc.pz; cur[3] = acc.th; cur[4] = acc.pot;
+                continue;
+            }
+            prev = acc5{cur[0], cur[1], cur[2], cur[3], cur[4]};
         }
-        const acc5 prev = acc5{cur[0], cur[1], cur[2], cur[3], cur[4]};
         cur[0] = acc.px; cur[1] = acc.py; cur[2] = acc.pz; cur[3] = acc.th; cur[4] = acc.pot;
         // error estimator: the differences of successive levels (where cancellation sits) and the
         // singular part are formed in FP64; the norms of the resulting J and dJ are compared in FP32
@@ -368,9 +404,9 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
             unconv = dotf(dJf, dJf) > tolf * tolf * dotf(Jf, Jf);
             if (CLS == kFar) unconv = unconv || fabsf((float)(acc.pot - prev.pot)) > tolf * fabsf((float)acc.pot);
         }
-        atomicMax(A.maxlev, level);
-        if (!unconv || level >= kmax) {
-            A.stop[t] = level;
+        atomicMax(A.maxlev, lev);
+        if (!unconv || lev >= kmax) {
+            A.stop[t] = lev;
             double *fa = A.fin_a + 5 * (long long)t;
             fa[0] = acc.px; fa[1] = acc.py; fa[2] = acc.pz; fa[3] = acc.th; fa[4] = acc.pot;
             if (mode == kAdaptiveCompat) {  // only the compat mode's buffer parity reads the previous level
@@ -378,7 +414,7 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
                 fb[0] = prev.px; fb[1] = prev.py; fb[2] = prev.pz; fb[3] = prev.th; fb[4] = prev.pot;
             }
         } else {
-            Lst.act_out[atomicAdd(Lst.cnt_out, 1)] = t;
+            out.act_out[atomicAdd(out.cnt_out, 1)] = t;
         }
     }
 }
@@ -1061,6 +1097,7 @@ static void level_chain_mixed(const ClassArgs &A, const QuadTablesF &Qf, const R
     k_level_mixed<CLS><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf, 0, cfg.mode, cfg.tol, cfg.max_level);
     ClassArgs B = A;
     for (int lev = 1; lev <= cfg.max_level; ++lev) {
+        if (!level_pass_needed(lev, cfg.mode)) continue;  // level 1 ran inside level 0's pass
         B.act_in = lev == 1 ? nullptr : (lev % 2 ? A.act_b : A.act_a);
         B.cnt_in = lev == 1 ? nullptr : A.cnt + (lev - 1);
         B.act_out = lev % 2 ? A.act_a : A.act_b;
@@ -1129,6 +1166,7 @@ __global__ void __launch_bounds__(256, MINB) k_batch_levels(const BatchSeg *__re
     const long long stride = (long long)gridDim.x * blockDim.x;
     const int lo = mode == kFixed ? level_fixed : 0, hi = mode == kFixed ? level_fixed : kmax;
     for (int level = lo; level <= hi; ++level) {
+        if (!level_pass_needed(level, mode)) continue;  // level 1 ran inside level 0's pass (uniform: mode is)
         for (int sgi = 0; sgi < nseg; ++sgi) {
             if (segs[sgi].cls != CLS) continue;
             const ClassArgs &A = segs[sgi].A;  // read in place, no per-thread copy
