@@ -559,10 +559,10 @@ def run_batch(batch, flush, stream, steps, warmup):
 
 
 # kernels of one batched step, whatever the number of segments (up to 2,048): closed forms with the
-# counter reset, tier 1 with the self pairs, tier 2, tier 2b, the adaptive potential (seed, 12
-# depths, final sums), one cooperative level kernel per pair class, and the fix-up (collect, FP64
-# pass, spread, finish)
-BATCH_LAUNCHES = 1 + 1 + 1 + 1 + (1 + 12 + 1) + 3 + 4
+# counter reset, one cooperative level kernel per pair class, then beside each other the fix-up
+# (collect, FP64 pass, spread, finish) and the potential stages (tier 1 with the self pairs, tier 2,
+# tier 2b, the adaptive potential: seed, 12 depths, final sums; the adjacent pairs' P)
+BATCH_LAUNCHES = 1 + 3 + 4 + (1 + 1 + 1 + (1 + 12 + 1) + 1)
 
 
 def uneven_batch_section(args):

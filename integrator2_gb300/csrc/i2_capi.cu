@@ -753,9 +753,15 @@ struct i2_batch {
     int threads = 256, blocks_per_sm = 0, g_cap = 32, variant = 0, sms = 0;
     cudaGraphExec_t graph = nullptr;
     bool graph_tried = false, graph_ok = false, last_graph = false;
+    // the potential stages run on `side`, forked from and joined to the run's stream
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     ~i2_batch()
     {
         if (graph) cudaGraphExecDestroy(graph);
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (side) cudaStreamDestroy(side);
     }
 };
 
@@ -794,18 +800,31 @@ void batch_prepare(i2_batch *b)
     b->dirty = false;
 }
 
-// the whole batch on a stream: counter resets, per-segment preludes, one cooperative level sweep
+// the whole batch on a stream: counter resets and closed forms, the cooperative level sweep (it
+// runs alone: a cooperative grid is one resident wave), then two branches that share no data --
+// the needle fix-up on `s` and the potential stages on the side stream, which fill the SMs the
+// fix-up's few blocks leave idle -- joined back to `s`
 void batch_enqueue(i2_batch *b, cudaStream_t s, int threads, int bps, int gcap, int variant)
 {
     const int persistent = std::max(1, b->sms) * 8;
     const int nseg = (int)b->segs.size();
     if (nseg == 0) return;
+    if (!b->side) {
+        I2_CHECK_CUDA(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+        I2_CHECK_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+        I2_CHECK_CUDA(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming));
+    }
     i2::RunConfig cfg = b->cfg;
     cfg.hard_tol = adaptive_tolerance(cfg, true);  // the batched form is mixed precision
-    i2::launch_batch_prelude(b->d_segs.ptr, nseg, b->totals, b->Q, b->Qf, cfg, persistent, s);
+    i2::launch_batch_singular(b->d_segs.ptr, nseg, b->totals, b->Qf, s);
     I2_REQUIRE(i2::batch_max_blocks_per_sm(threads, variant) > 0, I2_ERR_CUDA, "batch kernel cannot be resident with this block size");
     I2_CHECK_CUDA(i2::launch_batch_levels(b->d_segs.ptr, nseg, b->totals.present, b->Qf, b->cfg, b->sms, bps, threads, gcap, variant, s));
+    I2_CHECK_CUDA(cudaEventRecord(b->fork, s));
+    I2_CHECK_CUDA(cudaStreamWaitEvent(b->side, b->fork, 0));
+    i2::launch_batch_potential(b->d_segs.ptr, nseg, b->totals, b->Q, b->Qf, cfg, persistent, b->side);
     i2::launch_batch_fixup(b->d_segs.ptr, nseg, b->totals, b->Q, b->cfg, persistent, s);
+    I2_CHECK_CUDA(cudaEventRecord(b->join, b->side));
+    I2_CHECK_CUDA(cudaStreamWaitEvent(s, b->join, 0));
     I2_CHECK_CUDA(cudaGetLastError());
 }
 

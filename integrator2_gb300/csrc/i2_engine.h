@@ -128,10 +128,12 @@ struct BatchTotals {
     bool hard_lists = false;       // some adjacent segment has the potential's tier lists
     bool present[3] = {false, false, false};  // some segment holds pairs of class 0, 1, 2
 };
-// every segment's counter reset, tier 1 with the singular parts, tiers 2 / 2b, the adaptive
-// potential and the self pairs: one launch per stage for the whole batch
-void launch_batch_prelude(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTables &Q, const QuadTablesF &Qf,
-                          const RunConfig &cfg, int persistent_blocks, cudaStream_t s);
+// every segment's counter reset and the closed forms of its adjacent pairs: one launch
+void launch_batch_singular(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTablesF &Qf, cudaStream_t s);
+// tier 1 with the self pairs, tiers 2 / 2b, the adaptive potential and the adjacent pairs' P: one
+// launch per stage for the whole batch (independent of the level sweep and the needle fix-up)
+void launch_batch_potential(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTables &Q, const QuadTablesF &Qf,
+                            const RunConfig &cfg, int persistent_blocks, cudaStream_t s);
 // tier 2b and the adaptive potential of every segment's hard pairs (seed, depths, final sums),
 // in double-float (i2_kernels_df.cu)
 void launch_batch_pot_df(const BatchSeg *segs, int nseg, const QuadTables &Q, double tol, int persistent_blocks, cudaStream_t s);

@@ -1385,19 +1385,39 @@ __global__ void __launch_bounds__(128) k_batch_fix_finish(const BatchSeg *__rest
     }
 }
 
+// the adjacent pairs' P from the potential rules (padj), written after them: the batched step runs
+// the potential stages beside the needle fix-up, after the level sweep has finalised J
+__global__ void __launch_bounds__(256) k_batch_adjacent_potential(const BatchSeg *__restrict__ segs, int nseg)
+{
+    extern __shared__ long long prefix[];
+    const long long total = seg_prefix(segs, nseg, prefix, [](const BatchSeg &S) -> long long { return seg_adjacent(S) ? S.A.n : 0; });
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+        const int sg = seg_find(prefix, nseg, g);
+        const ClassArgs &A = segs[sg].A;
+        const long long t = g - prefix[sg];
+        A.P[t] = A.padj[t];
+    }
+}
+
 static size_t seg_smem(int nseg) { return (size_t)(nseg + 1) * sizeof(long long); }
 
-void launch_batch_prelude(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTables &Q, const QuadTablesF &Qf,
-                          const RunConfig &cfg, int persistent_blocks, cudaStream_t s)
+void launch_batch_singular(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTablesF &Qf, cudaStream_t s)
 {
     const int tpb = 128;
     // closed forms, with the counter reset in front (always launched: the reset is needed by
-    // every segment), then tier 1 with the self pairs
+    // every segment)
     for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
         const int nc = std::min(kBatchSegChunk, nseg - c0);
         const int blocks = std::max(blocks_for_m(nc, tpb), std::min(blocks_for_m(tot.adjacent_pairs, tpb), 1 << 16));
         k_batch_singular<<<std::max(1, blocks), tpb, seg_smem(nc), s>>>(segs + c0, nc, Qf);
     }
+}
+
+void launch_batch_potential(const BatchSeg *segs, int nseg, const BatchTotals &tot, const QuadTables &Q, const QuadTablesF &Qf,
+                            const RunConfig &cfg, int persistent_blocks, cudaStream_t s)
+{
+    const int tpb = 128;
+    // tier 1 with the self pairs, tiers 2 / 2b and the adaptive rule, then the adjacent pairs' P
     const long long warps = (kTier1Lanes * tot.adjacent_pairs + 31) / 32 + (tot.self_pairs + kSelfPairsPerWarp - 1) / kSelfPairsPerWarp;
     if (warps > 0) {
         const int blocks = (int)std::max(1LL, std::min((warps * 32 + tpb - 1) / tpb, 1LL << 16));
@@ -1412,6 +1432,13 @@ void launch_batch_prelude(const BatchSeg *segs, int nseg, const BatchTotals &tot
             k_batch_tier2<<<resident_grid((const void *)k_batch_tier2, tpb, seg_smem(nc)), tpb, seg_smem(nc), s>>>(segs + c0, nc, Qf, Q);
         }
         launch_batch_pot_df(segs, nseg, Q, cfg.hard_tol, persistent_blocks, s);
+    }
+    if (tot.adjacent_pairs > 0) {
+        const int blocks = std::max(1, std::min(blocks_for_m(tot.adjacent_pairs, 256), 1 << 16));
+        for (int c0 = 0; c0 < nseg; c0 += kBatchSegChunk) {
+            const int nc = std::min(kBatchSegChunk, nseg - c0);
+            k_batch_adjacent_potential<<<blocks, 256, seg_smem(nc), s>>>(segs + c0, nc);
+        }
     }
 }
 
