@@ -333,6 +333,15 @@ struct i2_evaluator {
     ClassResult results[4];
     Workspace ws;
     int persistent_blocks = 0;
+    // the mixed form runs an adjacent class's potential stages on `side`, beside its level chain
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    ~i2_evaluator()
+    {
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (side) cudaStreamDestroy(side);
+    }
 };
 
 // ------------------------------------------------------------------ pair lists (O(N))
@@ -681,7 +690,12 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
     const i2::QuadTables Q = ev->integrator->tables();
     if (ev->integrator->precision == I2_PRECISION_MIXED) {
         const i2::QuadTablesF Qf = tables_f32(Q);
-        i2::launch_class_mixed(cls, A, Q, Qf, cfg, ev->persistent_blocks, ev->stream);
+        if (!ev->side) {
+            I2_CHECK_CUDA(cudaStreamCreateWithFlags(&ev->side, cudaStreamNonBlocking));
+            I2_CHECK_CUDA(cudaEventCreateWithFlags(&ev->fork, cudaEventDisableTiming));
+            I2_CHECK_CUDA(cudaEventCreateWithFlags(&ev->join, cudaEventDisableTiming));
+        }
+        i2::launch_class_mixed(cls, A, Q, Qf, cfg, ev->persistent_blocks, ev->stream, i2::SideStream{ev->side, ev->fork, ev->join});
     } else {
         i2::launch_class_fp64(cls, A, Q, cfg, ev->persistent_blocks, ev->stream);
     }

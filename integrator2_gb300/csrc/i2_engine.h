@@ -106,8 +106,13 @@ void launch_prepare_panels(int nc, const double *V, const int *C, Panel *out, cu
 void launch_prepare_panels_f32(int nc, const double *V, const int *C, PanelF *out, cudaStream_t s);
 void launch_class_fp64(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks,
                        cudaStream_t s);
+// a second stream and two events: work forked from a run's stream and joined back to it
+struct SideStream {
+    cudaStream_t stream;
+    cudaEvent_t fork, join;
+};
 void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const QuadTablesF &Qf, const RunConfig &cfg,
-                        int persistent_blocks, cudaStream_t s);
+                        int persistent_blocks, cudaStream_t s, const SideStream &side);
 // batched form: one segment = the pairs of one class of one mesh
 struct BatchSeg {
     ClassArgs A;

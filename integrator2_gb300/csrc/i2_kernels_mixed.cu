@@ -1082,15 +1082,17 @@ void launch_prepare_panels_f32(int nc, const double *V, const int *C, PanelF *ou
     if (nc > 0) k_prepare_panels_f32<<<blocks_for_m(nc, 128), 128, 0, s>>>(nc, V, C, out);
 }
 
+// the level passes of one class; finalised on `s` once `join` (when given) has been reached there
 template <int CLS>
 static void level_chain_mixed(const ClassArgs &A, const QuadTablesF &Qf, const RunConfig &cfg, int persistent_blocks,
-                              cudaStream_t s)
+                              cudaStream_t s, cudaEvent_t join = nullptr)
 {
     const int tpb = 256;
     if (cfg.mode == kFixed) {
         const long long work = (long long)A.n * (cfg.level <= 2 ? (1 << (2 * cfg.level)) : 32);
         k_level_mixed<CLS><<<std::max(1, std::min(blocks_for_m(work, tpb), persistent_blocks * 8)), tpb, 0, s>>>(A, Qf, cfg.level, cfg.mode, cfg.tol,
                                                                                                         cfg.max_level);
+        if (join) cudaStreamWaitEvent(s, join, 0);
         launch_finalize(CLS, A, cfg.mode, s);
         return;
     }
@@ -1104,11 +1106,16 @@ static void level_chain_mixed(const ClassArgs &A, const QuadTablesF &Qf, const R
         B.cnt_out = A.cnt + lev;
         k_level_mixed<CLS><<<persistent_blocks, tpb, 0, s>>>(B, Qf, lev, cfg.mode, cfg.tol, cfg.max_level);
     }
+    if (join) cudaStreamWaitEvent(s, join, 0);
     launch_finalize(CLS, A, cfg.mode, s);
 }
 
+// Adjacent classes: after the closed forms, the potential stages (tier 1, 2, 2b, the adaptive
+// rule) run on the side stream while the level chain runs on `s` -- they share nothing until the
+// finalisation, which waits for both (the level kernels here are ordinary launches, so the two
+// chains' blocks share the SMs).
 void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const QuadTablesF &Qf, const RunConfig &cfg,
-                        int persistent_blocks, cudaStream_t s)
+                        int persistent_blocks, cudaStream_t s, const SideStream &side)
 {
     if (A.n <= 0) return;
     const int tpb = 128;
@@ -1118,24 +1125,38 @@ void launch_class_mixed(int cls, const ClassArgs &A, const QuadTables &Q, const 
         break;
     case kEdge:
         k_singular_mixed<kEdge><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
-        if (A.pot_off) cudaMemsetAsync(A.padj, 0xff, sizeof(double) * (size_t)A.n, s);  // J only: P reads NaN
-        else k_tier1_mixed<kEdge><<<blocks_for_m((long long)kTier1Lanes * A.n, tpb), tpb, 0, s>>>(A, Qf);
-        if (A.hard_list) {
-            k_pot_tier2_mixed<kEdge><<<resident_grid((const void *)k_pot_tier2_mixed<kEdge>, tpb, 0), tpb, 0, s>>>(A, Qf, Q);
-            launch_pot_tiers_hard_df(kEdge, A, Q, cfg, persistent_blocks, s);
+        if (A.pot_off) {
+            cudaMemsetAsync(A.padj, 0xff, sizeof(double) * (size_t)A.n, s);  // J only: P reads NaN
+            level_chain_mixed<kEdge>(A, Qf, cfg, persistent_blocks, s);
+        } else {
+            cudaEventRecord(side.fork, s);
+            cudaStreamWaitEvent(side.stream, side.fork, 0);
+            k_tier1_mixed<kEdge><<<blocks_for_m((long long)kTier1Lanes * A.n, tpb), tpb, 0, side.stream>>>(A, Qf);
+            if (A.hard_list) {
+                k_pot_tier2_mixed<kEdge><<<resident_grid((const void *)k_pot_tier2_mixed<kEdge>, tpb, 0), tpb, 0, side.stream>>>(A, Qf, Q);
+                launch_pot_tiers_hard_df(kEdge, A, Q, cfg, persistent_blocks, side.stream);
+            }
+            cudaEventRecord(side.join, side.stream);
+            level_chain_mixed<kEdge>(A, Qf, cfg, persistent_blocks, s, side.join);
         }
-        level_chain_mixed<kEdge>(A, Qf, cfg, persistent_blocks, s);
         launch_fp64_fixup(kEdge, A, Q, cfg, persistent_blocks, s);
         break;
     case kVertex:
         k_singular_mixed<kVertex><<<blocks_for_m(A.n, tpb), tpb, 0, s>>>(A, Qf);
-        if (A.pot_off) cudaMemsetAsync(A.padj, 0xff, sizeof(double) * (size_t)A.n, s);  // J only: P reads NaN
-        else k_tier1_mixed<kVertex><<<blocks_for_m((long long)kTier1Lanes * A.n, tpb), tpb, 0, s>>>(A, Qf);
-        if (A.hard_list) {
-            k_pot_tier2_mixed<kVertex><<<resident_grid((const void *)k_pot_tier2_mixed<kVertex>, tpb, 0), tpb, 0, s>>>(A, Qf, Q);
-            launch_pot_tiers_hard_df(kVertex, A, Q, cfg, persistent_blocks, s);
+        if (A.pot_off) {
+            cudaMemsetAsync(A.padj, 0xff, sizeof(double) * (size_t)A.n, s);  // J only: P reads NaN
+            level_chain_mixed<kVertex>(A, Qf, cfg, persistent_blocks, s);
+        } else {
+            cudaEventRecord(side.fork, s);
+            cudaStreamWaitEvent(side.stream, side.fork, 0);
+            k_tier1_mixed<kVertex><<<blocks_for_m((long long)kTier1Lanes * A.n, tpb), tpb, 0, side.stream>>>(A, Qf);
+            if (A.hard_list) {
+                k_pot_tier2_mixed<kVertex><<<resident_grid((const void *)k_pot_tier2_mixed<kVertex>, tpb, 0), tpb, 0, side.stream>>>(A, Qf, Q);
+                launch_pot_tiers_hard_df(kVertex, A, Q, cfg, persistent_blocks, side.stream);
+            }
+            cudaEventRecord(side.join, side.stream);
+            level_chain_mixed<kVertex>(A, Qf, cfg, persistent_blocks, s, side.join);
         }
-        level_chain_mixed<kVertex>(A, Qf, cfg, persistent_blocks, s);
         launch_fp64_fixup(kVertex, A, Q, cfg, persistent_blocks, s);
         break;
     default:
