@@ -734,9 +734,10 @@ def adjoint_section(args):
 
 
 # DRAM bytes (read + write) of one run of the disjoint class's FP32 level chain (k_level_mixed<2>,
-# levels 0..5) on this workload, measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum
-# summed over the chain's six launches); the chain is compute-bound, this is mostly per-pair state
-FAR_CHAIN_DRAM_BYTES = 147407616 + 91512576
+# levels 0..5 in five launches: levels 0 and 1 share one) on this workload, measured with ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum summed over the launches); the chain is
+# compute-bound, this is mostly per-pair state
+FAR_CHAIN_DRAM_BYTES = (21755136 + 32178944) + (46207744 + 6066688) + 1542144 + 120064 + 76288
 
 # The algorithmic work of one far-field point, frozen from the reference's formula (thetaPsi,
 # evaluatorJ3DK.cu:266-313; the hand count the roofline is defined on): about 150 flops, 3 sqrt,
