@@ -23,7 +23,11 @@
  *   - the potential channel and the self class are additions.
  *
  * Threading: handles are not thread-safe; distinct handles may be used from distinct threads.
- * All device work of an evaluator runs on its stream (i2_evaluator_set_stream).
+ * All device work of an evaluator is ordered on its stream (i2_evaluator_set_stream): the mixed
+ * form forks an adjacent class's potential stages onto a second stream the evaluator owns and joins
+ * them back by an event before the class's results are written, so work enqueued on the
+ * evaluator's stream afterwards, and a graph captured from it, see the finished class.  A batch
+ * does the same with its own second stream.
  */
 #ifndef INTEGRATOR2_GB300_H
 #define INTEGRATOR2_GB300_H
