@@ -1,6 +1,7 @@
-"""Mixed-precision form (FP32 bulk, FP64 singular parts / estimator / hard pairs) through the
-C-ABI: per class and per channel error against the FP64 form and against the oracle's
-high-order answer."""
+"""Mixed-precision form (FP32 bulk; double-float closed forms, tier 2b and adaptive potential; FP64
+estimator differences and needle pairs) through the C-ABI: per class and per channel error against
+the FP64 form and against the oracle's high-order answer; its device entry point captured into a
+CUDA graph."""
 import numpy as np
 import pytest
 
@@ -277,3 +278,48 @@ def test_mixed_adaptive_potential_of_hard_pairs(api):
         assert err[api.PRECISION_MIXED].max() < 1e-6, (cls, report[cls])
         assert np.sqrt(np.mean(err[api.PRECISION_MIXED] ** 2)) < 5e-8, (cls, report[cls])
     print("hard pairs (count, FP64 max, mixed max, mixed rms):", report)
+
+
+def test_mixed_device_entry_captured_in_a_graph(api):
+    """the device entry point of the mixed form forks an adjacent class's potential stages onto the
+    evaluator's second stream and joins them back before the class's results: captured from the
+    evaluator's stream into a CUDA graph, the replay writes exactly the direct run's J and P"""
+    import torch
+    from integrator2_gb300 import meshes, pairs as P
+    V, C = meshes.jittered_icosphere(3, 0.15, 7)
+    pl = P.build_pairs(V, C)
+    m = api.Mesh3D()
+    m.setGeometry(V, C)
+    m.prepareMesh(3.0)
+    it = api.NumericalIntegrator3D(m, api.qf3D13)
+    it.setErrorControl(api.RELATIVE_ERROR_CONTROL, 1e-6, 5)
+    it.setPrecision(api.PRECISION_MIXED)
+    ev = api.EvaluatorJ3DK(m, it)
+    stream = torch.cuda.Stream()
+    ev.setStream(stream.cuda_stream)
+    classes = (0, 1, 2)
+    d_pairs = {c: torch.from_numpy(np.ascontiguousarray(pl.by_class(c)[:, :2]).astype(np.int32)).cuda() for c in classes}
+    d_J = {c: torch.zeros(len(d_pairs[c]), 3, dtype=torch.float64, device="cuda") for c in classes}
+    d_P = {c: torch.zeros(len(d_pairs[c]), dtype=torch.float64, device="cuda") for c in classes}
+    torch.cuda.synchronize()
+
+    def run():
+        for c in classes:
+            ev.runClassDevice(c, d_pairs[c].data_ptr(), len(d_pairs[c]), 0, d_J[c].data_ptr(), d_P[c].data_ptr())
+
+    with torch.cuda.stream(stream):
+        run()  # direct; also sizes the workspaces and makes the second stream
+    stream.synchronize()
+    ref = {c: (d_J[c].clone(), d_P[c].clone()) for c in classes}
+    for c in classes:
+        d_J[c].zero_()
+        d_P[c].zero_()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        run()
+    g.replay()
+    torch.cuda.synchronize()
+    for c in classes:
+        assert torch.equal(d_J[c], ref[c][0]) and torch.equal(d_P[c], ref[c][1]), c
+        assert torch.isfinite(d_P[c]).all() and len(d_P[c]) > 0
