@@ -628,7 +628,7 @@ void run_class_device(i2_evaluator *ev, int cls, const int2 *d_pairs, int64_t n,
         W.pot_ctx.reserve((size_t)i2::kPotCtxDoubles * pot_ctx_capacity(n));
         W.pot_tri_a.reserve(9 * (size_t)pot_tri_capacity(n));
         W.pot_tri_b.reserve(9 * (size_t)pot_tri_capacity(n));
-        if (ev->integrator->precision == I2_PRECISION_MIXED) W.ctx_e.reserve((size_t)i2::kVertexCtxFloats * n);
+        if (ev->integrator->precision == I2_PRECISION_MIXED) W.ctx_e.reserve((size_t)i2::kPairCtxFloats * n);
     }
     // the run's counters (layout: kCnt* in i2_engine.h)
     I2_CHECK_CUDA(cudaMemsetAsync(W.cnt.ptr, 0, 16 * sizeof(int), ev->stream));
@@ -1416,7 +1416,7 @@ i2_status i2_batch_add(i2_batch_t *batch, const i2_mesh_t *mesh, i2_pair_class c
         }
         const bool adj = c == I2_SIMPLE_NEIGHBORS || c == I2_ATTACHED_NEIGHBORS;
         if (adj) {
-            sp->sing.reserve(4 * m); sp->padj.reserve(m); sp->hard_list.reserve(m); sp->tier2_list.reserve(m); sp->tier2b_list.reserve(m); sp->ctx_e.reserve((size_t)i2::kVertexCtxFloats * m);
+            sp->sing.reserve(4 * m); sp->padj.reserve(m); sp->hard_list.reserve(m); sp->tier2_list.reserve(m); sp->tier2b_list.reserve(m); sp->ctx_e.reserve((size_t)i2::kPairCtxFloats * m);
             sp->pot_q_a.reserve(pot_queue_capacity(m)); sp->pot_q_b.reserve(pot_queue_capacity(m)); sp->pot_qcnt.reserve(16); sp->pot_fx.reserve(m);
             sp->pot_ctx.reserve((size_t)i2::kPotCtxDoubles * pot_ctx_capacity(m));
             sp->pot_tri_a.reserve(9 * (size_t)pot_tri_capacity(m)); sp->pot_tri_b.reserve(9 * (size_t)pot_tri_capacity(m));

@@ -14,8 +14,12 @@ namespace i2 {
 
 // depth cap of the adaptive potential rule (sub-cell paths of up to 24 bits)
 constexpr int kHardMaxDepth = 12;
-// floats per common-vertex pair in ClassArgs::ctx_e
-constexpr int kVertexCtxFloats = 16;
+// a needle cell has a corner below 5 degrees: the mixed form computes the pairs that hold one (K_j
+// only, for the disjoint class) in FP64; cos 5 degrees, compared with the panel's largest corner cosine
+constexpr double kNeedleCos = 0.99619469809174553;
+// floats per adjacent pair in ClassArgs::ctx_e (mixed precision): the common-vertex asymptote's
+// directions, or the common-edge pair's shared-edge term and shared-edge frame
+constexpr int kPairCtxFloats = 20;
 // ClassArgs::cnt, 16 ints per class run: [L] pairs still active after level L (L = 1..7),
 // then the counters below
 constexpr int kCntHard = 8;       // pairs handed to the adaptive potential rule
@@ -61,8 +65,8 @@ struct ClassArgs {
     const int3 *cells = nullptr;
     const Panel *panels = nullptr;
     const PanelF *panels_f = nullptr;         // FP32 panel records (mixed precision)
-    float *ctx_e = nullptr;                   // per-pair asymptote constants of common-vertex pairs (mixed precision),
-                                              // kVertexCtxFloats floats per pair
+    float *ctx_e = nullptr;                   // per-pair constants of the adjacent classes (mixed precision),
+                                              // kPairCtxFloats floats per pair
     // per-pair state: regular-part sums (Psi, Theta, potential)
     double *cur = nullptr, *fin_a = nullptr, *fin_b = nullptr;
     int *stop = nullptr;
@@ -151,7 +155,7 @@ void launch_batch_fixup(const BatchSeg *segs, int nseg, const BatchTotals &tot, 
 void launch_adjoint(int cls, bool fp32, const int2 *pairs, int n, const int3 *cells, const double *V, const int *stop,
                     const int *maxlev, const RunConfig &cfg, double tier_tol, double top_tol, const double *gJ, const double *gP, double *gradV,
                     const QuadTables &Q, int persistent_blocks, cudaStream_t s);
-// mixed form: FP64 recomputation of the pairs with a needle cell (corner below 3 degrees)
+// mixed form: FP64 recomputation of the pairs with a needle cell (corner below 5 degrees, kNeedleCos)
 void launch_fp64_fixup(int cls, const ClassArgs &A, const QuadTables &Q, const RunConfig &cfg, int persistent_blocks, cudaStream_t s);
 // blocks of `kernel` that are resident at once on the current device (occupancy x SMs): the grid
 // of the FP64 warp-per-item passes, whose items go to the warps warp-major (warp_item_index), so

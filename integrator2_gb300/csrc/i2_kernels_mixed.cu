@@ -58,10 +58,23 @@ __global__ void k_prepare_panels_f32(int nc, const double *__restrict__ V, const
 }
 
 // ------------------------------------------------------------------ FP32 fused regular parts
+// A common-edge pair in the frame of its shared edge JB -> JC (K_j = (JA, JB, JC), D = K_i's vertex
+// off the edge, tc = unit(JC - JB), L = |JC - JB|, D_p = the part of D - JB normal to tc, h = |D_p|).
+// A point x of K_i with barycentric weights (l_B, l_C, l_D) lies at the distance a = l_C L + l_D dB
+// along the edge from JB, a' = l_B L + l_D dC back from JC, and p = l_D D_p off the edge line.  The
+// terms of theta that vanish on the shared edge are formed from a, a' and p: they are small
+// differences of offsets of size l, and FP32 offsets rounded at ulp(l) would leave them errors of
+// ulp(l) / |p| (4e-6 of J on a jittered 320-cell sphere).  The constants are rounded once from FP64
+// (store_edge_frame).
 struct EdgeCtxF {
-    f3 AB, AC;       // JB - JA, JC - JA (offsets are taken from JA, the vertex off the shared edge)
-    f3 ta, tb, tc;   // unit(JA - JC), unit(JB - JA), unit(JC - JB)
-    float ilvc;
+    f3 ta, tb;          // unit(JA - JC), unit(JB - JA) (the two log terms of Psi, from o_A)
+    float ilvc;         // 1 / L
+    float L, h, dB, dC; // dB = (D - JB).tc, dC = (JC - D).tc
+    float dn;           // n_j . D_p: the distance to K_j's plane is l_D dn
+    float g1, g2;       // D_p . (tb x tc), D_p . (ta x tc)
+    float h1, h2;       // (tb - tc) . D_p, (ta - tc) . D_p
+    float cb, ca;       // 1 - tb.tc, 1 - ta.tc (= |tb - tc|^2 / 2, |ta - tc|^2 / 2)
+    float BAtc, BAp;    // (JB - JA).tc, (JB - JA).D_p
 };
 struct VertexCtxF {
     f3 AB, AC;       // JB - JA, JC - JA (JA = shared vertex)
@@ -74,16 +87,42 @@ struct VertexCtxF {
     float inv_sqrt_si, lenBC;
 };
 
-__device__ __forceinline__ void edge_integrand_f(f3 oA, f3 oB, f3 oC, const PanelJf &K, const EdgeCtxF &E, f3 &psi, float &th)
+// The common-edge regular integrand (the FP64 form's edge_integrand) at the point with offset o_A
+// from JA and barycentric weights wb = (l_B, l_C, l_D) in K_i.  With o_B = a tc + p, o_C = -a' tc + p
+// and l_B = |o_B|, l_C = |o_C|, the solid angle's denominator
+//   l_A l_B l_C + (o_A.o_B) l_C + (o_B.o_C) l_A + (o_C.o_A) l_B = l_A Q + o_A.(l_C o_B + l_B o_C),
+//   Q = l_B l_C - a a' + p^2,   l_C o_B + l_B o_C = (l_C a - l_B a') tc + (l_B + l_C) p,
+// its height n_j.o_A = n_j.p, and the two edge angles' arguments
+//   (o_B x tb).tc = p.(tb x tc),  (tb - tc).(l_B tb + o_B) = (l_B - a)(1 - tb.tc) + (tb - tc).p
+// (and the same with o_C, ta, a') are rebuilt without cancellation where the point projects onto
+// the edge (a, a' > 0):
+//   l_B l_C - a a' = p^2 (a^2 + a'^2 + p^2) / (l_B l_C + a a'),
+//   l_C a - l_B a' = p^2 (a - a')(a + a') / (l_C a + l_B a'),   l_B - a = p^2 / (l_B + a);
+// outside that span the direct forms add terms of one sign.
+__device__ __forceinline__ void edge_integrand_f(f3 oA, f3 wb, const PanelJf &K, const EdgeCtxF &E, f3 &psi, float &th)
 {
-    const float lA = normf(oA), lB = normf(oB), lC = normf(oC);
+    const float lA = normf(oA);
     const float l1 = logf((lA + dotf(oA, E.tb)) * E.ilvc);
     const float l2 = logf((lA - dotf(oA, E.ta)) * E.ilvc);
     psi = l1 * E.tb + l2 * E.ta;
-    const float den = lA * lB * lC + dotf(oA, oB) * lC + dotf(oB, oC) * lA + dotf(oC, oA) * lB;
-    const float s1 = atan2f(dotf(crossf(oB, E.tb), E.tc), dotf(E.tb - E.tc, lB * E.tb + oB));
-    const float s2 = atan2f(dotf(crossf(oC, E.ta), E.tc), dotf(E.ta - E.tc, lC * E.ta - oC));
-    th = 2.0f * atan2f(2.0f * K.S * dotf(K.n, oA), den) - 2.0f * (s1 - s2);
+    const float lD = wb.z;
+    const float a = fmaf(wb.y, E.L, lD * E.dB), ap = fmaf(wb.x, E.L, lD * E.dC);
+    const float ph = lD * E.h, p2 = ph * ph;
+    const float lB = sqrtf(fmaf(a, a, p2)), lC = sqrtf(fmaf(ap, ap, p2));
+    float Q, W;
+    if (a > 0.0f && ap > 0.0f) {
+        Q = fmaf(p2, div_q(fmaf(a, a, fmaf(ap, ap, p2)), fmaf(lB, lC, a * ap)), p2);
+        W = div_q(p2 * (a - ap) * (a + ap), fmaf(lC, a, lB * ap));
+    } else {
+        Q = fmaf(lB, lC, fmaf(-a, ap, p2));
+        W = fmaf(lC, a, -lB * ap);
+    }
+    const float den = fmaf(lA, Q, fmaf(a + E.BAtc, W, (lB + lC) * fmaf(lD, E.BAp, p2)));
+    const float lBa = a > 0.0f ? div_q(p2, lB + a) : lB - a;
+    const float lCa = ap > 0.0f ? div_q(p2, lC + ap) : lC - ap;
+    const float s1 = atan2f(lD * E.g1, fmaf(lBa, E.cb, lD * E.h1));
+    const float s2 = atan2f(lD * E.g2, fmaf(lCa, E.ca, -lD * E.h2));
+    th = 2.0f * atan2f(2.0f * K.S * (lD * E.dn), den) - 2.0f * (s1 - s2);
 }
 
 __device__ __forceinline__ void vertex_integrand_f(f3 oA, f3 oB, f3 oC, const PanelJf &K, const VertexCtxF &Vx, f3 &psi, float &th)
@@ -210,6 +249,7 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
             EdgeCtxF E;
             VertexCtxF Vx;
             FarCtxF F;
+            TriF Tb;  // common edge: K_i's vertices as barycentric roles (x = JB, y = JC, z = off the edge)
             if (CLS == kFar) {
                 F.ea = df_edge(A.panels_f, pr.y, 2, 1);  // C - B
                 F.eb = -1.0f * K.AC;                      // A - C
@@ -219,27 +259,46 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
                 if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
                 else shifts_vertex(ci, cj, si, sj);
                 origin = sj;
-                const f3 AB = df_edge(A.panels_f, pr.y, (sj + 1) % 3, sj), AC = df_edge(A.panels_f, pr.y, (sj + 2) % 3, sj);
                 // unit edges of K_j in the rotated order, rounded from FP64 (the panel's unit edge
                 // k is opposite vertex k): the closed forms subtract the asymptote along the same
                 // directions, so FP32-normalised edges would leave a bias of a few ulps at every point
                 const float4 *uj = A.panels_f[pr.y].v + 7;
                 const f3 t_a = xyzf(uj[(sj + 1) % 3]), t_b = xyzf(uj[(sj + 2) % 3]), t_bc = xyzf(uj[sj]);
                 if (CLS == kEdge) {
-                    E.AB = AB;
-                    E.AC = AC;
                     E.ta = t_a;
                     E.tb = t_b;
                     E.ilvc = uj[sj].w;  // 1 / |JC - JB|, the edge opposite JA
-                    E.tc = t_bc;
+                    const float4 *ce = reinterpret_cast<const float4 *>(A.ctx_e + kPairCtxFloats * (long long)t);
+                    const float4 q1 = ce[1], q2 = ce[2], q3 = ce[3], q4 = ce[4];
+                    E.h = q1.x;
+                    E.dB = q1.w;
+                    E.dC = q2.x;
+                    E.dn = q2.y;
+                    E.g1 = q2.z;
+                    E.g2 = q2.w;
+                    E.h1 = q3.x;
+                    E.h2 = q3.y;
+                    E.cb = q3.z;
+                    E.ca = q3.w;
+                    E.BAtc = q4.x;
+                    E.BAp = q4.y;
+                    E.L = q4.z;
+                    const int jb = sj == 0 ? cj.y : (sj == 1 ? cj.z : cj.x);
+                    const int iv[3] = {ci.x, ci.y, ci.z};
+                    f3 role[3];
+#pragma unroll
+                    for (int k = 0; k < 3; ++k)
+                        role[k] = k == si ? f3{0.0f, 0.0f, 1.0f} : (iv[k] == jb ? f3{1.0f, 0.0f, 0.0f} : f3{0.0f, 1.0f, 0.0f});
+                    Tb = TriF{role[0], role[1], role[2]};
                 } else {
+                    const f3 AB = df_edge(A.panels_f, pr.y, (sj + 1) % 3, sj), AC = df_edge(A.panels_f, pr.y, (sj + 2) % 3, sj);
                     Vx.AB = AB;
                     Vx.AC = AC;
                     Vx.ta = t_a;
                     Vx.tb = t_b;
                     Vx.lenBC = A.panels_f[pr.y].v[2 + sj].w;  // |JC - JB|, the edge opposite JA
                     Vx.tbc = t_bc;
-                    const float4 *ce = reinterpret_cast<const float4 *>(A.ctx_e + kVertexCtxFloats * (long long)t);
+                    const float4 *ce = reinterpret_cast<const float4 *>(A.ctx_e + kPairCtxFloats * (long long)t);
                     const float4 q0 = ce[0], q1 = ce[1], q2 = ce[2], q3 = ce[3];
                     Vx.w1 = xyzf(q0);
                     Vx.p1 = f3{q0.w, q1.x, q1.y};
@@ -251,53 +310,44 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
                     Vx.inv_sqrt_si = A.panels_f[pr.x].v[5].w;
                 }
             }
-            // K_i's vertices as offsets from each vertex of K_j, in the (rotated) order the
-            // integrand expects: every point-to-vertex offset keeps full relative precision.
-            // The disjoint and common-vertex classes keep only the offsets from one vertex (A; the
-            // shared vertex for the common-vertex class) and form a point's offsets from the
-            // other two as (o_A - e_hi) - e_lo with K_j's edges in double-float: o_A's rounding is
-            // then a shift of the point shared by all three offsets (harmless), the two
-            // subtractions add half an ulp each, and no rounded edge vector enters the logs (that
-            // would be a per-pair bias, amplified by the cancellation in Psi).  Two sub-cell walks
-            // and 18 live floats fewer.  The common-edge class keeps three offset triangles: its
-            // points come close to two of K_j's vertices (the shared edge's ends), where an offset
-            // formed by subtraction would lose its relative precision.
-            TriF T0, T1, T2;
+            // K_i's vertices as offsets from K_j's vertex A (the shared vertex for the
+            // common-vertex class, the vertex off the shared edge for the common-edge class), exact
+            // in double-float and rounded once.  The disjoint and common-vertex classes form a
+            // point's offsets from the other two vertices as (o_A - e_hi) - e_lo with K_j's edges in
+            // double-float: o_A's rounding is then a shift of the point shared by all three offsets
+            // (harmless), the two subtractions add half an ulp each, and no rounded edge vector
+            // enters the logs (that would be a per-pair bias, amplified by the cancellation in Psi).
+            // The common-edge class needs no offsets from B and C: its points come close to the
+            // shared edge, where every offset from its ends would be rounded at ulp(offset) while
+            // the edge terms depend on the point's distance to the edge line.  It walks K_i's
+            // sub-cells a second time in barycentric coordinates (exact dyadic values at these
+            // levels), from which edge_integrand_f places the point in the shared edge's frame.
+            TriF T0;
             f3 ABh, ABl, ACh, ACl;
             df_offsets(A.panels_f, pr.x, pr.y, origin, T0.a, T0.b, T0.c);
             if (CLS != kEdge) {
                 df_edge_pair(A.panels_f, pr.y, (origin + 1) % 3, origin, ABh, ABl);
                 df_edge_pair(A.panels_f, pr.y, (origin + 2) % 3, origin, ACh, ACl);
-            } else {
-                df_offsets(A.panels_f, pr.x, pr.y, (origin + 1) % 3, T1.a, T1.b, T1.c);
-                df_offsets(A.panels_f, pr.x, pr.y, (origin + 2) % 3, T2.a, T2.b, T2.c);
             }
             // sub-cell sc of level lev into the Kahan sums k (sub-cell area Ss)
             auto add_subcell = [&](kahan5 &k, int lev, int sc, float Ss) {
                 const TriF U0 = subcellf(T0, lev, sc);
-                TriF U1, U2;
-                if (CLS == kEdge) {
-                    U1 = subcellf(T1, lev, sc);
-                    U2 = subcellf(T2, lev, sc);
-                }
+                TriF Ub;
+                if (CLS == kEdge) Ub = subcellf(Tb, lev, sc);
                 float c0 = 0, c1 = 0, c2 = 0, c3 = 0, c4 = 0;
 #pragma unroll 1
                 for (int g = 0; g < Qf.npts; ++g) {
                     const float l1 = Qf.L1[g], l2 = Qf.L2[g], l3 = Qf.L3[g];
                     const f3 oA = l1 * U0.a + l2 * U0.b + l3 * U0.c;
-                    f3 oB, oC;
-                    if (CLS != kEdge) {
-                        oB = (oA - ABh) - ABl;
-                        oC = (oA - ACh) - ACl;
-                    } else {
-                        oB = l1 * U1.a + l2 * U1.b + l3 * U1.c;
-                        oC = l1 * U2.a + l2 * U2.b + l3 * U2.c;
-                    }
                     f3 psi;
                     float th, pot = 0.0f;
-                    if (CLS == kFar) far_field_integrand_f(oA, oB, oC, K, F, psi, th, pot);
-                    else if (CLS == kEdge) edge_integrand_f(oA, oB, oC, K, E, psi, th);
-                    else vertex_integrand_f(oA, oB, oC, K, Vx, psi, th);
+                    if (CLS == kEdge) {
+                        edge_integrand_f(oA, l1 * Ub.a + l2 * Ub.b + l3 * Ub.c, K, E, psi, th);
+                    } else {
+                        const f3 oB = (oA - ABh) - ABl, oC = (oA - ACh) - ACl;
+                        if (CLS == kFar) far_field_integrand_f(oA, oB, oC, K, F, psi, th, pot);
+                        else vertex_integrand_f(oA, oB, oC, K, Vx, psi, th);
+                    }
                     const float w = Qf.w[g];
                     c0 = fmaf(w, psi.x, c0);
                     c1 = fmaf(w, psi.y, c1);
@@ -513,19 +563,41 @@ __device__ __forceinline__ void edge_sigma_setup(const ClassArgs &A, int2 pr, in
 // as a double's two halves
 __device__ __forceinline__ void store_edge_sigma(const ClassArgs &A, long long t, f3 m_in, float c, float h, double sig)
 {
-    float4 *ce = reinterpret_cast<float4 *>(A.ctx_e + kVertexCtxFloats * t);
+    float4 *ce = reinterpret_cast<float4 *>(A.ctx_e + kPairCtxFloats * t);
     ce[0] = make_float4(m_in.x, m_in.y, m_in.z, c);
     ce[1] = make_float4(h, __int_as_float(__double2hiint(sig)), __int_as_float(__double2loint(sig)), 0.0f);
 }
 
 __device__ __forceinline__ void load_edge_sigma(const ClassArgs &A, long long t, f3 &m_in, float &c, float &h, double &sig)
 {
-    const float4 *ce = reinterpret_cast<const float4 *>(A.ctx_e + kVertexCtxFloats * t);
+    const float4 *ce = reinterpret_cast<const float4 *>(A.ctx_e + kPairCtxFloats * t);
     const float4 a = ce[0], b = ce[1];
     m_in = f3{a.x, a.y, a.z};
     c = a.w;
     h = b.x;
     sig = __hiloint2double(__float_as_int(b.y), __float_as_int(b.z));
+}
+
+// the shared-edge frame of a common-edge pair (EdgeCtxF) in ctx_e after the shared-edge term:
+// [7] dB, [8..11] dC, n_j.D_p, D_p.(tb x tc), D_p.(ta x tc), [12..15] (tb - tc).D_p, (ta - tc).D_p,
+// 1 - tb.tc, 1 - ta.tc, [16..18] (JB - JA).tc, (JB - JA).D_p, L; formed in FP64 and rounded once
+// (h = |D_p| is the shared-edge term's h, [4])
+__device__ __forceinline__ void store_edge_frame(const ClassArgs &A, int2 pr, int si, int sj, long long t)
+{
+    const PanelJ K = load_panel(A.panels, pr.y);
+    const Tri Ti = load_tri(A.panels, pr.x);
+    const d3 Pi[3] = {Ti.a, Ti.b, Ti.c}, Pj[3] = {K.A, K.B, K.C};
+    const d3 JA = Pj[sj], JB = Pj[(sj + 1) % 3], JC = Pj[(sj + 2) % 3], D = Pi[si];
+    const d3 tc = unit(JC - JB), ta = unit(JA - JC), tb = unit(JB - JA);
+    const d3 w = D - JB, BA = JB - JA;
+    const double dB = dot(w, tc);
+    const d3 Dp = w - dB * tc, ub = tb - tc, ua = ta - tc;
+    float *ce = A.ctx_e + kPairCtxFloats * t;
+    ce[7] = (float)dB;
+    reinterpret_cast<float4 *>(ce)[2] =
+        make_float4((float)dot(JC - D, tc), (float)dot(K.n, Dp), (float)dot(Dp, cross(tb, tc)), (float)dot(Dp, cross(ta, tc)));
+    reinterpret_cast<float4 *>(ce)[3] = make_float4((float)dot(ub, Dp), (float)dot(ua, Dp), (float)(0.5 * dot(ub, ub)), (float)(0.5 * dot(ua, ua)));
+    reinterpret_cast<float4 *>(ce)[4] = make_float4((float)dot(BA, tc), (float)dot(BA, Dp), (float)norm(JC - JB), 0.0f);
 }
 
 template <int CLS>
@@ -546,8 +618,7 @@ __device__ __forceinline__ void singular_mixed_item(const ClassArgs &A, const Qu
     // reproduces the FP64 form.  Every other pair computes it in double-float, the pair translated
     // to K_j's vertex A in FP64 (the closed forms depend on vertex differences only) and
     // converted; the closed forms scale it by a power of two.
-    const double c3 = 0.99862953475457387;  // cos 3 degrees, as fixup_collect_item
-    if (A.panels[pr.x].v[2].w > c3 || A.panels[pr.y].v[2].w > c3) {
+    if (A.panels[pr.x].v[2].w > kNeedleCos || A.panels[pr.y].v[2].w > kNeedleCos) {  // as fixup_collect_item
         const Tri Ti = rotate(load_tri(A.panels, pr.x), si), Tj = rotate(Tri{Kd.A, Kd.B, Kd.C}, sj);
         d3 psi;
         double th;
@@ -558,13 +629,14 @@ __device__ __forceinline__ void singular_mixed_item(const ClassArgs &A, const Qu
             double sig;
             edge_sigma_setup(A, pr, si, sj, Si, m_in, c, h, sig);
             store_edge_sigma(A, t, m_in, c, h, sig);
+            store_edge_frame(A, pr, si, sj, t);
         } else {
             closed_vertex(Ti, Tj, ni, Kd.n, Si, psi, th);
             const d3 ta = unit(Tj.a - Tj.c), tb = unit(Tj.b - Tj.a);
             double dA, dB;
             const d3 e = vertex_direction(ni, Kd.n, ta, tb, dA, dB);
             const d3 w1 = cross(ta, e), p1 = e - ta, w2 = cross(tb, e), p2 = e + tb;
-            float4 *ce = reinterpret_cast<float4 *>(A.ctx_e + kVertexCtxFloats * (long long)t);
+            float4 *ce = reinterpret_cast<float4 *>(A.ctx_e + kPairCtxFloats * (long long)t);
             // w1, p1, w2, p2 (12 floats), then e
             ce[0] = make_float4((float)w1.x, (float)w1.y, (float)w1.z, (float)p1.x);
             ce[1] = make_float4((float)p1.y, (float)p1.z, (float)w2.x, (float)w2.y);
@@ -590,13 +662,14 @@ __device__ __forceinline__ void singular_mixed_item(const ClassArgs &A, const Qu
             const df3 mi = (1.0f / hd) * perp;
             const dfl cd = -dot(m, mi);
             store_edge_sigma(A, t, f3{mi.x.hi, mi.y.hi, mi.z.hi}, cd.hi, hd.hi, (double)(((5.0 / 9.0) * cd) * (dfl(Si) * hd)));
+            store_edge_frame(A, pr, si, sj, t);
         } else {
             closed_vertex(Ti, Tj, nid, njd, dfl(Si), psi, th);
             const df3 ta = unit(Tj.a - Tj.c), tb = unit(Tj.b - Tj.a);
             dfl dA, dB;
             const df3 e = vertex_direction(nid, njd, ta, tb, dA, dB);
             const df3 w1 = cross(ta, e), p1 = e - ta, w2 = cross(tb, e), p2 = e + tb;
-            float4 *ce = reinterpret_cast<float4 *>(A.ctx_e + kVertexCtxFloats * (long long)t);
+            float4 *ce = reinterpret_cast<float4 *>(A.ctx_e + kPairCtxFloats * (long long)t);
             // w1, p1, w2, p2 (12 floats), then e
             ce[0] = make_float4(w1.x.hi, w1.y.hi, w1.z.hi, p1.x.hi);
             ce[1] = make_float4(p1.y.hi, p1.z.hi, w2.x.hi, w2.y.hi);
@@ -706,7 +779,7 @@ __global__ void __launch_bounds__(128) k_pot_tier2_mixed(ClassArgs A, QuadTables
 }
 
 // ------------------------------------------------------------------ FP64 fix-up of ill-conditioned pairs
-// A pair that holds a needle cell (a corner angle below 3 degrees) is ill-conditioned: its J is
+// A pair that holds a needle cell (a corner angle below 5 degrees) is ill-conditioned: its J is
 // a small difference of large parts, and FP32 rounding of the bulk is amplified by a few thousand
 // there (measured: errors up to 1e-3 on the 20,480-triangle jittered sphere, whose two needles
 // have corners of 0.6 and 1.5 degrees).  After the mixed chain has finished, each such pair's
@@ -774,9 +847,8 @@ __device__ acc5 fixup_level_sum(const FixupPair<CLS> &p, const QuadTables &Q, in
 template <int CLS>
 __device__ __forceinline__ void fixup_collect_item(const ClassArgs &A, int *list, int *count, long long t)
 {
-    const double c3 = 0.99862953475457387;  // cos 3 degrees
     const int2 pr = A.pairs[t];
-    if ((CLS != kFar && A.panels[pr.x].v[2].w > c3) || A.panels[pr.y].v[2].w > c3) list[atomicAdd(count, 1)] = (int)t;
+    if ((CLS != kFar && A.panels[pr.x].v[2].w > kNeedleCos) || A.panels[pr.y].v[2].w > kNeedleCos) list[atomicAdd(count, 1)] = (int)t;
 }
 
 template <int CLS>

@@ -211,18 +211,18 @@ def test_run_stats_are_consistent(api):
 
 
 def test_fp64_fixup_of_needle_pairs_matches_fp64_form(api):
-    """pairs holding a needle cell (a corner below 3 degrees; for the disjoint class the cell K_j)
+    """pairs holding a needle cell (a corner below 5 degrees; for the disjoint class the cell K_j)
     are recomputed by the mixed form in FP64 with the FP64 form's relative refinement, their
     deepest levels spread over the GPU: J and P equal the FP64 form's to rounding and the kept
     levels are the same"""
     from integrator2_gb300 import meshes, pairs as P
-    V, C = meshes.jittered_icosphere(5, 0.15, 2026)  # two needles, corners of 0.6 and 1.5 degrees
+    V, C = meshes.jittered_icosphere(5, 0.15, 2026)  # needles: corners of 0.6, 1.5 and 3.6 degrees
     pl = P.build_pairs(V, C)
     e = np.linalg.norm(V[C[:, [1, 2, 0]]] - V[C], axis=2)
     a, b, c = e[:, 0], e[:, 1], e[:, 2]
     cos_max = np.max([(b * b + c * c - a * a) / (2 * b * c), (a * a + c * c - b * b) / (2 * a * c),
                       (a * a + b * b - c * c) / (2 * a * b)], axis=0)
-    needle = np.where(cos_max > np.cos(np.radians(3.0)))[0]
+    needle = np.where(cos_max > np.cos(np.radians(5.0)))[0]
     assert len(needle) >= 2
     m = api.Mesh3D()
     m.setGeometry(V, C)
