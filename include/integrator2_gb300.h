@@ -74,7 +74,8 @@ typedef enum i2_error_control {
 /* FP64: every stage in FP64 (matches the reference's CUDA build to 1e-12).  MIXED: the regular-part
  * quadrature in FP32 with compensated sums; the closed forms, the potential's tier 2b and adaptive
  * rule in double-float arithmetic on the FP32 pipe (about 2^-44 relative); the estimator's level
- * differences, pairs holding a needle cell and self pairs in FP64 */
+ * differences, pairs holding a needle cell (a corner below 5 degrees), adjacent pairs whose
+ * closed-form part exceeds J 48-fold, and self pairs in FP64 */
 typedef enum i2_precision { I2_PRECISION_FP64 = 0, I2_PRECISION_MIXED = 1 } i2_precision;
 
 typedef enum i2_channel {
@@ -191,10 +192,10 @@ i2_status i2_evaluator_result_count(const i2_evaluator_t *ev, i2_pair_class cls,
 /* statistics of the last run of a class (the reference prints per-cell refinement counts,
  * src/NumericalIntegrator3d.cu:494): out[0] pairs; out[1] pairs whose tier-1 potential check
  * failed; out[2] pairs that reached tier 2b; out[3] pairs given the adaptive potential rule;
- * out[4] adaptive-rule cells kept because a depth's list was full; out[5] needle pairs
- * recomputed in FP64 (mixed form); out[6] the class's last refinement level; out[6 + L] pairs
- * still unconverged after level L (L = 1..7, adaptive modes); out[14] of the needle pairs, those
- * whose levels 4-5 were spread over the GPU.  Synchronises the evaluator's stream. */
+ * out[4] adaptive-rule cells kept because a depth's list was full; out[5] pairs recomputed in
+ * FP64 by the mixed form (a needle cell, or a closed-form part 48 times J); out[6] the class's last
+ * refinement level; out[6 + L] pairs still unconverged after level L (L = 1..7, adaptive modes);
+ * out[14] of the out[5] pairs, those whose levels 4-5 were spread over the GPU.  Synchronises the evaluator's stream. */
 #define I2_RUN_STATS 15
 i2_status i2_evaluator_run_stats(const i2_evaluator_t *ev, i2_pair_class cls, int64_t *out, int32_t n);
 /* full-precision copy of a result channel (replaces subclassing for d_*Results) */
@@ -223,7 +224,7 @@ i2_status i2_evaluator_backward_class(i2_evaluator_t *ev, i2_pair_class cls, con
  * captured into a CUDA graph on the first i2_batch_run and replayed afterwards.  Settings
  * (rule, error control, potential rule) come from the integrator given at creation; the
  * batched form computes in mixed precision (FP32 bulk; double-float closed forms, tier 2b and
- * adaptive potential; FP64 estimator differences and needle pairs) whatever the integrator's
+ * adaptive potential; FP64 estimator differences, needle and high-ratio pairs) whatever the integrator's
  * precision. */
 typedef struct i2_batch i2_batch_t;
 i2_status i2_batch_create(const i2_integrator_t *settings, i2_batch_t **out);

@@ -17,6 +17,13 @@ constexpr int kHardMaxDepth = 12;
 // a needle cell has a corner below 5 degrees: the mixed form computes the pairs that hold one (K_j
 // only, for the disjoint class) in FP64; cos 5 degrees, compared with the panel's largest corner cosine
 constexpr double kNeedleCos = 0.99619469809174553;
+// the mixed form also recomputes in FP64 the adjacent pairs whose closed-form part exceeds the
+// complete J by this factor: their FP32 quadrature part is as large, and its rounding (0.5-1.3e-7
+// of J per unit of the ratio) is amplified by it.  48 bounds that amplification for 0.01 % of the
+// common-vertex pairs of the 20,480-triangle jittered sphere (15 pairs; their ratios reach 355);
+// 8 took 457 pairs there, cost 7 % of the step and left most of the FP32 tail, which is rounding
+// on moderately conditioned pairs
+constexpr double kFixRatio = 48.0;
 // floats per adjacent pair in ClassArgs::ctx_e (mixed precision): the common-vertex asymptote's
 // directions, or the common-edge pair's shared-edge term and shared-edge frame
 constexpr int kPairCtxFloats = 20;
@@ -25,7 +32,7 @@ constexpr int kPairCtxFloats = 20;
 constexpr int kCntHard = 8;       // pairs handed to the adaptive potential rule
 constexpr int kCntOverflow = 9;   // adaptive-rule cells kept because a depth's list was full
 constexpr int kCntTier2 = 10;     // pairs the tier-1 potential check rejected
-constexpr int kCntFixup = 11;     // needle pairs recomputed in FP64 (mixed form)
+constexpr int kCntFixup = 11;     // pairs recomputed in FP64 by the mixed form (needle cells, kFixRatio)
 constexpr int kCntTier2b = 12;    // pairs that reached tier 2b
 constexpr int kCntFixDeep = 13;   // FP64 fix-up pairs whose deeper levels were spread over the GPU
 // FP64 fix-up pairs per class run whose levels 4..5 can be spread over the GPU (820 KB of chunk

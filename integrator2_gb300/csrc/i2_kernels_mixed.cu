@@ -843,12 +843,23 @@ __device__ acc5 fixup_level_sum(const FixupPair<CLS> &p, const QuadTables &Q, in
 // A disjoint pair needs it only when K_j, the cell integrated in closed form, is the needle: its
 // two long, nearly antiparallel edges make Psi a small difference of nearly equal edge terms.  A
 // needle K_i is only a small area the quadrature runs over.  Adjacent pairs share vertices with
-// both cells, so either cell's needle counts there.
+// both cells, so either cell's needle counts there.  An adjacent pair is also gathered when its
+// closed-form part, (Theta_s n_j + Psi_s x n_j) / (4 pi), exceeds the finalised J by kFixRatio:
+// J is then a small difference of that part and an FP32 quadrature part of the same size (up to
+// 355x |J| among the 20,480-triangle jittered sphere's common-vertex pairs).
 template <int CLS>
 __device__ __forceinline__ void fixup_collect_item(const ClassArgs &A, int *list, int *count, long long t)
 {
     const int2 pr = A.pairs[t];
-    if ((CLS != kFar && A.panels[pr.x].v[2].w > kNeedleCos) || A.panels[pr.y].v[2].w > kNeedleCos) list[atomicAdd(count, 1)] = (int)t;
+    bool take = (CLS != kFar && A.panels[pr.x].v[2].w > kNeedleCos) || A.panels[pr.y].v[2].w > kNeedleCos;
+    if (CLS != kFar && !take) {
+        const double *sg = A.sing + 4 * t, *J = A.J3 + 3 * t;
+        const double4_32a nj4 = A.panels[pr.y].v[3];
+        const d3 ps = cross(mk(sg[0], sg[1], sg[2]), mk(nj4.x, nj4.y, nj4.z));
+        const double s2 = (sg[3] * sg[3] + dot(ps, ps)) * (kInv4Pi * kInv4Pi);  // |J_s|^2 (Psi_s x n_j is normal to n_j)
+        take = s2 > kFixRatio * kFixRatio * (J[0] * J[0] + J[1] * J[1] + J[2] * J[2]);
+    }
+    if (take) list[atomicAdd(count, 1)] = (int)t;
 }
 
 template <int CLS>
