@@ -250,6 +250,49 @@ def test_fp64_fixup_of_needle_pairs_matches_fp64_form(api):
     assert spread > 0  # levels 4-5 of some pairs ran spread over the GPU
 
 
+def test_fp64_fixup_of_high_ratio_pairs(api):
+    """an adjacent pair whose closed-form part exceeds its J 48-fold is recomputed in FP64 too (its
+    FP32 quadrature part is as large, and rounding is amplified by the ratio).  On a coarse sphere
+    jittered by 0.3 h the common-vertex class's fix-up takes the 170 needle pairs and the 13 others
+    above the ratio (closed forms and J from the oracle; the nearest ratio is 2 from the threshold),
+    and the class's worst pair is within 3e-6 of the FP64 form (8e-6 without the ratio); the routed
+    pairs, whose closed forms stay double-float, within 1e-8."""
+    from integrator2_gb300 import meshes, pairs as P
+    from oracle import oracle as O
+    V, C = meshes.jittered_icosphere(2, 0.3, 11)
+    V, C = np.ascontiguousarray(V), np.ascontiguousarray(C, np.int32)
+    pr = np.ascontiguousarray(P.build_pairs(V, C).by_class(P.VERTEX))
+    N, S, _ = O.cell_geometry(V, C)
+    _, Jo, _, _ = O.integrate(P.VERTEX, pr, V, C, mode=O.ADAPTIVE_RELATIVE, tol=1e-6)
+    s4 = np.zeros((len(pr), 4))
+    for k, (i, j) in enumerate(pr):
+        O.lib().o_closed_vertex(int(i), int(j), O._p(V), O._p(C), O._p(N), O._p(S), O._p(s4[k]))
+    nj = N[pr[:, 1]]
+    ratio = np.linalg.norm(s4[:, 3:4] * nj + np.cross(s4[:, :3], nj), axis=1) / (4 * np.pi) / np.linalg.norm(Jo, axis=1)
+    e = np.linalg.norm(V[C[:, [1, 2, 0]]] - V[C], axis=2)
+    a, b, c = e[:, 0], e[:, 1], e[:, 2]
+    cos_max = np.max([(b * b + c * c - a * a) / (2 * b * c), (a * a + c * c - b * b) / (2 * a * c),
+                      (a * a + b * b - c * c) / (2 * a * b)], axis=0)
+    needle = (cos_max > np.cos(np.radians(5.0)))[pr].any(axis=1)
+    high = ~needle & (ratio > 48.0)
+    assert needle.sum() == 170 and high.sum() == 13 and np.abs(ratio[~needle] - 48.0).min() > 2.0
+    m = api.Mesh3D()
+    m.setGeometry(V, C)
+    m.prepareMesh(3.0)
+    out = {}
+    for prec in (api.PRECISION_FP64, api.PRECISION_MIXED):
+        it = api.NumericalIntegrator3D(m, api.qf3D13)
+        it.setErrorControl(api.RELATIVE_ERROR_CONTROL, 1e-6, 5)
+        it.setPrecision(prec)
+        ev = api.EvaluatorJ3DK(m, it)
+        ev.runClass(P.VERTEX, pr)
+        out[prec] = (ev.getResults(P.VERTEX), ev.getRunStats(P.VERTEX))
+    (J64, _), (J32, st) = out[api.PRECISION_FP64], out[api.PRECISION_MIXED]
+    assert st["fp64_fixup"] == int(needle.sum() + high.sum()), st
+    err = rel_rows(J32, J64)
+    assert err[high].max() < 1e-8 and err.max() < 3e-6, (err[high].max(), err.max())
+
+
 def test_mixed_adaptive_potential_of_hard_pairs(api):
     """hard adjacent pairs (folded, or a corner below 10 degrees) take the adaptive potential rule
     in FP64 in both forms (the mixed form with a 2e-8 floor on its tolerance): the FP32 potential
