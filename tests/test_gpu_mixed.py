@@ -1,5 +1,5 @@
 """Mixed-precision form (FP32 bulk; double-float closed forms, tier 2b and adaptive potential; FP64
-estimator differences and needle pairs) through the C-ABI: per class and per channel error against
+estimator differences, needle and high-ratio pairs) through the C-ABI: per class and per channel error against
 the FP64 form and against the oracle's high-order answer; its device entry point captured into a
 CUDA graph."""
 import numpy as np
