@@ -98,13 +98,14 @@ struct VertexCtxF {
 // the edge (a, a' > 0):
 //   l_B l_C - a a' = p^2 (a^2 + a'^2 + p^2) / (l_B l_C + a a'),
 //   l_C a - l_B a' = p^2 (a - a')(a + a') / (l_C a + l_B a'),   l_B - a = p^2 / (l_B + a);
-// outside that span the direct forms add terms of one sign.
-__device__ __forceinline__ void edge_integrand_f(f3 oA, f3 wb, const PanelJf &K, const EdgeCtxF &E, f3 &psi, float &th)
+// outside that span the direct forms add terms of one sign.  Psi's two logs are returned as
+// scalars (lg): the lanes sum them, and psi_from_logs applies the FP64 unit edges once per pair.
+__device__ __forceinline__ void edge_integrand_f(f3 oA, f3 wb, const PanelJf &K, const EdgeCtxF &E, f3 &lg, float &th)
 {
     const float lA = normf(oA);
     const float l1 = logf((lA + dotf(oA, E.tb)) * E.ilvc);
     const float l2 = logf((lA - dotf(oA, E.ta)) * E.ilvc);
-    psi = l1 * E.tb + l2 * E.ta;
+    lg = f3{l1, l2, 0.0f};  // Psi = l1 tb + l2 ta, formed once per pair (psi_from_logs)
     const float lD = wb.z;
     const float a = fmaf(wb.y, E.L, lD * E.dB), ap = fmaf(wb.x, E.L, lD * E.dC);
     const float ph = lD * E.h, p2 = ph * ph;
@@ -125,13 +126,15 @@ __device__ __forceinline__ void edge_integrand_f(f3 oA, f3 wb, const PanelJf &K,
     th = 2.0f * atan2f(2.0f * K.S * (lD * E.dn), den) - 2.0f * (s1 - s2);
 }
 
-__device__ __forceinline__ void vertex_integrand_f(f3 oA, f3 oB, f3 oC, const PanelJf &K, const VertexCtxF &Vx, f3 &psi, float &th)
+// Psi = L_bc tbc + l1 ta + l2 tb; its three logs are returned as scalars (lg), summed by the
+// lanes and combined with the FP64 unit edges once per pair (psi_from_logs).
+__device__ __forceinline__ void vertex_integrand_f(f3 oA, f3 oB, f3 oC, const PanelJf &K, const VertexCtxF &Vx, f3 &lg, float &th)
 {
     const float lA = normf(oA), lB = normf(oB), lC = normf(oC);
     const float Lbc = edge_log_f32(lB, dotf(oB, Vx.tbc), oB, lC, dotf(oC, Vx.tbc), oC, Vx.tbc, Vx.lenBC);
     const float l1 = logf((lC + dotf(oC, Vx.ta)) * Vx.inv_sqrt_si);
     const float l2 = logf((lB - dotf(oB, Vx.tb)) * Vx.inv_sqrt_si);
-    psi = Lbc * Vx.tbc + l1 * Vx.ta + l2 * Vx.tb;
+    lg = f3{Lbc, l1, l2};
     const float den = lA * lB * lC + dotf(oA, oB) * lC + dotf(oB, oC) * lA + dotf(oC, oA) * lB;
     // The angle terms s1 = atan2(o_A.w1, l_A c1 - o_A.p1) and s2 = atan2(o_A.w2, l_A c2 - o_A.p2)
     // are both singular on the ray A + t e (the planes' intersection line, which may cross K_i):
@@ -198,6 +201,32 @@ __device__ __forceinline__ LevelLists level_lists(const ClassArgs &A, int level,
 __device__ __forceinline__ bool fuse_levels01(int level, int mode, int kmax) { return level == 0 && mode == kAdaptiveRelative && kmax >= 1; }
 __host__ __device__ __forceinline__ bool level_pass_needed(int level, int mode) { return !(level == 1 && mode == kAdaptiveRelative); }
 
+// Psi of an adjacent pair from the lanes' sums of its logs (common vertex: L_bc, l1, l2; common
+// edge: l1, l2), with K_j's unit edges in FP64 (K_j rotated by sj).  Summing the logs and applying
+// the directions once keeps their FP32 rounding out of Psi; over the common-vertex pairs of the
+// 20,480-triangle jittered sphere (FP32 emulation) that rounding was most of the error.  The
+// lanes' logs are scaled by an FP32 constant s' (1/sqrt(S_i), or 1/|JC - JB|) rounded once from
+// the exact s: every point's l1 and l2 carry ln(s'/s), which integrates to (s'/s - 1) S_i and is
+// taken off here (to first order; the second is below 1e-14).
+template <int CLS>
+__device__ __forceinline__ void psi_from_logs(const ClassArgs &A, int2 pr, int sj, acc5 &a)
+{
+    const double4_32a *pj = A.panels[pr.y].v;
+    const d3 ta = xyz(pj[4 + (sj + 1) % 3]), tb = xyz(pj[4 + (sj + 2) % 3]);
+    const double Si = A.panels[pr.x].v[0].w;
+    d3 p;
+    if (CLS == kVertex) {
+        const double dl = ((double)A.panels_f[pr.x].v[5].w * sqrt(Si) - 1.0) * Si;
+        p = a.px * xyz(pj[4 + sj]) + (a.py - dl) * ta + (a.pz - dl) * tb;
+    } else {
+        const double dl = ((double)A.panels_f[pr.y].v[7 + sj].w * pj[4 + sj].w - 1.0) * Si;
+        p = (a.px - dl) * tb + (a.py - dl) * ta;
+    }
+    a.px = p.x;
+    a.py = p.y;
+    a.pz = p.z;
+}
+
 template <int CLS>
 __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, const QuadTablesF &Qf, int level, int mode, double tol,
                                   int kmax, long long first, long long stride, int G_cap)
@@ -241,6 +270,7 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
         kahan5 ks0;  // level 0's sums when levels 0 and 1 are fused (ks then holds level 1's)
         kahan_zero(ks0);
         int2 pr = make_int2(0, 0);
+        int sj_pair = 0;  // K_j's rotation (adjacent classes)
         if (valid) {
             pr = A.pairs[t];
             const PanelJf K = load_panel_f(A.panels_f, pr.y);
@@ -259,6 +289,7 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
                 if (CLS == kEdge) shifts_edge(ci, cj, si, sj);
                 else shifts_vertex(ci, cj, si, sj);
                 origin = sj;
+                sj_pair = sj;
                 // unit edges of K_j in the rotated order, rounded from FP64 (the panel's unit edge
                 // k is opposite vertex k): the closed forms subtract the asymptote along the same
                 // directions, so FP32-normalised edges would leave a bias of a few ulps at every point
@@ -339,7 +370,7 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
                 for (int g = 0; g < Qf.npts; ++g) {
                     const float l1 = Qf.L1[g], l2 = Qf.L2[g], l3 = Qf.L3[g];
                     const f3 oA = l1 * U0.a + l2 * U0.b + l3 * U0.c;
-                    f3 psi;
+                    f3 psi;  // the disjoint class's Psi; the adjacent classes' log coefficients (psi_from_logs)
                     float th, pot = 0.0f;
                     if (CLS == kEdge) {
                         edge_integrand_f(oA, l1 * Ub.a + l2 * Ub.b + l3 * Ub.c, K, E, psi, th);
@@ -406,6 +437,7 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
         acc.pz = (double)ks.s[2] - (double)ks.c[2];
         acc.th = (double)ks.s[3] - (double)ks.c[3];
         acc.pot = (double)ks.s[4] - (double)ks.c[4];
+        if (CLS != kFar) psi_from_logs<CLS>(A, pr, sj_pair, acc);
         double *cur = A.cur + 5 * (long long)t;
         int lev = level;  // the level decided on below
         LevelLists out = Lst;
@@ -413,6 +445,7 @@ __device__ void level_items_mixed(const ClassArgs &A, const LevelLists &Lst, con
         if (fused01) {
             prev = acc5{(double)ks0.s[0] - (double)ks0.c[0], (double)ks0.s[1] - (double)ks0.c[1], (double)ks0.s[2] - (double)ks0.c[2],
                         (double)ks0.s[3] - (double)ks0.c[3], (double)ks0.s[4] - (double)ks0.c[4]};
+            if (CLS != kFar) psi_from_logs<CLS>(A, pr, sj_pair, prev);
             lev = 1;
             out = level_lists(A, 1, mode);
         } else {
