@@ -58,6 +58,13 @@ __global__ void k_prepare_panels_f32(int nc, const double *__restrict__ V, const
 }
 
 // ------------------------------------------------------------------ FP32 fused regular parts
+// The plain logs of the adjacent classes' integrands, ln((l + o.tau) s), have arguments that
+// vanish only on a ray from one of K_j's vertices along an edge line, which the cells of a valid
+// mesh keep away from.  Folded or overlapping cells can reach it, and there FP32 cancellation can
+// make the argument negative; the floor keeps the log finite (the FP64 form's argument stays a
+// small positive number there, and gives a large finite log too).
+constexpr float kLogArgFloor = 1.17549435e-38f;  // the smallest normal float
+
 // A common-edge pair in the frame of its shared edge JB -> JC (K_j = (JA, JB, JC), D = K_i's vertex
 // off the edge, tc = unit(JC - JB), L = |JC - JB|, D_p = the part of D - JB normal to tc, h = |D_p|).
 // A point x of K_i with barycentric weights (l_B, l_C, l_D) lies at the distance a = l_C L + l_D dB
@@ -103,8 +110,8 @@ struct VertexCtxF {
 __device__ __forceinline__ void edge_integrand_f(f3 oA, f3 wb, const PanelJf &K, const EdgeCtxF &E, f3 &lg, float &th)
 {
     const float lA = normf(oA);
-    const float l1 = logf((lA + dotf(oA, E.tb)) * E.ilvc);
-    const float l2 = logf((lA - dotf(oA, E.ta)) * E.ilvc);
+    const float l1 = logf(fmaxf((lA + dotf(oA, E.tb)) * E.ilvc, kLogArgFloor));
+    const float l2 = logf(fmaxf((lA - dotf(oA, E.ta)) * E.ilvc, kLogArgFloor));
     lg = f3{l1, l2, 0.0f};  // Psi = l1 tb + l2 ta, formed once per pair (psi_from_logs)
     const float lD = wb.z;
     const float a = fmaf(wb.y, E.L, lD * E.dB), ap = fmaf(wb.x, E.L, lD * E.dC);
@@ -132,8 +139,8 @@ __device__ __forceinline__ void vertex_integrand_f(f3 oA, f3 oB, f3 oC, const Pa
 {
     const float lA = normf(oA), lB = normf(oB), lC = normf(oC);
     const float Lbc = edge_log_f32(lB, dotf(oB, Vx.tbc), oB, lC, dotf(oC, Vx.tbc), oC, Vx.tbc, Vx.lenBC);
-    const float l1 = logf((lC + dotf(oC, Vx.ta)) * Vx.inv_sqrt_si);
-    const float l2 = logf((lB - dotf(oB, Vx.tb)) * Vx.inv_sqrt_si);
+    const float l1 = logf(fmaxf((lC + dotf(oC, Vx.ta)) * Vx.inv_sqrt_si, kLogArgFloor));
+    const float l2 = logf(fmaxf((lB - dotf(oB, Vx.tb)) * Vx.inv_sqrt_si, kLogArgFloor));
     lg = f3{Lbc, l1, l2};
     const float den = lA * lB * lC + dotf(oA, oB) * lC + dotf(oB, oC) * lA + dotf(oC, oA) * lB;
     // The angle terms s1 = atan2(o_A.w1, l_A c1 - o_A.p1) and s2 = atan2(o_A.w2, l_A c2 - o_A.p2)
