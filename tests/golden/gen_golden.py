@@ -5,6 +5,7 @@ Run here (where the reference checkout exists), not on the GPU machine:
     python tests/golden/gen_golden.py            # reference at /root/reference
     I2_REFERENCE=/path/to/integrator2 python tests/golden/gen_golden.py
     python tests/golden/gen_golden.py --only-all # only the all-disjoint fixture (ico1_all.npz)
+    python tests/golden/gen_golden.py --only-examples  # only the example-mesh fixture (cubehole.npz)
 
 It builds oracle/_ref/libi2ref.so (oracle/ref_build.sh: the reference's src/ compiled for the
 host through oracle/ref_shim.h, plus oracle/ref_driver.cu, which mirrors the reference's kernel
@@ -111,11 +112,21 @@ def point_samples(n=400, seed=11):
     return np.asarray(rows)
 
 
+def example_meshes():
+    """the reference's cubehole.dat example (a unit cube with a square hole: coplanar faces and
+    90-degree folds), its near-field classes at fixed levels 0 and 1"""
+    V, C = M.read_dat(os.path.join(REF, "examples", "cubehole.dat"))
+    run_mesh("cubehole", V, C, P.build_pairs(V, C), far_sample=2500, seed=4, modes=(0, 1))
+
+
 def main():
     subprocess.run([os.path.join(ROOT, "oracle", "ref_build.sh")], check=True,
                    env=dict(os.environ, I2_REFERENCE=REF))
     if O.ref_lib() is None:
         raise SystemExit("reference host library not built")
+    if "--only-examples" in sys.argv:
+        example_meshes()
+        return
     # full not-neighbours semantics (prepareMesh without a near-field cutoff + runAllPairs) on a
     # jittered 80-cell sphere
     V, C = M.jittered_icosphere(1, 0.15, 5)
@@ -159,6 +170,7 @@ def main():
     print(f"cases: {len(case)} two-triangle fixtures")
     np.savez_compressed(os.path.join(HERE, "theta_psi_points.npz"), rows=point_samples())
     print("theta_psi_points: 400 samples")
+    example_meshes()
 
 
 if __name__ == "__main__":

@@ -43,6 +43,28 @@ def test_adaptive_compat_matches_reference(mesh, cls):
     assert np.all((lev == it) | (lev == it - 1))
 
 
+def _tangential_where(J, n, mask):
+    """J, with only its part normal to n removed on the rows where mask is set"""
+    return np.where(mask[:, None], J - np.sum(J * n, axis=1)[:, None] * n, J)
+
+
+@pytest.mark.parametrize("cls", [O.VERTEX, O.EDGE, O.FAR])
+def test_cubehole_matches_reference(cls):
+    """the reference's cubehole.dat example (coplanar faces, 90-degree folds) at fixed levels 0
+    and 1; on common-edge pairs that take the coplanar branch, where the reference leaves Theta
+    unset (evaluatorJ3DK.cu:474-481), only J's part tangential to K_j is compared"""
+    g = np.load(os.path.join(GOLD, "cubehole.npz"))
+    pairs = g[f"pairs_{cls}"]
+    n, _, _ = O.cell_geometry(g["V"], g["C"])
+    n = n[pairs[:, 1]]
+    uninit = g["uninit_theta_1"] if cls == O.EDGE else np.zeros(len(pairs), bool)
+    if cls == O.EDGE:
+        assert uninit.sum() > 500
+    for tag, lev in (("L0", 0), ("L1", 1)):
+        _, J, _, _ = O.integrate(cls, pairs, g["V"], g["C"], mode=O.FIXED, level=lev)
+        assert _close(_tangential_where(J, n, uninit), _tangential_where(g[f"J_{cls}_{tag}"], n, uninit)) < TOL, (cls, tag)
+
+
 def test_two_triangle_fixtures():
     d = np.load(os.path.join(GOLD, "cases.npz"))
     names = sorted({k.split("|")[0] for k in d.files})
