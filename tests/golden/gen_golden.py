@@ -5,7 +5,7 @@ Run here (where the reference checkout exists), not on the GPU machine:
     python tests/golden/gen_golden.py            # reference at /root/reference
     I2_REFERENCE=/path/to/integrator2 python tests/golden/gen_golden.py
     python tests/golden/gen_golden.py --only-all # only the all-disjoint fixture (ico1_all.npz)
-    python tests/golden/gen_golden.py --only-examples  # only the example-mesh fixture (cubehole.npz)
+    python tests/golden/gen_golden.py --only-examples  # only the example-mesh fixtures (cubehole.npz, examples.npz)
 
 It builds oracle/_ref/libi2ref.so (oracle/ref_build.sh: the reference's src/ compiled for the
 host through oracle/ref_shim.h, plus oracle/ref_driver.cu, which mirrors the reference's kernel
@@ -50,13 +50,15 @@ def coplanar_edge_branch(V, C, pairs):
     return flags
 
 
-def run_mesh(name, V, C, pl: P.PairLists, far_sample=None, seed=0, modes=(0, 1, -1)):
+def run_mesh(name, V, C, pl: P.PairLists, far_sample=None, seed=0, modes=(0, 1, -1), sample=None):
+    """sample: at most this many pairs of every class (seeded); far_sample: of the disjoint class"""
     out = {"V": V, "C": C.astype(np.int32)}
     rng = np.random.default_rng(seed)
     for cls in CLASSES:
         pairs = pl.by_class(cls)
-        if cls == O.FAR and far_sample is not None and len(pairs) > far_sample:
-            pairs = pairs[np.sort(rng.choice(len(pairs), far_sample, replace=False))]
+        cap = far_sample if cls == O.FAR and far_sample is not None else sample
+        if cap is not None and len(pairs) > cap:
+            pairs = pairs[np.sort(rng.choice(len(pairs), cap, replace=False))]
         if len(pairs) == 0:
             continue
         out[f"pairs_{cls}"] = pairs.astype(np.int32)
@@ -112,11 +114,28 @@ def point_samples(n=400, seed=11):
     return np.asarray(rows)
 
 
+# the reference's example surfaces (README.md "Noticeable examples") at the scales it gives
+EXAMPLES = (("G1", "G1.dat", 1.0), ("Krylo01", "Krylo01.dat", 1.0), ("Girja", "Girja.dat", 1.0),
+            ("ellipsoid2000", "ellipsoid2000", 1.0), ("Fish", "Fish.dat", 100.0), ("s5m", "s5m.dat", 0.0005))
+
+
 def example_meshes():
     """the reference's cubehole.dat example (a unit cube with a square hole: coplanar faces and
-    90-degree folds), its near-field classes at fixed levels 0 and 1"""
+    90-degree folds), its near-field classes at fixed levels 0 and 1; and its example surfaces
+    at their scales, 800 seeded pairs of every class (examples.npz, keys "<mesh>|<field>")"""
     V, C = M.read_dat(os.path.join(REF, "examples", "cubehole.dat"))
     run_mesh("cubehole", V, C, P.build_pairs(V, C), far_sample=2500, seed=4, modes=(0, 1))
+    flat = {}
+    for k, (nm, fname, scale) in enumerate(EXAMPLES):
+        V, C = M.read_dat(os.path.join(REF, "examples", fname), scale)
+        run_mesh("_example", V, C, P.build_pairs(V, C), seed=10 + k, modes=(0, 1), sample=800)
+        path = os.path.join(HERE, "_example.npz")
+        with np.load(path) as d:
+            for key in d.files:
+                flat[f"{nm}|{key}"] = d[key]
+        os.remove(path)
+    np.savez_compressed(os.path.join(HERE, "examples.npz"), **flat)
+    print(f"examples: {len(EXAMPLES)} surfaces")
 
 
 def main():

@@ -97,6 +97,50 @@ def test_cubehole_matches_reference(api, cls):
         assert (r <= bar).all(), (cls, tag, int((r > bar).sum()), float((r / bar).max()))
 
 
+@pytest.mark.parametrize("mesh", ["G1", "Krylo01", "Girja", "ellipsoid2000", "Fish", "s5m"])
+def test_example_surfaces_match_reference(api, mesh):
+    """the reference's example surfaces (its README's list, at the scales it gives: Fish x 100,
+    s5m x 0.0005), 800 seeded pairs of every class, fixed levels 0 and 1, against the reference's
+    host build: twice the parity bar plus 4 times the near-collinear log-ratio noise
+    (log_ratio_noise), J's part tangential to K_j where the reference leaves Theta unset.  The
+    factor 2 is libm: on Krylo01 and s5m the reference's own CUDA build differs from its host build
+    by up to 1.3 times the single bar, and this form is within 0.21 times it of the CUDA build
+    (tests/test_gpu_ref_cuda.py).  On Girja.dat at scale 1
+    (cells of 2.5e-7) the reference's closed forms return NaN for 3 common-vertex and 10
+    common-edge pairs: their absolute thresholds misfire at that size, and the same pairs scaled
+    by 1024 are finite.  This form evaluates the closed forms at a power-of-two scale that brings
+    sqrt(S_i) into [0.5, 1) (1024 for those cells); there it matches the oracle on the mesh scaled
+    by 1024, with J scaled back by 1024^2."""
+    from oracle import oracle as O
+    d = np.load(os.path.join(GOLD, "examples.npz"))
+    V, C = d[f"{mesh}|V"], d[f"{mesh}|C"]
+    nrm = np.cross(V[C[:, 1]] - V[C[:, 0]], V[C[:, 2]] - V[C[:, 0]])
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    nan_pairs = 0
+    for cls in (0, 1, 2):
+        pairs = d[f"{mesh}|pairs_{cls}"]
+        n = nrm[pairs[:, 1]]
+        uninit = d[f"{mesh}|uninit_theta_1"] if cls == 1 else np.zeros(len(pairs), bool)
+
+        def tangential_where(J):
+            return np.where(uninit[:, None], J - np.sum(J * n, axis=1)[:, None] * n, J)
+
+        fin = np.isfinite(d[f"{mesh}|J_{cls}_L0"]).all(axis=1) & np.isfinite(d[f"{mesh}|J_{cls}_L1"]).all(axis=1)
+        nan_pairs += int((~fin).sum())
+        k = kappa(cls, pairs[fin], V, C)
+        for tag, lev in (("L0", 0), ("L1", 1)):
+            _, J, _, _ = run(api, V, C, cls, pairs, "fixed", lev)
+            assert np.isfinite(J).all(), (mesh, cls, tag)
+            Jr = tangential_where(d[f"{mesh}|J_{cls}_{tag}"])[fin]
+            r = rel_rows(tangential_where(J)[fin], Jr)
+            bar = 2.0 * (parity_bar(k) + 4.0 * log_ratio_noise(V, C, pairs[fin], lev, Jr))
+            assert (r <= bar).all(), (mesh, cls, tag, int((r > bar).sum()), float((r / bar).max()))
+            if not fin.all():
+                _, Js, _, _ = O.integrate(cls, pairs[~fin], V * 1024.0, C, mode=O.FIXED, level=lev)
+                assert rel_rows(J[~fin], Js / 1024.0 ** 2).max() < 1e-10, (mesh, cls, tag)
+    assert nan_pairs == (13 if mesh == "Girja" else 0)
+
+
 def test_two_triangle_fixtures(api):
     d = np.load(os.path.join(GOLD, "cases.npz"))
     names = sorted({k.split("|")[0] for k in d.files})
