@@ -24,6 +24,12 @@ constexpr double kNeedleCos = 0.99619469809174553;
 // 8 took 457 pairs there, cost 7 % of the step and left most of the FP32 tail, which is rounding
 // on moderately conditioned pairs
 constexpr double kFixRatio = 48.0;
+// the common-edge closed form divides by 1 - c^2 (c = cos of the angle between the shared edge's
+// neighbouring edges of the two cells, across the fold): a nearly coplanar pair whose cells have
+// nearly equal angles there, short of the coplanar branch, cancels by that factor; the mixed form
+// evaluates such pairs' closed form in FP64 below this value (double-float's 2^-44 would lose
+// 6e-14 / (1 - c^2) of it)
+constexpr double kEdgeClosedFormC2 = 1e-5;
 // floats per adjacent pair in ClassArgs::ctx_e (mixed precision): the common-vertex asymptote's
 // directions, or the common-edge pair's shared-edge term and shared-edge frame
 constexpr int kPairCtxFloats = 20;

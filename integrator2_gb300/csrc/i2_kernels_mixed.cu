@@ -640,6 +640,21 @@ __device__ __forceinline__ void store_edge_frame(const ClassArgs &A, int2 pr, in
     reinterpret_cast<float4 *>(ce)[4] = make_float4((float)dot(BA, tc), (float)dot(BA, Dp), (float)norm(JC - JB), 0.0f);
 }
 
+// true when the common-edge closed form's factor 1 / (sin a (1 - c^2)) (closed_edge_unit's q_edge,
+// c = c_mu or c_sigma) exceeds 1 / kEdgeClosedFormC2 outside the coplanar branch: the angles at the
+// shared edge's ends from cosines and sines of FP64 unit edges (Ti, Tj rotated as the closed form
+// takes them, the off-edge vertex first)
+__device__ __forceinline__ bool edge_closed_form_cancels(const Tri &Ti, const Tri &Tj, d3 ni, d3 nj)
+{
+    const d3 ica = unit(Ti.a - Ti.c), icb = unit(Ti.b - Ti.c), iba = unit(Ti.a - Ti.b), ibc = unit(Ti.c - Ti.b);
+    const d3 jba = unit(Tj.a - Tj.b), jbc = unit(Tj.c - Tj.b), jca = unit(Tj.a - Tj.c), jcb = unit(Tj.b - Tj.c);
+    const double ca = dot(ica, icb), sa = norm(cross(ica, icb)), cb = dot(ibc, iba), sb = norm(cross(ibc, iba));
+    const double cg = dot(jbc, jba), sg = norm(cross(jbc, jba)), cd = dot(jcb, jca), sd = norm(cross(jcb, jca));
+    const double cx = dot(ni, nj);
+    const double cmu = -(cb * cg + cx * sb * sg), csig = -(ca * cd + cx * sa * sd);
+    return 1.0 - cmu * cmu < kEdgeClosedFormC2 || 1.0 - csig * csig < kEdgeClosedFormC2;
+}
+
 template <int CLS>
 __device__ __forceinline__ void singular_mixed_item(const ClassArgs &A, const QuadTablesF &Qf, long long t)
 {
@@ -655,11 +670,16 @@ __device__ __forceinline__ void singular_mixed_item(const ClassArgs &A, const Qu
     // closed-form singular part (a4 / a5) and, for the vertex class, the asymptote's constants.
     // A pair that holds a needle cell is recomputed in FP64 after the level sweep, its J a small
     // difference of large parts: its closed form is FP64 too (the path below), so that the fix-up
-    // reproduces the FP64 form.  Every other pair computes it in double-float, the pair translated
-    // to K_j's vertex A in FP64 (the closed forms depend on vertex differences only) and
-    // converted; the closed forms scale it by a power of two.
-    if (A.panels[pr.x].v[2].w > kNeedleCos || A.panels[pr.y].v[2].w > kNeedleCos) {  // as fixup_collect_item
-        const Tri Ti = rotate(load_tri(A.panels, pr.x), si), Tj = rotate(Tri{Kd.A, Kd.B, Kd.C}, sj);
+    // reproduces the FP64 form.  So does a common-edge pair whose closed form cancels by more than
+    // double-float can carry (edge_closed_form_cancels: 8 of the 61,440 pairs of the 20,480-triangle
+    // jittered sphere, 11 to 16 in 800 on the reference's Fish and Krylo01 examples, where
+    // double-float gave errors up to 4e-5).  Every other pair computes it in double-float, the pair
+    // translated to K_j's vertex A in FP64 (the closed forms depend on vertex differences only)
+    // and converted; the closed forms scale it by a power of two.
+    const Tri Ti64 = rotate(load_tri(A.panels, pr.x), si), Tj64 = rotate(Tri{Kd.A, Kd.B, Kd.C}, sj);
+    if (A.panels[pr.x].v[2].w > kNeedleCos || A.panels[pr.y].v[2].w > kNeedleCos ||  // as fixup_collect_item
+        (CLS == kEdge && edge_closed_form_cancels(Ti64, Tj64, ni, Kd.n))) {
+        const Tri &Ti = Ti64, &Tj = Tj64;
         d3 psi;
         double th;
         if (CLS == kEdge) {
