@@ -27,9 +27,11 @@ constexpr double kFixRatio = 48.0;
 // the common-edge closed form divides by 1 - c^2 (c = cos of the angle between the shared edge's
 // neighbouring edges of the two cells, across the fold): a nearly coplanar pair whose cells have
 // nearly equal angles there, short of the coplanar branch, cancels by that factor; the mixed form
-// evaluates such pairs' closed form in FP64 below this value (double-float's 2^-44 would lose
-// 6e-14 / (1 - c^2) of it)
-constexpr double kEdgeClosedFormC2 = 1e-5;
+// evaluates such pairs' closed form in FP64 below this value.  Double-float lost about
+// 2e-15 / (1 - c^2) of J (4e-5 at 1 - c^2 = 5e-11 on the reference's Fish example), so 1e-7 keeps
+// it near 2e-8; 1e-5 sent 3.4 % of a jittered torus grid's common-edge pairs there, and the FP64
+// lanes slowed two thirds of its warps
+constexpr double kEdgeClosedFormC2 = 1e-7;
 // floats per adjacent pair in ClassArgs::ctx_e (mixed precision): the common-vertex asymptote's
 // directions, or the common-edge pair's shared-edge term and shared-edge frame
 constexpr int kPairCtxFloats = 20;

@@ -671,9 +671,9 @@ __device__ __forceinline__ void singular_mixed_item(const ClassArgs &A, const Qu
     // A pair that holds a needle cell is recomputed in FP64 after the level sweep, its J a small
     // difference of large parts: its closed form is FP64 too (the path below), so that the fix-up
     // reproduces the FP64 form.  So does a common-edge pair whose closed form cancels by more than
-    // double-float can carry (edge_closed_form_cancels: 8 of the 61,440 pairs of the 20,480-triangle
-    // jittered sphere, 11 to 16 in 800 on the reference's Fish and Krylo01 examples, where
-    // double-float gave errors up to 4e-5).  Every other pair computes it in double-float, the pair
+    // double-float can carry (edge_closed_form_cancels: none of the 61,440 pairs of the
+    // 20,480-triangle jittered sphere, 4 to 7 in 800 on the reference's Fish and Krylo01 examples,
+    // where double-float gave errors up to 4e-5).  Every other pair computes it in double-float, the pair
     // translated to K_j's vertex A in FP64 (the closed forms depend on vertex differences only)
     // and converted; the closed forms scale it by a power of two.
     const Tri Ti64 = rotate(load_tri(A.panels, pr.x), si), Tj64 = rotate(Tri{Kd.A, Kd.B, Kd.C}, sj);

@@ -362,7 +362,7 @@ def test_mixed_on_example_surfaces(api, mesh):
     offset once from its exact value still gives s5m's disjoint class p99 1.4e-5).  Measured
     there: J p99 up to 1.2e-5 (s5m disjoint) and max 2.9e-5 (s5m common vertex); the FP64 form is
     the one to use on such meshes.  The bars pin those figures.  (Fish's common-edge class reached
-    4e-5 until pairs whose closed form cancels by 1 - c^2 < 1e-5 took the FP64 closed form; it
+    4e-5 until pairs whose closed form cancels by 1 - c^2 < 1e-7 took the FP64 closed form; it
     is now 4e-7.)"""
     import os
     from tests._util import GOLD
