@@ -375,7 +375,7 @@ def test_mixed_on_example_surfaces(api, mesh):
         J32, P32, _ = _run(api, V, C, cls, pr, api.PRECISION_MIXED)
         assert np.isfinite(J32).all() and np.isfinite(P32).all(), (mesh, cls)
         eJ, eP = rel_rows(J32, J64), np.abs(P32 - P64) / np.abs(P64)
-        if well_conditioned:
+        if well_conditioned or cls == 1:  # the common-edge class keeps it everywhere (s5m: 1.1e-6)
             assert eJ.max() < 2e-6 and eP.max() < 2e-6 and np.percentile(eJ, 99) <= 1e-6 and np.percentile(eP, 99) <= 1e-6, (mesh, cls, eJ.max(), eP.max())
         else:
             assert eJ.max() < 1e-4 and eP.max() < 1e-4 and np.percentile(eJ, 99) < 2e-5 and np.percentile(eP, 99) < 2e-5, (mesh, cls, eJ.max(), eP.max())
