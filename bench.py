@@ -254,6 +254,41 @@ def accuracy(V, C, lists, J, P, levels, nsample=400):
     return out
 
 
+def example_surfaces_section():
+    """the mixed form against the FP64 form on the reference's example surfaces at the scales its
+    README gives (the meshes and 800 seeded pairs per class each from tests/golden/examples.npz;
+    relative control 1e-6): per class the 99th percentile and the maximum of the per-pair relative
+    error of J and P.  The first three are well-conditioned; Girja, Fish and s5m hold pairs whose
+    sensitivity to relative coordinate perturbations runs into the thousands, where FP32 point
+    positions limit the mixed form to about that sensitivity x 1e-8."""
+    from integrator2_gb300 import api
+    d = np.load(os.path.join(ROOT, "tests", "golden", "examples.npz"))
+    out = {}
+    for mesh in ("G1", "Krylo01", "ellipsoid2000", "Girja", "Fish", "s5m"):
+        V, C = d[f"{mesh}|V"], d[f"{mesh}|C"]
+        row = {}
+        for cls, name in ((0, "vertex"), (1, "edge"), (2, "near")):
+            pr = np.ascontiguousarray(d[f"{mesh}|pairs_{cls}"])
+            res = {}
+            for prec in (api.PRECISION_FP64, api.PRECISION_MIXED):
+                m = api.Mesh3D()
+                m.setGeometry(V, C)
+                m.prepareMesh(NEAR)
+                it = api.NumericalIntegrator3D(m, api.qf3D13)
+                it.setErrorControl(api.RELATIVE_ERROR_CONTROL, 1e-6, 5)
+                it.setPrecision(prec)
+                ev = api.EvaluatorJ3DK(m, it)
+                ev.runClass(cls, pr)
+                res[prec] = (ev.getResults(cls), ev.getPotentials(cls))
+            (J64, P64), (Jm, Pm) = res[api.PRECISION_FP64], res[api.PRECISION_MIXED]
+            eJ = np.linalg.norm(Jm - J64, axis=1) / np.linalg.norm(J64, axis=1)
+            eP = np.abs(Pm - P64) / np.abs(P64)
+            row[name] = {"pairs": int(len(pr)), "J_p99": float(np.percentile(eJ, 99)), "J_max": float(eJ.max()),
+                         "P_p99": float(np.percentile(eP, 99)), "P_max": float(eP.max())}
+        out[mesh] = row
+    return {"vs": "FP64 form, relative control 1e-6", "scales": {"Fish": 100.0, "s5m": 0.0005}, "meshes": out}
+
+
 def level0_j_only(stream, precision):
     """the library on the reference's own workload: J only (potential off), fixed refinement
     level 0, qf3D13, the reference's three classes on C1 and C2, per class through the device
@@ -957,6 +992,8 @@ def gpu_arm(args):
                                          "--impl reference times the reference's CUDA build on it (reference_cuda)"}
     if "adjoint" in sections:
         line["adjoint"] = adjoint_section(args)
+    if "examples" in sections:
+        line["example_surfaces_mixed_vs_fp64"] = example_surfaces_section()
     if "batch" in forms:
         line["batch"] = {"shape": {"threads": forms["batch"]["shape"][0], "blocks_per_sm": forms["batch"]["shape"][1],
                                    "lanes_per_pair": forms["batch"]["shape"][2],
@@ -990,10 +1027,11 @@ def main():
                     help="c5 section: share of every class's pairs the timed backward pass covers (1 = all 194 M pairs, minutes)")
     ap.add_argument("--forms", default="fp64,mixed,batch",
                     help="forms to run: fp64, mixed (per-class chains), batch (headline when present)")
-    ap.add_argument("--sections", default="uneven,c5,adjoint,level0",
+    ap.add_argument("--sections", default="uneven,c5,adjoint,level0,examples",
                     help="side sections after the C2 line: uneven (48 meshes, batched vs per class), c5 (2 M triangles), "
                          "adjoint (C4), level0 (plain FP64, J only, fixed level 0 on C1/C2: the reference's own "
-                         "workload; --impl reference times the reference's CUDA build on it); empty for the C2 line alone")
+                         "workload; --impl reference times the reference's CUDA build on it), examples (mixed vs FP64 "
+                         "on the reference's example surfaces); empty for the C2 line alone")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
